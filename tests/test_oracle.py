@@ -1,0 +1,132 @@
+"""Pins the CPU oracle against the reference's own golden outputs (no GPU needed).
+
+* standalone mode == standalone/loop.op, digit for digit
+* union-find replay == test/union_find.op (parents, roots, tree sizes)
+* cluster labels == the reference union_find.h (both unify variants) on dumped configurations
+* ED restatement == loop.op's diagonalization blocks
+* philox mode: statistics within 3 sigma of exact diagonalization
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle_lib as orc
+
+
+def _fmt(x):
+    return "%g" % x
+
+
+def test_philox_known_answers():
+    # Random123 known-answer vectors for philox4x32-10.
+    assert [hex(x) for x in orc.philox_raw([0, 0, 0, 0], [0, 0])] == \
+        ["0x6627e8d5", "0xe169c58d", "0xbc57ac4c", "0x9b00dbd8"]
+    assert [hex(x) for x in orc.philox_raw([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2)] == \
+        ["0x408f276d", "0x41c83b0e", "0xa20bc7c6", "0x6d5451fd"]
+    assert [hex(x) for x in orc.philox_raw([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344],
+                                           [0xA4093822, 0x299F31D0])] == \
+        ["0xd16cfe09", "0x94fdcceb", "0x5001e420", "0x24126ea1"]
+
+
+def test_float_log_exp_accuracy():
+    L = orc.lib()
+    for u in np.linspace(1e-7, 1 - 1e-7, 2001).astype(np.float32):
+        ref = math.log(float(u))
+        assert abs(L.orc_log_spec(float(u)) - ref) <= 3e-7 * max(1.0, abs(ref))
+    for x in np.linspace(-80, 80, 1601).astype(np.float32):
+        ref = math.exp(float(x))
+        assert abs(L.orc_exp_spec(float(x)) - ref) <= 4e-7 * ref
+
+
+def test_standalone_matches_golden(golden):
+    g = golden("standalone_loop_op.json")
+    out, _ = orc.standalone(g["L"], g["T"], g["sweeps"], g["therm"])
+    names = ["Number of Clusters        = ", "Energy Density            = ",
+             "Uniform Susceptibility    = ", "Staggered Magnetization^2 = ",
+             "Staggered Susceptibility  = "]
+    lines = [n + _fmt(out[2 * i]) + " +- " + _fmt(out[2 * i + 1]) for i, n in enumerate(names)]
+    assert lines == g["lines"][4:9]
+
+
+def test_union_find_replay_matches_golden(golden):
+    g = golden("union_find_op.json")
+    n = g["n"]
+    parent, root, weight = orc.uf_replay(n, g["pairs"])
+    listing = []
+    for i in range(n):
+        if parent[i] < 0:
+            listing.append("node %d is root and tree size is %d" % (i, weight[i]))
+        else:
+            listing.append("node %d's parent is %d and its root is %d" % (i, parent[i], root[i]))
+    for i in range(n):
+        if parent[i] < 0:
+            listing.append("node %d is root" % i)
+        else:
+            listing.append("node %d's parent is %d and its root is %d" % (i, parent[i], root[i]))
+    assert listing == g["listing"]
+
+
+def _canon(labels):
+    """Canonical partition: relabel clusters by first appearance."""
+    m = {}
+    return [m.setdefault(x, len(m)) for x in labels]
+
+
+@pytest.mark.parametrize("idx", range(7))
+def test_uf_labels_match_reference_union_find(golden, idx):
+    c = golden("uf_labels.json")[idx]
+    lab_d, nc_d = orc.uf_label(c["dim"], c["L"], c["bonds"], c["graphs"], deterministic=True)
+    lab_w, nc_w = orc.uf_label(c["dim"], c["L"], c["bonds"], c["graphs"], deterministic=False)
+    assert nc_d == c["nc"] and nc_w == c["nc"]
+    assert lab_d.tolist() == c["labels_deterministic"]
+    assert lab_w.tolist() == c["labels_weighted"]
+    assert _canon(c["labels_deterministic"]) == _canon(c["labels_weighted"])
+
+
+def test_ed_matches_golden(golden):
+    for b in golden("loop_op.json"):
+        if b["algorithm"] != "diagonalization":
+            continue
+        r = orc.ed.thermal(1, b["L"], b["T"], jxy=b["jxy"], jz=b["jz"])
+        for k, (v, _) in b["values"].items():
+            assert r[k] == pytest.approx(v, rel=2e-5, abs=2e-6), k
+
+
+def _check_vs_ed(dim, L, T, jxy, jz, h, therm, sweeps, seed, keys):
+    beta = 1.0 / T
+    o = orc.Oracle(dim, L, beta, jxy, jz, h, seed=seed)
+    o.sweep(therm)
+    o.clear_records()
+    o.sweep(sweeps)
+    obs = orc.observables(o.records(), dim, L, beta, jxy, jz, h)
+    ref = orc.ed.thermal(dim, L, T, jxy=jxy, jz=jz, h=h)
+    N = L ** dim
+    for k in keys:
+        if k == "Specific Heat":
+            m, e = orc.specific_heat(obs, beta, N)
+        else:
+            m, e = orc.binned(obs[k])
+        assert abs(m - ref[k]) <= 3.5 * e + 1e-12, (k, m, e, ref[k])
+
+
+def test_philox_heisenberg_chain_vs_ed():
+    _check_vs_ed(1, 4, 0.25, 1.0, 1.0, 0.0, 1000, 40000, 7,
+                 ["Energy", "Specific Heat", "Susceptibility", "Staggered Magnetization^2",
+                  "Staggered Susceptibility"])
+
+
+def test_philox_ising_chain_vs_ed():
+    _check_vs_ed(1, 4, 0.5, 0.0, 1.0, 0.0, 1000, 40000, 8,
+                 ["Energy", "Specific Heat", "Susceptibility", "Staggered Magnetization^2"])
+
+
+def test_philox_xxz_field_chain_vs_ed():
+    _check_vs_ed(1, 6, 0.5, 1.0, 0.5, 0.3, 1000, 40000, 9,
+                 ["Energy", "Specific Heat", "Magnetization", "Susceptibility",
+                  "Staggered Susceptibility"])
+
+
+def test_philox_square_vs_ed():
+    _check_vs_ed(2, 2, 0.5, 1.0, 1.0, 0.0, 1000, 20000, 10,
+                 ["Energy", "Susceptibility", "Staggered Magnetization^2"])
