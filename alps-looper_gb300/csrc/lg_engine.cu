@@ -1,0 +1,887 @@
+// Host side of the GB300 loop-cluster engine: the C ABI of include/looper_gpu.h.
+//
+// An Engine owns one ragged arena of independent chains (a single chain is an arena of one):
+// static lattice tables, persistent per-site state, per-sweep vertex / segment buffers sized
+// from the expected operator count, and a CUDA graph holding one sweep of every chain.  Sweeps
+// run in chunks; after each chunk the exact per-sweep records come back to the host, which turns
+// them into the reference's observables with a rebinning accumulator.
+//
+// A sweep that would overflow the vertex capacity is detected on the device right after the
+// bond scan, before any persistent state is touched; the engine then grows the buffers and
+// replays that sweep with the same random numbers, so capacity never changes a trajectory.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/looper_gpu.h"
+#include "lg_kernels.cuh"
+#include "lg_host.h"
+
+using namespace lg;
+
+// kernel launches in one sweep (enqueue_sweep)
+static const int kSweepLaunches = 19;
+// timed stages of one sweep, in launch order (an event is recorded after each stage)
+static const int kNumStages = 11;
+static const char* kStageNames[kNumStages] = {
+    "k_begin+k_insert<count>", "scan(bonds)", "k_insert<write>", "k_site_count+scan(sites)",
+    "k_merge", "k_union", "k_compress", "k_accumulate", "k_cluster", "k_flip_vertex",
+    "k_site_end+k_end"};
+
+static std::atomic<uint64_t> g_launches{0};
+static thread_local std::string g_err;
+
+int lg_fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define LG_CUDA(call)                                                                        \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return lg_fail(LG_EDEVICE, "%s failed: %s", #call, cudaGetErrorString(e_));            \
+  } while (0)
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~DBuf() { if (p) cudaFree(p); }
+  int alloc(size_t count) {
+    if (p) { cudaFree(p); p = nullptr; }
+    n = count;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) { p = nullptr; n = 0; return lg_fail(LG_ENOMEM, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e)); }
+    return LG_OK;
+  }
+};
+
+// ----------------------------------------------------------------------------------------------
+struct Engine {
+  std::vector<ChainSpec> spec;
+  std::vector<ChainAcc> acc;
+  int C = 0, N = 0, NB = 0;
+  std::vector<DChain> hch;
+  std::vector<int> h_bond_s0, h_bond_s1, h_inc_off, h_inc;
+  std::vector<uint8_t> h_inc_side, h_bond_dir0;
+  std::vector<int> h_site_chain, h_bond_chain;
+
+  DBuf<DChain> d_ch;
+  DBuf<int> d_bond_s0, d_bond_s1, d_bond_chain, d_inc_off, d_inc, d_site_chain;
+  DBuf<uint8_t> d_bond_dir0, d_inc_side;
+  DBuf<int8_t> d_gauge;
+  DBuf<uint32_t> d_sweep;
+  DBuf<int> d_ch_slot_off;
+  DBuf<uint8_t> d_spin0;
+  DBuf<int> d_off_base, d_off_cnt;
+  DBuf<int> d_bond_cnt, d_bond_ptr, d_site_cnt, d_sbase, d_partial;
+  DBuf<uint64_t> d_vtime;
+  DBuf<uint8_t> d_vcode, d_vnew;
+  DBuf<int> d_vslot;
+  DBuf<uint64_t> d_stime;
+  DBuf<uint8_t> d_sinfo, d_sdir, d_flip;
+  DBuf<int> d_svert, d_parent;
+  DBuf<unsigned long long> d_cls;
+  DBuf<unsigned int> d_cnt0;
+  DBuf<unsigned long long> d_rec;
+  DBuf<Ctl> d_ctl;
+
+  int nv_cap = 0, ns_cap = 0;
+  int rec_rows = 64;
+  cudaStream_t st = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool use_graph = true;
+  int nsm = 148;
+  bool keep_records = false;
+  std::vector<uint64_t> kept;   // raw records of chain 0 (test seam)
+  std::vector<uint64_t> hrec;
+
+  ~Engine() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  Arena arena() {
+    Arena A;
+    A.ch = d_ch.p; A.C = C; A.N = N; A.NB = NB;
+    A.bond_s0 = d_bond_s0.p; A.bond_s1 = d_bond_s1.p; A.bond_chain = d_bond_chain.p;
+    A.bond_dir0 = d_bond_dir0.p; A.inc_off = d_inc_off.p; A.inc = d_inc.p;
+    A.inc_side = d_inc_side.p; A.gauge = d_gauge.p; A.site_chain = d_site_chain.p;
+    A.ch_sweep = d_sweep.p; A.ch_slot_off = d_ch_slot_off.p;
+    A.spin0 = d_spin0.p; A.off_base = d_off_base.p; A.off_cnt = d_off_cnt.p;
+    A.bond_cnt = d_bond_cnt.p; A.bond_ptr = d_bond_ptr.p; A.site_cnt = d_site_cnt.p;
+    A.sbase = d_sbase.p;
+    A.vtime = d_vtime.p; A.vcode = d_vcode.p; A.vnew = d_vnew.p; A.vslot = d_vslot.p;
+    A.stime = d_stime.p; A.sinfo = d_sinfo.p; A.svert = d_svert.p; A.sdir = d_sdir.p;
+    A.parent = d_parent.p; A.flip = d_flip.p; A.cls = d_cls.p; A.cnt0 = d_cnt0.p;
+    A.rec = d_rec.p; A.ctl = d_ctl.p;
+    return A;
+  }
+
+  // ---- construction ----
+  int build(const std::vector<ChainSpec>& specs) {
+    spec = specs;
+    C = (int)spec.size();
+    acc.assign(C, ChainAcc());
+    int dev = 0;
+    LG_CUDA(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    LG_CUDA(cudaGetDeviceProperties(&prop, dev));
+    nsm = prop.multiProcessorCount;
+    LG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    // static tables
+    long long nsite = 0, nbond = 0;
+    for (auto& s : spec) { nsite += s.N; nbond += s.NB; }
+    if (nsite + 2 * 64ll > (1ll << 30) || nbond > (1ll << 30))
+      return lg_fail(LG_EBUDGET, "arena too large (%lld sites, %lld bonds)", nsite, nbond);
+    N = (int)nsite; NB = (int)nbond;
+    hch.resize(C);
+    h_bond_s0.resize(NB); h_bond_s1.resize(NB); h_bond_chain.resize(NB); h_bond_dir0.resize(NB);
+    h_site_chain.resize(N);
+    std::vector<int8_t> h_gauge(N);
+    h_inc_off.assign(N + 1, 0);
+    int so = 0, bo = 0;
+    for (int c = 0; c < C; ++c) {
+      const ChainSpec& s = spec[c];
+      hch[c] = s.dchain;
+      hch[c].site_off = so; hch[c].nsites = s.N;
+      hch[c].bond_off = bo; hch[c].nbonds = s.NB;
+      for (int i = 0; i < s.N; ++i) { h_site_chain[so + i] = c; h_gauge[so + i] = (int8_t)s.gauge[i]; }
+      for (int b = 0; b < s.NB; ++b) {
+        h_bond_s0[bo + b] = so + s.s0[b];
+        h_bond_s1[bo + b] = so + s.s1[b];
+        h_bond_chain[bo + b] = c;
+      }
+      so += s.N; bo += s.NB;
+    }
+    // incident bonds per site, ascending bond id
+    std::vector<int> deg(N, 0);
+    for (int b = 0; b < NB; ++b) { deg[h_bond_s0[b]]++; deg[h_bond_s1[b]]++; }
+    for (int s = 0; s < N; ++s) {
+      if (deg[s] > MAXZ) return lg_fail(LG_EUNSUPPORTED, "site coordination %d > %d", deg[s], MAXZ);
+      h_inc_off[s + 1] = h_inc_off[s] + deg[s];
+    }
+    h_inc.assign(h_inc_off[N], 0);
+    h_inc_side.assign(h_inc_off[N], 0);
+    std::vector<int> fill(N, 0);
+    for (int b = 0; b < NB; ++b) {
+      int a = h_bond_s0[b], t = h_bond_s1[b];
+      int ia = h_inc_off[a] + fill[a]++;
+      h_inc[ia] = b; h_inc_side[ia] = 0;
+      int it = h_inc_off[t] + fill[t]++;
+      h_inc[it] = b; h_inc_side[it] = 1;
+    }
+    // bonds were visited in ascending order, so each site's list is ascending already
+    for (int b = 0; b < NB; ++b) {
+      int a = h_bond_s0[b];
+      for (int j = h_inc_off[a]; j < h_inc_off[a + 1]; ++j)
+        if (h_inc[j] == b && h_inc_side[j] == 0) { h_bond_dir0[b] = (uint8_t)(j - h_inc_off[a]); break; }
+    }
+    int rc;
+    if ((rc = d_ch.alloc(C)) || (rc = d_bond_s0.alloc(NB)) || (rc = d_bond_s1.alloc(NB)) ||
+        (rc = d_bond_chain.alloc(NB)) || (rc = d_bond_dir0.alloc(NB)) ||
+        (rc = d_inc_off.alloc(N + 1)) || (rc = d_inc.alloc(h_inc.size())) ||
+        (rc = d_inc_side.alloc(h_inc.size())) || (rc = d_gauge.alloc(N)) ||
+        (rc = d_site_chain.alloc(N)) || (rc = d_sweep.alloc(C)) ||
+        (rc = d_ch_slot_off.alloc(C + 1)) || (rc = d_spin0.alloc(N)) ||
+        (rc = d_off_base.alloc(N)) || (rc = d_off_cnt.alloc(N)) || (rc = d_bond_cnt.alloc(NB)) ||
+        (rc = d_bond_ptr.alloc(NB + 1)) || (rc = d_site_cnt.alloc(N)) ||
+        (rc = d_sbase.alloc(N + 1)) || (rc = d_ctl.alloc(1)))
+      return rc;
+    int maxparts = std::max((NB + SCAN_TILE - 1) / SCAN_TILE, (N + SCAN_TILE - 1) / SCAN_TILE);
+    if ((rc = d_partial.alloc(maxparts + 1))) return rc;
+    LG_CUDA(cudaMemcpy(d_ch.p, hch.data(), C * sizeof(DChain), cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_bond_s0.p, h_bond_s0.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_bond_s1.p, h_bond_s1.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_bond_chain.p, h_bond_chain.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_bond_dir0.p, h_bond_dir0.data(), NB, cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_inc_off.p, h_inc_off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_inc.p, h_inc.data(), h_inc.size() * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_inc_side.p, h_inc_side.data(), h_inc_side.size(), cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_gauge.p, h_gauge.data(), N, cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_site_chain.p, h_site_chain.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    std::vector<uint32_t> sw(C);
+    for (int c = 0; c < C; ++c) sw[c] = (uint32_t)spec[c].mcs;
+    LG_CUDA(cudaMemcpy(d_sweep.p, sw.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    // per-sweep buffers from the expected operator count
+    double est = 0;
+    for (auto& s : spec) est += s.expected_vertices();
+    long long cap = (long long)(1.3 * est) + 4096;
+    LG_CUDA(cudaMemset(d_ctl.p, 0, sizeof(Ctl)));
+    if ((rc = alloc_dynamic(cap, false))) return rc;
+    // initial spins (one launch per distinct init mode)
+    Arena A = arena();
+    int random = spec.empty() ? 0 : spec[0].init_spins;
+    k_init_spins<<<std::max(1, std::min((N + 255) / 256, nsm * 8)), 256, 0, st>>>(A, random);
+    ++g_launches;
+    LG_CUDA(cudaGetLastError());
+    for (int c = 0; c < C; ++c)
+      if (spec[c].init_spins != random) {
+        std::vector<uint8_t> sp(spec[c].N);
+        for (int i = 0; i < spec[c].N; ++i)
+          sp[i] = spec[c].init_spins ? (uint8_t)(philox(spec[c].dchain.seed, 0xFFFFFFFFu, (uint32_t)i, TAG_SPIN, 0).x & 1u) : 0;
+        LG_CUDA(cudaMemcpyAsync(d_spin0.p + hch[c].site_off, sp.data(), sp.size(), cudaMemcpyHostToDevice, st));
+      }
+    LG_CUDA(cudaStreamSynchronize(st));
+    return LG_OK;
+  }
+
+  // (Re)allocate the per-sweep buffers for cap vertices; with keep, preserve the persistent
+  // off-diagonal lists that live at the front of each site's segment range.
+  int alloc_dynamic(long long cap, bool keep) {
+    if (cap > (1ll << 30) - N) return lg_fail(LG_EBUDGET, "vertex capacity %lld too large", cap);
+    int new_nv = (int)cap;
+    int new_ns = 2 * new_nv + N;
+    DBuf<uint64_t> old_t;
+    DBuf<uint8_t> old_d;
+    size_t keep_n = 0;
+    if (keep) {
+      std::swap(old_t.p, d_stime.p); std::swap(old_t.n, d_stime.n);
+      std::swap(old_d.p, d_sdir.p); std::swap(old_d.n, d_sdir.n);
+      keep_n = (size_t)ns_cap;
+    }
+    int rc;
+    if ((rc = d_vtime.alloc(new_nv)) || (rc = d_vcode.alloc(new_nv)) || (rc = d_vnew.alloc(new_nv)) ||
+        (rc = d_vslot.alloc(2 * (size_t)new_nv)) || (rc = d_stime.alloc(new_ns)) ||
+        (rc = d_sinfo.alloc(new_ns)) || (rc = d_svert.alloc(new_ns)) || (rc = d_sdir.alloc(new_ns)) ||
+        (rc = d_parent.alloc(new_ns)) || (rc = d_flip.alloc(new_ns)) ||
+        (rc = d_cls.alloc(4 * (size_t)new_ns)) || (rc = d_cnt0.alloc(4 * (size_t)new_ns)) ||
+        (rc = d_rec.alloc((size_t)rec_rows * C * REC_WORDS)))
+      return rc;
+    if (keep) {
+      LG_CUDA(cudaMemcpy(d_stime.p, old_t.p, keep_n * sizeof(uint64_t), cudaMemcpyDeviceToDevice));
+      LG_CUDA(cudaMemcpy(d_sdir.p, old_d.p, keep_n, cudaMemcpyDeviceToDevice));
+    }
+    nv_cap = new_nv;
+    ns_cap = new_ns;
+    Ctl hc;
+    LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    hc.nv_cap = nv_cap; hc.ns_cap = ns_cap;
+    LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
+    drop_graph();
+    return LG_OK;
+  }
+
+  void drop_graph() {
+    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+  }
+
+  int grid_for(long long n, int threads, int per_sm = 8) {
+    long long g = (n + threads - 1) / threads;
+    long long m = (long long)nsm * per_sm;
+    if (g > m) g = m;
+    if (g < 1) g = 1;
+    return (int)g;
+  }
+
+  void scan(const int* in, int* out, int n, int* total, int cap, int per_item, int extra,
+            cudaEvent_t* ev = nullptr) {
+    int parts = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (parts < 1) parts = 1;
+    k_scan_reduce<<<parts, SCAN_THREADS, 0, st>>>(in, n, d_partial.p, d_ctl.p);
+    k_scan_partials<<<1, 1024, 0, st>>>(d_partial.p, parts, total, cap, per_item, extra, d_ctl.p);
+    k_scan_apply<<<parts, SCAN_THREADS, 0, st>>>(in, out, n, d_partial.p, d_ctl.p);
+    if (ev) cudaEventRecord(*ev, st);
+    g_launches += 3;
+  }
+
+  // The sweep of every chain, as a fixed sequence of launches (capturable).  With ev != nullptr
+  // an event is recorded after each stage (kNumStages events) for per-kernel timing.
+  void enqueue_sweep(cudaEvent_t* ev = nullptr) {
+    Arena A = arena();
+    Ctl* ctl = d_ctl.p;
+    auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
+    k_begin<<<grid_for((long long)C * REC_WORDS, 256), 256, 0, st>>>(A);
+    k_insert<false><<<grid_for(NB, 256, 16), 256, 0, st>>>(A);
+    mark(0);
+    scan(d_bond_cnt.p, d_bond_ptr.p, NB, &ctl->nv_total, nv_cap, 1, 0, ev ? ev + 1 : nullptr);
+    k_insert<true><<<grid_for(NB, 256, 16), 256, 0, st>>>(A);
+    mark(2);
+    k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
+    scan(d_site_cnt.p, d_sbase.p, N, &ctl->ns_total, ns_cap, 1, 0, ev ? ev + 3 : nullptr);
+    k_merge<<<grid_for(N, 128, 16), 128, 0, st>>>(A);
+    mark(4);
+    k_union<<<grid_for(nv_cap, 256), 256, 0, st>>>(A);
+    mark(5);
+    k_compress<<<grid_for(ns_cap, 256), 256, 0, st>>>(A);
+    mark(6);
+    k_accumulate<<<grid_for(ns_cap, 256), 256, 0, st>>>(A);
+    mark(7);
+    k_cluster<<<grid_for(ns_cap, 256), 256, 0, st>>>(A);
+    mark(8);
+    k_flip_vertex<<<grid_for(nv_cap, 256), 256, 0, st>>>(A);
+    mark(9);
+    k_site_end<<<grid_for(N, 128, 16), 128, 0, st>>>(A);
+    k_end<<<grid_for(C, 128), 128, 0, st>>>(A);
+    k_step<<<1, 1, 0, st>>>(ctl);
+    mark(10);
+    g_launches += 13;
+  }
+
+  int ensure_graph() {
+    if (!use_graph || gexec) return LG_OK;
+    LG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    uint64_t before = g_launches.load();
+    enqueue_sweep();
+    g_launches = before;  // counted when the graph is launched
+    LG_CUDA(cudaStreamEndCapture(st, &graph));
+    LG_CUDA(cudaGraphInstantiate(&gexec, graph, 0));
+    return LG_OK;
+  }
+
+  // Run n sweeps of every chain.  With ms != nullptr every sweep is bracketed by events and
+  // preceded by an L2 flush of flush_bytes (outside the brackets).
+  int run(long long n, float* ms = nullptr, size_t flush_bytes = 0) {
+    DBuf<uint8_t> flushbuf;
+    std::vector<cudaEvent_t> ev;
+    if (ms) {
+      if (flush_bytes) { int rc = flushbuf.alloc(flush_bytes); if (rc) return rc; }
+      ev.resize(2 * rec_rows);
+      for (auto& e : ev) LG_CUDA(cudaEventCreate(&e));
+    }
+    struct EvGuard { std::vector<cudaEvent_t>& v; ~EvGuard() { for (auto e : v) cudaEventDestroy(e); } } guard{ev};
+    long long done_total = 0;
+    while (n > 0) {
+      int m = (int)std::min<long long>(n, rec_rows);
+      int rc = ensure_graph();
+      if (rc) return rc;
+      for (int i = 0; i < m; ++i) {
+        if (ms) {
+          if (flush_bytes) LG_CUDA(cudaMemsetAsync(flushbuf.p, i & 0xFF, flush_bytes, st));
+          LG_CUDA(cudaEventRecord(ev[2 * i], st));
+        }
+        if (gexec) {
+          LG_CUDA(cudaGraphLaunch(gexec, st));
+          g_launches += kSweepLaunches;
+        } else {
+          enqueue_sweep();
+        }
+        if (ms) LG_CUDA(cudaEventRecord(ev[2 * i + 1], st));
+      }
+      LG_CUDA(cudaGetLastError());
+      Ctl hc;
+      LG_CUDA(cudaMemcpyAsync(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+      LG_CUDA(cudaStreamSynchronize(st));
+      int done = (int)hc.step;
+      if (done > 0) {
+        hrec.resize((size_t)done * C * REC_WORDS);
+        LG_CUDA(cudaMemcpy(hrec.data(), d_rec.p, hrec.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        consume(done);
+        if (ms)
+          for (int i = 0; i < done; ++i)
+            LG_CUDA(cudaEventElapsedTime(&ms[done_total + i], ev[2 * i], ev[2 * i + 1]));
+      }
+      done_total += done;
+      Ctl z = hc;
+      z.step = 0;
+      z.err = 0;
+      if (hc.err == ERR_ITERCAP)
+        return lg_fail(LG_EITERCAP, "union-find iteration cap hit");
+      if (hc.err == ERR_OVERFLOW) {
+        long long need = std::max<long long>((long long)hc.nv_total, nv_cap);
+        LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
+        rc = alloc_dynamic((long long)(need * 1.25) + 4096, true);
+        if (rc) return rc;
+      } else {
+        LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
+      }
+      n -= done;
+    }
+    return LG_OK;
+  }
+
+  // n sweeps launched kernel by kernel with events between stages (no graph).
+  int profile(long long n, size_t flush_bytes, double* kernel_ms, long long* vertices) {
+    DBuf<uint8_t> flushbuf;
+    if (flush_bytes) { int rc = flushbuf.alloc(flush_bytes); if (rc) return rc; }
+    cudaEvent_t ev[kNumStages + 1];
+    for (auto& e : ev) LG_CUDA(cudaEventCreate(&e));
+    struct G { cudaEvent_t* e; ~G() { for (int i = 0; i <= kNumStages; ++i) cudaEventDestroy(e[i]); } } g{ev};
+    for (int k = 0; k < kNumStages; ++k) kernel_ms[k] = 0;
+    long long verts = 0;
+    while (n > 0) {
+      if (flush_bytes) LG_CUDA(cudaMemsetAsync(flushbuf.p, (int)(n & 0xFF), flush_bytes, st));
+      LG_CUDA(cudaEventRecord(ev[kNumStages], st));
+      enqueue_sweep(ev);
+      LG_CUDA(cudaGetLastError());
+      Ctl hc;
+      LG_CUDA(cudaMemcpyAsync(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+      LG_CUDA(cudaStreamSynchronize(st));
+      if (hc.err) {
+        long long left = n;
+        int rc = run(1);  // resolves an overflow (grows, replays) like lg_run
+        if (rc) return rc;
+        n = left - 1;
+        continue;
+      }
+      float t;
+      LG_CUDA(cudaEventElapsedTime(&t, ev[kNumStages], ev[0]));
+      kernel_ms[0] += t;
+      for (int k = 1; k < kNumStages; ++k) {
+        LG_CUDA(cudaEventElapsedTime(&t, ev[k - 1], ev[k]));
+        kernel_ms[k] += t;
+      }
+      verts += hc.nv_total;
+      hrec.resize((size_t)C * REC_WORDS);
+      LG_CUDA(cudaMemcpy(hrec.data(), d_rec.p, hrec.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+      consume(1);
+      Ctl z = hc;
+      z.step = 0;
+      LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
+      --n;
+    }
+    *vertices = verts;
+    return LG_OK;
+  }
+
+  void consume(int rows) {
+    for (int r = 0; r < rows; ++r) {
+      for (int c = 0; c < C; ++c) {
+        const uint64_t* rec = hrec.data() + ((size_t)r * C + c) * REC_WORDS;
+        ChainSpec& s = spec[c];
+        if (keep_records && c == 0) kept.insert(kept.end(), rec, rec + REC_WORDS);
+        s.last_nop = rec[R_NOP];
+        if (s.mcs >= (uint64_t)s.therm && s.mcs < (uint64_t)(s.therm + s.sweeps))
+          acc[c].push(s, rec);
+        ++s.mcs;
+      }
+    }
+  }
+
+  // ---- state access (test seams, checkpoints) ----
+  int get_state(int c, std::vector<int32_t>& spins, std::vector<int32_t>& bonds,
+                std::vector<double>& times) {
+    const ChainSpec& s = spec[c];
+    int so = hch[c].site_off;
+    std::vector<uint8_t> sp(s.N);
+    std::vector<int> ob(s.N), oc(s.N);
+    LG_CUDA(cudaMemcpy(sp.data(), d_spin0.p + so, s.N, cudaMemcpyDeviceToHost));
+    LG_CUDA(cudaMemcpy(ob.data(), d_off_base.p + so, s.N * sizeof(int), cudaMemcpyDeviceToHost));
+    LG_CUDA(cudaMemcpy(oc.data(), d_off_cnt.p + so, s.N * sizeof(int), cudaMemcpyDeviceToHost));
+    spins.assign(sp.begin(), sp.end());
+    std::vector<std::pair<uint64_t, int>> ops;
+    for (int i = 0; i < s.N; ++i) {
+      if (!oc[i]) continue;
+      std::vector<uint64_t> t(oc[i]);
+      std::vector<uint8_t> d(oc[i]);
+      LG_CUDA(cudaMemcpy(t.data(), d_stime.p + ob[i], oc[i] * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+      LG_CUDA(cudaMemcpy(d.data(), d_sdir.p + ob[i], oc[i], cudaMemcpyDeviceToHost));
+      int gs = so + i;
+      for (int j = 0; j < oc[i]; ++j) {
+        int idx = h_inc_off[gs] + d[j];
+        if (h_inc_side[idx] != 0) continue;  // take each operator once, from its source site
+        ops.push_back({t[j], h_inc[idx] - hch[c].bond_off});
+      }
+    }
+    std::sort(ops.begin(), ops.end());
+    bonds.resize(ops.size()); times.resize(ops.size());
+    for (size_t i = 0; i < ops.size(); ++i) {
+      bonds[i] = ops[i].second;
+      double t; std::memcpy(&t, &ops[i].first, 8); times[i] = t;
+    }
+    return LG_OK;
+  }
+
+  // Off-diagonal lists of every site as (time bits, incident-bond index) pairs.
+  typedef std::vector<std::vector<std::pair<uint64_t, uint8_t>>> SiteLists;
+
+  int download_lists(SiteLists& L) {
+    std::vector<int> ob(N), oc(N);
+    LG_CUDA(cudaMemcpy(ob.data(), d_off_base.p, N * sizeof(int), cudaMemcpyDeviceToHost));
+    LG_CUDA(cudaMemcpy(oc.data(), d_off_cnt.p, N * sizeof(int), cudaMemcpyDeviceToHost));
+    L.assign(N, {});
+    for (int i = 0; i < N; ++i) {
+      if (!oc[i]) continue;
+      std::vector<uint64_t> t(oc[i]);
+      std::vector<uint8_t> d(oc[i]);
+      LG_CUDA(cudaMemcpy(t.data(), d_stime.p + ob[i], oc[i] * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+      LG_CUDA(cudaMemcpy(d.data(), d_sdir.p + ob[i], oc[i], cudaMemcpyDeviceToHost));
+      L[i].resize(oc[i]);
+      for (int j = 0; j < oc[i]; ++j) L[i][j] = {t[j], d[j]};
+    }
+    return LG_OK;
+  }
+
+  // Lay the lists out contiguously from segment 0 and upload them.
+  int upload_lists(const SiteLists& L) {
+    std::vector<int> ob(N), oc(N);
+    long long total = 0;
+    for (int i = 0; i < N; ++i) { ob[i] = (int)total; oc[i] = (int)L[i].size(); total += oc[i]; }
+    if (total > ns_cap) {
+      int rc = alloc_dynamic(total + 4096, false);
+      if (rc) return rc;
+    }
+    std::vector<uint64_t> t(total);
+    std::vector<uint8_t> d(total);
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < oc[i]; ++j) { t[ob[i] + j] = L[i][j].first; d[ob[i] + j] = L[i][j].second; }
+    LG_CUDA(cudaMemcpy(d_off_base.p, ob.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_off_cnt.p, oc.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    if (total) {
+      LG_CUDA(cudaMemcpy(d_stime.p, t.data(), total * sizeof(uint64_t), cudaMemcpyHostToDevice));
+      LG_CUDA(cudaMemcpy(d_sdir.p, d.data(), total, cudaMemcpyHostToDevice));
+    }
+    return LG_OK;
+  }
+
+  int set_state(int c, const int32_t* spins, const int32_t* bonds, const double* times, long long n,
+                uint64_t sweep) {
+    const ChainSpec& s = spec[c];
+    const int so = hch[c].site_off;
+    SiteLists L;
+    int rc = download_lists(L);
+    if (rc) return rc;
+    for (int i = 0; i < s.N; ++i) L[so + i].clear();
+    std::vector<std::vector<std::pair<uint64_t, int>>> tmp(s.N);  // (time bits, global bond)
+    for (long long i = 0; i < n; ++i) {
+      const int b = bonds[i];
+      if (b < 0 || b >= s.NB || !(times[i] >= 0.0 && times[i] < 1.0))
+        return lg_fail(LG_EINVAL, "operator %lld out of range", i);
+      uint64_t tb;
+      std::memcpy(&tb, &times[i], 8);
+      tmp[s.s0[b]].push_back({tb, b + hch[c].bond_off});
+      tmp[s.s1[b]].push_back({tb, b + hch[c].bond_off});
+    }
+    for (int i = 0; i < s.N; ++i) {
+      auto& T = tmp[i];
+      std::stable_sort(T.begin(), T.end());  // (time, bond): the order the sweep produces
+      const int gs = so + i;
+      for (auto& e : T) {
+        int dir = -1;
+        for (int j = h_inc_off[gs]; j < h_inc_off[gs + 1]; ++j)
+          if (h_inc[j] == e.second) { dir = j - h_inc_off[gs]; break; }
+        L[gs].push_back({e.first, (uint8_t)dir});
+      }
+    }
+    if ((rc = upload_lists(L))) return rc;
+    std::vector<uint8_t> sp(s.N);
+    for (int i = 0; i < s.N; ++i) sp[i] = (uint8_t)(spins[i] & 1);
+    LG_CUDA(cudaMemcpy(d_spin0.p + so, sp.data(), s.N, cudaMemcpyHostToDevice));
+    uint32_t sw = (uint32_t)sweep;
+    LG_CUDA(cudaMemcpy(d_sweep.p + c, &sw, sizeof(uint32_t), cudaMemcpyHostToDevice));
+    spec[c].mcs = sweep;
+    return LG_OK;
+  }
+
+  // Cluster labels of an explicit configuration (single-chain engine): fills the bond vertex
+  // lists from the given time order and runs the segment merge + union-find kernels.
+  int uf_label(long long nops, const int32_t* bonds, const int32_t* graphs, std::vector<int32_t>& labels,
+               long long* nc) {
+    const ChainSpec& s = spec[0];
+    std::vector<int> cnt(NB, 0);
+    for (long long i = 0; i < nops; ++i) {
+      if (bonds[i] < 0 || bonds[i] >= NB || graphs[i] < 0 || graphs[i] > 3)
+        return lg_fail(LG_EINVAL, "vertex %lld out of range", i);
+      cnt[bonds[i]]++;
+    }
+    std::vector<int> ptr(NB + 1, 0);
+    for (int b = 0; b < NB; ++b) ptr[b + 1] = ptr[b] + cnt[b];
+    if (nops > nv_cap) { int rc = alloc_dynamic(nops + 1024, false); if (rc) return rc; }
+    std::vector<uint64_t> vt(nops);
+    std::vector<uint8_t> vc(nops);
+    std::vector<int> fillp(ptr.begin(), ptr.end() - 1);
+    std::vector<int> vidx(nops);
+    for (long long i = 0; i < nops; ++i) {
+      int b = bonds[i];
+      int v = fillp[b]++;
+      vt[v] = (uint64_t)(i + 1);  // strictly increasing keys reproduce the given order
+      vc[v] = (uint8_t)(graphs[i] << 1);
+      vidx[i] = v;
+    }
+    LG_CUDA(cudaMemcpy(d_bond_cnt.p, cnt.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_bond_ptr.p, ptr.data(), (NB + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    if (nops) {
+      LG_CUDA(cudaMemcpy(d_vtime.p, vt.data(), nops * sizeof(uint64_t), cudaMemcpyHostToDevice));
+      LG_CUDA(cudaMemcpy(d_vcode.p, vc.data(), nops, cudaMemcpyHostToDevice));
+    }
+    Ctl hc{};
+    hc.nv_total = (int)nops; hc.nv_cap = nv_cap; hc.ns_cap = ns_cap;
+    LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
+    Arena A = arena();
+    k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
+    scan(d_site_cnt.p, d_sbase.p, N, &d_ctl.p->ns_total, ns_cap, 1, 0);
+    k_merge<<<grid_for(N, 128, 16), 128, 0, st>>>(A);
+    k_union<<<grid_for(nops, 256), 256, 0, st>>>(A);
+    k_compress<<<grid_for(2 * nops + N, 256), 256, 0, st>>>(A);
+    g_launches += 4;
+    LG_CUDA(cudaGetLastError());
+    LG_CUDA(cudaStreamSynchronize(st));
+    LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    if (hc.err) return lg_fail(LG_EITERCAP, "union-find failed (%d)", hc.err);
+    long long ns = 2 * nops + N;
+    std::vector<int> par(ns), sb(N + 1), vs(2 * std::max<long long>(nops, 1));
+    LG_CUDA(cudaMemcpy(par.data(), d_parent.p, ns * sizeof(int), cudaMemcpyDeviceToHost));
+    LG_CUDA(cudaMemcpy(sb.data(), d_sbase.p, (N + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    if (nops) LG_CUDA(cudaMemcpy(vs.data(), d_vslot.p, 2 * nops * sizeof(int), cudaMemcpyDeviceToHost));
+    // fragments: site bottoms, then graph-0 vertices in the given order
+    std::vector<int> froot;
+    froot.reserve(N + nops);
+    for (int i = 0; i < N; ++i) froot.push_back(par[sb[i]]);
+    for (long long i = 0; i < nops; ++i)
+      if (graphs[i] == 0) froot.push_back(par[vs[2 * (size_t)vidx[i]]]);
+    std::vector<int> minfrag(ns, -1);
+    for (size_t f = 0; f < froot.size(); ++f)
+      if (minfrag[froot[f]] < 0) minfrag[froot[f]] = (int)f;  // fragments visited in index order
+    std::vector<int> id(froot.size(), -1);
+    long long n_c = 0;
+    for (size_t f = 0; f < froot.size(); ++f)
+      if (minfrag[froot[f]] == (int)f) id[f] = (int)n_c++;
+    labels.resize(froot.size());
+    for (size_t f = 0; f < froot.size(); ++f) labels[f] = id[minfrag[froot[f]]];
+    *nc = n_c;
+    (void)s;
+    return LG_OK;
+  }
+
+  int set_beta(int c, double beta) {
+    int rc = spec[c].set_beta(beta);
+    if (rc) return rc;
+    hch[c].inv_rate = spec[c].dchain.inv_rate;
+    hch[c].flip_coef = spec[c].dchain.flip_coef;
+    LG_CUDA(cudaMemcpy(d_ch.p + c, &hch[c], sizeof(DChain), cudaMemcpyHostToDevice));
+    acc[c] = ChainAcc();
+    return LG_OK;
+  }
+};
+
+// ================================================================================================
+// C ABI
+// ================================================================================================
+struct lg_chain {
+  std::shared_ptr<Engine> eng;
+  int index = 0;
+};
+struct lg_batch {
+  std::shared_ptr<Engine> eng;
+  std::vector<lg_chain> views;
+};
+
+extern "C" {
+
+int lg_last_error(char* buf, size_t n) {
+  if (buf && n) { std::snprintf(buf, n, "%s", g_err.c_str()); }
+  return (int)g_err.size();
+}
+
+uint64_t lg_kernel_launches(void) { return g_launches.load(); }
+
+const char* lg_version(void) {
+  static std::string v;
+  if (v.empty()) {
+    int rt = 0; cudaRuntimeGetVersion(&rt);
+    v = "looper_gb300 1.0 (sm_103a; CUDA runtime " + std::to_string(rt) + ")";
+  }
+  return v.c_str();
+}
+
+int lg_create(const lg_params* p, lg_chain** out) {
+  if (!p || !out) return lg_fail(LG_EINVAL, "null argument");
+  ChainSpec s;
+  int rc = s.init(*p);
+  if (rc) return rc;
+  auto e = std::make_shared<Engine>();
+  rc = e->build({s});
+  if (rc) return rc;
+  lg_chain* c = new lg_chain();
+  c->eng = e;
+  *out = c;
+  return LG_OK;
+}
+
+int lg_destroy(lg_chain* c) { delete c; return LG_OK; }
+
+int lg_run(lg_chain* c, int64_t n) {
+  if (!c || n < 0) return lg_fail(LG_EINVAL, "bad argument");
+  if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_run on a batch member; use lg_batch_run");
+  return c->eng->run(n);
+}
+
+int lg_is_thermalized(const lg_chain* c) {
+  const ChainSpec& s = c->eng->spec[c->index];
+  return s.mcs >= (uint64_t)s.therm ? 1 : 0;
+}
+
+double lg_progress(const lg_chain* c) {
+  const ChainSpec& s = c->eng->spec[c->index];
+  double tot = (double)(s.therm + s.sweeps);
+  return tot > 0 ? std::min(1.0, (double)s.mcs / tot) : 1.0;
+}
+
+int lg_observables(lg_chain* c, lg_obs* out) {
+  if (!c || !out) return lg_fail(LG_EINVAL, "null argument");
+  c->eng->acc[c->index].report(c->eng->spec[c->index], out);
+  return LG_OK;
+}
+
+int lg_set_beta(lg_chain* c, double beta) { return c->eng->set_beta(c->index, beta); }
+
+double lg_weight_parameter(lg_chain* c) { return (double)c->eng->spec[c->index].last_nop; }
+
+double lg_log_weight(double gw, double beta) { return std::log(beta) * gw; }
+
+int lg_get_state(lg_chain* c, int32_t* spins, int32_t* bonds, double* times, int64_t cap,
+                 int64_t* n) {
+  std::vector<int32_t> sp, bd;
+  std::vector<double> tm;
+  int rc = c->eng->get_state(c->index, sp, bd, tm);
+  if (rc) return rc;
+  if (spins) std::memcpy(spins, sp.data(), sp.size() * sizeof(int32_t));
+  int64_t m = std::min<int64_t>(cap, (int64_t)bd.size());
+  if (bonds && m > 0) std::memcpy(bonds, bd.data(), m * sizeof(int32_t));
+  if (times && m > 0) std::memcpy(times, tm.data(), m * sizeof(double));
+  if (n) *n = (int64_t)bd.size();
+  return LG_OK;
+}
+
+int lg_set_state(lg_chain* c, const int32_t* spins, const int32_t* bonds, const double* times,
+                 int64_t n, uint64_t sweep) {
+  return c->eng->set_state(c->index, spins, bonds, times, n, sweep);
+}
+
+int lg_keep_records(lg_chain* c, int on) {
+  if (c->index != 0) return lg_fail(LG_EINVAL, "records are kept for chain 0 only");
+  c->eng->keep_records = on != 0;
+  return LG_OK;
+}
+
+int lg_fetch_records(lg_chain* c, uint64_t* out, int64_t cap, int64_t* n) {
+  auto& k = c->eng->kept;
+  int64_t rows = (int64_t)(k.size() / LG_RECORD_WORDS);
+  int64_t m = std::min(rows, cap);
+  if (out && m > 0) std::memcpy(out, k.data(), m * LG_RECORD_WORDS * sizeof(uint64_t));
+  k.erase(k.begin(), k.begin() + m * LG_RECORD_WORDS);
+  if (n) *n = m;
+  return LG_OK;
+}
+
+int lg_save(lg_chain* c, void* buf, size_t* size) {
+  std::vector<int32_t> sp, bd;
+  std::vector<double> tm;
+  int rc = c->eng->get_state(c->index, sp, bd, tm);
+  if (rc) return rc;
+  std::vector<uint8_t> blob;
+  checkpoint_encode(c->eng->spec[c->index], sp, bd, tm, blob);
+  if (!buf) { *size = blob.size(); return LG_OK; }
+  if (*size < blob.size()) { *size = blob.size(); return lg_fail(LG_EINVAL, "buffer too small"); }
+  std::memcpy(buf, blob.data(), blob.size());
+  *size = blob.size();
+  return LG_OK;
+}
+
+int lg_load(lg_chain* c, const void* buf, size_t size) {
+  std::vector<int32_t> sp, bd;
+  std::vector<double> tm;
+  uint64_t mcs = 0;
+  int rc = checkpoint_decode(c->eng->spec[c->index], (const uint8_t*)buf, size, sp, bd, tm, &mcs);
+  if (rc) return rc;
+  return c->eng->set_state(c->index, sp.data(), bd.data(), tm.data(), (int64_t)bd.size(), mcs);
+}
+
+int lg_uf_label(int lattice, int L, int64_t nops, const int32_t* bonds, const int32_t* graphs,
+                int32_t* labels, int64_t cap, int64_t* nfrag, int64_t* nc) {
+  lg_params p;
+  lg_params_default(&p);
+  p.lattice = lattice; p.L = L; p.T = 1.0; p.Jxy = 0.0; p.Jz = 1.0;  // no sign check needed
+  ChainSpec s;
+  int rc = s.init(p);
+  if (rc) return rc;
+  Engine e;
+  rc = e.build({s});
+  if (rc) return rc;
+  std::vector<int32_t> lab;
+  long long n_c = 0;
+  rc = e.uf_label(nops, bonds, graphs, lab, &n_c);
+  if (rc) return rc;
+  if (nfrag) *nfrag = (int64_t)lab.size();
+  if (nc) *nc = n_c;
+  if (labels) std::memcpy(labels, lab.data(), std::min<int64_t>(cap, (int64_t)lab.size()) * sizeof(int32_t));
+  return (int64_t)lab.size() > cap ? lg_fail(LG_EINVAL, "labels buffer too small") : LG_OK;
+}
+
+int lg_batch_create(int n, const lg_params* p, lg_batch** out) {
+  if (n <= 0 || !p || !out) return lg_fail(LG_EINVAL, "bad argument");
+  std::vector<ChainSpec> specs(n);
+  for (int i = 0; i < n; ++i) {
+    int rc = specs[i].init(p[i]);
+    if (rc) return rc;
+  }
+  auto e = std::make_shared<Engine>();
+  int rc = e->build(specs);
+  if (rc) return rc;
+  lg_batch* b = new lg_batch();
+  b->eng = e;
+  b->views.resize(n);
+  for (int i = 0; i < n; ++i) { b->views[i].eng = e; b->views[i].index = i; }
+  *out = b;
+  return LG_OK;
+}
+
+int lg_batch_destroy(lg_batch* b) { delete b; return LG_OK; }
+int lg_batch_run(lg_batch* b, int64_t n) { return b->eng->run(n); }
+int lg_batch_size(const lg_batch* b) { return b->eng->C; }
+lg_chain* lg_batch_chain(lg_batch* b, int i) {
+  return (i >= 0 && i < (int)b->views.size()) ? &b->views[i] : nullptr;
+}
+int lg_batch_observables(lg_batch* b, int chain, lg_obs* out) {
+  if (chain < 0 || chain >= b->eng->C) return lg_fail(LG_EINVAL, "chain index");
+  b->eng->acc[chain].report(b->eng->spec[chain], out);
+  return LG_OK;
+}
+int lg_batch_stats(const lg_batch* b, int64_t* total_sites, int64_t* site_sweeps) {
+  long long ts = 0, ss = 0;
+  for (auto& s : b->eng->spec) { ts += s.N; ss += (long long)s.N * (long long)s.mcs; }
+  if (total_sites) *total_sites = ts;
+  if (site_sweeps) *site_sweeps = ss;
+  return LG_OK;
+}
+
+
+int lg_time_sweeps(lg_chain* c, int64_t n, size_t flush_bytes, float* ms) {
+  if (!c || n < 0 || !ms) return lg_fail(LG_EINVAL, "bad argument");
+  return c->eng->run(n, ms, flush_bytes);
+}
+
+int lg_batch_time_sweeps(lg_batch* b, int64_t n, size_t flush_bytes, float* ms) {
+  if (!b || n < 0 || !ms) return lg_fail(LG_EINVAL, "bad argument");
+  return b->eng->run(n, ms, flush_bytes);
+}
+
+int lg_profile_sweeps(lg_chain* c, int64_t n, size_t flush_bytes, double* kernel_ms,
+                      int64_t* vertices) {
+  long long v = 0;
+  int rc = c->eng->profile(n, flush_bytes, kernel_ms, &v);
+  if (vertices) *vertices = v;
+  return rc;
+}
+
+int lg_batch_profile_sweeps(lg_batch* b, int64_t n, size_t flush_bytes, double* kernel_ms,
+                            int64_t* vertices) {
+  long long v = 0;
+  int rc = b->eng->profile(n, flush_bytes, kernel_ms, &v);
+  if (vertices) *vertices = v;
+  return rc;
+}
+
+int lg_num_kernels(void) { return kNumStages; }
+const char* lg_kernel_name(int k) { return (k >= 0 && k < kNumStages) ? kStageNames[k] : ""; }
+
+}  // extern "C"
+

@@ -1,0 +1,453 @@
+// Host-side model setup, observables and checkpoints of the GB300 loop-cluster engine.
+#include "lg_host.h"
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+using namespace lg;
+
+// ---------------------------------------------------------------------------------------------
+// Parameters
+// ---------------------------------------------------------------------------------------------
+extern "C" void lg_params_default(lg_params* p) {
+  std::memset(p, 0, sizeof(*p));
+  p->lattice = LG_CHAIN;
+  p->L = 8;
+  p->T = 0.2;
+  p->beta = 0.0;
+  p->J = 1.0;
+  p->Jz = NAN;
+  p->Jxy = NAN;
+  p->h = 0.0;
+  p->force_scatter = 0.0;
+  p->sweeps = 65536;          // montecarlo.h:41 SWEEPS default [65536:]
+  p->thermalization = -1;     // SWEEPS/8 (montecarlo.h:44)
+  p->seed = 29833;
+  p->init_spins = 0;
+  p->disable_improved_estimator = 0;
+}
+
+static std::string trim(std::string s) {
+  size_t a = 0, b = s.size();
+  while (a < b && std::isspace((unsigned char)s[a])) ++a;
+  while (b > a && std::isspace((unsigned char)s[b - 1])) --b;
+  s = s.substr(a, b - a);
+  if (s.size() >= 2 && s.front() == '"' && s.back() == '"') s = s.substr(1, s.size() - 2);
+  return s;
+}
+
+// number, or number/number (e.g. T = 1/4)
+static bool parse_num(const std::string& v, double* out) {
+  char* end = nullptr;
+  double a = std::strtod(v.c_str(), &end);
+  if (end == v.c_str()) return false;
+  while (*end == ' ') ++end;
+  if (*end == '/') {
+    char* e2 = nullptr;
+    double b = std::strtod(end + 1, &e2);
+    if (e2 == end + 1 || b == 0) return false;
+    while (*e2 == ' ') ++e2;
+    if (*e2) return false;
+    a /= b;
+  } else if (*end) {
+    return false;
+  }
+  *out = a;
+  return true;
+}
+
+extern "C" int lg_params_parse(const char* text, lg_params* p) {
+  if (!text || !p) return lg_fail(LG_EINVAL, "null argument");
+  std::string all(text);
+  size_t i = 0;
+  while (i < all.size()) {
+    size_t j = all.find_first_of(";\n", i);
+    if (j == std::string::npos) j = all.size();
+    std::string line = all.substr(i, j - i);
+    i = j + 1;
+    size_t hash = line.find('#');
+    if (hash != std::string::npos) line = line.substr(0, hash);
+    size_t eq = line.find('=');
+    if (eq == std::string::npos) continue;
+    std::string key = trim(line.substr(0, eq)), val = trim(line.substr(eq + 1));
+    double x = 0;
+    auto num = [&](double* dst) -> int {
+      if (!parse_num(val, &x)) return lg_fail(LG_EINVAL, "bad value for %s: '%s'", key.c_str(), val.c_str());
+      *dst = x;
+      return LG_OK;
+    };
+    int rc = LG_OK;
+    if (key == "LATTICE") {
+      if (val == "chain lattice" || val == "chain") p->lattice = LG_CHAIN;
+      else if (val == "square lattice" || val == "square") p->lattice = LG_SQUARE;
+      else if (val == "simple cubic lattice" || val == "cubic lattice" || val == "cubic") p->lattice = LG_CUBIC;
+      else return lg_fail(LG_EUNSUPPORTED, "LATTICE '%s' not supported", val.c_str());
+    } else if (key == "L") {
+      double d; rc = num(&d); p->L = (int)d;
+    } else if (key == "T") {
+      rc = num(&p->T);
+    } else if (key == "BETA" || key == "INVERSE_TEMPERATURE") {
+      rc = num(&p->beta);
+    } else if (key == "TEMPERATURE") {
+      rc = num(&p->T);
+    } else if (key == "J") {
+      rc = num(&p->J);
+    } else if (key == "Jz") {
+      rc = num(&p->Jz);
+    } else if (key == "Jxy") {
+      rc = num(&p->Jxy);
+    } else if (key == "h") {
+      rc = num(&p->h);
+    } else if (key == "FORCE_SCATTER") {
+      rc = num(&p->force_scatter);
+    } else if (key == "SWEEPS") {
+      double d; rc = num(&d); p->sweeps = (uint64_t)d;
+    } else if (key == "THERMALIZATION") {
+      double d; rc = num(&d); p->thermalization = (int64_t)d;
+    } else if (key == "SEED") {
+      double d; rc = num(&d); p->seed = (uint64_t)d;
+    } else if (key == "INITIAL_SPINS") {
+      if (val == "up") p->init_spins = 0;
+      else if (val == "random") p->init_spins = 1;
+      else return lg_fail(LG_EINVAL, "INITIAL_SPINS must be up or random");
+    } else if (key == "DISABLE_IMPROVED_ESTIMATOR") {
+      p->disable_improved_estimator = (val == "0" || val == "false") ? 0 : 1;
+    }
+    if (rc) return rc;
+  }
+  return LG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Model
+// ---------------------------------------------------------------------------------------------
+static double crop0(double x) { return x > 0 ? x : 0; }
+static double crop01(double x) { return x < 0 ? 0 : (x > 1 ? 1 : x); }
+
+static uint64_t prob32(double p) {  // round(p 2^32) clamped to [0, 2^32]
+  if (!(p > 0)) return 0;
+  if (p >= 1) return 1ull << 32;
+  return (uint64_t)std::floor(p * 4294967296.0 + 0.5);
+}
+
+int ChainSpec::init(const lg_params& p) {
+  if (p.lattice < LG_CHAIN || p.lattice > LG_CUBIC) return lg_fail(LG_EUNSUPPORTED, "unknown LATTICE %d", p.lattice);
+  if (p.L < 2) return lg_fail(LG_EINVAL, "L must be >= 2 (got %d)", p.L);
+  dim = p.lattice;
+  L = p.L;
+  long long n = 1;
+  for (int i = 0; i < dim; ++i) n *= L;
+  if (n > (1ll << 22)) return lg_fail(LG_EBUDGET, "%lld sites exceed the per-chain limit of 2^22", n);
+  N = (int)n;
+  NB = N * dim;
+  s0.resize(NB); s1.resize(NB); gauge.resize(N);
+  for (int s = 0; s < N; ++s) {
+    int x[3] = {0, 0, 0}, r = s, par = 0;
+    for (int i = 0; i < dim; ++i) { x[i] = r % L; r /= L; par += x[i]; }
+    gauge[s] = (par % 2 == 0) ? 1 : -1;
+    for (int i = 0; i < dim; ++i) {
+      int y[3] = {x[0], x[1], x[2]};
+      y[i] = (y[i] + 1) % L;
+      int t = 0;
+      for (int j = dim - 1; j >= 0; --j) t = t * L + y[j];
+      s0[s * dim + i] = s;
+      s1[s * dim + i] = t;
+    }
+  }
+  bipartite = (L % 2 == 0);
+  double b = p.beta > 0 ? p.beta : (p.T > 0 ? 1.0 / p.T : -1.0);
+  if (!(b > 0) || !std::isfinite(b)) return lg_fail(LG_EINVAL, "temperature must be positive");
+  jz = std::isnan(p.Jz) ? p.J : p.Jz;
+  jxy = std::isnan(p.Jxy) ? p.J : p.Jxy;
+  h = p.h;
+  if (!std::isfinite(jz) || !std::isfinite(jxy) || !std::isfinite(h))
+    return lg_fail(LG_EINVAL, "couplings must be finite");
+  // An antiferromagnetic exchange in the xy plane has negative off-diagonal weights; they cancel
+  // only on bipartite lattices (model_parameter.h:615-662).  Signed models are not supported.
+  if (jxy > 0 && !bipartite)
+    return lg_fail(LG_EUNSUPPORTED, "Jxy > 0 on a non-bipartite lattice (odd L) has a sign problem");
+  force_scatter = crop01(p.force_scatter);
+  // graph weights: weight_impl.h:282-315 with Jx = Jy = Jxy (Jm = 0)
+  const double jp = std::fabs(jxy), a = force_scatter;
+  v[0] = v[1] = v[2] = v[3] = 0;
+  if (jp + std::fabs(jz) > 1e-12) {
+    if (jp - jz > 2 * a * jp) {
+      v[0] = crop0(std::min(jp / 2, (jp + jz) / 4));
+      v[1] = crop0(std::min(jp / 2, (jp - jz) / 4));
+      v[2] = crop0(-(jp - jz) / 2);
+      v[3] = crop0(-(jp + jz) / 2);
+    } else {
+      v[0] = (1 - a) * jp / 2;
+      v[1] = a * jp / 2;
+      v[2] = -((1 - 2 * a) * jp - jz) / 2;
+      v[3] = 0;
+    }
+  }
+  W = v[0] + v[1] + v[2] + v[3];
+  energy_offset = NB * W / 2;
+  field = std::fabs(h) > 1e-12;
+  improved = !field && !p.disable_improved_estimator;   // path_integral.C:217
+  sweeps = (int64_t)p.sweeps;
+  therm = p.thermalization >= 0 ? p.thermalization : (int64_t)(p.sweeps >> 3);
+  init_spins = p.init_spins ? 1 : 0;
+  mcs = 0;
+  dchain = DChain{};
+  dchain.seed = p.seed;
+  if (W > 0) {
+    dchain.T0 = prob32(v[0] / W);
+    dchain.T1 = prob32((v[0] + v[1]) / W);
+    dchain.T2 = prob32((v[0] + v[1] + v[2]) / W);
+  }
+  const double s01 = v[0] + v[1];
+  dchain.Poff = prob32(s01 > 0 ? v[0] / s01 : 1.0);
+  dchain.field = field ? 1 : 0;
+  return set_beta(b);
+}
+
+int ChainSpec::set_beta(double b) {
+  if (!(b > 0) || !std::isfinite(b)) return lg_fail(LG_EINVAL, "beta must be positive");
+  beta = b;
+  dchain.inv_rate = W > 0 ? (float)(1.0 / (beta * W)) : 0.0f;
+  dchain.flip_coef = (float)(beta * h * std::ldexp(1.0, -40));
+  return LG_OK;
+}
+
+double ChainSpec::expected_vertices() const {
+  const double m = beta * W * NB;  // expected diagonal proposals per sweep
+  return 1.6 * m + 8 * std::sqrt(m) + 64;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Observables
+// ---------------------------------------------------------------------------------------------
+static double i64(uint64_t x) { return (double)(int64_t)x; }
+static double u128d(const uint64_t* r, int i) { return (double)r[i] + std::ldexp((double)r[i + 1], 64); }
+
+void record_values(const ChainSpec& s, const uint64_t* r, double* v) {
+  const double beta = s.beta, V = (double)s.N;
+  const double nop = (double)r[R_NOP];
+  double ene = s.energy_offset - nop / beta;                       // path_integral.C:850
+  if (s.field) ene += -s.h * i64(r[R_FLD]) * std::ldexp(1.0, -40) / 2;  // :852-859
+  v[RAW_E] = ene;
+  v[RAW_E2] = ene * ene - nop / (beta * beta);                     // energy.h:83
+  v[RAW_NC] = (double)r[R_NC];
+  v[RAW_NOP] = nop;
+  const double t80 = std::ldexp(1.0, -80), t40 = std::ldexp(1.0, -40);
+  if (s.improved) {                                                // susceptibility.h:200-254
+    const double m2 = (double)r[R_M0SQ] / 4, m4 = u128d(r, R_M0Q) / 16;
+    const double sm2 = (double)r[R_SM0SQ] / 4, sm4 = u128d(r, R_SM0Q) / 16;
+    v[RAW_M] = 0.0;
+    v[RAW_ABSM] = std::fabs(i64(r[R_M0])) / 2;
+    v[RAW_M2] = m2;
+    v[RAW_M4] = 3 * m2 * m2 - 2 * m4;
+    v[RAW_CHI] = beta * u128d(r, R_MSQ) * t80 / 4 / V;
+    v[RAW_SM2] = sm2;
+    v[RAW_SM4] = 3 * sm2 * sm2 - 2 * sm4;
+    v[RAW_SCHI] = beta * u128d(r, R_SMSQ) * t80 / 4 / V;
+    v[RAW_GM2] = (double)r[R_N0SQ] / 4;
+    v[RAW_GCHI] = beta * u128d(r, R_LSQ) * t80 / 4 / V;
+  } else {                                                         // susceptibility.h:303-335
+    const double m = i64(r[R_M0]) / 2, sm = i64(r[R_SM0]) / 2;
+    const double ma = i64(r[R_MA]) * t40 / 2, sma = i64(r[R_SMA]) * t40 / 2;
+    v[RAW_M] = m;
+    v[RAW_ABSM] = std::fabs(m);
+    v[RAW_M2] = m * m;
+    v[RAW_M4] = m * m * m * m;
+    v[RAW_CHI] = beta * ma * ma / V;
+    v[RAW_SM2] = sm * sm;
+    v[RAW_SM4] = sm * sm * sm * sm;
+    v[RAW_SCHI] = beta * sma * sma / V;
+    v[RAW_GM2] = 0;
+    v[RAW_GCHI] = 0;
+  }
+}
+
+void BinAcc::push(double x) {
+  ++count;
+  sum += x;
+  sum2 += x * x;
+  cur += x;
+  if (++fill == bin_size) {
+    bins.push_back(cur / (double)bin_size);
+    cur = 0;
+    fill = 0;
+    if (bins.size() == 128) {
+      for (size_t i = 0; i < 64; ++i) bins[i] = 0.5 * (bins[2 * i] + bins[2 * i + 1]);
+      bins.resize(64);
+      bin_size *= 2;
+    }
+  }
+}
+
+static double bins_error(const std::vector<double>& b) {
+  const size_t n = b.size();
+  if (n < 2) return INFINITY;
+  double m = 0;
+  for (double x : b) m += x;
+  m /= (double)n;
+  double v = 0;
+  for (double x : b) v += (x - m) * (x - m);
+  return std::sqrt(v / (double)(n - 1) / (double)n);
+}
+
+double BinAcc::error() const { return bins_error(bins); }
+
+double BinAcc::tau() const {
+  if (count < 2) return 0;
+  const double m = mean();
+  const double var = std::max(0.0, sum2 / (double)count - m * m);
+  const double naive = std::sqrt(var / (double)(count - 1));
+  const double e = error();
+  if (!(naive > 0) || !std::isfinite(e)) return 0;
+  return 0.5 * ((e / naive) * (e / naive) - 1);
+}
+
+void ChainAcc::push(const ChainSpec& s, const uint64_t* rec) {
+  double v[NUM_RAW];
+  record_values(s, rec, v);
+  for (int i = 0; i < NUM_RAW; ++i) raw[i].push(v[i]);
+}
+
+// jackknife over aligned bins of f(a, b)
+template <class F>
+static void jackknife2(const BinAcc& A, const BinAcc& B, F f, double* mean, double* err) {
+  const size_t n = std::min(A.bins.size(), B.bins.size());
+  *mean = f(A.mean(), B.mean());
+  if (n < 2) { *err = INFINITY; return; }
+  double sa = 0, sb = 0;
+  for (size_t i = 0; i < n; ++i) { sa += A.bins[i]; sb += B.bins[i]; }
+  std::vector<double> jk(n);
+  double m = 0;
+  for (size_t i = 0; i < n; ++i) {
+    jk[i] = f((sa - A.bins[i]) / (double)(n - 1), (sb - B.bins[i]) / (double)(n - 1));
+    m += jk[i];
+  }
+  m /= (double)n;
+  double v = 0;
+  for (double x : jk) v += (x - m) * (x - m);
+  *err = std::sqrt((double)(n - 1) / (double)n * v);
+}
+
+void ChainAcc::report(const ChainSpec& s, lg_obs* out) const {
+  std::memset(out, 0, sizeof(*out));
+  const double V = (double)s.N, beta = s.beta;
+  out->count = (uint64_t)raw[RAW_E].count;
+  out->beta = beta;
+  out->volume = V;
+  out->improved = s.improved ? 1 : 0;
+  auto put = [&](int o, const BinAcc& a, double scale) {
+    out->mean[o] = a.mean() * scale;
+    out->error[o] = a.error() * scale;
+    out->tau[o] = a.tau();
+  };
+  put(LG_OBS_ENERGY, raw[RAW_E], 1.0);
+  put(LG_OBS_ENERGY_DENSITY, raw[RAW_E], 1.0 / V);
+  put(LG_OBS_ENERGY2, raw[RAW_E2], 1.0);
+  put(LG_OBS_MAGNETIZATION, raw[RAW_M], 1.0);
+  put(LG_OBS_ABS_MAGNETIZATION, raw[RAW_ABSM], 1.0);
+  put(LG_OBS_MAGNETIZATION2, raw[RAW_M2], 1.0);
+  put(LG_OBS_MAGNETIZATION4, raw[RAW_M4], 1.0);
+  put(LG_OBS_SUSCEPTIBILITY, raw[RAW_CHI], 1.0);
+  put(LG_OBS_STAG_MAGNETIZATION2, raw[RAW_SM2], 1.0);
+  put(LG_OBS_STAG_MAGNETIZATION4, raw[RAW_SM4], 1.0);
+  put(LG_OBS_STAG_SUSCEPTIBILITY, raw[RAW_SCHI], 1.0);
+  put(LG_OBS_GEN_MAGNETIZATION2, raw[RAW_GM2], 1.0);
+  put(LG_OBS_GEN_SUSCEPTIBILITY, raw[RAW_GCHI], 1.0);
+  put(LG_OBS_NUM_CLUSTERS, raw[RAW_NC], 1.0);
+  put(LG_OBS_NUM_OPERATORS, raw[RAW_NOP], 1.0);
+  // evaluators: energy.h:89-101, susceptibility.h:340-374
+  double m, e;
+  jackknife2(raw[RAW_E], raw[RAW_E2], [&](double a, double b) { return beta * beta * (b - a * a) / V; }, &m, &e);
+  out->mean[LG_OBS_SPECIFIC_HEAT] = m;
+  out->error[LG_OBS_SPECIFIC_HEAT] = e;
+  jackknife2(raw[RAW_M2], raw[RAW_M4], [](double a, double b) { return b != 0 ? a * a / b : 0.0; }, &m, &e);
+  out->mean[LG_OBS_BINDER] = m;
+  out->error[LG_OBS_BINDER] = e;
+  jackknife2(raw[RAW_SM2], raw[RAW_SM4], [](double a, double b) { return b != 0 ? a * a / b : 0.0; }, &m, &e);
+  out->mean[LG_OBS_STAG_BINDER] = m;
+  out->error[LG_OBS_STAG_BINDER] = e;
+}
+
+extern "C" const char* lg_obs_name(int i) {
+  static const char* names[LG_NUM_OBS] = {
+      "Energy", "Energy Density", "Energy^2", "Specific Heat", "Magnetization",
+      "|Magnetization|", "Magnetization^2", "Magnetization^4", "Susceptibility",
+      "Staggered Magnetization^2", "Staggered Magnetization^4", "Staggered Susceptibility",
+      "Generalized Magnetization^2", "Generalized Susceptibility", "Number of Clusters",
+      "Number of Operators", "Binder Ratio of Magnetization",
+      "Binder Ratio of Staggered Magnetization"};
+  return (i >= 0 && i < LG_NUM_OBS) ? names[i] : "";
+}
+
+// ---------------------------------------------------------------------------------------------
+// Checkpoint: the worker's save/load content (path_integral.C:111-124: mcs, spins, operators).
+// Layout (little endian): "LGCK" u32 version=1, u32 dim, u32 L, u64 mcs, u64 n_ops,
+// N x u8 spins, n_ops x (i32 bond, f64 time), u64 FNV-1a of everything before it.
+// ---------------------------------------------------------------------------------------------
+static uint64_t fnv1a(const uint8_t* p, size_t n) {
+  uint64_t h = 1469598103934665603ull;
+  for (size_t i = 0; i < n; ++i) { h ^= p[i]; h *= 1099511628211ull; }
+  return h;
+}
+
+template <class T>
+static void put_raw(std::vector<uint8_t>& b, const T& x) {
+  const uint8_t* p = reinterpret_cast<const uint8_t*>(&x);
+  b.insert(b.end(), p, p + sizeof(T));
+}
+
+void checkpoint_encode(const ChainSpec& s, const std::vector<int32_t>& spins,
+                       const std::vector<int32_t>& bonds, const std::vector<double>& times,
+                       std::vector<uint8_t>& blob) {
+  blob.clear();
+  blob.insert(blob.end(), {'L', 'G', 'C', 'K'});
+  put_raw(blob, (uint32_t)1);
+  put_raw(blob, (uint32_t)s.dim);
+  put_raw(blob, (uint32_t)s.L);
+  put_raw(blob, (uint64_t)s.mcs);
+  put_raw(blob, (uint64_t)bonds.size());
+  for (int x : spins) blob.push_back((uint8_t)(x & 1));
+  for (size_t i = 0; i < bonds.size(); ++i) { put_raw(blob, bonds[i]); put_raw(blob, times[i]); }
+  put_raw(blob, fnv1a(blob.data(), blob.size()));
+}
+
+int checkpoint_decode(const ChainSpec& s, const uint8_t* buf, size_t size,
+                      std::vector<int32_t>& spins, std::vector<int32_t>& bonds,
+                      std::vector<double>& times, uint64_t* mcs) {
+  const size_t head = 4 + 4 + 4 + 4 + 8 + 8;
+  if (!buf || size < head + 8) return lg_fail(LG_ECORRUPT, "checkpoint too short");
+  uint64_t h;
+  std::memcpy(&h, buf + size - 8, 8);
+  if (h != fnv1a(buf, size - 8)) return lg_fail(LG_ECORRUPT, "checkpoint checksum mismatch");
+  if (std::memcmp(buf, "LGCK", 4) != 0) return lg_fail(LG_ECORRUPT, "not a checkpoint");
+  uint32_t ver, dim, L;
+  uint64_t m, n;
+  std::memcpy(&ver, buf + 4, 4);
+  std::memcpy(&dim, buf + 8, 4);
+  std::memcpy(&L, buf + 12, 4);
+  std::memcpy(&m, buf + 16, 8);
+  std::memcpy(&n, buf + 24, 8);
+  if (ver != 1) return lg_fail(LG_ECORRUPT, "checkpoint version %u", ver);
+  if ((int)dim != s.dim || (int)L != s.L) return lg_fail(LG_ECORRUPT, "checkpoint lattice mismatch");
+  if (size != head + (size_t)s.N + n * 12 + 8) return lg_fail(LG_ECORRUPT, "checkpoint size mismatch");
+  const uint8_t* p = buf + head;
+  spins.resize(s.N);
+  for (int i = 0; i < s.N; ++i) spins[i] = p[i];
+  p += s.N;
+  bonds.resize(n);
+  times.resize(n);
+  for (uint64_t i = 0; i < n; ++i) {
+    std::memcpy(&bonds[i], p, 4);
+    std::memcpy(&times[i], p + 4, 8);
+    p += 12;
+    if (bonds[i] < 0 || bonds[i] >= s.NB || !(times[i] >= 0.0 && times[i] < 1.0))
+      return lg_fail(LG_ECORRUPT, "checkpoint operator %llu out of range", (unsigned long long)i);
+  }
+  *mcs = m;
+  return LG_OK;
+}

@@ -1,0 +1,63 @@
+// Host-side model setup, observables and checkpoints of the GB300 loop-cluster engine.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/looper_gpu.h"
+#include "lg_types.h"
+
+int lg_fail(int code, const char* fmt, ...);
+
+// One chain's model, lattice and Monte Carlo schedule, validated from lg_params.
+struct ChainSpec {
+  int dim = 1, L = 0, N = 0, NB = 0;
+  std::vector<int> s0, s1, gauge;
+  bool bipartite = true;
+  double beta = 1, jxy = 1, jz = 1, h = 0, force_scatter = 0;
+  double v[4] = {0, 0, 0, 0};   // graph weights of one bond (xxz graphs 0..3)
+  double W = 0;                 // sum of v
+  double energy_offset = 0;     // sum over bonds of W/2 (weight_impl.h:187,199)
+  int64_t therm = 0, sweeps = 0;
+  uint64_t mcs = 0;             // sweeps done
+  uint64_t last_nop = 0;
+  int init_spins = 0;
+  bool field = false, improved = true;
+  lg::DChain dchain{};
+
+  int init(const lg_params& p);
+  int set_beta(double b);
+  double expected_vertices() const;
+};
+
+// Rebinning accumulator: up to 128 bin means, bin size doubling as data come in.
+struct BinAcc {
+  std::vector<double> bins;
+  int64_t bin_size = 1, fill = 0, count = 0;
+  double cur = 0, sum = 0, sum2 = 0;
+  void push(double x);
+  double mean() const { return count ? sum / count : 0.0; }
+  double error() const;
+  double tau() const;
+};
+
+enum {
+  RAW_E = 0, RAW_E2, RAW_M, RAW_ABSM, RAW_M2, RAW_M4, RAW_CHI, RAW_SM2, RAW_SM4, RAW_SCHI,
+  RAW_GM2, RAW_GCHI, RAW_NC, RAW_NOP, NUM_RAW
+};
+
+struct ChainAcc {
+  BinAcc raw[NUM_RAW];
+  void push(const ChainSpec& s, const uint64_t* rec);
+  void report(const ChainSpec& s, lg_obs* out) const;
+};
+
+// Observable values of one sweep record (path_integral.C:827-862).
+void record_values(const ChainSpec& s, const uint64_t* rec, double* v);
+
+void checkpoint_encode(const ChainSpec& s, const std::vector<int32_t>& spins,
+                       const std::vector<int32_t>& bonds, const std::vector<double>& times,
+                       std::vector<uint8_t>& blob);
+int checkpoint_decode(const ChainSpec& s, const uint8_t* buf, size_t size,
+                      std::vector<int32_t>& spins, std::vector<int32_t>& bonds,
+                      std::vector<double>& times, uint64_t* mcs);

@@ -1,0 +1,371 @@
+"""Python binding of the GB300 loop-cluster engine (ctypes over include/looper_gpu.h).
+
+`LoopWorker` mirrors looper's path-integral worker plug-in (path_integral.C:57-124): it is
+constructed from the worker's parameters, `run()` performs one sweep of update + measurement,
+`is_thermalized()` / `progress()` report the schedule, `save()` / `load()` checkpoint the
+configuration and `set_beta()` / `weight_parameter()` / `log_weight()` are the exchange Monte
+Carlo hooks.  `Batch` runs many independent chains in one arena.
+
+There is no CPU fallback: importing this module fails if the CUDA library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "liblooper_gb300.so")
+
+CHAIN, SQUARE, CUBIC = 1, 2, 3
+LATTICES = {"chain lattice": CHAIN, "chain": CHAIN, "square lattice": SQUARE, "square": SQUARE,
+            "simple cubic lattice": CUBIC, "cubic": CUBIC}
+RECORD_WORDS = 32
+NUM_OBS = 18
+
+ERRORS = {0: "LG_OK", -1: "LG_EINVAL", -2: "LG_ENOMEM", -3: "LG_EDEVICE", -4: "LG_EUNSUPPORTED",
+          -5: "LG_EITERCAP", -6: "LG_EBUDGET", -7: "LG_ECORRUPT", -8: "LG_ENOTREADY"}
+
+
+class LoopError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (ERRORS.get(code, code), msg))
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("lattice", ctypes.c_int), ("L", ctypes.c_int), ("T", ctypes.c_double),
+                ("beta", ctypes.c_double), ("J", ctypes.c_double), ("Jz", ctypes.c_double),
+                ("Jxy", ctypes.c_double), ("h", ctypes.c_double),
+                ("force_scatter", ctypes.c_double), ("sweeps", ctypes.c_uint64),
+                ("thermalization", ctypes.c_int64), ("seed", ctypes.c_uint64),
+                ("init_spins", ctypes.c_int), ("disable_improved_estimator", ctypes.c_int)]
+
+
+class Obs(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_uint64), ("beta", ctypes.c_double), ("volume", ctypes.c_double),
+                ("improved", ctypes.c_int), ("mean", ctypes.c_double * NUM_OBS),
+                ("error", ctypes.c_double * NUM_OBS), ("tau", ctypes.c_double * NUM_OBS)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("looper_gb300: %s is missing; build it with "
+                              "python alps-looper_gb300/build.py" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i64, u64 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64
+        sig = {
+            "lg_params_default": (None, [vp]),
+            "lg_params_parse": (ctypes.c_int, [ctypes.c_char_p, vp]),
+            "lg_obs_name": (ctypes.c_char_p, [ctypes.c_int]),
+            "lg_create": (ctypes.c_int, [vp, vp]),
+            "lg_destroy": (ctypes.c_int, [vp]),
+            "lg_run": (ctypes.c_int, [vp, i64]),
+            "lg_is_thermalized": (ctypes.c_int, [vp]),
+            "lg_progress": (ctypes.c_double, [vp]),
+            "lg_observables": (ctypes.c_int, [vp, vp]),
+            "lg_save": (ctypes.c_int, [vp, vp, vp]),
+            "lg_load": (ctypes.c_int, [vp, vp, ctypes.c_size_t]),
+            "lg_set_beta": (ctypes.c_int, [vp, ctypes.c_double]),
+            "lg_weight_parameter": (ctypes.c_double, [vp]),
+            "lg_log_weight": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
+            "lg_last_error": (ctypes.c_int, [vp, ctypes.c_size_t]),
+            "lg_get_state": (ctypes.c_int, [vp, vp, vp, vp, i64, vp]),
+            "lg_set_state": (ctypes.c_int, [vp, vp, vp, vp, i64, u64]),
+            "lg_fetch_records": (ctypes.c_int, [vp, vp, i64, vp]),
+            "lg_keep_records": (ctypes.c_int, [vp, ctypes.c_int]),
+            "lg_uf_label": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, i64, vp, vp, vp, i64, vp, vp]),
+            "lg_batch_create": (ctypes.c_int, [ctypes.c_int, vp, vp]),
+            "lg_batch_destroy": (ctypes.c_int, [vp]),
+            "lg_batch_run": (ctypes.c_int, [vp, i64]),
+            "lg_batch_observables": (ctypes.c_int, [vp, ctypes.c_int, vp]),
+            "lg_batch_size": (ctypes.c_int, [vp]),
+            "lg_batch_stats": (ctypes.c_int, [vp, vp, vp]),
+            "lg_batch_chain": (vp, [vp, ctypes.c_int]),
+            "lg_time_sweeps": (ctypes.c_int, [vp, i64, ctypes.c_size_t, vp]),
+            "lg_batch_time_sweeps": (ctypes.c_int, [vp, i64, ctypes.c_size_t, vp]),
+            "lg_profile_sweeps": (ctypes.c_int, [vp, i64, ctypes.c_size_t, vp, vp]),
+            "lg_batch_profile_sweeps": (ctypes.c_int, [vp, i64, ctypes.c_size_t, vp, vp]),
+            "lg_num_kernels": (ctypes.c_int, []),
+            "lg_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
+            "lg_kernel_launches": (u64, []),
+            "lg_version": (ctypes.c_char_p, []),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(1024)
+    lib().lg_last_error(buf, 1024)
+    return buf.value.decode()
+
+
+def check(rc):
+    if rc != 0:
+        raise LoopError(rc, last_error())
+    return rc
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def make_params(**kw) -> Params:
+    """Parameters with the worker's key names: LATTICE, L, T, BETA, J, Jz, Jxy, h, SWEEPS,
+    THERMALIZATION, SEED, FORCE_SCATTER, INITIAL_SPINS, DISABLE_IMPROVED_ESTIMATOR (lower-case
+    aliases accepted)."""
+    p = Params()
+    lib().lg_params_default(ctypes.byref(p))
+    for k, v in kw.items():
+        key = k.upper() if k.upper() in ("LATTICE", "BETA", "SWEEPS", "THERMALIZATION", "SEED",
+                                         "FORCE_SCATTER", "INITIAL_SPINS",
+                                         "DISABLE_IMPROVED_ESTIMATOR") else k
+        if key == "LATTICE":
+            p.lattice = LATTICES[v] if isinstance(v, str) else int(v)
+        elif key == "L":
+            p.L = int(v)
+        elif key == "T":
+            p.T = float(v)
+        elif key == "BETA":
+            p.beta = float(v)
+        elif key in ("J", "Jz", "Jxy", "h"):
+            setattr(p, key, float(v))
+        elif key == "SWEEPS":
+            p.sweeps = int(v)
+        elif key == "THERMALIZATION":
+            p.thermalization = int(v)
+        elif key == "SEED":
+            p.seed = int(v)
+        elif key == "FORCE_SCATTER":
+            p.force_scatter = float(v)
+        elif key == "INITIAL_SPINS":
+            p.init_spins = 1 if v in ("random", 1, True) else 0
+        elif key == "DISABLE_IMPROVED_ESTIMATOR":
+            p.disable_improved_estimator = 1 if v else 0
+        else:
+            raise KeyError(k)
+    return p
+
+
+def parse_params(text: str) -> Params:
+    p = Params()
+    lib().lg_params_default(ctypes.byref(p))
+    check(lib().lg_params_parse(text.encode(), ctypes.byref(p)))
+    return p
+
+
+def obs_names():
+    return [lib().lg_obs_name(i).decode() for i in range(NUM_OBS)]
+
+
+def _obs_dict(o: Obs):
+    names = obs_names()
+    return {n: (o.mean[i], o.error[i]) for i, n in enumerate(names)} | {
+        "count": o.count, "improved": bool(o.improved)}
+
+
+def _time(fn, h, n, flush_bytes):
+    ms = np.zeros(max(int(n), 1), dtype=np.float32)
+    check(fn(h, int(n), int(flush_bytes), _p(ms)))
+    return ms[:int(n)]
+
+
+def _profile(fn, h, n, flush_bytes):
+    k = lib().lg_num_kernels()
+    out = np.zeros(k, dtype=np.float64)
+    v = ctypes.c_int64()
+    check(fn(h, int(n), int(flush_bytes), _p(out), ctypes.byref(v)))
+    names = [lib().lg_kernel_name(i).decode() for i in range(k)]
+    return dict(zip(names, out.tolist())), v.value
+
+
+class LoopWorker:
+    """One chain: looper's "loop; path integral" worker on the GPU."""
+
+    def __init__(self, params: Params | None = None, _handle=None, _owner=None, **kw):
+        self._owner = _owner
+        if _handle is not None:
+            self._h = ctypes.c_void_p(_handle)
+            self._own = False
+        else:
+            if params is None:
+                params = make_params(**kw)
+            h = ctypes.c_void_p()
+            check(lib().lg_create(ctypes.byref(params), ctypes.byref(h)))
+            self._h = h
+            self._own = True
+        self.params = params
+
+    def close(self):
+        if getattr(self, "_own", False) and self._h:
+            lib().lg_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, nsweeps: int = 1):
+        check(lib().lg_run(self._h, int(nsweeps)))
+
+    def is_thermalized(self) -> bool:
+        return bool(lib().lg_is_thermalized(self._h))
+
+    def progress(self) -> float:
+        return lib().lg_progress(self._h)
+
+    def observables(self):
+        o = Obs()
+        check(lib().lg_observables(self._h, ctypes.byref(o)))
+        return _obs_dict(o)
+
+    def set_beta(self, beta: float):
+        check(lib().lg_set_beta(self._h, float(beta)))
+
+    def weight_parameter(self) -> float:
+        return lib().lg_weight_parameter(self._h)
+
+    @staticmethod
+    def log_weight(gw: float, beta: float) -> float:
+        return lib().lg_log_weight(float(gw), float(beta))
+
+    def save(self) -> bytes:
+        n = ctypes.c_size_t(0)
+        check(lib().lg_save(self._h, None, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        check(lib().lg_save(self._h, buf, ctypes.byref(n)))
+        return buf.raw[:n.value]
+
+    def load(self, blob: bytes):
+        buf = ctypes.create_string_buffer(blob, len(blob))
+        check(lib().lg_load(self._h, buf, len(blob)))
+
+    def time_sweeps(self, n, flush_bytes=0):
+        """Device time (ms) of each of n sweeps, L2 flushed between sweeps."""
+        return _time(lib().lg_time_sweeps, self._h, n, flush_bytes)
+
+    def profile_sweeps(self, n, flush_bytes=0):
+        """Per-stage device time (ms, summed over n sweeps) and operators processed."""
+        return _profile(lib().lg_profile_sweeps, self._h, n, flush_bytes)
+
+    # ---- test seams ----
+    def num_sites(self):
+        L = self.params.L
+        return L ** self.params.lattice
+
+    def state(self):
+        N = self.num_sites()
+        spins = np.zeros(N, dtype=np.int32)
+        n = ctypes.c_int64()
+        check(lib().lg_get_state(self._h, _p(spins), None, None, 0, ctypes.byref(n)))
+        bonds = np.zeros(max(n.value, 1), dtype=np.int32)
+        times = np.zeros(max(n.value, 1), dtype=np.float64)
+        check(lib().lg_get_state(self._h, _p(spins), _p(bonds), _p(times), n.value, ctypes.byref(n)))
+        return spins, bonds[:n.value].copy(), times[:n.value].copy()
+
+    def set_state(self, spins, bonds, times, sweep):
+        spins = np.ascontiguousarray(spins, dtype=np.int32)
+        bonds = np.ascontiguousarray(bonds, dtype=np.int32)
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        check(lib().lg_set_state(self._h, _p(spins), _p(bonds), _p(times), len(bonds), int(sweep)))
+
+    def keep_records(self, on=True):
+        check(lib().lg_keep_records(self._h, 1 if on else 0))
+
+    def fetch_records(self, cap=1 << 20):
+        out = np.zeros(cap * RECORD_WORDS, dtype=np.uint64)
+        n = ctypes.c_int64()
+        check(lib().lg_fetch_records(self._h, _p(out), cap, ctypes.byref(n)))
+        return out[:n.value * RECORD_WORDS].reshape(n.value, RECORD_WORDS).copy()
+
+
+class Batch:
+    """Many independent chains (possibly of different sizes and temperatures) in one arena."""
+
+    def __init__(self, params_list):
+        arr = (Params * len(params_list))(*params_list)
+        h = ctypes.c_void_p()
+        check(lib().lg_batch_create(len(params_list), arr, ctypes.byref(h)))
+        self._h = h
+        self.params = list(params_list)
+
+    def close(self):
+        if self._h:
+            lib().lg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return lib().lg_batch_size(self._h)
+
+    def run(self, nsweeps: int = 1):
+        check(lib().lg_batch_run(self._h, int(nsweeps)))
+
+    def observables(self, i):
+        o = Obs()
+        check(lib().lg_batch_observables(self._h, i, ctypes.byref(o)))
+        return _obs_dict(o)
+
+    def stats(self):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().lg_batch_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def time_sweeps(self, n, flush_bytes=0):
+        return _time(lib().lg_batch_time_sweeps, self._h, n, flush_bytes)
+
+    def profile_sweeps(self, n, flush_bytes=0):
+        return _profile(lib().lg_batch_profile_sweeps, self._h, n, flush_bytes)
+
+    def chain(self, i) -> LoopWorker:
+        h = lib().lg_batch_chain(self._h, i)
+        if not h:
+            raise IndexError(i)
+        return LoopWorker(self.params[i], _handle=h, _owner=self)
+
+
+def uf_label(lattice, L, bonds, graphs):
+    """Reference-numbered cluster labels of a time-ordered configuration, on the GPU."""
+    bonds = np.ascontiguousarray(bonds, dtype=np.int32)
+    graphs = np.ascontiguousarray(graphs, dtype=np.int32)
+    cap = L ** lattice + len(bonds) + 1
+    lab = np.zeros(cap, dtype=np.int32)
+    nf, nc = ctypes.c_int64(), ctypes.c_int64()
+    check(lib().lg_uf_label(int(lattice), int(L), len(bonds), _p(bonds), _p(graphs), _p(lab), cap,
+                            ctypes.byref(nf), ctypes.byref(nc)))
+    return lab[:nf.value].copy(), nc.value
+
+
+def kernel_launches() -> int:
+    return lib().lg_kernel_launches()
+
+
+def version() -> str:
+    return lib().lg_version().decode()
+
+
+def exported_symbols():
+    """Names declared in include/looper_gpu.h."""
+    import re
+    hdr = os.path.join(os.path.dirname(HERE), "include", "looper_gpu.h")
+    text = open(hdr).read()
+    return sorted(set(re.findall(r"\b(lg_[a-z_0-9]+)\s*\(", text)))

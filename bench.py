@@ -1,0 +1,338 @@
+"""Benchmark: loop-cluster sweeps on one GB300 (MC sweeps*sites/s).
+
+Workload (one step = one sweep of update + measurement, path_integral.C:355-864): S=1/2
+Heisenberg antiferromagnet on a periodic 128x128 square lattice (16384 sites, 32768 bonds),
+J = 1, beta = 64 (about 1.2 M operators), seed 7, iid random initial spins.  The chain is brought
+near equilibrium (untimed) before the warm-up steps.  Between timed steps a 256 MiB device write
+flushes the L2 cache (outside the timed brackets); each step is timed with CUDA events on the
+engine's own stream.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With N > 1 (torchrun) every rank runs its own independent replica chain (the path does not
+shard; replicas only) and rank 0 prints the aggregate.  --impl reference times the CPU
+loop-cluster update (the oracle's restatement of path_integral.C with the same random streams)
+on this host's cores for the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "alps-looper_gb300"))
+sys.path.insert(0, os.path.join(REPO, "tests"))
+
+L_SIDE = 128
+BETA = 64.0
+SEED = 7
+N_SITES = L_SIDE * L_SIDE
+FLUSH_BYTES = 256 << 20
+PRE_THERM = 256
+METRIC = "MC sweeps*sites/s"
+UNIT = "sweeps*sites/s"
+WORKLOAD = ("square 128x128 S=1/2 Heisenberg AF, J=1, beta=64, periodic (16384 sites, "
+            "32768 bonds, ~1.2M operators/sweep)")
+
+
+def _rank_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _dist_init(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def _reduce_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _reduce_sum(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def _traffic_from_profile():
+    """DRAM bytes per sweep from the committed ncu summary, when present."""
+    path = os.path.join(REPO, "profiles", "sweep_square128_b64.md")
+    try:
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_sweep:"):
+                return float(ln.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+def _params(lg, seed=SEED, sweeps=1 << 13, therm=1 << 10):
+    return lg.make_params(LATTICE="square", L=L_SIDE, BETA=BETA, J=1.0, SEED=seed,
+                          SWEEPS=sweeps, THERMALIZATION=therm, INITIAL_SPINS="random")
+
+
+def cpu_port_rate(seconds=12.0, threads=1, state=None, warm=3):
+    """Oracle (CPU restatement) sweeps*sites/s on this host for the bench workload."""
+    import oracle_lib as orc
+    chains = [orc.Oracle(2, L_SIDE, BETA, 1.0, 1.0, 0.0, seed=SEED + 1000 * i)
+              for i in range(threads)]
+    for o in chains:
+        if state is not None:
+            o.set_state(*state, 0)
+        o.sweep(warm)
+    done = [0] * threads
+    stop = time.perf_counter() + seconds
+
+    def work(i):
+        while time.perf_counter() < stop:
+            chains[i].sweep(1)
+            done[i] += 1
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    el = time.perf_counter() - t0
+    for o in chains:
+        o.close()
+    return sum(done) * N_SITES / el, sum(done), el
+
+
+def run_ours(args, dist, ws, rank, local):
+    import looper_gb300 as lg
+    lg.lib()
+    w = lg.LoopWorker(_params(lg, seed=SEED + 7919 * rank))
+    w.run(PRE_THERM)
+    w.time_sweeps(max(3, args.warmup), FLUSH_BYTES)
+    clk = Clocks(local) if rank == 0 else None
+    if clk:
+        clk.start()
+    _barrier(dist)
+    l0 = lg.kernel_launches()
+    ms = w.time_sweeps(args.steps, FLUSH_BYTES)
+    launches = lg.kernel_launches() - l0
+    _barrier(dist)
+    clocks = clk.stop() if clk else None
+    total_ms = float(ms.sum())
+    total_ms = _reduce_max(dist, total_ms)
+    value = ws * args.steps * N_SITES / (total_ms / 1e3)
+    # per-stage profile (events between launches) for the roofline
+    prof, verts = w.profile_sweeps(16, FLUSH_BYTES)
+    nv_mean = verts / 16.0
+    sweep_ms = sum(prof.values()) / 16.0
+    bytes_alg = 64.0 * nv_mean + 16.0 * N_SITES  # per sweep (algorithmic)
+    peak, peak_kind = _peaks()
+    achieved = bytes_alg / (total_ms / args.steps / 1e3) / 1e9
+    dom = max(prof, key=prof.get)
+    shares = {k: round(v / sum(prof.values()), 4) for k, v in prof.items()}
+    traffic = _traffic_from_profile()
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_kind": peak_kind, "scope": "one sweep (all kernels of the CUDA graph)",
+                "algorithmic_bytes_per_sweep": int(bytes_alg),
+                "dominant_kernel": dom, "dominant_share": shares[dom],
+                "stage_ms_per_sweep": {k: round(v / 16.0, 5) for k, v in prof.items()},
+                "profiled_sweep_ms": round(sweep_ms, 5)}
+    # end to end through the public C ABI: create + run + observables, host wall clock
+    t0 = time.perf_counter()
+    e = lg.LoopWorker(_params(lg, seed=SEED + 31 + rank))
+    e.run(args.steps)
+    obs = e.observables()
+    e2e_s = time.perf_counter() - t0
+    e2e_s = _reduce_max(dist, e2e_s)
+    e2e = {"value": ws * args.steps * N_SITES / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": round((2 * 32768 * 4 + 4 * 16384 * 4 + 16384) / args.steps, 1),
+           "d2h_bytes_per_step": 32 * 8 + 32,
+           "scope": "lg_create + lg_run(steps) + lg_observables from a cold start"}
+    e.close()
+    cpu = None
+    if rank == 0:
+        state = w.state()
+        rate, n, el = cpu_port_rate(seconds=args.cpu_seconds, threads=1, state=state)
+        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "%d sweeps of the same 128x128 beta=64 chain started from the GPU's "
+                         "equilibrated state, %.1f s, 1 thread (CPU restatement of "
+                         "path_integral.C in oracle/)" % (n, el)}
+    w.close()
+    if rank != 0:
+        return None
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64 (FP64 times on a 2^-52 grid)",
+        "data": "synthetic (seeded Philox streams; iid random initial spins)",
+        "config": {"workload": WORKLOAD, "lattice": "square", "L": L_SIDE, "beta": BETA,
+                   "J": 1.0, "seed": SEED, "step": "one sweep",
+                   "pre_thermalization_sweeps": PRE_THERM,
+                   "l2": "flushed between steps (256 MiB device write, untimed)",
+                   "parallelism": "replicas" if ws > 1 else "single chain"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+        "clocks": clocks,
+        "observables": {"Energy Density": obs["Energy Density"][0],
+                        "sweeps_measured": int(obs["count"])},
+    }
+    return out
+
+
+def run_reference(args, dist, ws, rank, local):
+    if rank != 0:
+        return None
+    threads = max(1, os.cpu_count() or 1)
+    steps = max(1, min(args.steps, 16))
+    import oracle_lib as orc
+    chains = [orc.Oracle(2, L_SIDE, BETA, 1.0, 1.0, 0.0, seed=SEED + 1000 * i)
+              for i in range(threads)]
+
+    def work(i, n):
+        chains[i].sweep(n)
+
+    def par(n):
+        ths = [threading.Thread(target=work, args=(i, n)) for i in range(threads)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+
+    par(max(3, min(args.warmup, 4)))
+    t0 = time.perf_counter()
+    par(steps)
+    el = time.perf_counter() - t0
+    value = threads * steps * N_SITES / el
+    for o in chains:
+        o.close()
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp64 times", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "lattice": "square", "L": L_SIDE, "beta": BETA,
+                   "step": "one sweep per thread"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d threads x %d sweeps after %d warm-up sweeps from a "
+                                   "random start (the reference's path_integral binary needs "
+                                   "ALPS and does not build here)" % (threads, steps,
+                                                                      max(3, min(args.warmup, 4)))},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--warmup", type=int, default=8)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    ws, rank, local = _rank_info()
+    if ws > 1 and args.impl == "ours":
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = _dist_init(ws)
+    if args.impl == "reference":
+        out = run_reference(args, dist, ws, rank, local)
+    else:
+        out = run_ours(args, dist, ws, rank, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

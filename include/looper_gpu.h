@@ -1,0 +1,209 @@
+/*
+ * looper_gpu.h — C ABI of the GB300 loop-cluster engine.
+ *
+ * This is the drop-in boundary for looper's continuous-imaginary-time loop-cluster worker
+ * ("loop; path integral", path_integral.C:872-876).  Every entry point below replaces one member
+ * of that worker's plug-in interface (class loop_worker : alps::parapack::mc_worker,
+ * path_integral.C:57-124) or one of its parameter / observable conventions.  Plain C types only:
+ * no pointer into device memory crosses this boundary; the library owns all device state.
+ *
+ * Errors: every function returns an int status (LG_OK = 0, negative on failure) and the message
+ * of the last failure on the calling thread is available from lg_last_error().  Exceptions never
+ * cross the boundary.  This replaces the worker's boost::throw_exception(std::invalid_argument /
+ * logic_error / runtime_error) reporting (path_integral.C:212-213, model.h:62-80,
+ * temperature.h:100, graph_impl.h:593,606, weight_impl.h:205-212).
+ *
+ * Threading: a handle is not thread-safe; drive each handle from one host thread.  The device
+ * work of a handle is ordered on its own CUDA stream.
+ */
+#ifndef LOOPER_GPU_H
+#define LOOPER_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------- */
+enum {
+  LG_OK = 0,
+  LG_EINVAL = -1,        /* invalid parameter (std::invalid_argument in the reference)        */
+  LG_ENOMEM = -2,        /* device or host allocation failed                                  */
+  LG_EDEVICE = -3,       /* CUDA error                                                         */
+  LG_EUNSUPPORTED = -4,  /* model outside the supported set (e.g. sign problem, S > 1/2)      */
+  LG_EITERCAP = -5,      /* a device loop hit its iteration cap and stopped                  */
+  LG_EBUDGET = -6,       /* a request exceeds the memory budget                               */
+  LG_ECORRUPT = -7,      /* checkpoint data rejected                                          */
+  LG_ENOTREADY = -8      /* nothing to report yet                                             */
+};
+
+/* ---- lattices (ALPS LATTICE names) ---------------------------------------------------------
+ * periodic, nearest neighbour: site = x + L*y + L*L*z; bond = site*dim + d joins site and
+ * site + e_d.  Sublattice gauge +1/-1 by the parity of x+y+z (lattice.h:601). */
+enum { LG_CHAIN = 1, LG_SQUARE = 2, LG_CUBIC = 3 };
+
+/* ---- model / run parameters --------------------------------------------------------------
+ * Replaces the alps::Parameters read by loop_worker's constructor (path_integral.C:202-305):
+ * LATTICE, L (lattice_helper, lattice.h:290-315); MODEL "spin" couplings J, Jz, Jxy, h
+ * (model_parameter.h:62-70, S=1/2 only); T or BETA (temperature.h:43-54); SWEEPS and
+ * THERMALIZATION (montecarlo.h:41-45: THERMALIZATION defaults to SWEEPS/8);
+ * DISABLE_IMPROVED_ESTIMATOR (path_integral.C:217); FORCE_SCATTER (weight_impl.h:289);
+ * SEED.  NaN in jz / jxy means "not given": they then default to J (ALPS spin model). */
+typedef struct lg_params {
+  int lattice;                    /* LG_CHAIN, LG_SQUARE, LG_CUBIC                              */
+  int L;                          /* linear size, >= 2                                          */
+  double T;                       /* temperature (used when beta <= 0)                          */
+  double beta;                    /* inverse temperature; > 0 overrides T                       */
+  double J, Jz, Jxy;              /* couplings; H_b = Jz SzSz + Jxy/2 (S+S- + S-S+)            */
+  double h;                       /* longitudinal field, H_s = -h Sz                            */
+  double force_scatter;           /* FORCE_SCATTER in [0,1], default 0                          */
+  uint64_t sweeps;                /* SWEEPS (measurement sweeps)                                */
+  int64_t thermalization;         /* THERMALIZATION; < 0 means SWEEPS/8                         */
+  uint64_t seed;                  /* SEED                                                        */
+  int init_spins;                 /* 0: all up (path_integral.C:225), 1: iid from the seed      */
+  int disable_improved_estimator; /* DISABLE_IMPROVED_ESTIMATOR                                  */
+} lg_params;
+
+/* Fill defaults: chain, L=8, T=0.2, J=1, Jz=Jxy=NaN, h=0, SWEEPS=65536 (montecarlo.h:41),
+ * THERMALIZATION=-1, SEED=29833, all spins up. */
+void lg_params_default(lg_params* p);
+
+/* Parse ALPS-style "KEY = value" lines (';' or newline separated, '#' comments) into *p.
+ * Keys: LATTICE ("chain lattice" | "square lattice" | "simple cubic lattice"), L, T, BETA, J,
+ * Jz, Jxy, h, FORCE_SCATTER, SWEEPS, THERMALIZATION, SEED, INITIAL_SPINS ("up" | "random"),
+ * DISABLE_IMPROVED_ESTIMATOR.  Unknown keys are ignored, as ALPS does for keys a worker does not
+ * read.  Returns LG_EINVAL with a message on a malformed value. */
+int lg_params_parse(const char* text, lg_params* p);
+
+/* ---- observables -------------------------------------------------------------------------
+ * Names follow the reference's ObservableSet entries (energy.h:79-84, susceptibility.h:200-254
+ * and :303-335, path_integral.C:832-861) and the evaluators (energy.h:89-101,
+ * susceptibility.h:340-374).  With the improved estimator (no field) the (Staggered)
+ * Magnetization^2/^4 and Susceptibility entries are the improved ones; with a field they are
+ * the normal estimators. */
+enum {
+  LG_OBS_ENERGY = 0,                 /* "Energy"                                  */
+  LG_OBS_ENERGY_DENSITY,             /* "Energy Density"                          */
+  LG_OBS_ENERGY2,                    /* "Energy^2"                                */
+  LG_OBS_SPECIFIC_HEAT,              /* "Specific Heat" (evaluator)               */
+  LG_OBS_MAGNETIZATION,              /* "Magnetization"                           */
+  LG_OBS_ABS_MAGNETIZATION,          /* "|Magnetization|"                         */
+  LG_OBS_MAGNETIZATION2,             /* "Magnetization^2"                         */
+  LG_OBS_MAGNETIZATION4,             /* "Magnetization^4"                         */
+  LG_OBS_SUSCEPTIBILITY,             /* "Susceptibility"                          */
+  LG_OBS_STAG_MAGNETIZATION2,        /* "Staggered Magnetization^2"               */
+  LG_OBS_STAG_MAGNETIZATION4,        /* "Staggered Magnetization^4"               */
+  LG_OBS_STAG_SUSCEPTIBILITY,        /* "Staggered Susceptibility"                */
+  LG_OBS_GEN_MAGNETIZATION2,         /* "Generalized Magnetization^2" (improved)  */
+  LG_OBS_GEN_SUSCEPTIBILITY,         /* "Generalized Susceptibility" (improved)   */
+  LG_OBS_NUM_CLUSTERS,               /* "Number of Clusters"                      */
+  LG_OBS_NUM_OPERATORS,              /* operator count n_v (weight_parameter)     */
+  LG_OBS_BINDER,                     /* "Binder Ratio of Magnetization"           */
+  LG_OBS_STAG_BINDER,                /* "Binder Ratio of Staggered Magnetization" */
+  LG_NUM_OBS
+};
+
+typedef struct lg_obs {
+  uint64_t count;                    /* measured sweeps                                         */
+  double beta, volume;               /* "Inverse Temperature", "Volume"                        */
+  int improved;                      /* 1 if the improved estimator is in use                  */
+  double mean[LG_NUM_OBS];
+  double error[LG_NUM_OBS];          /* binning error (largest level with >= 64 bins)          */
+  double tau[LG_NUM_OBS];            /* integrated autocorrelation time estimate               */
+} lg_obs;
+
+/* Observable name (the reference's ObservableSet key) for an LG_OBS_* index. */
+const char* lg_obs_name(int index);
+
+/* ---- one chain: the loop_worker interface ------------------------------------------------- */
+typedef struct lg_chain lg_chain;
+
+/* loop_worker::loop_worker(alps::Parameters const&)   (path_integral.C:202-305) */
+int lg_create(const lg_params* p, lg_chain** out);
+/* ~loop_worker   (path_integral.C:73-89) */
+int lg_destroy(lg_chain* c);
+/* loop_worker::run(ObservableSet&) called nsweeps times: one sweep of update + measurement each
+ * (path_integral.C:323-351 -> dispatch :355-864). */
+int lg_run(lg_chain* c, int64_t nsweeps);
+/* loop_worker::is_thermalized() / progress()   (path_integral.C:92-93, montecarlo.h:58-61) */
+int lg_is_thermalized(const lg_chain* c);
+double lg_progress(const lg_chain* c);
+/* ObservableSet contents after the runs so far (init_observables :307-321 + evaluators). */
+int lg_observables(lg_chain* c, lg_obs* out);
+/* loop_worker::save / load (path_integral.C:111-124): mcs, spins, operator string.
+ * lg_save with buf == NULL stores the required size in *size. */
+int lg_save(lg_chain* c, void* buf, size_t* size);
+int lg_load(lg_chain* c, const void* buf, size_t size);
+/* Exchange Monte Carlo hooks (path_integral.C:97-109). */
+int lg_set_beta(lg_chain* c, double beta);
+double lg_weight_parameter(lg_chain* c);
+double lg_log_weight(double gw, double beta);
+/* Message of the last failure on this thread. */
+int lg_last_error(char* buf, size_t n);
+
+/* ---- test seams --------------------------------------------------------------------------
+ * Persistent configuration: spins at tau = 0 (0 up, 1 down) and the off-diagonal operators
+ * (bond, FP64 time in [0,1)), time ordered.  *n receives the operator count. */
+int lg_get_state(lg_chain* c, int32_t* spins, int32_t* bonds, double* times, int64_t cap,
+                 int64_t* n);
+int lg_set_state(lg_chain* c, const int32_t* spins, const int32_t* bonds, const double* times,
+                 int64_t n, uint64_t sweep);
+/* Raw per-sweep measurement records (LG_RECORD_WORDS uint64 each, exact integer sums) of every
+ * sweep run so far whose records have not been fetched, oldest first. */
+#define LG_RECORD_WORDS 32
+int lg_fetch_records(lg_chain* c, uint64_t* out, int64_t cap, int64_t* n);
+/* Keep raw records for lg_fetch_records (off by default). */
+int lg_keep_records(lg_chain* c, int on);
+
+/* Cluster labels of a given cluster-construction configuration, computed on the GPU by the
+ * segment union-find.  The configuration is a time-ordered vertex list (bond, graph 0..3) on a
+ * periodic lattice.  Labels follow the reference's fragment numbering and id assignment
+ * (graph_impl.h:285-288, path_integral.C:482, union_find.h:324-343 with the deterministic
+ * unify of union_find.h:231-233): fragment i < N is the bottom of site i, fragment N + k the
+ * k-th graph-0 vertex in time order; ids increase with the smallest fragment index of a cluster.
+ * labels must hold N + (number of graph-0 vertices) entries. */
+int lg_uf_label(int lattice, int L, int64_t nops, const int32_t* bonds, const int32_t* graphs,
+                int32_t* labels, int64_t cap, int64_t* nfrag, int64_t* nc);
+
+/* ---- batched chains: many independent chains in one ragged arena -------------------------- */
+typedef struct lg_batch lg_batch;
+int lg_batch_create(int n, const lg_params* p, lg_batch** out);
+int lg_batch_destroy(lg_batch* b);
+/* nsweeps sweeps of every chain (each chain stops at THERMALIZATION + SWEEPS). */
+int lg_batch_run(lg_batch* b, int64_t nsweeps);
+int lg_batch_observables(lg_batch* b, int chain, lg_obs* out);
+int lg_batch_size(const lg_batch* b);
+/* Total sites and sweeps done so far (for throughput accounting). */
+int lg_batch_stats(const lg_batch* b, int64_t* total_sites, int64_t* site_sweeps);
+/* Access one chain of a batch through the single-chain test seams. */
+lg_chain* lg_batch_chain(lg_batch* b, int i);
+
+/* ---- measurement seams (benchmarks) -------------------------------------------------------
+ * Run n sweeps of every chain of a handle (as lg_run / lg_batch_run), each sweep bracketed by
+ * CUDA events on the engine's own stream, with a device write of flush_bytes (an L2 flush)
+ * between sweeps outside the brackets.  ms[i] receives the device time of sweep i. */
+int lg_time_sweeps(lg_chain* c, int64_t n, size_t flush_bytes, float* ms);
+int lg_batch_time_sweeps(lg_batch* b, int64_t n, size_t flush_bytes, float* ms);
+/* Per-kernel profile: n sweeps launched kernel by kernel with an event after every launch;
+ * kernel_ms[k] accumulates the device time of kernel k (lg_num_kernels() entries), *vertices
+ * the operators processed (summed over sweeps and chains). */
+int lg_profile_sweeps(lg_chain* c, int64_t n, size_t flush_bytes, double* kernel_ms,
+                      int64_t* vertices);
+int lg_batch_profile_sweeps(lg_batch* b, int64_t n, size_t flush_bytes, double* kernel_ms,
+                            int64_t* vertices);
+int lg_num_kernels(void);
+const char* lg_kernel_name(int k);
+
+/* ---- build / device info ------------------------------------------------------------------ */
+/* Number of device kernel launches issued by this process so far (all handles). */
+uint64_t lg_kernel_launches(void);
+/* Version string (engine and CUDA). */
+const char* lg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LOOPER_GPU_H */

@@ -1,0 +1,71 @@
+"""The C-ABI library builds, loads and exports every entry point of include/looper_gpu.h.
+
+No device work here: only host-side entry points (parameter defaults/parsing, names) are called.
+"""
+import ctypes
+import math
+import os
+import subprocess
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lg():
+    sys.path.insert(0, os.path.join(REPO, "alps-looper_gb300"))
+    import build as b
+    b.build()
+    import looper_gb300 as m
+    return m
+
+
+def test_exports_every_declared_symbol(lg):
+    names = lg.exported_symbols()
+    assert len(names) >= 25
+    L = ctypes.CDLL(lg.LIB_PATH)
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_nm_dynamic_symbols(lg):
+    out = subprocess.run(["nm", "-D", "--defined-only", lg.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    syms = {ln.split()[-1] for ln in out.splitlines() if ln.strip()}
+    for n in lg.exported_symbols():
+        assert n in syms, n
+
+
+def test_params_defaults_follow_reference(lg):
+    p = lg.make_params()
+    assert p.lattice == lg.CHAIN and p.L == 8 and p.sweeps == 65536
+    assert p.thermalization == -1  # SWEEPS/8 (montecarlo.h:41-45)
+    assert math.isnan(p.Jz) and math.isnan(p.Jxy)
+
+
+def test_params_parse_alps_keys(lg):
+    p = lg.parse_params('LATTICE = "square lattice"; L = 128\nT = 1/64 # comment\nJ = 1;\n'
+                        'SWEEPS = 8192; THERMALIZATION = 1024; SEED = 7\nh = 0.3\nJz = 0.5\n'
+                        'INITIAL_SPINS = random')
+    assert p.lattice == lg.SQUARE and p.L == 128
+    assert p.T == pytest.approx(1 / 64)
+    assert p.sweeps == 8192 and p.thermalization == 1024 and p.seed == 7
+    assert p.h == 0.3 and p.Jz == 0.5 and math.isnan(p.Jxy) and p.init_spins == 1
+
+
+def test_params_parse_rejects_bad_values(lg):
+    with pytest.raises(lg.LoopError) as e:
+        lg.parse_params("L = abc")
+    assert e.value.code == -1
+    with pytest.raises(lg.LoopError) as e:
+        lg.parse_params('LATTICE = "triangular lattice"')
+    assert e.value.code == -4
+
+
+def test_obs_names_match_reference_keys(lg):
+    names = lg.obs_names()
+    for key in ("Energy", "Energy Density", "Specific Heat", "Susceptibility",
+                "Staggered Magnetization^2", "Staggered Susceptibility", "Number of Clusters"):
+        assert key in names
