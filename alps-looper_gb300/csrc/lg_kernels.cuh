@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256) k_insert(Arena A) {
       const uint32_t wg = (k & 1u) ? r.w : r.y;
       ++k;
       const float gap = __fmul_rn(-log_open(uniform_open(wu)), ch.inv_rate);
-      const uint64_t q = gap_fix52(gap);
+      const uint64_t q = gap_fix52(gap, ((uint64_t)(wu & 0x1FFu) << 16) | (wg & 0xFFFFu));
       if (q >= FIX52_ONE) { more = false; return; }
       tq += q;
       if (tq >= FIX52_ONE) { more = false; return; }

@@ -87,8 +87,10 @@ __device__ __forceinline__ float exp_clamped(float x) {
 constexpr uint64_t FIX52_ONE = 1ull << 52;
 constexpr uint64_t TIME_INF = ~0ull;  // sorts after every time bit pattern in [0,1)
 
-// floor(g * 2^52) for a float 0 <= g < 1; returns FIX52_ONE when g >= 1.
-__device__ __forceinline__ uint64_t gap_fix52(float g) {
+// Gap g (float, 0 <= g < 1) on the 2^-52 grid: floor(g * 2^52) with the bits below g's float
+// resolution taken from `dither`, which spreads the gap uniformly over its float ulp (times stay
+// continuous at 2^-52 and two gaps coincide only with probability ~2^-52).  FIX52_ONE if g >= 1.
+__device__ __forceinline__ uint64_t gap_fix52(float g, uint64_t dither) {
   uint32_t b = __float_as_uint(g);
   uint32_t ex = (b >> 23) & 0xFFu;
   if (ex == 0) return 0;
@@ -96,7 +98,8 @@ __device__ __forceinline__ uint64_t gap_fix52(float g) {
   if (e >= 0) return FIX52_ONE;
   uint64_t m = (uint64_t)((b & 0x7FFFFFu) | 0x800000u);
   int sh = e + 29;
-  return sh >= 0 ? (m << sh) : (m >> (-sh));
+  if (sh < 0) return m >> (-sh);
+  return (m << sh) | (dither & ((1ull << sh) - 1));
 }
 
 // Bit pattern of the FP64 value k * 2^-52 (exact for k < 2^52).

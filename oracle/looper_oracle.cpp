@@ -134,8 +134,10 @@ static float exp_spec(float x) {
 
 static const uint64_t FIX52_ONE = 1ull << 52;
 
-// floor(g * 2^52) for a non-negative float g < 1; *ge1 is set when g >= 1.
-static uint64_t float_to_fix52(float g, bool* ge1) {
+// floor(g * 2^52) for a non-negative float g < 1, with the bits below the float's own
+// resolution filled from `dither` (a uniform spread of the gap over its float ulp, so that
+// times are continuous on the 2^-52 grid); *ge1 is set when g >= 1.
+static uint64_t float_to_fix52(float g, uint64_t dither, bool* ge1) {
   uint32_t b = f_bits(g);
   *ge1 = false;
   uint32_t ex = (b >> 23) & 0xFFu;
@@ -144,7 +146,8 @@ static uint64_t float_to_fix52(float g, bool* ge1) {
   if (e >= 0) { *ge1 = true; return 0; }
   uint64_t m = (uint64_t)((b & 0x7FFFFFu) | 0x800000u);
   int sh = e + 29;
-  return sh >= 0 ? (m << sh) : (m >> (-sh));
+  if (sh < 0) return m >> (-sh);
+  return (m << sh) | (dither & ((1ull << sh) - 1));
 }
 
 // Exact FP64 value of k * 2^-52 (k < 2^52).
@@ -362,7 +365,8 @@ struct chain_t {
           uint32_t wu = w[(k & 1) * 2], wg = w[(k & 1) * 2 + 1];
           float gap = -log_spec(uniform_open(wu)) * inv_rate;
           bool ge1;
-          uint64_t q = float_to_fix52(gap, &ge1);
+          uint64_t dither = ((uint64_t)(wu & 0x1FFu) << 16) | (wg & 0xFFFFu);
+          uint64_t q = float_to_fix52(gap, dither, &ge1);
           if (ge1) break;
           tq += q;
           if (tq >= FIX52_ONE) break;
@@ -720,12 +724,12 @@ void orc_clear_records(void* h) { static_cast<orc::chain_t*>(h)->records.clear()
 int orc_get_state(void* h, int* spins, int* bonds, double* times, int cap) {
   orc::chain_t* c = static_cast<orc::chain_t*>(h);
   for (int s = 0; s < c->lat.N; ++s) spins[s] = c->spins[s];
-  int n = 0;
-  for (auto& o : c->ops) {
-    if (!o.offdiag) continue;
-    if (n < cap) { bonds[n] = o.bond; times[n] = o.t; }
-    ++n;
-  }
+  std::vector<std::pair<uint64_t, int>> v;
+  for (auto& o : c->ops)
+    if (o.offdiag) v.push_back({orc::d_bits(o.t), o.bond});
+  std::sort(v.begin(), v.end());  // (time, bond)
+  int n = (int)v.size();
+  for (int i = 0; i < n && i < cap; ++i) { bonds[i] = v[i].second; times[i] = orc::bits_d(v[i].first); }
   return n;
 }
 
