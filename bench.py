@@ -240,7 +240,7 @@ def run_ours(args, dist, ws, rank, local):
            "scope": "lg_create + lg_run(steps) + lg_observables from a cold start"}
     e.close()
     cpu = None
-    if rank == 0:
+    if rank == 0 and args.cpu_seconds > 0:
         state = w.state()
         rate, n, el = cpu_port_rate(seconds=args.cpu_seconds, threads=1, state=state)
         cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
