@@ -28,13 +28,12 @@
 using namespace lg;
 
 // kernel launches in one sweep (enqueue_sweep)
-static const int kSweepLaunches = 19;
+static const int kSweepLaunches = 18;
 // timed stages of one sweep, in launch order (an event is recorded after each stage)
-static const int kNumStages = 11;
+static const int kNumStages = 10;
 static const char* kStageNames[kNumStages] = {
     "k_begin+k_insert<count>", "scan(bonds)", "k_insert<write>", "k_site_count+scan(sites)",
-    "k_merge", "k_union", "k_compress", "k_accumulate", "k_cluster", "k_flip_vertex",
-    "k_site_end+k_end"};
+    "k_merge", "k_union", "k_accumulate", "k_cluster", "k_flip_vertex", "k_site_end+k_end"};
 
 static std::atomic<uint64_t> g_launches{0};
 static thread_local std::string g_err;
@@ -265,6 +264,9 @@ struct Engine {
         (rc = d_cls.alloc(4 * (size_t)new_ns)) || (rc = d_cnt0.alloc(4 * (size_t)new_ns)) ||
         (rc = d_rec.alloc((size_t)rec_rows * C * REC_WORDS)))
       return rc;
+    // cluster class sums must start at zero (k_cluster clears what it consumes)
+    LG_CUDA(cudaMemset(d_cls.p, 0, 4 * (size_t)new_ns * sizeof(unsigned long long)));
+    LG_CUDA(cudaMemset(d_cnt0.p, 0, 4 * (size_t)new_ns * sizeof(unsigned int)));
     if (keep) {
       LG_CUDA(cudaMemcpy(d_stime.p, old_t.p, keep_n * sizeof(uint64_t), cudaMemcpyDeviceToDevice));
       LG_CUDA(cudaMemcpy(d_sdir.p, old_d.p, keep_n, cudaMemcpyDeviceToDevice));
@@ -317,23 +319,21 @@ struct Engine {
     mark(2);
     k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
     scan(d_site_cnt.p, d_sbase.p, N, &ctl->ns_total, ns_cap, 1, 0, ev ? ev + 3 : nullptr);
-    k_merge<<<grid_for(N, 128, 16), 128, 0, st>>>(A);
+    k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A);
     mark(4);
     k_union<<<grid_for(nv_cap, 256), 256, 0, st>>>(A);
     mark(5);
-    k_compress<<<grid_for(ns_cap, 256), 256, 0, st>>>(A);
-    mark(6);
     k_accumulate<<<grid_for(ns_cap, 256), 256, 0, st>>>(A);
+    mark(6);
+    k_cluster<<<grid_for((ns_cap + CL_TILE - 1) / CL_TILE * (long long)CL_THREADS, CL_THREADS), CL_THREADS, 0, st>>>(A);
     mark(7);
-    k_cluster<<<grid_for(ns_cap, 256), 256, 0, st>>>(A);
-    mark(8);
     k_flip_vertex<<<grid_for(nv_cap, 256), 256, 0, st>>>(A);
-    mark(9);
-    k_site_end<<<grid_for(N, 128, 16), 128, 0, st>>>(A);
+    mark(8);
+    k_site_end<<<grid_for((long long)N * 32, 256, 16), 256, 0, st>>>(A);
     k_end<<<grid_for(C, 128), 128, 0, st>>>(A);
     k_step<<<1, 1, 0, st>>>(ctl);
-    mark(10);
-    g_launches += 13;
+    mark(9);
+    g_launches += 12;
   }
 
   int ensure_graph() {
@@ -618,7 +618,7 @@ struct Engine {
     Arena A = arena();
     k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
     scan(d_site_cnt.p, d_sbase.p, N, &d_ctl.p->ns_total, ns_cap, 1, 0);
-    k_merge<<<grid_for(N, 128, 16), 128, 0, st>>>(A);
+    k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A);
     k_union<<<grid_for(nops, 256), 256, 0, st>>>(A);
     k_compress<<<grid_for(2 * nops + N, 256), 256, 0, st>>>(A);
     g_launches += 4;

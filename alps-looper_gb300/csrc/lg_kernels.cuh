@@ -297,69 +297,184 @@ __global__ void k_site_count(Arena A) {
 // tau = 0) and carries the spin after that endpoint.  Ties: (time, off-diagonal first, bond).
 // Also: union-find initialisation and the temporal closure (top segment hooked to the bottom,
 // path_integral.C:584-589).
-__global__ void __launch_bounds__(128) k_merge(Arena A) {
+//
+// One warp per site.  The incident lists (<= MERGE_CAP endpoints) are staged in shared memory;
+// every endpoint finds its merged rank by binary search in the other lists (no sequential
+// merge), the spins follow from a warp prefix-XOR of the off-diagonal flags in merged order, and
+// the segment arrays are written coalesced.  Sites with more endpoints use the one-thread merge.
+constexpr int MERGE_WARPS = 4;
+constexpr int MERGE_CAP = 768;
+
+// number of entries of list [lo, hi) ordered before key (t, dg); `inclusive` counts equal keys
+__device__ __forceinline__ int merge_count(const uint64_t* T, const uint8_t* Cd, int lo, int hi,
+                                           uint64_t t, uint8_t dg, bool inclusive) {
+  int a = lo, b = hi;
+  while (a < b) {
+    const int m = (a + b) >> 1;
+    const uint64_t tm = T[m];
+    const uint8_t dm = (uint8_t)(~Cd[m] & 1u);
+    const bool before = tm < t || (tm == t && (dm < dg || (inclusive && dm == dg)));
+    if (before) a = m + 1; else b = m;
+  }
+  return a - lo;
+}
+
+__device__ void merge_site_serial(Arena& A, int s) {
+  const int j0 = A.inc_off[s];
+  const int z = A.inc_off[s + 1] - j0;
+  const int base = A.sbase[s];
+  const int k = A.sbase[s + 1] - base - 1;
+  const uint8_t gneg = A.gauge[s] < 0 ? SI_GNEG : 0;
+  int cur[MAXZ], end[MAXZ];
+  uint64_t ht[MAXZ];
+  uint8_t hc[MAXZ], side[MAXZ];
+#pragma unroll
+  for (int d = 0; d < MAXZ; ++d) {
+    if (d < z) {
+      const int b = A.inc[j0 + d];
+      cur[d] = A.bond_ptr[b];
+      end[d] = A.bond_ptr[b + 1];
+      side[d] = A.inc_side[j0 + d];
+      ht[d] = cur[d] < end[d] ? A.vtime[cur[d]] : TIME_INF;
+      hc[d] = cur[d] < end[d] ? A.vcode[cur[d]] : 0;
+    } else {
+      cur[d] = end[d] = 0; ht[d] = TIME_INF; hc[d] = 0; side[d] = 0;
+    }
+  }
+  uint8_t spin = A.spin0[s];
+  A.stime[base] = 0ull;
+  A.sinfo[base] = (uint8_t)(spin | gneg | SI_FIRST | (k == 0 ? SI_LAST : 0));
+  A.svert[base] = -1;
+  A.sdir[base] = 0xFF;
+  A.parent[base] = base;
+  for (int j = 1; j <= k; ++j) {
+    int best = 0;
+    uint64_t bt = ht[0];
+    uint8_t bdiag = (uint8_t)(~hc[0] & 1u);
+#pragma unroll
+    for (int d = 1; d < MAXZ; ++d) {
+      const uint8_t dg = (uint8_t)(~hc[d] & 1u);
+      if (ht[d] < bt || (ht[d] == bt && dg < bdiag)) { best = d; bt = ht[d]; bdiag = dg; }
+    }
+    const int x = base + j;
+    int v = 0;
+    uint8_t sd = 0, code = 0;
+#pragma unroll
+    for (int d = 0; d < MAXZ; ++d) {
+      if (d == best) {
+        v = cur[d]; sd = side[d]; code = hc[d];
+        ++cur[d];
+        ht[d] = cur[d] < end[d] ? A.vtime[cur[d]] : TIME_INF;
+        hc[d] = cur[d] < end[d] ? A.vcode[cur[d]] : 0;
+      }
+    }
+    if (code & 1u) spin ^= 1u;
+    A.stime[x] = bt;
+    A.sinfo[x] = (uint8_t)(spin | gneg | (j == k ? SI_LAST : 0));
+    A.svert[x] = v;
+    A.sdir[x] = (uint8_t)best;
+    A.parent[x] = x;
+    A.vslot[2 * v + sd] = x;
+  }
+  if (k > 0) A.parent[base + k] = base;
+}
+
+__global__ void __launch_bounds__(MERGE_WARPS * 32) k_merge(Arena A) {
   if (A.ctl->err) return;
-  LG_GRID_STRIDE(s, A.N) {
+  __shared__ uint64_t sT[MERGE_WARPS][MERGE_CAP];   // staged times, list by list
+  __shared__ uint8_t sC[MERGE_WARPS][MERGE_CAP];    // staged codes
+  __shared__ uint16_t mE[MERGE_WARPS][MERGE_CAP];   // merged order -> staged index
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < A.N; s += warps) {
     const int j0 = A.inc_off[s];
     const int z = A.inc_off[s + 1] - j0;
     const int base = A.sbase[s];
     const int k = A.sbase[s + 1] - base - 1;
-    const uint8_t gneg = A.gauge[s] < 0 ? SI_GNEG : 0;
-    int cur[MAXZ], end[MAXZ];
-    uint64_t ht[MAXZ];
-    uint8_t hc[MAXZ], side[MAXZ];
+    const int c = A.site_chain[s];
+    if (lane == 0) {
+      if (s == A.ch[c].site_off) A.ch_slot_off[c] = base;
+      if (s == A.N - 1) A.ch_slot_off[A.C] = base + k + 1;
+    }
+    if (k > MERGE_CAP) {
+      if (lane == 0) merge_site_serial(A, s);
+      __syncwarp();
+      continue;
+    }
+    // stage the incident lists: list d occupies [off[d], off[d+1])
+    int off[MAXZ + 1];
+    int ptr[MAXZ];
+    off[0] = 0;
 #pragma unroll
     for (int d = 0; d < MAXZ; ++d) {
       if (d < z) {
         const int b = A.inc[j0 + d];
-        cur[d] = A.bond_ptr[b];
-        end[d] = A.bond_ptr[b + 1];
-        side[d] = A.inc_side[j0 + d];
-        ht[d] = cur[d] < end[d] ? A.vtime[cur[d]] : TIME_INF;
-        hc[d] = cur[d] < end[d] ? A.vcode[cur[d]] : 0;
+        ptr[d] = A.bond_ptr[b];
+        off[d + 1] = off[d] + (A.bond_ptr[b + 1] - ptr[d]);
       } else {
-        cur[d] = end[d] = 0; ht[d] = TIME_INF; hc[d] = 0; side[d] = 0;
+        ptr[d] = 0; off[d + 1] = off[d];
       }
     }
-    uint8_t spin = A.spin0[s];
-    A.stime[base] = 0ull;
-    A.sinfo[base] = (uint8_t)(spin | gneg | SI_FIRST | (k == 0 ? SI_LAST : 0));
-    A.svert[base] = -1;
-    A.sdir[base] = 0xFF;
-    A.parent[base] = base;
-    for (int j = 1; j <= k; ++j) {
-      int best = 0;
-      uint64_t bt = ht[0];
-      uint8_t bdiag = (uint8_t)(~hc[0] & 1u);
 #pragma unroll
-      for (int d = 1; d < MAXZ; ++d) {
-        const uint8_t dg = (uint8_t)(~hc[d] & 1u);
-        if (ht[d] < bt || (ht[d] == bt && dg < bdiag)) { best = d; bt = ht[d]; bdiag = dg; }
+    for (int d = 0; d < MAXZ; ++d) {
+      for (int i = lane; i < off[d + 1] - off[d]; i += 32) {
+        sT[w][off[d] + i] = A.vtime[ptr[d] + i];
+        sC[w][off[d] + i] = A.vcode[ptr[d] + i];
       }
-      const int x = base + j;
-      int v = 0;
-      uint8_t sd = 0, code = 0;
-#pragma unroll
-      for (int d = 0; d < MAXZ; ++d) {
-        if (d == best) {
-          v = cur[d]; sd = side[d]; code = hc[d];
-          ++cur[d];
-          ht[d] = cur[d] < end[d] ? A.vtime[cur[d]] : TIME_INF;
-          hc[d] = cur[d] < end[d] ? A.vcode[cur[d]] : 0;
-        }
-      }
-      if (code & 1u) spin ^= 1u;
-      A.stime[x] = bt;
-      A.sinfo[x] = (uint8_t)(spin | gneg | (j == k ? SI_LAST : 0));
-      A.svert[x] = v;
-      A.sdir[x] = (uint8_t)best;
-      A.parent[x] = x;
-      A.vslot[2 * v + sd] = x;
     }
-    if (k > 0) A.parent[base + k] = base;  // closure: top segment joins the bottom one
-    const int c = A.site_chain[s];
-    if (s == A.ch[c].site_off) A.ch_slot_off[c] = base;
-    if (s == A.N - 1) A.ch_slot_off[A.C] = base + k + 1;
+    __syncwarp();
+    // merged rank of every endpoint
+    for (int e = lane; e < k; e += 32) {
+      int d = 0;
+#pragma unroll
+      for (int q = 1; q < MAXZ; ++q) if (e >= off[q]) d = q;
+      const uint64_t t = sT[w][e];
+      const uint8_t dg = (uint8_t)(~sC[w][e] & 1u);
+      int r = 0;
+#pragma unroll
+      for (int q = 0; q < MAXZ; ++q) {
+        if (q == d) r += e - off[q];
+        else if (off[q + 1] > off[q]) r += merge_count(sT[w], sC[w], off[q], off[q + 1], t, dg, q < d);
+      }
+      mE[w][r] = (uint16_t)e;
+    }
+    __syncwarp();
+    // segments: prefix XOR of off-diagonal flags gives each segment's spin
+    const uint8_t gneg = A.gauge[s] < 0 ? SI_GNEG : 0;
+    uint32_t carry = A.spin0[s];
+    if (lane == 0) {
+      A.stime[base] = 0ull;
+      A.sinfo[base] = (uint8_t)(carry | gneg | SI_FIRST | (k == 0 ? SI_LAST : 0));
+      A.svert[base] = -1;
+      A.sdir[base] = 0xFF;
+      A.parent[base] = base;
+    }
+    for (int r0 = 0; r0 < k; r0 += 32) {
+      const int r = r0 + lane;
+      const bool ok = r < k;
+      const int e = ok ? mE[w][r] : 0;
+      const uint8_t cd = ok ? sC[w][e] : 0;
+      const unsigned ball = __ballot_sync(0xFFFFFFFFu, ok && (cd & 1u));
+      const uint32_t spin = carry ^ (__popc(ball & (0xFFFFFFFFu >> (31 - lane))) & 1u);
+      if (ok) {
+        int d = 0;
+#pragma unroll
+        for (int q = 1; q < MAXZ; ++q) if (e >= off[q]) d = q;
+        int pd = 0, od = 0;
+#pragma unroll
+        for (int q = 0; q < MAXZ; ++q) if (q == d) { pd = ptr[q]; od = off[q]; }
+        const int v = pd + (e - od);
+        const int x = base + 1 + r;
+        A.stime[x] = sT[w][e];
+        A.sinfo[x] = (uint8_t)(spin | gneg | (r == k - 1 ? SI_LAST : 0));
+        A.svert[x] = v;
+        A.sdir[x] = (uint8_t)d;
+        A.parent[x] = (r == k - 1) ? base : x;  // closure: top segment joins the bottom one
+        A.vslot[2 * v + A.inc_side[j0 + d]] = x;
+      }
+      carry ^= __popc(ball) & 1u;
+    }
+    __syncwarp();
   }
 }
 
@@ -433,21 +548,87 @@ __global__ void __launch_bounds__(256) k_compress(Arena A) {
   }
 }
 
-// Per segment: its length in 2^-40 units goes to one of four class sums of its cluster,
-// class = (spin, gauge sign).  Bottom segments also count into the tau = 0 class counts.
-// These eight integers per cluster determine every improved estimator of
-// susceptibility.h:96-156 and the field weight of cluster.h:54-59.
+// Per segment: find its cluster root (and store it: parent := root), then add the segment's
+// length in 2^-40 units to one of four class sums of the root, class = (spin, gauge sign).
+// Bottom segments also count into the tau = 0 class counts.  These eight integers per cluster
+// determine every improved estimator of susceptibility.h:96-156 and the field weight of
+// cluster.h:54-59.
+//
+// At low temperature a few clusters own a large share of all segments, so the additions are
+// combined before they reach global memory: lanes of a warp with the same (root, class) are
+// summed with match_any + redux, and each block keeps a shared-memory hash of (root, class) sums
+// for its tile of ACC_TILE consecutive segments, flushed with one global atomic per entry.
+// The class sums are zero on entry: k_cluster clears what it consumes.
+constexpr int ACC_TILE = 1024;
+constexpr int ACC_HASH = 1024;   // power of two
+
+__device__ __forceinline__ unsigned long long group_sum_u48(unsigned mask, unsigned long long v) {
+  unsigned long long s = 0;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const unsigned limb = (unsigned)((v >> (16 * q)) & 0xFFFFull);
+    s += (unsigned long long)__reduce_add_sync(mask, limb) << (16 * q);
+  }
+  return s;
+}
+
 __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
   if (A.ctl->err) return;
+  __shared__ int hkey[ACC_HASH];
+  __shared__ unsigned long long hval[ACC_HASH * 4];
   const int ns = A.ctl->ns_total;
-  LG_GRID_STRIDE(x, ns) {
-    const uint8_t info = A.sinfo[x];
-    const int64_t ta = bits_fix40(A.stime[x]);
-    const int64_t tb = (info & SI_LAST) ? ((int64_t)1 << 40) : bits_fix40(A.stime[x + 1]);
-    const int q = (info & SI_SPIN) * 2 + ((info & SI_GNEG) ? 1 : 0);
-    const int r = A.parent[x];
-    atomicAdd(A.cls + 4 * (size_t)r + q, (unsigned long long)(tb - ta));
-    if (info & SI_FIRST) atomicAdd(A.cnt0 + 4 * (size_t)r + q, 1u);
+  const int ntiles = (ns + ACC_TILE - 1) / ACC_TILE;
+  const int lane = threadIdx.x & 31;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (int i = threadIdx.x; i < ACC_HASH; i += blockDim.x) {
+      hkey[i] = -1;
+      hval[4 * i] = hval[4 * i + 1] = hval[4 * i + 2] = hval[4 * i + 3] = 0ull;
+    }
+    __syncthreads();
+    const int t0 = tile * ACC_TILE;
+    for (int i = threadIdx.x; i < ACC_TILE; i += blockDim.x) {
+      const int x = t0 + i;
+      const bool valid = x < ns;
+      int root = 0, q = 0;
+      unsigned long long len = 0;
+      if (valid) {
+        int r = x, p = A.parent[x];
+        while (p != r) { r = p; p = A.parent[r]; }
+        if (r != x) A.parent[x] = r;
+        root = r;
+        const uint8_t info = A.sinfo[x];
+        const int64_t ta = bits_fix40(A.stime[x]);
+        const int64_t tb = (info & SI_LAST) ? ((int64_t)1 << 40) : bits_fix40(A.stime[x + 1]);
+        len = (unsigned long long)(tb - ta);
+        q = (info & SI_SPIN) * 2 + ((info & SI_GNEG) ? 1 : 0);
+        if (info & SI_FIRST) atomicAdd(A.cnt0 + 4 * (size_t)r + q, 1u);
+      }
+      const unsigned long long key = valid ? (((unsigned long long)root << 2) | (unsigned)q) : ~0ull;
+      const unsigned mask = __match_any_sync(0xFFFFFFFFu, key);
+      const unsigned long long sum = group_sum_u48(mask, len);
+      if (valid && lane == __ffs(mask) - 1 && sum) {
+        unsigned h = ((unsigned)root * 2654435761u) >> 22;  // 10-bit hash
+        bool done = false;
+        for (int probe = 0; probe < 32; ++probe) {
+          const int k = atomicCAS(hkey + h, -1, root);
+          if (k == -1 || k == root) { atomicAdd(hval + 4 * h + q, sum); done = true; break; }
+          h = (h + 1) & (ACC_HASH - 1);
+        }
+        if (!done) atomicAdd(A.cls + 4 * (size_t)root + q, sum);
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < ACC_HASH; i += blockDim.x) {
+      const int k = hkey[i];
+      if (k >= 0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const unsigned long long v = hval[4 * i + q];
+          if (v) atomicAdd(A.cls + 4 * (size_t)k + q, v);
+        }
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -493,97 +674,187 @@ __device__ __forceinline__ u128 warp_sum_u128(u128 v) {
   return s;
 }
 
+__device__ __forceinline__ int chain_of_segment(const Arena& A, int x) {
+  int lo = 0, hi = A.C - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (A.ch_slot_off[mid] <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// The 18 per-sweep sums a cluster root contributes to its chain's record.
+struct RootSums {
+  unsigned long long q[10];  // R_NC, R_M0, R_SM0, R_M0SQ, R_N0SQ, R_SM0SQ, R_SN0SQ, R_FLD, R_MA, R_SMA
+  u128 w[8];                 // R_M0Q, R_N0Q, R_SM0Q, R_SN0Q, R_LSQ, R_MSQ, R_SLSQ, R_SMSQ
+};
+__device__ __constant__ int kRecQ[10] = {R_NC, R_M0, R_SM0, R_M0SQ, R_N0SQ, R_SM0SQ, R_SN0SQ,
+                                         R_FLD, R_MA, R_SMA};
+__device__ __constant__ int kRecW[8] = {R_M0Q, R_N0Q, R_SM0Q, R_SN0Q, R_LSQ, R_MSQ, R_SLSQ, R_SMSQ};
+constexpr int NLIMB = 10 * 4 + 8 * 8;  // 16-bit limbs of the sums
+
+__device__ __forceinline__ void add_u128(u128& a, u128 b) {
+  const unsigned long long lo = a.lo + b.lo;
+  a.hi += b.hi + (lo < a.lo ? 1ull : 0ull);
+  a.lo = lo;
+}
+
+// Flip decision and record contribution of root x of chain c; clears the root's class sums.
+__device__ __forceinline__ void root_sums(const Arena& A, int x, int c, RootSums& R) {
+  const DChain ch = A.ch[c];
+  unsigned long long* S = A.cls + 4 * (size_t)x;
+  unsigned* K = A.cnt0 + 4 * (size_t)x;
+  const long long s0 = (long long)S[0], s1 = (long long)S[1], s2 = (long long)S[2],
+                  s3 = (long long)S[3];
+  const long long k0 = K[0], k1 = K[1], k2 = K[2], k3 = K[3];
+  S[0] = S[1] = S[2] = S[3] = 0ull;
+  K[0] = K[1] = K[2] = K[3] = 0u;
+  const long long Ls = s0 + s1 + s2 + s3, Ms = s0 + s1 - s2 - s3;
+  const long long SLs = s0 - s1 + s2 - s3, SMs = s0 - s1 - s2 + s3;
+  const long long n0 = k0 + k1 + k2 + k3, m0 = k0 + k1 - k2 - k3;
+  const long long sn0 = k0 - k1 + k2 - k3, sm0 = k0 - k1 - k2 + k3;
+  const uint32_t key = (uint32_t)(x - A.ch_slot_off[c]);
+  const rnd4 r = philox(ch.seed, A.ch_sweep[c], key, TAG_FLIP, 0);
+  uint8_t f;
+  if (!ch.field) {
+    f = r.x < 0x80000000u ? 1 : 0;
+  } else {
+    const float xf = __fmul_rn(__ll2float_rn(Ms), ch.flip_coef);
+    const float e = exp_clamped(xf);
+    f = __fmul_rn(uniform_open(r.x), __fadd_rn(1.0f, e)) < 1.0f ? 1 : 0;
+  }
+  A.flip[x] = f;
+  R.q[0] = 1ull;
+  R.q[1] = (unsigned long long)m0;
+  R.q[2] = (unsigned long long)sm0;
+  R.q[3] = (unsigned long long)(m0 * m0);
+  R.q[4] = (unsigned long long)(n0 * n0);
+  R.q[5] = (unsigned long long)(sm0 * sm0);
+  R.q[6] = (unsigned long long)(sn0 * sn0);
+  R.q[7] = (unsigned long long)(f ? -Ms : Ms);
+  R.q[8] = (unsigned long long)Ms;
+  R.q[9] = (unsigned long long)SMs;
+  R.w[0] = mul64(R.q[3], R.q[3]);
+  R.w[1] = mul64(R.q[4], R.q[4]);
+  R.w[2] = mul64(R.q[5], R.q[5]);
+  R.w[3] = mul64(R.q[6], R.q[6]);
+  auto ab = [](long long v) { return (unsigned long long)(v < 0 ? -v : v); };
+  R.w[4] = mul64(ab(Ls), ab(Ls));
+  R.w[5] = mul64(ab(Ms), ab(Ms));
+  R.w[6] = mul64(ab(SLs), ab(SLs));
+  R.w[7] = mul64(ab(SMs), ab(SMs));
+}
+
+__device__ __forceinline__ void record_atomics(const Arena& A, int c, const RootSums& R) {
+  unsigned long long* row = rec_row(A, c);
+#pragma unroll
+  for (int i = 0; i < 10; ++i) if (R.q[i]) atomicAdd(row + kRecQ[i], R.q[i]);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) if (R.w[i].lo | R.w[i].hi) atomic_add_u128(row + kRecW[i], R.w[i]);
+}
+
 // Per cluster root: flip decision (path_integral.C:780-803) and the exact per-sweep sums of the
 // improved estimator collector (susceptibility.h:182-198), cluster count (:774-778), field
 // energy (:852-859) and the normal time-integrated magnetisations (susceptibility.h:283-297).
-__global__ void __launch_bounds__(256) k_cluster(Arena A) {
+// Each block handles tiles of CL_TILE consecutive segments; a tile inside one chain is reduced
+// in registers and shared memory (16-bit limbs, exact) and adds to the record once.
+constexpr int CL_TILE = 4096;
+constexpr int CL_THREADS = 256;
+
+__global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
   if (A.ctl->err) return;
+  __shared__ unsigned limbs[CL_THREADS / 32][NLIMB];
+  __shared__ unsigned long long tot[NLIMB];
+  __shared__ int roots[CL_TILE];
+  __shared__ int nroots;
   const int ns = A.ctl->ns_total;
-  const int lane = threadIdx.x & 31;
-  const int wstride = gridDim.x * blockDim.x;
-  for (int wbase = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; wbase < ns; wbase += wstride) {
-    const int x = wbase + lane;
-    const bool is_root = x < ns && A.parent[x] == x;
-    int c = 0;
-    unsigned long long q[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    u128 w[8];
+  const int ntiles = (ns + CL_TILE - 1) / CL_TILE;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int t0 = tile * CL_TILE;
+    const int t1 = min(t0 + CL_TILE, ns);
+    if (threadIdx.x == 0) nroots = 0;
+    __syncthreads();
+    // compact this tile's roots so that every lane works on one
+    for (int b = t0 + wid * 32; b < t1; b += blockDim.x) {
+      const int x = b + lane;
+      const bool r = x < t1 && A.parent[x] == x;
+      const unsigned ball = __ballot_sync(0xFFFFFFFFu, r);
+      int base = 0;
+      if (lane == 0 && ball) base = atomicAdd(&nroots, __popc(ball));
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (r) roots[base + __popc(ball & ((1u << lane) - 1u))] = x;
+    }
+    __syncthreads();
+    const int nr = nroots;
+    const int cf = chain_of_segment(A, t0), cl = chain_of_segment(A, t1 - 1);
+    const bool uniform = cf == cl;
+    RootSums acc;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) w[i] = {0, 0};
-    if (is_root) {
-      // chain of this segment (binary search over chain segment offsets)
-      int lo = 0, hi = A.C - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (A.ch_slot_off[mid] <= x) lo = mid; else hi = mid - 1;
-      }
-      c = lo;
-      const DChain ch = A.ch[c];
-      const unsigned long long* S = A.cls + 4 * (size_t)x;
-      const unsigned* K = A.cnt0 + 4 * (size_t)x;
-      const long long s0 = (long long)S[0], s1 = (long long)S[1], s2 = (long long)S[2],
-                      s3 = (long long)S[3];
-      const long long k0 = K[0], k1 = K[1], k2 = K[2], k3 = K[3];
-      const long long Ls = s0 + s1 + s2 + s3, Ms = s0 + s1 - s2 - s3;
-      const long long SLs = s0 - s1 + s2 - s3, SMs = s0 - s1 - s2 + s3;
-      const long long n0 = k0 + k1 + k2 + k3, m0 = k0 + k1 - k2 - k3;
-      const long long sn0 = k0 - k1 + k2 - k3, sm0 = k0 - k1 - k2 + k3;
-      const uint32_t key = (uint32_t)(x - A.ch_slot_off[c]);
-      const rnd4 r = philox(ch.seed, A.ch_sweep[c], key, TAG_FLIP, 0);
-      uint8_t f;
-      if (!ch.field) {
-        f = r.x < 0x80000000u ? 1 : 0;
+    for (int i = 0; i < 10; ++i) acc.q[i] = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc.w[i] = {0, 0};
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+      const int x = roots[i];
+      RootSums R;
+      if (uniform) {
+        root_sums(A, x, cf, R);
+#pragma unroll
+        for (int k = 0; k < 10; ++k) acc.q[k] += R.q[k];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) add_u128(acc.w[k], R.w[k]);
       } else {
-        const float xf = __fmul_rn(__ll2float_rn(Ms), ch.flip_coef);
-        const float e = exp_clamped(xf);
-        f = __fmul_rn(uniform_open(r.x), __fadd_rn(1.0f, e)) < 1.0f ? 1 : 0;
+        const int c = chain_of_segment(A, x);
+        root_sums(A, x, c, R);
+        record_atomics(A, c, R);
       }
-      A.flip[x] = f;
-      q[0] = 1ull;
-      q[1] = (unsigned long long)m0;
-      q[2] = (unsigned long long)sm0;
-      q[3] = (unsigned long long)(m0 * m0);
-      q[4] = (unsigned long long)(n0 * n0);
-      q[5] = (unsigned long long)(sm0 * sm0);
-      q[6] = (unsigned long long)(sn0 * sn0);
-      q[7] = (unsigned long long)(f ? -Ms : Ms);
-      q[8] = (unsigned long long)Ms;
-      q[9] = (unsigned long long)SMs;
-      w[0] = mul64(q[3], q[3]);
-      w[1] = mul64(q[4], q[4]);
-      w[2] = mul64(q[5], q[5]);
-      w[3] = mul64(q[6], q[6]);
-      auto ab = [](long long v) { return (unsigned long long)(v < 0 ? -v : v); };
-      w[4] = mul64(ab(Ls), ab(Ls));
-      w[5] = mul64(ab(Ms), ab(Ms));
-      w[6] = mul64(ab(SLs), ab(SLs));
-      w[7] = mul64(ab(SMs), ab(SMs));
     }
-    const unsigned any = __ballot_sync(0xFFFFFFFFu, is_root);
-    if (!any) continue;
-    const int leader = __ffs(any) - 1;
-    const int c0 = __shfl_sync(0xFFFFFFFFu, c, leader);
-    const bool uniform = __all_sync(0xFFFFFFFFu, !is_root || c == c0);
-    const int qw[10] = {R_NC, R_M0, R_SM0, R_M0SQ, R_N0SQ, R_SM0SQ, R_SN0SQ, R_FLD, R_MA, R_SMA};
-    const int ww[8] = {R_M0Q, R_N0Q, R_SM0Q, R_SN0Q, R_LSQ, R_MSQ, R_SLSQ, R_SMSQ};
     if (uniform) {
-      unsigned long long* row = rec_row(A, c0);
 #pragma unroll
-      for (int i = 0; i < 10; ++i) {
-        const unsigned long long t = warp_sum_u64(q[i]);
-        if (lane == leader && t) atomicAdd(row + qw[i], t);
+      for (int i = 0; i < 10; ++i)
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+          const unsigned v = __reduce_add_sync(0xFFFFFFFFu, (unsigned)((acc.q[i] >> (16 * l)) & 0xFFFFull));
+          if (lane == 0) limbs[wid][4 * i + l] = v;
+        }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+          const unsigned long long wv = l < 4 ? acc.w[i].lo : acc.w[i].hi;
+          const unsigned v = __reduce_add_sync(0xFFFFFFFFu, (unsigned)((wv >> (16 * (l & 3))) & 0xFFFFull));
+          if (lane == 0) limbs[wid][40 + 8 * i + l] = v;
+        }
+      __syncthreads();
+      for (int j = threadIdx.x; j < NLIMB; j += blockDim.x) {
+        unsigned long long sum = 0;
+        for (int w = 0; w < CL_THREADS / 32; ++w) sum += limbs[w][j];
+        tot[j] = sum;
       }
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const u128 t = warp_sum_u128(w[i]);
-        if (lane == leader && (t.lo | t.hi)) atomic_add_u128(row + ww[i], t);
+      __syncthreads();
+      if (threadIdx.x < 18) {
+        unsigned long long* row = rec_row(A, cf);
+        const int i = threadIdx.x;
+        if (i < 10) {
+          unsigned long long v = 0;
+          for (int l = 0; l < 4; ++l) v += tot[4 * i + l] << (16 * l);
+          if (v) atomicAdd(row + kRecQ[i], v);
+        } else {
+          const int k = i - 10;
+          u128 v = {0, 0};
+          for (int l = 0; l < 8; ++l) {
+            const unsigned long long t = tot[40 + 8 * k + l];
+            const int sh = 16 * l;
+            u128 add;
+            add.lo = sh < 64 ? (t << sh) : 0ull;
+            add.hi = sh == 0 ? 0ull : (sh < 64 ? (t >> (64 - sh)) : (t << (sh - 64)));
+            add_u128(v, add);
+          }
+          if (v.lo | v.hi) atomic_add_u128(row + kRecW[k], v);
+        }
       }
-    } else if (is_root) {
-      unsigned long long* row = rec_row(A, c);
-#pragma unroll
-      for (int i = 0; i < 10; ++i) if (q[i]) atomicAdd(row + qw[i], q[i]);
-#pragma unroll
-      for (int i = 0; i < 8; ++i) if (w[i].lo | w[i].hi) atomic_add_u128(row + ww[i], w[i]);
     }
+    __syncthreads();
   }
 }
 
@@ -606,26 +877,41 @@ __global__ void __launch_bounds__(256) k_flip_vertex(Arena A) {
   }
 }
 
-// Per site: flip the tau = 0 spin with its bottom segment's cluster (path_integral.C:822-823)
-// and compact the off-diagonal endpoints (time order kept) in place at the start of the site's
-// segment range: this is the next sweep's off-diagonal list.
-__global__ void __launch_bounds__(128) k_site_end(Arena A) {
+// Per site (one warp each): flip the tau = 0 spin with its bottom segment's cluster
+// (path_integral.C:822-823) and compact the off-diagonal endpoints (time order kept) in place at
+// the start of the site's segment range: this is the next sweep's off-diagonal list.  Every
+// lane reads its chunk before any lane writes, and a kept endpoint never moves forward, so the
+// in-place compaction reads no overwritten slot.
+__global__ void __launch_bounds__(256) k_site_end(Arena A) {
   if (A.ctl->err) return;
-  LG_GRID_STRIDE(s, A.N) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < A.N; s += warps) {
     const int base = A.sbase[s];
     const int k = A.sbase[s + 1] - base - 1;
-    if (A.flip[A.parent[base]]) A.spin0[s] ^= 1u;
+    if (lane == 0 && A.flip[A.parent[base]]) A.spin0[s] ^= 1u;
     int n = 0;
-    for (int j = 1; j <= k; ++j) {
-      const int x = base + j;
-      if (A.vnew[A.svert[x]]) {
-        A.stime[base + n] = A.stime[x];
-        A.sdir[base + n] = A.sdir[x];
-        ++n;
+    for (int j0 = 1; j0 <= k; j0 += 32) {
+      const int j = j0 + lane;
+      bool keep = false;
+      uint64_t t = 0;
+      uint8_t d = 0;
+      if (j <= k) {
+        const int x = base + j;
+        keep = A.vnew[A.svert[x]] != 0;
+        if (keep) { t = A.stime[x]; d = A.sdir[x]; }
       }
+      const unsigned ball = __ballot_sync(0xFFFFFFFFu, keep);
+      __syncwarp();
+      if (keep) {
+        const int pos = n + __popc(ball & ((1u << lane) - 1u));
+        A.stime[base + pos] = t;
+        A.sdir[base + pos] = d;
+      }
+      n += __popc(ball);
+      __syncwarp();
     }
-    A.off_base[s] = base;
-    A.off_cnt[s] = n;
+    if (lane == 0) { A.off_base[s] = base; A.off_cnt[s] = n; }
   }
 }
 
