@@ -312,10 +312,10 @@ struct Engine {
     Ctl* ctl = d_ctl.p;
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
     k_begin<<<grid_for((long long)C * REC_WORDS, 256), 256, 0, st>>>(A);
-    k_insert<false><<<grid_for(NB, 256, 16), 256, 0, st>>>(A);
+    k_insert<false><<<grid_for((long long)N * 32, INS_WARPS * 32, 16), INS_WARPS * 32, 0, st>>>(A);
     mark(0);
     scan(d_bond_cnt.p, d_bond_ptr.p, NB, &ctl->nv_total, nv_cap, 1, 0, ev ? ev + 1 : nullptr);
-    k_insert<true><<<grid_for(NB, 256, 16), 256, 0, st>>>(A);
+    k_insert<true><<<grid_for((long long)N * 32, INS_WARPS * 32, 16), INS_WARPS * 32, 0, st>>>(A);
     mark(2);
     k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
     scan(d_site_cnt.p, d_sbase.p, N, &ctl->ns_total, ns_cap, 1, 0, ev ? ev + 3 : nullptr);

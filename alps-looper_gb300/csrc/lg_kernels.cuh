@@ -105,9 +105,8 @@ __global__ void k_begin(Arena A) {
 // diagonal operators are dropped (path_integral.C:515-518).
 // The output list is time ordered; at equal times off-diagonal operators come first.
 template <bool WRITE>
-__global__ void __launch_bounds__(256) k_insert(Arena A) {
-  if (A.ctl->err) return;
-  LG_GRID_STRIDE(b, A.NB) {
+__device__ void insert_bond_serial(const Arena& A, int b) {
+  {
     const int c = A.bond_chain[b];
     const DChain ch = A.ch[c];
     const uint32_t sweep = A.ch_sweep[c];
@@ -180,6 +179,156 @@ __global__ void __launch_bounds__(256) k_insert(Arena A) {
       }
     }
     if (!WRITE) A.bond_cnt[b] = out;
+  }
+}
+
+
+// Warp-parallel form of the same insertion.  One warp per site s handles the bonds s owns
+// (s is their source).  The off-diagonal lists of s and of each partner site are staged in
+// shared memory; 32 proposals are generated at once (a warp prefix sum of the integer gaps gives
+// their times), each proposal's spin parities are binary searches in the staged lists, and the
+// time-ordered output is assembled by ranks: an accepted proposal lands after the own
+// off-diagonal operators at or before its time, an own off-diagonal operator after the accepted
+// proposals strictly before it.  Lists beyond the staging capacity take the serial path, which
+// produces the same output.
+constexpr int INS_WARPS = 4;
+constexpr int INS_CAP = 256;      // staged off-diagonal endpoints per site
+constexpr int INS_ACC = 512;      // staged accepted proposals per bond
+
+__device__ __forceinline__ int count_le(const uint64_t* T, int n, uint64_t t) {
+  int a = 0, b = n;
+  while (a < b) { const int m = (a + b) >> 1; if (T[m] <= t) a = m + 1; else b = m; }
+  return a;
+}
+__device__ __forceinline__ int count_lt(const uint64_t* T, int n, uint64_t t) {
+  int a = 0, b = n;
+  while (a < b) { const int m = (a + b) >> 1; if (T[m] < t) a = m + 1; else b = m; }
+  return a;
+}
+
+template <bool WRITE>
+__global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
+  if (A.ctl->err) return;
+  __shared__ uint64_t offS[INS_WARPS][INS_CAP];
+  __shared__ uint8_t dirS[INS_WARPS][INS_CAP];
+  __shared__ uint64_t offT[INS_WARPS][INS_CAP];
+  __shared__ uint64_t ownT[INS_WARPS][INS_CAP];
+  __shared__ uint64_t accT[INS_WARPS][INS_ACC];
+  __shared__ uint8_t accG[INS_WARPS][INS_ACC];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < A.N; s += warps) {
+    const int j0 = A.inc_off[s];
+    const int z = A.inc_off[s + 1] - j0;
+    const int ns_off = A.off_cnt[s];
+    const int sb = A.off_base[s];
+    const bool s_fits = ns_off <= INS_CAP;
+    if (s_fits) {
+      for (int i = lane; i < ns_off; i += 32) { offS[w][i] = A.stime[sb + i]; dirS[w][i] = A.sdir[sb + i]; }
+    }
+    const uint32_t ps0 = A.spin0[s];
+    for (int d = 0; d < z; ++d) {
+      if (A.inc_side[j0 + d] != 0) continue;  // bonds owned by s: s is the source
+      const int b = A.inc[j0 + d];
+      const int t = A.bond_s1[b];
+      const int nt_off = A.off_cnt[t];
+      if (!s_fits || nt_off > INS_CAP) {
+        if (lane == 0) insert_bond_serial<WRITE>(A, b);
+        __syncwarp();
+        continue;
+      }
+      const int tb_ = A.off_base[t];
+      __syncwarp();
+      for (int i = lane; i < nt_off; i += 32) offT[w][i] = A.stime[tb_ + i];
+      // own off-diagonal operators of bond b, in time order
+      int nown = 0;
+      for (int i0 = 0; i0 < ns_off; i0 += 32) {
+        const int i = i0 + lane;
+        const bool own = i < ns_off && dirS[w][i] == (uint8_t)d;
+        const unsigned ball = __ballot_sync(0xFFFFFFFFu, own);
+        if (own) ownT[w][nown + __popc(ball & lt)] = offS[w][i];
+        nown += __popc(ball);
+      }
+      __syncwarp();
+      const int c = A.bond_chain[b];
+      const DChain ch = A.ch[c];
+      const uint32_t sweep = A.ch_sweep[c];
+      const uint32_t bl = (uint32_t)(b - ch.bond_off);
+      const uint32_t pt0 = A.spin0[t];
+      // diagonal proposals, 32 at a time
+      int nacc = 0;
+      bool acc_fits = true;
+      bool more = ch.inv_rate > 0.0f;
+      uint64_t tbase = 0;
+      uint32_t k0 = 0;
+      while (more) {
+        const uint32_t k = k0 + lane;
+        const rnd4 r = philox(ch.seed, sweep, bl, TAG_PROPOSAL, k >> 1);
+        const uint32_t wu = (k & 1u) ? r.z : r.x;
+        const uint32_t wg = (k & 1u) ? r.w : r.y;
+        const float gap = __fmul_rn(-log_open(uniform_open(wu)), ch.inv_rate);
+        uint64_t q = gap_fix52(gap, ((uint64_t)(wu & 0x1FFu) << 16) | (wg & 0xFFFFu));
+        const bool stop = q >= FIX52_ONE;
+        if (stop) q = 0;
+        uint64_t incl = q;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint64_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const uint64_t tq = tbase + incl;
+        const unsigned stops = __ballot_sync(0xFFFFFFFFu, stop);
+        const bool valid = ((stops & (lt | (1u << lane))) == 0) && tq < FIX52_ONE;
+        const unsigned vb = __ballot_sync(0xFFFFFFFFu, valid);
+        bool accept = false;
+        uint64_t tp = 0;
+        uint32_t g = 0;
+        if (valid) {
+          tp = fix52_bits(tq);
+          g = (uint32_t)((uint64_t)wg >= ch.T0) + (uint32_t)((uint64_t)wg >= ch.T1) +
+              (uint32_t)((uint64_t)wg >= ch.T2);
+          const uint32_t ps = ps0 ^ (uint32_t)(count_le(offS[w], ns_off, tp) & 1);
+          const uint32_t pt = pt0 ^ (uint32_t)(count_le(offT[w], nt_off, tp) & 1);
+          accept = (((g & 1u) ^ ps ^ pt) & 1u) != 0;
+        }
+        const unsigned ab = __ballot_sync(0xFFFFFFFFu, accept);
+        if (WRITE && accept) {
+          const int pos = nacc + __popc(ab & lt);
+          if (pos < INS_ACC) { accT[w][pos] = tp; accG[w][pos] = (uint8_t)g; }
+        }
+        nacc += __popc(ab);
+        more = vb == 0xFFFFFFFFu;
+        tbase = __shfl_sync(0xFFFFFFFFu, tq, 31);
+        k0 += 32;
+      }
+      if (WRITE && nacc > INS_ACC) acc_fits = false;
+      if (!WRITE) {
+        if (lane == 0) A.bond_cnt[b] = nacc + nown;
+      } else if (!acc_fits) {
+        __syncwarp();
+        if (lane == 0) insert_bond_serial<true>(A, b);
+      } else {
+        __syncwarp();
+        const int out0 = A.bond_ptr[b];
+        for (int j = lane; j < nacc; j += 32) {
+          const uint64_t tp = accT[w][j];
+          const int pos = j + count_le(ownT[w], nown, tp);
+          A.vtime[out0 + pos] = tp;
+          A.vcode[out0 + pos] = (uint8_t)(accG[w][j] << 1);
+        }
+        for (int i = lane; i < nown; i += 32) {
+          const uint64_t to = ownT[w][i];
+          const int pos = i + count_lt(accT[w], nacc, to);
+          const rnd4 ro = philox(ch.seed, sweep, bl, TAG_OFFDIAG, (uint32_t)i >> 2);
+          const uint32_t wv = (i & 3) == 0 ? ro.x : (i & 3) == 1 ? ro.y : (i & 3) == 2 ? ro.z : ro.w;
+          const uint32_t g = ((uint64_t)wv < ch.Poff) ? 0u : 1u;
+          A.vtime[out0 + pos] = to;
+          A.vcode[out0 + pos] = (uint8_t)((g << 1) | 1u);
+        }
+      }
+      __syncwarp();
+    }
   }
 }
 
