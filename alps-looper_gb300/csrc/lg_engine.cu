@@ -885,3 +885,5 @@ const char* lg_kernel_name(int k) { return (k >= 0 && k < kNumStages) ? kStageNa
 
 }  // extern "C"
 
+// Allocation-free variant of lg_uf_label (same translation unit: it launches these kernels).
+#include "lg_static.cu"

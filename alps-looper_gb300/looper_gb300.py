@@ -82,6 +82,7 @@ def lib():
             "lg_fetch_records": (ctypes.c_int, [vp, vp, i64, vp]),
             "lg_keep_records": (ctypes.c_int, [vp, ctypes.c_int]),
             "lg_uf_label": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, i64, vp, vp, vp, i64, vp, vp]),
+            "lg_uf_label_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, i64, vp, vp, vp, vp, vp, vp]),
             "lg_batch_create": (ctypes.c_int, [ctypes.c_int, vp, vp]),
             "lg_batch_destroy": (ctypes.c_int, [vp]),
             "lg_batch_run": (ctypes.c_int, [vp, i64]),
@@ -353,6 +354,15 @@ def uf_label(lattice, L, bonds, graphs):
     check(lib().lg_uf_label(int(lattice), int(L), len(bonds), _p(bonds), _p(graphs), _p(lab), cap,
                             ctypes.byref(nf), ctypes.byref(nc)))
     return lab[:nf.value].copy(), nc.value
+
+
+def uf_label_static(lattice, L, nops, d_bonds, d_graphs, d_labels, stream=0):
+    """Allocation-free labelling: device pointers in and out (see lg_uf_label_static)."""
+    nf, nc = ctypes.c_int64(), ctypes.c_int64()
+    check(lib().lg_uf_label_static(int(lattice), int(L), int(nops), ctypes.c_void_p(d_bonds),
+                                   ctypes.c_void_p(d_graphs), ctypes.c_void_p(d_labels),
+                                   ctypes.byref(nf), ctypes.byref(nc), ctypes.c_void_p(stream)))
+    return nf.value, nc.value
 
 
 def kernel_launches() -> int:
