@@ -192,6 +192,48 @@ def cpu_port_rate(seconds=12.0, threads=1, state=None, warm=3):
     return sum(done) * N_SITES / el, sum(done), el
 
 
+def batched_params(lg, n=512, seed=99):
+    """512 square-lattice Heisenberg AFs: L uniform in {8,12,...,64}, T log-uniform in
+    [0.02, 2], seed 99 (the batched-chain workload)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    Ls = rng.choice(np.arange(8, 65, 4), size=n)
+    Ts = np.exp(rng.uniform(math.log(0.02), math.log(2.0), size=n))
+    return [lg.make_params(LATTICE="square", L=int(L), T=float(T), J=1.0, SEED=seed * 1000 + i,
+                           SWEEPS=1 << 12, THERMALIZATION=1 << 10, INITIAL_SPINS="random")
+            for i, (L, T) in enumerate(zip(Ls, Ts))]
+
+
+def run_batched(lg, steps, therm, plain_sample=16):
+    """Batched arena vs the plain path on the same chains (one chain per launch sequence)."""
+    ps = batched_params(lg)
+    sites = sum(p.L * p.L for p in ps)
+    b = lg.Batch(ps)
+    b.run(therm)
+    b.time_sweeps(3, FLUSH_BYTES)
+    ms = b.time_sweeps(steps, FLUSH_BYTES)
+    t_b = float(ms.sum()) / 1e3
+    value_b = steps * sites / t_b
+    # plain path: a sample of the same chains run alone, sweep by sweep
+    idx = list(range(0, len(ps), max(1, len(ps) // plain_sample)))[:plain_sample]
+    t_p, s_p = 0.0, 0
+    for i in idx:
+        w = lg.LoopWorker(ps[i])
+        w.run(min(therm, 64))
+        m = w.time_sweeps(max(4, steps // 4), FLUSH_BYTES)
+        t_p += float(m.mean()) / 1e3
+        s_p += ps[i].L * ps[i].L
+        w.close()
+    value_p = s_p / t_p
+    b.close()
+    return {"workload": "512 square Heisenberg AF chains, L uniform in {8..64}, T log-uniform "
+                        "[0.02,2], seed 99 (%d sites)" % sites,
+            "value": value_b, "unit": UNIT, "ms_per_sweep": t_b * 1e3 / steps,
+            "steps": steps, "thermalization_sweeps": therm,
+            "plain_value": value_p, "plain_sample_chains": len(idx),
+            "speedup_vs_plain": value_b / value_p}
+
+
 def run_ours(args, dist, ws, rank, local):
     import looper_gb300 as lg
     lg.lib()
@@ -248,6 +290,9 @@ def run_ours(args, dist, ws, rank, local):
                          "equilibrated state, %.1f s, 1 thread (CPU restatement of "
                          "path_integral.C in oracle/)" % (n, el)}
     w.close()
+    batched = None
+    if rank == 0 and args.batched_steps > 0:
+        batched = run_batched(lg, args.batched_steps, args.batched_therm)
     if rank != 0:
         return None
     out = {
@@ -262,6 +307,7 @@ def run_ours(args, dist, ws, rank, local):
                    "parallelism": "replicas" if ws > 1 else "single chain"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
         "clocks": clocks,
+        "batched": batched,
         "observables": {"Energy Density": obs["Energy Density"][0],
                         "sweeps_measured": int(obs["count"])},
     }
@@ -317,6 +363,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--batched-steps", type=int, default=16)
+    ap.add_argument("--batched-therm", type=int, default=128)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = _rank_info()
