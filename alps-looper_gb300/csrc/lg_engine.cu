@@ -89,6 +89,9 @@ struct Engine {
   DBuf<uint8_t> d_spin0;
   DBuf<int> d_off_base, d_off_cnt;
   DBuf<int> d_bond_cnt, d_bond_ptr, d_site_cnt, d_sbase, d_partial;
+  DBuf<int> d_slab_off;
+  DBuf<uint64_t> d_slab_time;
+  DBuf<uint8_t> d_slab_code, d_slab_ok;
   DBuf<uint64_t> d_vtime;
   DBuf<uint8_t> d_vcode, d_vnew;
   DBuf<int> d_vslot;
@@ -126,6 +129,8 @@ struct Engine {
     A.ch_sweep = d_sweep.p; A.ch_slot_off = d_ch_slot_off.p;
     A.spin0 = d_spin0.p; A.off_base = d_off_base.p; A.off_cnt = d_off_cnt.p;
     A.bond_cnt = d_bond_cnt.p; A.bond_ptr = d_bond_ptr.p; A.site_cnt = d_site_cnt.p;
+    A.slab_off = d_slab_off.p; A.slab_time = d_slab_time.p; A.slab_code = d_slab_code.p;
+    A.slab_ok = d_slab_ok.p;
     A.sbase = d_sbase.p;
     A.vtime = d_vtime.p; A.vcode = d_vcode.p; A.vnew = d_vnew.p; A.vslot = d_vslot.p;
     A.stime = d_stime.p; A.sinfo = d_sinfo.p; A.svert = d_svert.p; A.sdir = d_sdir.p;
@@ -204,6 +209,25 @@ struct Engine {
         (rc = d_bond_ptr.alloc(NB + 1)) || (rc = d_site_cnt.alloc(N)) ||
         (rc = d_sbase.alloc(N + 1)) || (rc = d_ctl.alloc(1)))
       return rc;
+    // per-bond slabs for the count pass: room for about twice the expected vertices of a bond
+    {
+      std::vector<int> so(NB + 1, 0);
+      long long tot = 0;
+      for (int c = 0; c < C; ++c) {
+        const double lam = spec[c].NB ? spec[c].expected_vertices() / 1.6 / spec[c].NB : 0.0;
+        int cap = (int)(2.0 * lam + 8.0 * std::sqrt(lam) + 16.0);
+        cap = (cap + 7) & ~7;
+        cap = std::min(std::max(cap, 16), 1024);
+        for (int b = 0; b < spec[c].NB; ++b) { so[hch[c].bond_off + b] = (int)tot; tot += cap; }
+      }
+      if (tot > (1ll << 31) - 1) return lg_fail(LG_EBUDGET, "slab space too large");
+      so[NB] = (int)tot;
+      if ((rc = d_slab_off.alloc(NB + 1)) || (rc = d_slab_time.alloc(tot)) ||
+          (rc = d_slab_code.alloc(tot)) || (rc = d_slab_ok.alloc(NB)))
+        return rc;
+      LG_CUDA(cudaMemcpy(d_slab_off.p, so.data(), (NB + 1) * sizeof(int), cudaMemcpyHostToDevice));
+      LG_CUDA(cudaMemset(d_slab_ok.p, 0, NB));
+    }
     int maxparts = std::max((NB + SCAN_TILE - 1) / SCAN_TILE, (N + SCAN_TILE - 1) / SCAN_TILE);
     if ((rc = d_partial.alloc(maxparts + 1))) return rc;
     LG_CUDA(cudaMemcpy(d_ch.p, hch.data(), C * sizeof(DChain), cudaMemcpyHostToDevice));

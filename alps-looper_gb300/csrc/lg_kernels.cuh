@@ -60,6 +60,10 @@ struct Arena {
   // per-sweep
   int* bond_cnt;           // NB
   int* bond_ptr;           // NB+1
+  const int* slab_off;     // NB+1: per-bond slab of the count pass (vertices in final order)
+  uint64_t* slab_time;
+  uint8_t* slab_code;
+  uint8_t* slab_ok;        // NB: 1 when the bond's list fit its slab
   int* site_cnt;           // N
   int* sbase;              // N+1
   uint64_t* vtime;
@@ -206,6 +210,10 @@ __device__ __forceinline__ int count_lt(const uint64_t* T, int n, uint64_t t) {
   return a;
 }
 
+// Count pass (WRITE = false): counts the new vertices of every owned bond and stores the bond's
+// finished list (time order, graphs chosen) in its slab when it fits.  Write pass: copies the
+// slabs to the compact bond-major arrays; only bonds whose list overflowed their slab (or the
+// staging capacity) are recomputed, with the same random numbers.
 template <bool WRITE>
 __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
   if (A.ctl->err) return;
@@ -221,6 +229,21 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < A.N; s += warps) {
     const int j0 = A.inc_off[s];
     const int z = A.inc_off[s + 1] - j0;
+    bool all_slab = WRITE;
+    if (WRITE) {
+      // copy the finished lists of the owned bonds
+      for (int d = 0; d < z; ++d) {
+        if (A.inc_side[j0 + d] != 0) continue;
+        const int b = A.inc[j0 + d];
+        if (!A.slab_ok[b]) { all_slab = false; continue; }
+        const int n = A.bond_cnt[b], so = A.slab_off[b], out0 = A.bond_ptr[b];
+        for (int i = lane; i < n; i += 32) {
+          A.vtime[out0 + i] = A.slab_time[so + i];
+          A.vcode[out0 + i] = A.slab_code[so + i];
+        }
+      }
+      if (all_slab) continue;
+    }
     const int ns_off = A.off_cnt[s];
     const int sb = A.off_base[s];
     const bool s_fits = ns_off <= INS_CAP;
@@ -231,10 +254,14 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
     for (int d = 0; d < z; ++d) {
       if (A.inc_side[j0 + d] != 0) continue;  // bonds owned by s: s is the source
       const int b = A.inc[j0 + d];
+      if (WRITE && A.slab_ok[b]) continue;
       const int t = A.bond_s1[b];
       const int nt_off = A.off_cnt[t];
       if (!s_fits || nt_off > INS_CAP) {
-        if (lane == 0) insert_bond_serial<WRITE>(A, b);
+        if (lane == 0) {
+          insert_bond_serial<WRITE>(A, b);
+          if (!WRITE) A.slab_ok[b] = 0;
+        }
         __syncwarp();
         continue;
       }
@@ -258,7 +285,6 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
       const uint32_t pt0 = A.spin0[t];
       // diagonal proposals, 32 at a time
       int nacc = 0;
-      bool acc_fits = true;
       bool more = ch.inv_rate > 0.0f;
       uint64_t tbase = 0;
       uint32_t k0 = 0;
@@ -293,7 +319,7 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
           accept = (((g & 1u) ^ ps ^ pt) & 1u) != 0;
         }
         const unsigned ab = __ballot_sync(0xFFFFFFFFu, accept);
-        if (WRITE && accept) {
+        if (accept) {
           const int pos = nacc + __popc(ab & lt);
           if (pos < INS_ACC) { accT[w][pos] = tp; accG[w][pos] = (uint8_t)g; }
         }
@@ -302,20 +328,32 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
         tbase = __shfl_sync(0xFFFFFFFFu, tq, 31);
         k0 += 32;
       }
-      if (WRITE && nacc > INS_ACC) acc_fits = false;
+      const int n = nacc + nown;
+      bool fits = nacc <= INS_ACC;
+      uint64_t* dt = A.vtime;
+      uint8_t* dc = A.vcode;
+      int out0 = 0;
       if (!WRITE) {
-        if (lane == 0) A.bond_cnt[b] = nacc + nown;
-      } else if (!acc_fits) {
-        __syncwarp();
-        if (lane == 0) insert_bond_serial<true>(A, b);
+        if (lane == 0) A.bond_cnt[b] = n;
+        fits = fits && n <= A.slab_off[b + 1] - A.slab_off[b];
+        if (lane == 0) A.slab_ok[b] = fits ? 1 : 0;
+        dt = A.slab_time;
+        dc = A.slab_code;
+        out0 = A.slab_off[b];
       } else {
-        __syncwarp();
-        const int out0 = A.bond_ptr[b];
+        out0 = A.bond_ptr[b];
+        if (!fits) {
+          __syncwarp();
+          if (lane == 0) insert_bond_serial<true>(A, b);
+        }
+      }
+      __syncwarp();
+      if (fits) {
         for (int j = lane; j < nacc; j += 32) {
           const uint64_t tp = accT[w][j];
           const int pos = j + count_le(ownT[w], nown, tp);
-          A.vtime[out0 + pos] = tp;
-          A.vcode[out0 + pos] = (uint8_t)(accG[w][j] << 1);
+          dt[out0 + pos] = tp;
+          dc[out0 + pos] = (uint8_t)(accG[w][j] << 1);
         }
         for (int i = lane; i < nown; i += 32) {
           const uint64_t to = ownT[w][i];
@@ -323,8 +361,8 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
           const rnd4 ro = philox(ch.seed, sweep, bl, TAG_OFFDIAG, (uint32_t)i >> 2);
           const uint32_t wv = (i & 3) == 0 ? ro.x : (i & 3) == 1 ? ro.y : (i & 3) == 2 ? ro.z : ro.w;
           const uint32_t g = ((uint64_t)wv < ch.Poff) ? 0u : 1u;
-          A.vtime[out0 + pos] = to;
-          A.vcode[out0 + pos] = (uint8_t)((g << 1) | 1u);
+          dt[out0 + pos] = to;
+          dc[out0 + pos] = (uint8_t)((g << 1) | 1u);
         }
       }
       __syncwarp();
