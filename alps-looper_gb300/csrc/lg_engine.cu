@@ -85,6 +85,8 @@ struct Engine {
   DBuf<uint8_t> d_bond_dir0, d_inc_side;
   DBuf<int8_t> d_gauge;
   DBuf<uint32_t> d_sweep;
+  DBuf<uint8_t> d_active;
+  std::vector<uint8_t> h_active;
   DBuf<int> d_ch_slot_off;
   DBuf<uint8_t> d_spin0;
   DBuf<int> d_off_base, d_off_cnt;
@@ -126,7 +128,7 @@ struct Engine {
     A.bond_s0 = d_bond_s0.p; A.bond_s1 = d_bond_s1.p; A.bond_chain = d_bond_chain.p;
     A.bond_dir0 = d_bond_dir0.p; A.inc_off = d_inc_off.p; A.inc = d_inc.p;
     A.inc_side = d_inc_side.p; A.gauge = d_gauge.p; A.site_chain = d_site_chain.p;
-    A.ch_sweep = d_sweep.p; A.ch_slot_off = d_ch_slot_off.p;
+    A.ch_sweep = d_sweep.p; A.ch_slot_off = d_ch_slot_off.p; A.ch_active = d_active.p;
     A.spin0 = d_spin0.p; A.off_base = d_off_base.p; A.off_cnt = d_off_cnt.p;
     A.bond_cnt = d_bond_cnt.p; A.bond_ptr = d_bond_ptr.p; A.site_cnt = d_site_cnt.p;
     A.slab_off = d_slab_off.p; A.slab_time = d_slab_time.p; A.slab_code = d_slab_code.p;
@@ -203,7 +205,7 @@ struct Engine {
         (rc = d_bond_chain.alloc(NB)) || (rc = d_bond_dir0.alloc(NB)) ||
         (rc = d_inc_off.alloc(N + 1)) || (rc = d_inc.alloc(h_inc.size())) ||
         (rc = d_inc_side.alloc(h_inc.size())) || (rc = d_gauge.alloc(N)) ||
-        (rc = d_site_chain.alloc(N)) || (rc = d_sweep.alloc(C)) ||
+        (rc = d_site_chain.alloc(N)) || (rc = d_sweep.alloc(C)) || (rc = d_active.alloc(C)) ||
         (rc = d_ch_slot_off.alloc(C + 1)) || (rc = d_spin0.alloc(N)) ||
         (rc = d_off_base.alloc(N)) || (rc = d_off_cnt.alloc(N)) || (rc = d_bond_cnt.alloc(NB)) ||
         (rc = d_bond_ptr.alloc(NB + 1)) || (rc = d_site_cnt.alloc(N)) ||
@@ -240,6 +242,8 @@ struct Engine {
     LG_CUDA(cudaMemcpy(d_inc_side.p, h_inc_side.data(), h_inc_side.size(), cudaMemcpyHostToDevice));
     LG_CUDA(cudaMemcpy(d_gauge.p, h_gauge.data(), N, cudaMemcpyHostToDevice));
     LG_CUDA(cudaMemcpy(d_site_chain.p, h_site_chain.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    h_active.assign(C, 1);
+    LG_CUDA(cudaMemcpy(d_active.p, h_active.data(), C, cudaMemcpyHostToDevice));
     std::vector<uint32_t> sw(C);
     for (int c = 0; c < C; ++c) sw[c] = (uint32_t)spec[c].mcs;
     LG_CUDA(cudaMemcpy(d_sweep.p, sw.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice));
@@ -675,6 +679,56 @@ struct Engine {
     return LG_OK;
   }
 
+  // Retire (or re-enable) a chain: a retired chain inserts no operators and costs almost nothing.
+  int set_active(int c, bool on) {
+    h_active[c] = on ? 1 : 0;
+    LG_CUDA(cudaMemcpyAsync(d_active.p + c, &h_active[c], 1, cudaMemcpyHostToDevice, st));
+    LG_CUDA(cudaStreamSynchronize(st));
+    return LG_OK;
+  }
+
+  // Take over chains of another arena on the same device: from[c] is the index of new chain c
+  // in `old` (or -1 for a new chain).  Spins, off-diagonal lists, sweep counters, schedule and
+  // observable accumulators move; the old arena must not be used afterwards.
+  int adopt(Engine& old, const std::vector<int>& from) {
+    std::vector<int> map(N, -1);
+    std::vector<uint32_t> sw(C);
+    LG_CUDA(cudaMemcpy(sw.data(), d_sweep.p, C * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    for (int c = 0; c < C; ++c) {
+      const int o = from[c];
+      if (o < 0) continue;
+      if (old.spec[o].N != spec[c].N) return lg_fail(LG_EINVAL, "adopt: size mismatch");
+      for (int i = 0; i < spec[c].N; ++i) map[hch[c].site_off + i] = old.hch[o].site_off + i;
+      spec[c].mcs = old.spec[o].mcs;
+      spec[c].last_nop = old.spec[o].last_nop;
+      acc[c] = old.acc[o];
+      sw[c] = (uint32_t)old.spec[o].mcs;
+    }
+    LG_CUDA(cudaMemcpy(d_sweep.p, sw.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    DBuf<int> dmap, dcnt, dbase;
+    int rc;
+    if ((rc = dmap.alloc(N)) || (rc = dcnt.alloc(N)) || (rc = dbase.alloc(N + 1))) return rc;
+    LG_CUDA(cudaMemcpy(dmap.p, map.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    Arena A = arena();
+    k_repack_count<<<grid_for(N, 256), 256, 0, st>>>(A, dmap.p, old.d_off_cnt.p, dcnt.p);
+    LG_CUDA(cudaMemsetAsync(d_ctl.p, 0, sizeof(int), st));
+    scan(dcnt.p, dbase.p, N, &d_ctl.p->ns_total, 0x7FFFFFFF, 0, 0);
+    LG_CUDA(cudaMemcpyAsync(d_off_cnt.p, dcnt.p, N * sizeof(int), cudaMemcpyDeviceToDevice, st));
+    int total = 0;
+    LG_CUDA(cudaMemcpyAsync(&total, dbase.p + N, sizeof(int), cudaMemcpyDeviceToHost, st));
+    LG_CUDA(cudaStreamSynchronize(st));
+    if (total > ns_cap) {
+      if ((rc = alloc_dynamic(total + 4096, false))) return rc;
+      A = arena();
+    }
+    k_repack_copy<<<grid_for((long long)N * 32, 256), 256, 0, st>>>(A, dmap.p, old.d_spin0.p,
+        old.d_off_base.p, old.d_stime.p, old.d_sdir.p, dbase.p);
+    g_launches += 5;
+    LG_CUDA(cudaGetLastError());
+    LG_CUDA(cudaStreamSynchronize(st));
+    return LG_OK;
+  }
+
   int set_beta(int c, double beta) {
     int rc = spec[c].set_beta(beta);
     if (rc) return rc;
@@ -911,3 +965,6 @@ const char* lg_kernel_name(int k) { return (k >= 0 && k < kNumStages) ? kStageNa
 
 // Allocation-free variant of lg_uf_label (same translation unit: it launches these kernels).
 #include "lg_static.cu"
+
+// Request server with continuous batching over one arena.
+#include "lg_server.cu"

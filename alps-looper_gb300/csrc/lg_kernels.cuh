@@ -52,6 +52,7 @@ struct Arena {
   const int* site_chain;   // N
   // per-chain mutable
   uint32_t* ch_sweep;      // C
+  const uint8_t* ch_active;  // C: 0 = retired chain (inserts nothing; its state is dropped)
   int* ch_slot_off;        // C+1 (this sweep)
   // persistent site state
   uint8_t* spin0;
@@ -229,6 +230,12 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < A.N; s += warps) {
     const int j0 = A.inc_off[s];
     const int z = A.inc_off[s + 1] - j0;
+    if (!A.ch_active[A.site_chain[s]]) {
+      if (!WRITE && lane == 0)
+        for (int d = 0; d < z; ++d)
+          if (A.inc_side[j0 + d] == 0) { A.bond_cnt[A.inc[j0 + d]] = 0; A.slab_ok[A.inc[j0 + d]] = 1; }
+      continue;
+    }
     bool all_slab = WRITE;
     if (WRITE) {
       // copy the finished lists of the owned bonds
@@ -1115,6 +1122,30 @@ __global__ void k_end(Arena A) {
 __global__ void k_step(Ctl* ctl) {
   if (ctl->err) return;
   ctl->step += 1u;
+}
+
+// Moving chains into a new arena: site s of the new arena takes the state of site map[s] of
+// the old one (map[s] < 0: a new chain, left as initialised).  Pass 1 gathers list lengths.
+__global__ void k_repack_count(Arena A, const int* map, const int* old_off_cnt, int* cnt) {
+  LG_GRID_STRIDE(s, A.N) cnt[s] = map[s] >= 0 ? old_off_cnt[map[s]] : 0;
+}
+
+// Pass 2 (one warp per site): copy the spin and the off-diagonal list to its new place.
+__global__ void k_repack_copy(Arena A, const int* map, const uint8_t* old_spin0,
+                              const int* old_off_base, const uint64_t* old_stime,
+                              const uint8_t* old_sdir, const int* new_base) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < A.N; s += warps) {
+    const int o = map[s];
+    if (o < 0) continue;
+    const int n = A.off_cnt[s], src = old_off_base[o], dst = new_base[s];
+    for (int i = lane; i < n; i += 32) {
+      A.stime[dst + i] = old_stime[src + i];
+      A.sdir[dst + i] = old_sdir[src + i];
+    }
+    if (lane == 0) { A.spin0[s] = old_spin0[o]; A.off_base[s] = dst; }
+  }
 }
 
 // Initial spins: all up, or iid from the chain's seed.

@@ -50,6 +50,24 @@ class Obs(ctypes.Structure):
                 ("error", ctypes.c_double * NUM_OBS), ("tau", ctypes.c_double * NUM_OBS)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_double), ("sweeps_per_tick", ctypes.c_int),
+                ("rebuild_interval_s", ctypes.c_double), ("max_active", ctypes.c_int)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int), ("t_submit", ctypes.c_double),
+                ("t_start", ctypes.c_double), ("t_finish", ctypes.c_double),
+                ("sweeps", ctypes.c_uint64), ("sites", ctypes.c_int64), ("obs", Obs)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("rejected", ctypes.c_uint64), ("rebuilds", ctypes.c_uint64),
+                ("site_sweeps", ctypes.c_int64), ("queued", ctypes.c_int64),
+                ("active_bytes", ctypes.c_double), ("elapsed_s", ctypes.c_double)]
+
+
 _lib = None
 
 
@@ -96,6 +114,14 @@ def lib():
             "lg_batch_profile_sweeps": (ctypes.c_int, [vp, i64, ctypes.c_size_t, vp, vp]),
             "lg_num_kernels": (ctypes.c_int, []),
             "lg_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
+            "lg_server_config_default": (None, [vp]),
+            "lg_request_bytes": (ctypes.c_double, [vp]),
+            "lg_server_create": (ctypes.c_int, [vp, vp]),
+            "lg_server_submit": (ctypes.c_int, [vp, vp, vp]),
+            "lg_server_poll": (ctypes.c_int, [vp, vp, ctypes.c_int, vp]),
+            "lg_server_wait": (ctypes.c_int, [vp, ctypes.c_double]),
+            "lg_server_get_stats": (ctypes.c_int, [vp, vp]),
+            "lg_server_destroy": (ctypes.c_int, [vp]),
             "lg_kernel_launches": (u64, []),
             "lg_version": (ctypes.c_char_p, []),
         }
@@ -342,6 +368,66 @@ class Batch:
         if not h:
             raise IndexError(i)
         return LoopWorker(self.params[i], _handle=h, _owner=self)
+
+
+def request_bytes(params: Params) -> float:
+    """Device bytes the server's admission control expects a request to need."""
+    return lib().lg_request_bytes(ctypes.byref(params))
+
+
+class Server:
+    """Request server with continuous batching (lg_server_*)."""
+
+    def __init__(self, budget_bytes=None, sweeps_per_tick=None, rebuild_interval_s=None,
+                 max_active=None):
+        c = ServerConfig()
+        lib().lg_server_config_default(ctypes.byref(c))
+        if budget_bytes is not None:
+            c.budget_bytes = float(budget_bytes)
+        if sweeps_per_tick is not None:
+            c.sweeps_per_tick = int(sweeps_per_tick)
+        if rebuild_interval_s is not None:
+            c.rebuild_interval_s = float(rebuild_interval_s)
+        if max_active is not None:
+            c.max_active = int(max_active)
+        h = ctypes.c_void_p()
+        check(lib().lg_server_create(ctypes.byref(c), ctypes.byref(h)))
+        self._h = h
+
+    def submit(self, params: Params) -> int:
+        i = ctypes.c_uint64()
+        check(lib().lg_server_submit(self._h, ctypes.byref(params), ctypes.byref(i)))
+        return i.value
+
+    def poll(self, cap=4096):
+        arr = (Result * cap)()
+        n = ctypes.c_int()
+        check(lib().lg_server_poll(self._h, arr, cap, ctypes.byref(n)))
+        out = []
+        for r in arr[:n.value]:
+            out.append({"id": r.id, "status": r.status, "t_submit": r.t_submit,
+                        "t_start": r.t_start, "t_finish": r.t_finish, "sweeps": r.sweeps,
+                        "sites": r.sites, "obs": _obs_dict(r.obs) if r.status == 0 else None})
+        return out
+
+    def wait(self, timeout_s=600.0):
+        check(lib().lg_server_wait(self._h, float(timeout_s)))
+
+    def stats(self):
+        st = ServerStats()
+        check(lib().lg_server_get_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def close(self):
+        if self._h:
+            lib().lg_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def uf_label(lattice, L, bonds, graphs):

@@ -234,6 +234,77 @@ def run_batched(lg, steps, therm, plain_sample=16):
             "speedup_vs_plain": value_b / value_p}
 
 
+def served_requests(lg, n=4096, seed=2024):
+    """The served stream: Poisson arrivals at 200/s; lattice uniform over {chain L in [32,4096],
+    square L in [8,96], cubic L in [6,24]} (L rounded up to even: odd periodic lattices with an
+    antiferromagnetic xy coupling have a sign problem), beta log-uniform in [0.5,64],
+    Jz/Jxy uniform in [0.5,1.5] with Jxy = 1, h uniform in [0,0.5], SWEEPS in {2^10, 2^12}."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1 / 200.0, size=n))
+    out = []
+    for i in range(n):
+        kind = int(rng.integers(0, 3))
+        if kind == 0:
+            lat, L = "chain", int(rng.integers(32, 4097))
+        elif kind == 1:
+            lat, L = "square", int(rng.integers(8, 97))
+        else:
+            lat, L = "cubic", int(rng.integers(6, 25))
+        L += L % 2
+        beta = math.exp(rng.uniform(math.log(0.5), math.log(64.0)))
+        r = rng.uniform(0.5, 1.5)
+        h = rng.uniform(0.0, 0.5)
+        sw = int(rng.choice([1 << 10, 1 << 12]))
+        out.append((float(arrivals[i]),
+                    lg.make_params(LATTICE=lat, L=L, BETA=beta, Jxy=1.0, Jz=r, h=h, SWEEPS=sw,
+                                   SEED=seed * 100000 + i, INITIAL_SPINS="random")))
+    return out
+
+
+def run_served(lg, n_requests, plain_sample=12):
+    reqs = served_requests(lg)[:n_requests]
+    srv = lg.Server(sweeps_per_tick=16, rebuild_interval_s=0.02)
+    t0 = time.perf_counter()
+    for t_arr, p in reqs:
+        d = t0 + t_arr - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        srv.submit(p)
+    srv.wait(3600)
+    wall = time.perf_counter() - t0
+    res = srv.poll()
+    st = srv.stats()
+    srv.close()
+    ok = [r for r in res if r["status"] == 0]
+    lat = sorted(r["t_finish"] - r["t_submit"] for r in ok)
+    work = sum(r["sites"] * r["sweeps"] for r in ok)
+    served = work / wall
+    # plain path: the same requests one at a time (sampled; wall clock per sweep through lg_run)
+    idx = list(range(0, len(reqs), max(1, len(reqs) // plain_sample)))[:plain_sample]
+    t_plain, w_plain = 0.0, 0
+    for i in idx:
+        p = reqs[i][1]
+        w = lg.LoopWorker(p)
+        w.run(4)
+        t1 = time.perf_counter()
+        w.run(16)
+        per = (time.perf_counter() - t1) / 16
+        total_sweeps = p.sweeps + (p.sweeps >> 3)
+        t_plain += per * total_sweeps
+        w_plain += p.L ** p.lattice * total_sweeps
+        w.close()
+    plain = w_plain / t_plain
+    q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))] if lat else None  # noqa: E731
+    return {"workload": "served stream: first %d of 4096 Poisson requests (200/s, seed 2024)"
+                        % len(reqs),
+            "value": served, "unit": UNIT, "wall_s": wall, "completed": len(ok),
+            "rejected": int(st["rejected"]), "rebuilds": int(st["rebuilds"]),
+            "latency_p50_s": q(0.50), "latency_p99_s": q(0.99),
+            "plain_value": plain, "plain_sample_requests": len(idx),
+            "speedup_vs_plain": served / plain}
+
+
 def run_ours(args, dist, ws, rank, local):
     import looper_gb300 as lg
     lg.lib()
@@ -293,6 +364,9 @@ def run_ours(args, dist, ws, rank, local):
     batched = None
     if rank == 0 and args.batched_steps > 0:
         batched = run_batched(lg, args.batched_steps, args.batched_therm)
+    served = None
+    if rank == 0 and args.served_requests > 0:
+        served = run_served(lg, args.served_requests)
     if rank != 0:
         return None
     out = {
@@ -308,6 +382,7 @@ def run_ours(args, dist, ws, rank, local):
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
         "clocks": clocks,
         "batched": batched,
+        "served": served,
         "observables": {"Energy Density": obs["Energy Density"][0],
                         "sweeps_measured": int(obs["count"])},
     }
@@ -365,6 +440,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--batched-steps", type=int, default=16)
     ap.add_argument("--batched-therm", type=int, default=128)
+    ap.add_argument("--served-requests", type=int, default=48)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = _rank_info()

@@ -195,6 +195,48 @@ int lg_batch_stats(const lg_batch* b, int64_t* total_sites, int64_t* site_sweeps
 /* Access one chain of a batch through the single-chain test seams. */
 lg_chain* lg_batch_chain(lg_batch* b, int i);
 
+/* ---- request server: continuous batching over one device arena ---------------------------
+ * Serving form of the worker (no counterpart in the reference, whose scheduler runs one
+ * worker per clone; see path_integral.C:872-876 for the worker it batches).  Requests (lg_params)
+ * are queued, admitted in arrival order while their estimated device memory (from the expected
+ * operator count beta * W * N_bonds) fits the budget, and run together in one arena whose sweeps
+ * are CUDA graphs; chain state stays on the device between sweeps and moves device to device when
+ * the arena is rebuilt.  Each result equals the result of the same request run alone (lg_create
+ * + lg_run + lg_observables), bit for bit. */
+typedef struct lg_server lg_server;
+typedef struct lg_server_config {
+  double budget_bytes;       /* device memory budget for admitted requests (default 150e9)    */
+  int sweeps_per_tick;       /* sweeps between admission / retirement points (default 16)    */
+  double rebuild_interval_s; /* minimum time between arena rebuilds while busy (0.02 s)      */
+  int max_active;            /* maximum chains in the arena (default 4096)                   */
+} lg_server_config;
+typedef struct lg_result {
+  uint64_t id;
+  int status;                /* LG_OK, or LG_EBUDGET when the request can never fit          */
+  double t_submit, t_start, t_finish;   /* seconds since lg_server_create                    */
+  uint64_t sweeps;           /* THERMALIZATION + SWEEPS run                                  */
+  int64_t sites;
+  lg_obs obs;
+} lg_result;
+typedef struct lg_server_stats {
+  uint64_t submitted, completed, rejected, rebuilds;
+  int64_t site_sweeps;       /* sweeps x sites of active chains run so far                   */
+  int64_t queued;
+  double active_bytes;
+  double elapsed_s;
+} lg_server_stats;
+void lg_server_config_default(lg_server_config* c);
+/* Estimated device bytes of one request (the admission figure); < 0 for invalid parameters. */
+double lg_request_bytes(const lg_params* p);
+int lg_server_create(const lg_server_config* c, lg_server** out);
+int lg_server_submit(lg_server* s, const lg_params* p, uint64_t* id);
+/* Completed results since the last poll (non-blocking). */
+int lg_server_poll(lg_server* s, lg_result* out, int cap, int* n);
+/* Block until every submitted request finished (LG_ENOTREADY on timeout). */
+int lg_server_wait(lg_server* s, double timeout_s);
+int lg_server_get_stats(lg_server* s, lg_server_stats* out);
+int lg_server_destroy(lg_server* s);
+
 /* ---- measurement seams (benchmarks) -------------------------------------------------------
  * Run n sweeps of every chain of a handle (as lg_run / lg_batch_run), each sweep bracketed by
  * CUDA events on the engine's own stream, with a device write of flush_bytes (an L2 flush)

@@ -69,3 +69,14 @@ def test_obs_names_match_reference_keys(lg):
     for key in ("Energy", "Energy Density", "Specific Heat", "Susceptibility",
                 "Staggered Magnetization^2", "Staggered Susceptibility", "Number of Clusters"):
         assert key in names
+
+
+def test_request_bytes_estimate(lg):
+    small = lg.request_bytes(lg.make_params(LATTICE="square", L=8, T=1.0))
+    big = lg.request_bytes(lg.make_params(LATTICE="square", L=64, T=1.0))
+    cold = lg.request_bytes(lg.make_params(LATTICE="square", L=64, T=0.02))
+    assert 0 < small < big < cold
+    # about 1e7 operators at beta = 64 on 128x128 needs a few hundred MB, not GB
+    b = lg.request_bytes(lg.make_params(LATTICE="square", L=128, BETA=64.0))
+    assert 1e8 < b < 2e9
+    assert lg.request_bytes(lg.make_params(LATTICE="square", L=7, T=1.0)) < 0  # sign problem
