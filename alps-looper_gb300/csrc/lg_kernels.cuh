@@ -797,18 +797,15 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
         q = (info & SI_SPIN) * 2 + ((info & SI_GNEG) ? 1 : 0);
         if (info & SI_FIRST) atomicAdd(A.cnt0 + 4 * (size_t)r + q, 1u);
       }
-      const unsigned long long key = valid ? (((unsigned long long)root << 2) | (unsigned)q) : ~0ull;
-      const unsigned mask = __match_any_sync(0xFFFFFFFFu, key);
-      const unsigned long long sum = group_sum_u48(mask, len);
-      if (valid && lane == __ffs(mask) - 1 && sum) {
+      if (valid && len) {
         unsigned h = ((unsigned)root * 2654435761u) >> 22;  // 10-bit hash
         bool done = false;
         for (int probe = 0; probe < 32; ++probe) {
           const int k = atomicCAS(hkey + h, -1, root);
-          if (k == -1 || k == root) { atomicAdd(hval + 4 * h + q, sum); done = true; break; }
+          if (k == -1 || k == root) { atomicAdd(hval + 4 * h + q, len); done = true; break; }
           h = (h + 1) & (ACC_HASH - 1);
         }
-        if (!done) atomicAdd(A.cls + 4 * (size_t)root + q, sum);
+        if (!done) atomicAdd(A.cls + 4 * (size_t)root + q, len);
       }
     }
     __syncthreads();
