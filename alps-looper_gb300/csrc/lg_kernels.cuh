@@ -197,8 +197,8 @@ __device__ void insert_bond_serial(const Arena& A, int b) {
 // proposals strictly before it.  Lists beyond the staging capacity take the serial path, which
 // produces the same output.
 constexpr int INS_WARPS = 4;
-constexpr int INS_CAP = 256;      // staged off-diagonal endpoints per site
-constexpr int INS_ACC = 512;      // staged accepted proposals per bond
+constexpr int INS_CAP = 128;      // staged off-diagonal endpoints per site
+constexpr int INS_ACC = 128;      // staged accepted proposals per bond
 
 __device__ __forceinline__ int count_le(const uint64_t* T, int n, uint64_t t) {
   int a = 0, b = n;
@@ -296,10 +296,13 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
       uint64_t tbase = 0;
       uint32_t k0 = 0;
       while (more) {
-        const uint32_t k = k0 + lane;
-        const rnd4 r = philox(ch.seed, sweep, bl, TAG_PROPOSAL, k >> 1);
-        const uint32_t wu = (k & 1u) ? r.z : r.x;
-        const uint32_t wg = (k & 1u) ? r.w : r.y;
+        const uint32_t k = k0 + lane;  // k0 is a multiple of 32: lanes 2i, 2i+1 share a block
+        rnd4 r = {0, 0, 0, 0};
+        if ((lane & 1) == 0) r = philox(ch.seed, sweep, bl, TAG_PROPOSAL, k >> 1);
+        const uint32_t rz = __shfl_xor_sync(0xFFFFFFFFu, r.z, 1);
+        const uint32_t rw = __shfl_xor_sync(0xFFFFFFFFu, r.w, 1);
+        const uint32_t wu = (k & 1u) ? rz : r.x;
+        const uint32_t wg = (k & 1u) ? rw : r.y;
         const float gap = __fmul_rn(-log_open(uniform_open(wu)), ch.inv_rate);
         uint64_t q = gap_fix52(gap, ((uint64_t)(wu & 0x1FFu) << 16) | (wg & 0xFFFFu));
         const bool stop = q >= FIX52_ONE;
@@ -497,7 +500,7 @@ __global__ void k_site_count(Arena A) {
 // merge), the spins follow from a warp prefix-XOR of the off-diagonal flags in merged order, and
 // the segment arrays are written coalesced.  Sites with more endpoints use the one-thread merge.
 constexpr int MERGE_WARPS = 4;
-constexpr int MERGE_CAP = 768;
+constexpr int MERGE_CAP = 384;
 
 // number of entries of list [lo, hi) ordered before key (t, dg); `inclusive` counts equal keys
 __device__ __forceinline__ int merge_count(const uint64_t* T, const uint8_t* Cd, int lo, int hi,
@@ -573,7 +576,7 @@ __device__ void merge_site_serial(Arena& A, int s) {
   if (k > 0) A.parent[base + k] = base;
 }
 
-__global__ void __launch_bounds__(MERGE_WARPS * 32) k_merge(Arena A) {
+__global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A) {
   if (A.ctl->err) return;
   __shared__ uint64_t sT[MERGE_WARPS][MERGE_CAP];   // staged times, list by list
   __shared__ uint8_t sC[MERGE_WARPS][MERGE_CAP];    // staged codes
@@ -890,7 +893,8 @@ __device__ __forceinline__ void add_u128(u128& a, u128 b) {
   a.lo = lo;
 }
 
-// Flip decision and record contribution of root x of chain c; clears the root's class sums.
+// Flip decision of root x of chain c and its record contribution, added into R; clears the
+// root's class sums.
 __device__ __forceinline__ void root_sums(const Arena& A, int x, int c, RootSums& R) {
   const DChain ch = A.ch[c];
   unsigned long long* S = A.cls + 4 * (size_t)x;
@@ -900,10 +904,7 @@ __device__ __forceinline__ void root_sums(const Arena& A, int x, int c, RootSums
   const long long k0 = K[0], k1 = K[1], k2 = K[2], k3 = K[3];
   S[0] = S[1] = S[2] = S[3] = 0ull;
   K[0] = K[1] = K[2] = K[3] = 0u;
-  const long long Ls = s0 + s1 + s2 + s3, Ms = s0 + s1 - s2 - s3;
-  const long long SLs = s0 - s1 + s2 - s3, SMs = s0 - s1 - s2 + s3;
-  const long long n0 = k0 + k1 + k2 + k3, m0 = k0 + k1 - k2 - k3;
-  const long long sn0 = k0 - k1 + k2 - k3, sm0 = k0 - k1 - k2 + k3;
+  const long long Ms = s0 + s1 - s2 - s3, SMs = s0 - s1 - s2 + s3;
   const uint32_t key = (uint32_t)(x - A.ch_slot_off[c]);
   const rnd4 r = philox(ch.seed, A.ch_sweep[c], key, TAG_FLIP, 0);
   uint8_t f;
@@ -915,25 +916,32 @@ __device__ __forceinline__ void root_sums(const Arena& A, int x, int c, RootSums
     f = __fmul_rn(uniform_open(r.x), __fadd_rn(1.0f, e)) < 1.0f ? 1 : 0;
   }
   A.flip[x] = f;
-  R.q[0] = 1ull;
-  R.q[1] = (unsigned long long)m0;
-  R.q[2] = (unsigned long long)sm0;
-  R.q[3] = (unsigned long long)(m0 * m0);
-  R.q[4] = (unsigned long long)(n0 * n0);
-  R.q[5] = (unsigned long long)(sm0 * sm0);
-  R.q[6] = (unsigned long long)(sn0 * sn0);
-  R.q[7] = (unsigned long long)(f ? -Ms : Ms);
-  R.q[8] = (unsigned long long)Ms;
-  R.q[9] = (unsigned long long)SMs;
-  R.w[0] = mul64(R.q[3], R.q[3]);
-  R.w[1] = mul64(R.q[4], R.q[4]);
-  R.w[2] = mul64(R.q[5], R.q[5]);
-  R.w[3] = mul64(R.q[6], R.q[6]);
   auto ab = [](long long v) { return (unsigned long long)(v < 0 ? -v : v); };
-  R.w[4] = mul64(ab(Ls), ab(Ls));
-  R.w[5] = mul64(ab(Ms), ab(Ms));
-  R.w[6] = mul64(ab(SLs), ab(SLs));
-  R.w[7] = mul64(ab(SMs), ab(SMs));
+  {
+    const long long n0 = k0 + k1 + k2 + k3, m0 = k0 + k1 - k2 - k3;
+    const long long sn0 = k0 - k1 + k2 - k3, sm0 = k0 - k1 - k2 + k3;
+    const unsigned long long m0sq = (unsigned long long)(m0 * m0), n0sq = (unsigned long long)(n0 * n0);
+    const unsigned long long sm0sq = (unsigned long long)(sm0 * sm0), sn0sq = (unsigned long long)(sn0 * sn0);
+    R.q[0] += 1ull;
+    R.q[1] += (unsigned long long)m0;
+    R.q[2] += (unsigned long long)sm0;
+    R.q[3] += m0sq;
+    R.q[4] += n0sq;
+    R.q[5] += sm0sq;
+    R.q[6] += sn0sq;
+    add_u128(R.w[0], mul64(m0sq, m0sq));
+    add_u128(R.w[1], mul64(n0sq, n0sq));
+    add_u128(R.w[2], mul64(sm0sq, sm0sq));
+    add_u128(R.w[3], mul64(sn0sq, sn0sq));
+  }
+  R.q[7] += (unsigned long long)(f ? -Ms : Ms);
+  R.q[8] += (unsigned long long)Ms;
+  R.q[9] += (unsigned long long)SMs;
+  const unsigned long long L = ab(s0 + s1 + s2 + s3), SL = ab(s0 - s1 + s2 - s3);
+  add_u128(R.w[4], mul64(L, L));
+  add_u128(R.w[5], mul64(ab(Ms), ab(Ms)));
+  add_u128(R.w[6], mul64(SL, SL));
+  add_u128(R.w[7], mul64(ab(SMs), ab(SMs)));
 }
 
 __device__ __forceinline__ void record_atomics(const Arena& A, int c, const RootSums& R) {
@@ -987,14 +995,14 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
     for (int i = 0; i < 8; ++i) acc.w[i] = {0, 0};
     for (int i = threadIdx.x; i < nr; i += blockDim.x) {
       const int x = roots[i];
-      RootSums R;
       if (uniform) {
-        root_sums(A, x, cf, R);
-#pragma unroll
-        for (int k = 0; k < 10; ++k) acc.q[k] += R.q[k];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) add_u128(acc.w[k], R.w[k]);
+        root_sums(A, x, cf, acc);
       } else {
+        RootSums R;
+#pragma unroll
+        for (int k = 0; k < 10; ++k) R.q[k] = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) R.w[k] = {0, 0};
         const int c = chain_of_segment(A, x);
         root_sums(A, x, c, R);
         record_atomics(A, c, R);
