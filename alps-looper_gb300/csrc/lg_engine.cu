@@ -349,7 +349,7 @@ struct Engine {
     scan(d_site_cnt.p, d_sbase.p, N, &ctl->ns_total, ns_cap, 1, 0, ev ? ev + 3 : nullptr);
     k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A);
     mark(4);
-    k_union<<<grid_for(nv_cap, 256), 256, 0, st>>>(A);
+    k_union<<<(nv_cap + 255) / 256, 256, 0, st>>>(A);  // one vertex per thread: no straggler tail
     mark(5);
     k_accumulate<<<grid_for(ns_cap, 256), 256, 0, st>>>(A);
     mark(6);
