@@ -351,11 +351,11 @@ struct Engine {
     mark(4);
     k_union<<<(nv_cap + 255) / 256, 256, 0, st>>>(A);  // one vertex per thread: no straggler tail
     mark(5);
-    k_accumulate<<<grid_for(ns_cap, 256), 256, 0, st>>>(A);
+    k_accumulate<<<(ns_cap + ACC_TILE - 1) / ACC_TILE, 256, 0, st>>>(A);  // one tile per block
     mark(6);
-    k_cluster<<<grid_for((ns_cap + CL_TILE - 1) / CL_TILE * (long long)CL_THREADS, CL_THREADS), CL_THREADS, 0, st>>>(A);
+    k_cluster<<<(ns_cap + CL_TILE - 1) / CL_TILE, CL_THREADS, 0, st>>>(A);  // one tile per block
     mark(7);
-    k_flip_vertex<<<grid_for(nv_cap, 256), 256, 0, st>>>(A);
+    k_flip_vertex<<<(nv_cap + 255) / 256, 256, 0, st>>>(A);
     mark(8);
     k_site_end<<<grid_for((long long)N * 32, 256, 16), 256, 0, st>>>(A);
     k_end<<<grid_for(C, 128), 128, 0, st>>>(A);
