@@ -893,17 +893,31 @@ __device__ __forceinline__ void add_u128(u128& a, u128 b) {
   a.lo = lo;
 }
 
+// The eight class integers of a root (four time-integrated length sums, four tau = 0 counts).
+struct RootClass { unsigned long long S[4]; unsigned K[4]; };
+
+__device__ __forceinline__ RootClass load_root_class(const Arena& A, int x) {
+  RootClass rc;
+  const ulonglong2* S = reinterpret_cast<const ulonglong2*>(A.cls + 4 * (size_t)x);
+  const ulonglong2 a = S[0], b = S[1];
+  rc.S[0] = a.x; rc.S[1] = a.y; rc.S[2] = b.x; rc.S[3] = b.y;
+  const uint4 k = *reinterpret_cast<const uint4*>(A.cnt0 + 4 * (size_t)x);
+  rc.K[0] = k.x; rc.K[1] = k.y; rc.K[2] = k.z; rc.K[3] = k.w;
+  return rc;
+}
+
 // Flip decision of root x of chain c and its record contribution, added into R; clears the
 // root's class sums.
-__device__ __forceinline__ void root_sums(const Arena& A, int x, int c, RootSums& R) {
+__device__ __forceinline__ void root_sums(const Arena& A, int x, int c, const RootClass& rcl,
+                                          RootSums& R) {
   const DChain ch = A.ch[c];
-  unsigned long long* S = A.cls + 4 * (size_t)x;
-  unsigned* K = A.cnt0 + 4 * (size_t)x;
-  const long long s0 = (long long)S[0], s1 = (long long)S[1], s2 = (long long)S[2],
-                  s3 = (long long)S[3];
-  const long long k0 = K[0], k1 = K[1], k2 = K[2], k3 = K[3];
-  S[0] = S[1] = S[2] = S[3] = 0ull;
-  K[0] = K[1] = K[2] = K[3] = 0u;
+  ulonglong2* S = reinterpret_cast<ulonglong2*>(A.cls + 4 * (size_t)x);
+  S[0] = make_ulonglong2(0ull, 0ull);
+  S[1] = make_ulonglong2(0ull, 0ull);
+  *reinterpret_cast<uint4*>(A.cnt0 + 4 * (size_t)x) = make_uint4(0u, 0u, 0u, 0u);
+  const long long s0 = (long long)rcl.S[0], s1 = (long long)rcl.S[1], s2 = (long long)rcl.S[2],
+                  s3 = (long long)rcl.S[3];
+  const long long k0 = rcl.K[0], k1 = rcl.K[1], k2 = rcl.K[2], k3 = rcl.K[3];
   const long long Ms = s0 + s1 - s2 - s3, SMs = s0 - s1 - s2 + s3;
   const uint32_t key = (uint32_t)(x - A.ch_slot_off[c]);
   const rnd4 r = philox(ch.seed, A.ch_sweep[c], key, TAG_FLIP, 0);
@@ -993,10 +1007,16 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
     for (int i = 0; i < 10; ++i) acc.q[i] = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc.w[i] = {0, 0};
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-      const int x = roots[i];
+    // software-pipelined: the next root's class sums are loaded while this one is processed
+    int i = threadIdx.x;
+    int x = i < nr ? roots[i] : 0;
+    RootClass cur = i < nr ? load_root_class(A, x) : RootClass{};
+    while (i < nr) {
+      const int inext = i + blockDim.x;
+      const int xnext = inext < nr ? roots[inext] : 0;
+      RootClass nxt = inext < nr ? load_root_class(A, xnext) : RootClass{};
       if (uniform) {
-        root_sums(A, x, cf, acc);
+        root_sums(A, x, cf, cur, acc);
       } else {
         RootSums R;
 #pragma unroll
@@ -1004,9 +1024,12 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) R.w[k] = {0, 0};
         const int c = chain_of_segment(A, x);
-        root_sums(A, x, c, R);
+        root_sums(A, x, c, cur, R);
         record_atomics(A, c, R);
       }
+      i = inext;
+      x = xnext;
+      cur = nxt;
     }
     if (uniform) {
 #pragma unroll
