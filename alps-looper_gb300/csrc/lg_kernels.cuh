@@ -783,32 +783,43 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
     }
     __syncthreads();
     const int t0 = tile * ACC_TILE;
-    for (int i = threadIdx.x; i < ACC_TILE; i += blockDim.x) {
-      const int x = t0 + i;
-      const bool valid = x < ns;
-      int root = 0, q = 0;
-      unsigned long long len = 0;
-      if (valid) {
-        int r = x, p = A.parent[x];
-        while (p != r) { r = p; p = A.parent[r]; }
-        if (r != x) A.parent[x] = r;
-        root = r;
-        const uint8_t info = A.sinfo[x];
-        const int64_t ta = bits_fix40(A.stime[x]);
-        const int64_t tb = (info & SI_LAST) ? ((int64_t)1 << 40) : bits_fix40(A.stime[x + 1]);
-        len = (unsigned long long)(tb - ta);
-        q = (info & SI_SPIN) * 2 + ((info & SI_GNEG) ? 1 : 0);
-        if (info & SI_FIRST) atomicAdd(A.cnt0 + 4 * (size_t)r + q, 1u);
+    constexpr int PER = ACC_TILE / 256;  // segments per thread (blockDim.x == 256)
+    int xs[PER], par[PER];
+    uint8_t info[PER];
+    uint64_t ta[PER], tb[PER];
+    // issue every load of this thread's segments first, then walk and add
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int x = t0 + threadIdx.x + j * 256;
+      xs[j] = x;
+      if (x < ns) {
+        par[j] = A.parent[x];
+        info[j] = A.sinfo[x];
+        ta[j] = A.stime[x];
+        tb[j] = (info[j] & SI_LAST) ? 0ull : A.stime[x + 1];
       }
-      if (valid && len) {
-        unsigned h = ((unsigned)root * 2654435761u) >> 22;  // 10-bit hash
+    }
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int x = xs[j];
+      if (x >= ns) continue;
+      int r = x, p = par[j];
+      while (p != r) { r = p; p = A.parent[r]; }
+      if (r != x) A.parent[x] = r;
+      const int64_t lo = bits_fix40(ta[j]);
+      const int64_t hi = (info[j] & SI_LAST) ? ((int64_t)1 << 40) : bits_fix40(tb[j]);
+      const unsigned long long len = (unsigned long long)(hi - lo);
+      const int q = (info[j] & SI_SPIN) * 2 + ((info[j] & SI_GNEG) ? 1 : 0);
+      if (info[j] & SI_FIRST) atomicAdd(A.cnt0 + 4 * (size_t)r + q, 1u);
+      if (len) {
+        unsigned h = ((unsigned)r * 2654435761u) >> 22;  // 10-bit hash
         bool done = false;
         for (int probe = 0; probe < 32; ++probe) {
-          const int k = atomicCAS(hkey + h, -1, root);
-          if (k == -1 || k == root) { atomicAdd(hval + 4 * h + q, len); done = true; break; }
+          const int k = atomicCAS(hkey + h, -1, r);
+          if (k == -1 || k == r) { atomicAdd(hval + 4 * h + q, len); done = true; break; }
           h = (h + 1) & (ACC_HASH - 1);
         }
-        if (!done) atomicAdd(A.cls + 4 * (size_t)root + q, len);
+        if (!done) atomicAdd(A.cls + 4 * (size_t)r + q, len);
       }
     }
     __syncthreads();
