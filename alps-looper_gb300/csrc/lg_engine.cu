@@ -6,9 +6,10 @@
 // run in chunks; after each chunk the exact per-sweep records come back to the host, which turns
 // them into the reference's observables with a rebinning accumulator.
 //
-// A sweep that would overflow the vertex capacity is detected on the device right after the
-// bond scan, before any persistent state is touched; the engine then grows the buffers and
-// replays that sweep with the same random numbers, so capacity never changes a trajectory.
+// A sweep that would overflow the vertex capacity is detected on the device by the insertion
+// pass, before any persistent state is touched; the engine then grows the buffers to the demand
+// it counted and replays that sweep with the same random numbers, so capacity never changes a
+// trajectory.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,12 +29,12 @@
 using namespace lg;
 
 // kernel launches in one sweep (enqueue_sweep)
-static const int kSweepLaunches = 18;
+static const int kSweepLaunches = 14;
 // timed stages of one sweep, in launch order (an event is recorded after each stage)
-static const int kNumStages = 10;
+static const int kNumStages = 8;
 static const char* kStageNames[kNumStages] = {
-    "k_begin+k_insert<count>", "scan(bonds)", "k_insert<write>", "k_site_count+scan(sites)",
-    "k_merge", "k_union", "k_accumulate", "k_cluster", "k_flip_vertex", "k_site_end+k_end"};
+    "k_begin+k_insert", "k_site_count+scan(sites)", "k_merge", "k_union", "k_accumulate",
+    "k_cluster", "k_flip_vertex", "k_site_end+k_end"};
 
 static std::atomic<uint64_t> g_launches{0};
 static thread_local std::string g_err;
@@ -91,9 +92,6 @@ struct Engine {
   DBuf<uint8_t> d_spin0;
   DBuf<int> d_off_base, d_off_cnt;
   DBuf<int> d_bond_cnt, d_bond_ptr, d_site_cnt, d_sbase, d_partial;
-  DBuf<int> d_slab_off;
-  DBuf<uint64_t> d_slab_time;
-  DBuf<uint8_t> d_slab_code, d_slab_ok;
   DBuf<uint64_t> d_vtime;
   DBuf<uint8_t> d_vcode, d_vnew;
   DBuf<int> d_vslot;
@@ -131,8 +129,6 @@ struct Engine {
     A.ch_sweep = d_sweep.p; A.ch_slot_off = d_ch_slot_off.p; A.ch_active = d_active.p;
     A.spin0 = d_spin0.p; A.off_base = d_off_base.p; A.off_cnt = d_off_cnt.p;
     A.bond_cnt = d_bond_cnt.p; A.bond_ptr = d_bond_ptr.p; A.site_cnt = d_site_cnt.p;
-    A.slab_off = d_slab_off.p; A.slab_time = d_slab_time.p; A.slab_code = d_slab_code.p;
-    A.slab_ok = d_slab_ok.p;
     A.sbase = d_sbase.p;
     A.vtime = d_vtime.p; A.vcode = d_vcode.p; A.vnew = d_vnew.p; A.vslot = d_vslot.p;
     A.stime = d_stime.p; A.sinfo = d_sinfo.p; A.svert = d_svert.p; A.sdir = d_sdir.p;
@@ -211,25 +207,6 @@ struct Engine {
         (rc = d_bond_ptr.alloc(NB + 1)) || (rc = d_site_cnt.alloc(N)) ||
         (rc = d_sbase.alloc(N + 1)) || (rc = d_ctl.alloc(1)))
       return rc;
-    // per-bond slabs for the count pass: room for about twice the expected vertices of a bond
-    {
-      std::vector<int> so(NB + 1, 0);
-      long long tot = 0;
-      for (int c = 0; c < C; ++c) {
-        const double lam = spec[c].NB ? spec[c].expected_vertices() / 1.6 / spec[c].NB : 0.0;
-        int cap = (int)(2.0 * lam + 8.0 * std::sqrt(lam) + 16.0);
-        cap = (cap + 7) & ~7;
-        cap = std::min(std::max(cap, 16), 1024);
-        for (int b = 0; b < spec[c].NB; ++b) { so[hch[c].bond_off + b] = (int)tot; tot += cap; }
-      }
-      if (tot > (1ll << 31) - 1) return lg_fail(LG_EBUDGET, "slab space too large");
-      so[NB] = (int)tot;
-      if ((rc = d_slab_off.alloc(NB + 1)) || (rc = d_slab_time.alloc(tot)) ||
-          (rc = d_slab_code.alloc(tot)) || (rc = d_slab_ok.alloc(NB)))
-        return rc;
-      LG_CUDA(cudaMemcpy(d_slab_off.p, so.data(), (NB + 1) * sizeof(int), cudaMemcpyHostToDevice));
-      LG_CUDA(cudaMemset(d_slab_ok.p, 0, NB));
-    }
     int maxparts = std::max((NB + SCAN_TILE - 1) / SCAN_TILE, (N + SCAN_TILE - 1) / SCAN_TILE);
     if ((rc = d_partial.alloc(maxparts + 1))) return rc;
     LG_CUDA(cudaMemcpy(d_ch.p, hch.data(), C * sizeof(DChain), cudaMemcpyHostToDevice));
@@ -340,28 +317,25 @@ struct Engine {
     Ctl* ctl = d_ctl.p;
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
     k_begin<<<grid_for((long long)C * REC_WORDS, 256), 256, 0, st>>>(A);
-    k_insert<false><<<grid_for((long long)N * 32, INS_WARPS * 32, 16), INS_WARPS * 32, 0, st>>>(A);
+    k_insert<<<grid_for((long long)N * 32, INS_WARPS * 32, 16), INS_WARPS * 32, 0, st>>>(A);
     mark(0);
-    scan(d_bond_cnt.p, d_bond_ptr.p, NB, &ctl->nv_total, nv_cap, 1, 0, ev ? ev + 1 : nullptr);
-    k_insert<true><<<grid_for((long long)N * 32, INS_WARPS * 32, 16), INS_WARPS * 32, 0, st>>>(A);
-    mark(2);
-    k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
-    scan(d_site_cnt.p, d_sbase.p, N, &ctl->ns_total, ns_cap, 1, 0, ev ? ev + 3 : nullptr);
+    k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A, 1);
+    scan(d_site_cnt.p, d_sbase.p, N, &ctl->ns_total, ns_cap, 1, 0, ev ? ev + 1 : nullptr);
     k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A);
-    mark(4);
-    k_union<<<(nv_cap + 255) / 256, 256, 0, st>>>(A);  // one vertex per thread: no straggler tail
-    mark(5);
+    mark(2);
+    k_union<<<(ns_cap + UN_WARPS * UN_CHUNK - 1) / (UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);  // one chunk per warp
+    mark(3);
     k_accumulate<<<(ns_cap + ACC_TILE - 1) / ACC_TILE, 256, 0, st>>>(A);  // one tile per block
-    mark(6);
+    mark(4);
     k_cluster<<<(ns_cap + CL_TILE - 1) / CL_TILE, CL_THREADS, 0, st>>>(A);  // one tile per block
-    mark(7);
+    mark(5);
     k_flip_vertex<<<(nv_cap + 255) / 256, 256, 0, st>>>(A);
-    mark(8);
+    mark(6);
     k_site_end<<<grid_for((long long)N * 32, 256, 16), 256, 0, st>>>(A);
     k_end<<<grid_for(C, 128), 128, 0, st>>>(A);
     k_step<<<1, 1, 0, st>>>(ctl);
-    mark(9);
-    g_launches += 12;
+    mark(7);
+    g_launches += 11;
   }
 
   int ensure_graph() {
@@ -424,7 +398,7 @@ struct Engine {
       if (hc.err == ERR_ITERCAP)
         return lg_fail(LG_EITERCAP, "union-find iteration cap hit");
       if (hc.err == ERR_OVERFLOW) {
-        long long need = std::max<long long>((long long)hc.nv_total, nv_cap);
+        long long need = std::max<long long>((long long)std::min<unsigned long long>(hc.nv_alloc, 1ull << 40), nv_cap);
         LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
         rc = alloc_dynamic((long long)(need * 1.25) + 4096, true);
         if (rc) return rc;
@@ -644,10 +618,10 @@ struct Engine {
     hc.nv_total = (int)nops; hc.nv_cap = nv_cap; hc.ns_cap = ns_cap;
     LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
     Arena A = arena();
-    k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
+    k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A, 0);
     scan(d_site_cnt.p, d_sbase.p, N, &d_ctl.p->ns_total, ns_cap, 1, 0);
     k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A);
-    k_union<<<grid_for(nops, 256), 256, 0, st>>>(A);
+    k_union<<<grid_for(2 * nops + N, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
     k_compress<<<grid_for(2 * nops + N, 256), 256, 0, st>>>(A);
     g_launches += 4;
     LG_CUDA(cudaGetLastError());

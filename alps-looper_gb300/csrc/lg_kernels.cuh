@@ -3,9 +3,8 @@
 // One sweep of every chain in the arena (path_integral.C:355-864) is this kernel sequence:
 //
 //   k_begin          zero this sweep's measurement records                   (:472-479 reset)
-//   k_insert<0>      per bond: count vertices of the new operator string      (:403-577)
-//   scan             bond vertex offsets; capacity check
-//   k_insert<1>      per bond: write vertices (time, graph, type)             (:403-577)
+//   k_insert         per bond: new operator string (time, graph, type), written at a vertex
+//                    range claimed with one atomic add; capacity check          (:403-577)
 //   k_site_count     per site: number of segments = 1 + incident vertices
 //   scan             site segment offsets
 //   k_merge          per site: time-ordered segment list, union-find init,
@@ -21,8 +20,11 @@
 // Memory layout (HBM, struct of arrays, 32-bit indices):
 //   sites    spin0[N] u8, off_base[N], off_cnt[N]     persistent between sweeps
 //   bonds    s0/s1[NB], chain[NB], dir0[NB] u8         static
-//   vertices (bond-major CSR by bond_ptr) vtime u64 (FP64 bits), vcode u8 = g<<1|offdiag,
-//            vnew u8, vslot[2] i32 (segment of the leg on source / target site)
+//   vertices (one contiguous time-ordered range per bond: bond_ptr[b], bond_cnt[b]; the ranges
+//            are claimed in whatever order the warps finish, which changes no result: cluster
+//            roots are segment indices and every sum is an exact integer)
+//            vtime u64 (FP64 bits), vcode u8 = g<<1|offdiag, vnew u8,
+//            vslot[2] i32 (segment of the leg on source / target site)
 //   segments (site-major CSR by sbase, k_s+1 per site, bottom segment first) stime u64,
 //            sinfo u8, svert i32, sdir u8, parent i32, flip u8, cls[4] u64, cnt0[4] u32
 //   records  rec[step][chain][32] u64 — exact integer sums (see the R_* word map)
@@ -35,7 +37,9 @@
 namespace lg {
 
 // sinfo bits
-enum : uint8_t { SI_SPIN = 1, SI_GNEG = 2, SI_FIRST = 4, SI_LAST = 8 };
+// SI_SRC: the segment starts at the source-side leg of its vertex; bits 5-6: the vertex's graph
+enum : uint8_t { SI_SPIN = 1, SI_GNEG = 2, SI_FIRST = 4, SI_LAST = 8, SI_SRC = 16 };
+constexpr int SI_GSHIFT = 5;
 
 struct Arena {
   // static
@@ -59,12 +63,8 @@ struct Arena {
   int* off_base;
   int* off_cnt;
   // per-sweep
-  int* bond_cnt;           // NB
-  int* bond_ptr;           // NB+1
-  const int* slab_off;     // NB+1: per-bond slab of the count pass (vertices in final order)
-  uint64_t* slab_time;
-  uint8_t* slab_code;
-  uint8_t* slab_ok;        // NB: 1 when the bond's list fit its slab
+  int* bond_cnt;           // NB: vertices of the bond this sweep
+  int* bond_ptr;           // NB(+1): first vertex of the bond's range
   int* site_cnt;           // N
   int* sbase;              // N+1
   uint64_t* vtime;
@@ -93,6 +93,7 @@ __device__ __forceinline__ unsigned long long* rec_row(const Arena& A, int c) {
 // ---------------------------------------------------------------------------------------------
 __global__ void k_begin(Arena A) {
   if (A.ctl->err) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl->nv_alloc = 0ull;
   LG_GRID_STRIDE(i, A.C * REC_WORDS) {
     A.rec[(size_t)A.ctl->step * A.C * REC_WORDS + i] = 0ull;
   }
@@ -109,8 +110,9 @@ __global__ void k_begin(Arena A) {
 // and draw a new graph with probability v0/(v0+v1) for g = 0 (graph_impl.h:323-327).  Old
 // diagonal operators are dropped (path_integral.C:515-518).
 // The output list is time ordered; at equal times off-diagonal operators come first.
+// Returns the number of vertices; with WRITE the list is stored from vertex out0 on.
 template <bool WRITE>
-__device__ void insert_bond_serial(const Arena& A, int b) {
+__device__ int insert_bond_serial(const Arena& A, int b, int out0) {
   {
     const int c = A.bond_chain[b];
     const DChain ch = A.ch[c];
@@ -147,7 +149,7 @@ __device__ void insert_bond_serial(const Arena& A, int b) {
     };
     next_prop();
 
-    int out = WRITE ? A.bond_ptr[b] : 0;
+    int out = out0;
     uint32_t ordinal = 0;
     rnd4 ro = {0, 0, 0, 0};
     while (true) {
@@ -183,8 +185,30 @@ __device__ void insert_bond_serial(const Arena& A, int b) {
         next_prop();
       }
     }
-    if (!WRITE) A.bond_cnt[b] = out;
+    return out - out0;
   }
+}
+
+// Claims n vertices for bond b; returns the first, or -1 (and flags the sweep) when the vertex
+// buffers are too small.  The claim is made even then, so that nv_alloc ends at the demand.
+__device__ __forceinline__ int claim_vertices(const Arena& A, int b, int n) {
+  if (n == 0) { A.bond_cnt[b] = 0; A.bond_ptr[b] = 0; return 0; }
+  const unsigned long long at = atomicAdd(&A.ctl->nv_alloc, (unsigned long long)n);
+  A.bond_cnt[b] = n;
+  if (at + (unsigned long long)n > (unsigned long long)A.ctl->nv_cap) {
+    A.bond_ptr[b] = 0;
+    atomicExch(&A.ctl->err, ERR_OVERFLOW);
+    return -1;
+  }
+  A.bond_ptr[b] = (int)at;
+  return (int)at;
+}
+
+// One-thread insertion of bond b: count, claim, write (the same list as the warp form).
+__device__ void insert_bond_alone(const Arena& A, int b) {
+  const int n = insert_bond_serial<false>(A, b, 0);
+  const int at = claim_vertices(A, b, n);
+  if (at >= 0) insert_bond_serial<true>(A, b, at);
 }
 
 
@@ -211,11 +235,8 @@ __device__ __forceinline__ int count_lt(const uint64_t* T, int n, uint64_t t) {
   return a;
 }
 
-// Count pass (WRITE = false): counts the new vertices of every owned bond and stores the bond's
-// finished list (time order, graphs chosen) in its slab when it fits.  Write pass: copies the
-// slabs to the compact bond-major arrays; only bonds whose list overflowed their slab (or the
-// staging capacity) are recomputed, with the same random numbers.
-template <bool WRITE>
+// The vertex count n of a bond is known once its proposals are drawn, so the warp claims its
+// range of n vertices (claim_vertices) before it writes the list there: one pass, no scan.
 __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
   if (A.ctl->err) return;
   __shared__ uint64_t offS[INS_WARPS][INS_CAP];
@@ -231,25 +252,10 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
     const int j0 = A.inc_off[s];
     const int z = A.inc_off[s + 1] - j0;
     if (!A.ch_active[A.site_chain[s]]) {
-      if (!WRITE && lane == 0)
+      if (lane == 0)
         for (int d = 0; d < z; ++d)
-          if (A.inc_side[j0 + d] == 0) { A.bond_cnt[A.inc[j0 + d]] = 0; A.slab_ok[A.inc[j0 + d]] = 1; }
+          if (A.inc_side[j0 + d] == 0) { A.bond_cnt[A.inc[j0 + d]] = 0; A.bond_ptr[A.inc[j0 + d]] = 0; }
       continue;
-    }
-    bool all_slab = WRITE;
-    if (WRITE) {
-      // copy the finished lists of the owned bonds
-      for (int d = 0; d < z; ++d) {
-        if (A.inc_side[j0 + d] != 0) continue;
-        const int b = A.inc[j0 + d];
-        if (!A.slab_ok[b]) { all_slab = false; continue; }
-        const int n = A.bond_cnt[b], so = A.slab_off[b], out0 = A.bond_ptr[b];
-        for (int i = lane; i < n; i += 32) {
-          A.vtime[out0 + i] = A.slab_time[so + i];
-          A.vcode[out0 + i] = A.slab_code[so + i];
-        }
-      }
-      if (all_slab) continue;
     }
     const int ns_off = A.off_cnt[s];
     const int sb = A.off_base[s];
@@ -261,14 +267,10 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
     for (int d = 0; d < z; ++d) {
       if (A.inc_side[j0 + d] != 0) continue;  // bonds owned by s: s is the source
       const int b = A.inc[j0 + d];
-      if (WRITE && A.slab_ok[b]) continue;
       const int t = A.bond_s1[b];
       const int nt_off = A.off_cnt[t];
       if (!s_fits || nt_off > INS_CAP) {
-        if (lane == 0) {
-          insert_bond_serial<WRITE>(A, b);
-          if (!WRITE) A.slab_ok[b] = 0;
-        }
+        if (lane == 0) insert_bond_alone(A, b);
         __syncwarp();
         continue;
       }
@@ -339,31 +341,18 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
         k0 += 32;
       }
       const int n = nacc + nown;
-      bool fits = nacc <= INS_ACC;
-      uint64_t* dt = A.vtime;
-      uint8_t* dc = A.vcode;
       int out0 = 0;
-      if (!WRITE) {
-        if (lane == 0) A.bond_cnt[b] = n;
-        fits = fits && n <= A.slab_off[b + 1] - A.slab_off[b];
-        if (lane == 0) A.slab_ok[b] = fits ? 1 : 0;
-        dt = A.slab_time;
-        dc = A.slab_code;
-        out0 = A.slab_off[b];
-      } else {
-        out0 = A.bond_ptr[b];
-        if (!fits) {
-          __syncwarp();
-          if (lane == 0) insert_bond_serial<true>(A, b);
-        }
-      }
-      __syncwarp();
-      if (fits) {
+      if (lane == 0) out0 = claim_vertices(A, b, n);
+      out0 = __shfl_sync(0xFFFFFFFFu, out0, 0);
+      if (out0 >= 0 && nacc > INS_ACC) {
+        // more accepted proposals than the staging holds: the one-thread form writes the list
+        if (lane == 0) insert_bond_serial<true>(A, b, out0);
+      } else if (out0 >= 0) {
         for (int j = lane; j < nacc; j += 32) {
           const uint64_t tp = accT[w][j];
           const int pos = j + count_le(ownT[w], nown, tp);
-          dt[out0 + pos] = tp;
-          dc[out0 + pos] = (uint8_t)(accG[w][j] << 1);
+          A.vtime[out0 + pos] = tp;
+          A.vcode[out0 + pos] = (uint8_t)(accG[w][j] << 1);
         }
         for (int i = lane; i < nown; i += 32) {
           const uint64_t to = ownT[w][i];
@@ -371,8 +360,8 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
           const rnd4 ro = philox(ch.seed, sweep, bl, TAG_OFFDIAG, (uint32_t)i >> 2);
           const uint32_t wv = (i & 3) == 0 ? ro.x : (i & 3) == 1 ? ro.y : (i & 3) == 2 ? ro.z : ro.w;
           const uint32_t g = ((uint64_t)wv < ch.Poff) ? 0u : 1u;
-          dt[out0 + pos] = to;
-          dc[out0 + pos] = (uint8_t)((g << 1) | 1u);
+          A.vtime[out0 + pos] = to;
+          A.vcode[out0 + pos] = (uint8_t)((g << 1) | 1u);
         }
       }
       __syncwarp();
@@ -479,8 +468,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const int* in, int*
 }
 
 // ---------------------------------------------------------------------------------------------
-__global__ void k_site_count(Arena A) {
+// Per site: number of segments.  In a sweep (from_claims) the vertex total is also taken from
+// the insertion's claims; the labelling paths set it themselves.
+__global__ void k_site_count(Arena A, int from_claims) {
   if (A.ctl->err) return;
+  if (from_claims && blockIdx.x == 0 && threadIdx.x == 0) A.ctl->nv_total = (int)A.ctl->nv_alloc;
   LG_GRID_STRIDE(s, A.N) {
     int k = 1;
     for (int j = A.inc_off[s]; j < A.inc_off[s + 1]; ++j) k += A.bond_cnt[A.inc[j]];
@@ -530,7 +522,7 @@ __device__ void merge_site_serial(Arena& A, int s) {
     if (d < z) {
       const int b = A.inc[j0 + d];
       cur[d] = A.bond_ptr[b];
-      end[d] = A.bond_ptr[b + 1];
+      end[d] = cur[d] + A.bond_cnt[b];
       side[d] = A.inc_side[j0 + d];
       ht[d] = cur[d] < end[d] ? A.vtime[cur[d]] : TIME_INF;
       hc[d] = cur[d] < end[d] ? A.vcode[cur[d]] : 0;
@@ -567,7 +559,8 @@ __device__ void merge_site_serial(Arena& A, int s) {
     }
     if (code & 1u) spin ^= 1u;
     A.stime[x] = bt;
-    A.sinfo[x] = (uint8_t)(spin | gneg | (j == k ? SI_LAST : 0));
+    A.sinfo[x] = (uint8_t)(spin | gneg | (j == k ? SI_LAST : 0) | (sd == 0 ? SI_SRC : 0) |
+                           ((code >> 1) << SI_GSHIFT));
     A.svert[x] = v;
     A.sdir[x] = (uint8_t)best;
     A.parent[x] = x;
@@ -607,7 +600,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A) {
       if (d < z) {
         const int b = A.inc[j0 + d];
         ptr[d] = A.bond_ptr[b];
-        off[d + 1] = off[d] + (A.bond_ptr[b + 1] - ptr[d]);
+        off[d + 1] = off[d] + A.bond_cnt[b];
       } else {
         ptr[d] = 0; off[d + 1] = off[d];
       }
@@ -662,12 +655,14 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A) {
         for (int q = 0; q < MAXZ; ++q) if (q == d) { pd = ptr[q]; od = off[q]; }
         const int v = pd + (e - od);
         const int x = base + 1 + r;
+        const uint8_t side = A.inc_side[j0 + d];
         A.stime[x] = sT[w][e];
-        A.sinfo[x] = (uint8_t)(spin | gneg | (r == k - 1 ? SI_LAST : 0));
+        A.sinfo[x] = (uint8_t)(spin | gneg | (r == k - 1 ? SI_LAST : 0) | (side == 0 ? SI_SRC : 0) |
+                               ((cd >> 1) << SI_GSHIFT));
         A.svert[x] = v;
         A.sdir[x] = (uint8_t)d;
         A.parent[x] = (r == k - 1) ? base : x;  // closure: top segment joins the bottom one
-        A.vslot[2 * v + A.inc_side[j0 + d]] = x;
+        A.vslot[2 * v + side] = x;
       }
       carry ^= __popc(ball) & 1u;
     }
@@ -708,24 +703,48 @@ __device__ __forceinline__ bool uf_union(int* P, int a, int b) {
 // reconnect (graph_impl.h:280-295) in segment form: g = 0 joins the two lower legs and the two
 // upper legs; g = 1 joins lower-left with upper-right and lower-right with upper-left; frozen
 // graphs (g & 2) join all four legs.
-__global__ void __launch_bounds__(256) k_union(Arena A) {
+//
+// The warps run over chunks of 64 consecutive segments (site-major order); the source-side
+// segments of a chunk, about half of them, are compacted so that every lane makes the unions of
+// one vertex.  Neighbouring warps so work on neighbouring sites, whatever order the vertex
+// ranges were claimed in, which keeps the union-find trees of concurrently running blocks local.
+constexpr int UN_WARPS = 8;
+constexpr int UN_CHUNK = 64;
+
+__global__ void __launch_bounds__(UN_WARPS * 32) k_union(Arena A) {
   if (A.ctl->err) return;
-  const int nv = A.ctl->nv_total;
+  __shared__ int pend[UN_WARPS][UN_CHUNK];
+  const int ns = A.ctl->ns_total;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const long long stride = (long long)gridDim.x * UN_WARPS * UN_CHUNK;
   bool ok = true;
-  LG_GRID_STRIDE(v, nv) {
-    const int a = A.vslot[2 * v], b = A.vslot[2 * v + 1];
-    const int g = A.vcode[v] >> 1;
-    if (g & 2) {
-      ok &= uf_union(A.parent, a - 1, b - 1);
-      ok &= uf_union(A.parent, a, b);
-      ok &= uf_union(A.parent, a - 1, a);
-    } else if (g == 0) {
-      ok &= uf_union(A.parent, a - 1, b - 1);
-      ok &= uf_union(A.parent, a, b);
-    } else {
-      ok &= uf_union(A.parent, a - 1, b);
-      ok &= uf_union(A.parent, b - 1, a);
+  for (long long c0 = ((long long)blockIdx.x * UN_WARPS + w) * UN_CHUNK; c0 < ns; c0 += stride) {
+    const int x0 = (int)c0 + lane, x1 = x0 + 32;
+    const bool s0 = x0 < ns && (A.sinfo[x0] & SI_SRC);
+    const bool s1 = x1 < ns && (A.sinfo[x1] & SI_SRC);
+    const unsigned m0 = __ballot_sync(0xFFFFFFFFu, s0), m1 = __ballot_sync(0xFFFFFFFFu, s1);
+    const int n0 = __popc(m0), tot = n0 + __popc(m1);
+    if (s0) pend[w][__popc(m0 & lt)] = x0;
+    if (s1) pend[w][n0 + __popc(m1 & lt)] = x1;
+    __syncwarp();
+    for (int j = lane; j < tot; j += 32) {
+      const int a = pend[w][j];
+      const int g = A.sinfo[a] >> SI_GSHIFT;
+      const int b = A.vslot[2 * A.svert[a] + 1];
+      if (g & 2) {
+        ok &= uf_union(A.parent, a - 1, b - 1);
+        ok &= uf_union(A.parent, a, b);
+        ok &= uf_union(A.parent, a - 1, a);
+      } else if (g == 0) {
+        ok &= uf_union(A.parent, a - 1, b - 1);
+        ok &= uf_union(A.parent, a, b);
+      } else {
+        ok &= uf_union(A.parent, a - 1, b);
+        ok &= uf_union(A.parent, b - 1, a);
+      }
     }
+    __syncwarp();
   }
   if (!ok) atomicExch(&A.ctl->err, ERR_ITERCAP);
 }
@@ -1151,8 +1170,8 @@ __global__ void __launch_bounds__(256) k_site_end(Arena A) {
 __global__ void k_end(Arena A) {
   if (A.ctl->err) return;
   LG_GRID_STRIDE(c, A.C) {
-    const DChain ch = A.ch[c];
-    const int nv = A.bond_ptr[ch.bond_off + ch.nbonds] - A.bond_ptr[ch.bond_off];
+    // every vertex adds one segment at each of its two sites
+    const int nv = (A.ch_slot_off[c + 1] - A.ch_slot_off[c] - A.ch[c].nsites) / 2;
     rec_row(A, c)[R_NOP] = (unsigned long long)nv;
     A.ch_sweep[c] += 1u;
   }

@@ -39,7 +39,9 @@ struct Ctl {
   uint32_t step;     // record row of the current sweep
   int nv_cap;
   int ns_cap;
-  int pad[2];
+  // vertex slots claimed by the insertion pass; 64-bit so that it counts the whole demand of a
+  // sweep that overflows nv_cap (the engine grows to it and replays the sweep)
+  unsigned long long nv_alloc;
 };
 
 }  // namespace lg
