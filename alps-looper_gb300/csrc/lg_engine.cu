@@ -28,8 +28,6 @@
 
 using namespace lg;
 
-// kernel launches in one sweep (enqueue_sweep)
-static const int kSweepLaunches = 14;
 // timed stages of one sweep, in launch order (an event is recorded after each stage)
 static const int kNumStages = 8;
 static const char* kStageNames[kNumStages] = {
@@ -71,6 +69,20 @@ struct DBuf {
   }
 };
 
+// Launch shape of an arena's sweep.  No choice here changes a result: every variant computes the
+// same vertices, segments, clusters and exact sums.
+//   narrow_k  chains whose expected endpoints per site (2 beta W N_b / N) are below this use the
+//             thread-per-bond / thread-per-site kernels, the others a warp per site
+//   acc_tile  segments per block in k_accumulate (512, 1024, 2048)
+//   cl_tile   segments per block in k_cluster (2048, 4096, 8192)
+//   un_warps  warps per block in k_union (4, 8, 16)
+struct Shape {
+  double narrow_k = 32.0;
+  int acc_tile = 1024;
+  int cl_tile = 4096;
+  int un_warps = 8;
+};
+
 // ----------------------------------------------------------------------------------------------
 struct Engine {
   std::vector<ChainSpec> spec;
@@ -105,6 +117,14 @@ struct Engine {
 
   int nv_cap = 0, ns_cap = 0;
   int rec_rows = 64;
+  // site / bond classes of the current shape (nullptr list: all sites, in order)
+  Shape shape;
+  DBuf<int> d_wide_sites, d_narrow_sites, d_narrow_bonds;
+  const int* wide_list = nullptr;
+  int n_wide = 0, n_narrow = 0, n_narrow_b = 0;
+  int sweep_launches = 0;         // kernel launches of one sweep
+  cudaStream_t st2 = nullptr;     // the narrow kernels run beside the wide ones
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaStream_t st = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -117,6 +137,9 @@ struct Engine {
   ~Engine() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -148,6 +171,9 @@ struct Engine {
     LG_CUDA(cudaGetDeviceProperties(&prop, dev));
     nsm = prop.multiProcessorCount;
     LG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    LG_CUDA(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+    LG_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    LG_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     // static tables
     long long nsite = 0, nbond = 0;
     for (auto& s : spec) { nsite += s.N; nbond += s.NB; }
@@ -230,6 +256,7 @@ struct Engine {
     long long cap = (long long)(1.3 * est) + 4096;
     LG_CUDA(cudaMemset(d_ctl.p, 0, sizeof(Ctl)));
     if ((rc = alloc_dynamic(cap, false))) return rc;
+    if ((rc = set_shape(shape))) return rc;
     // initial spins (one launch per distinct init mode)
     Arena A = arena();
     int random = spec.empty() ? 0 : spec[0].init_spins;
@@ -286,6 +313,47 @@ struct Engine {
     return LG_OK;
   }
 
+  // Expected endpoints per site of chain c: the narrow / wide criterion.
+  double endpoints_per_site(int c) const {
+    const ChainSpec& s = spec[c];
+    return s.N ? 2.0 * s.beta * s.W * s.NB / s.N : 0.0;
+  }
+
+  // Adopt a launch shape: classify chains as narrow or wide and upload the class lists.
+  int set_shape(const Shape& sh) {
+    if (!(sh.acc_tile == 512 || sh.acc_tile == 1024 || sh.acc_tile == 2048) ||
+        !(sh.cl_tile == 2048 || sh.cl_tile == 4096 || sh.cl_tile == 8192) ||
+        !(sh.un_warps == 4 || sh.un_warps == 8 || sh.un_warps == 16) || !(sh.narrow_k >= 0))
+      return lg_fail(LG_EINVAL, "bad launch shape");
+    std::vector<int> ws, nsl, nbl;
+    for (int c = 0; c < C; ++c) {
+      const bool narrow = endpoints_per_site(c) < sh.narrow_k;
+      for (int i = 0; i < spec[c].N; ++i) (narrow ? nsl : ws).push_back(hch[c].site_off + i);
+      if (narrow)
+        for (int b = 0; b < spec[c].NB; ++b) nbl.push_back(hch[c].bond_off + b);
+    }
+    int rc;
+    n_wide = (int)ws.size();
+    n_narrow = (int)nsl.size();
+    n_narrow_b = (int)nbl.size();
+    wide_list = nullptr;
+    if (n_narrow > 0 && n_wide > 0) {
+      if ((rc = d_wide_sites.alloc(n_wide))) return rc;
+      LG_CUDA(cudaMemcpy(d_wide_sites.p, ws.data(), n_wide * sizeof(int), cudaMemcpyHostToDevice));
+      wide_list = d_wide_sites.p;
+    }
+    if (n_narrow > 0) {
+      if ((rc = d_narrow_sites.alloc(n_narrow)) || (rc = d_narrow_bonds.alloc(std::max(n_narrow_b, 1))))
+        return rc;
+      LG_CUDA(cudaMemcpy(d_narrow_sites.p, nsl.data(), n_narrow * sizeof(int), cudaMemcpyHostToDevice));
+      if (n_narrow_b)
+        LG_CUDA(cudaMemcpy(d_narrow_bonds.p, nbl.data(), n_narrow_b * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    shape = sh;
+    drop_graph();
+    return LG_OK;
+  }
+
   void drop_graph() {
     if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
     if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
@@ -299,6 +367,7 @@ struct Engine {
     return (int)g;
   }
 
+  // Three-kernel exclusive scan on the engine's stream (launches are counted by the caller).
   void scan(const int* in, int* out, int n, int* total, int cap, int per_item, int extra,
             cudaEvent_t* ev = nullptr) {
     int parts = (n + SCAN_TILE - 1) / SCAN_TILE;
@@ -307,35 +376,89 @@ struct Engine {
     k_scan_partials<<<1, 1024, 0, st>>>(d_partial.p, parts, total, cap, per_item, extra, d_ctl.p);
     k_scan_apply<<<parts, SCAN_THREADS, 0, st>>>(in, out, n, d_partial.p, d_ctl.p);
     if (ev) cudaEventRecord(*ev, st);
-    g_launches += 3;
   }
 
   // The sweep of every chain, as a fixed sequence of launches (capturable).  With ev != nullptr
-  // an event is recorded after each stage (kNumStages events) for per-kernel timing.
+  // an event is recorded after each stage (kNumStages events) for per-kernel timing.  When an
+  // arena has both narrow and wide chains, the narrow kernels of a stage run on a second stream
+  // beside the wide ones (a fork and a join in the captured graph).
   void enqueue_sweep(cudaEvent_t* ev = nullptr) {
     Arena A = arena();
     Ctl* ctl = d_ctl.p;
+    int launches = 0;
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
+    const bool both = n_wide > 0 && n_narrow > 0;
+    cudaStream_t sn = both ? st2 : st;
+    auto fork = [&]() { if (both) { cudaEventRecord(ev_fork, st); cudaStreamWaitEvent(st2, ev_fork, 0); } };
+    auto join = [&]() { if (both) { cudaEventRecord(ev_join, st2); cudaStreamWaitEvent(st, ev_join, 0); } };
     k_begin<<<grid_for((long long)C * REC_WORDS, 256), 256, 0, st>>>(A);
-    k_insert<<<grid_for((long long)N * 32, INS_WARPS * 32, 16), INS_WARPS * 32, 0, st>>>(A);
+    ++launches;
+    fork();
+    if (n_wide) {
+      k_insert<<<grid_for((long long)n_wide * 32, INS_WARPS * 32, 16), INS_WARPS * 32, 0, st>>>(A, wide_list, n_wide);
+      ++launches;
+    }
+    if (n_narrow_b) {
+      k_insert_narrow<<<grid_for(n_narrow_b, 256, 16), 256, 0, sn>>>(A, d_narrow_bonds.p, n_narrow_b);
+      ++launches;
+    }
+    join();
     mark(0);
     k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A, 1);
     scan(d_site_cnt.p, d_sbase.p, N, &ctl->ns_total, ns_cap, 1, 0, ev ? ev + 1 : nullptr);
-    k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A);
+    launches += 4;
+    fork();
+    if (n_wide) {
+      k_merge<<<grid_for((long long)n_wide * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A, wide_list, n_wide);
+      ++launches;
+    }
+    if (n_narrow) {
+      k_merge_narrow<<<grid_for(n_narrow, 256, 16), 256, 0, sn>>>(A, d_narrow_sites.p, n_narrow);
+      ++launches;
+    }
+    join();
     mark(2);
-    k_union<<<(ns_cap + UN_WARPS * UN_CHUNK - 1) / (UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);  // one chunk per warp
+    {
+      const int w = shape.un_warps, per = w * UN_CHUNK;
+      const int g = (ns_cap + per - 1) / per;  // one chunk per warp: no straggler tail
+      if (w == 4) k_union<4><<<g, 4 * 32, 0, st>>>(A);
+      else if (w == 16) k_union<16><<<g, 16 * 32, 0, st>>>(A);
+      else k_union<8><<<g, 8 * 32, 0, st>>>(A);
+    }
     mark(3);
-    k_accumulate<<<(ns_cap + ACC_TILE - 1) / ACC_TILE, 256, 0, st>>>(A);  // one tile per block
+    {
+      const int t = shape.acc_tile, g = (ns_cap + t - 1) / t;  // one tile per block
+      if (t == 512) k_accumulate<512><<<g, 256, 0, st>>>(A);
+      else if (t == 2048) k_accumulate<2048><<<g, 256, 0, st>>>(A);
+      else k_accumulate<1024><<<g, 256, 0, st>>>(A);
+    }
     mark(4);
-    k_cluster<<<(ns_cap + CL_TILE - 1) / CL_TILE, CL_THREADS, 0, st>>>(A);  // one tile per block
+    {
+      const int t = shape.cl_tile, g = (ns_cap + t - 1) / t;  // one tile per block
+      if (t == 2048) k_cluster<2048><<<g, CL_THREADS, 0, st>>>(A);
+      else if (t == 8192) k_cluster<8192><<<g, CL_THREADS, 0, st>>>(A);
+      else k_cluster<4096><<<g, CL_THREADS, 0, st>>>(A);
+    }
     mark(5);
     k_flip_vertex<<<(nv_cap + 255) / 256, 256, 0, st>>>(A);
     mark(6);
-    k_site_end<<<grid_for((long long)N * 32, 256, 16), 256, 0, st>>>(A);
+    launches += 4;
+    fork();
+    if (n_wide) {
+      k_site_end<<<grid_for((long long)n_wide * 32, 256, 16), 256, 0, st>>>(A, wide_list, n_wide);
+      ++launches;
+    }
+    if (n_narrow) {
+      k_site_end_narrow<<<grid_for(n_narrow, 256, 16), 256, 0, sn>>>(A, d_narrow_sites.p, n_narrow);
+      ++launches;
+    }
+    join();
     k_end<<<grid_for(C, 128), 128, 0, st>>>(A);
     k_step<<<1, 1, 0, st>>>(ctl);
     mark(7);
-    g_launches += 11;
+    launches += 2;
+    sweep_launches = launches;
+    g_launches += launches;
   }
 
   int ensure_graph() {
@@ -372,7 +495,7 @@ struct Engine {
         }
         if (gexec) {
           LG_CUDA(cudaGraphLaunch(gexec, st));
-          g_launches += kSweepLaunches;
+          g_launches += sweep_launches;
         } else {
           enqueue_sweep();
         }
@@ -452,6 +575,75 @@ struct Engine {
     }
     *vertices = verts;
     return LG_OK;
+  }
+
+  // Launch-shape autotuner.  Each candidate shape is timed over `trial` sweeps (per-stage events,
+  // L2 flushed before each sweep); the candidates are searched one coordinate at a time, starting
+  // with the narrow / wide split, and the fastest shape is kept.  The timed sweeps are the
+  // chains' own sweeps: no shape changes a result, so tuning costs no extra sweeps.
+  int autotune(int trial, size_t flush_bytes, std::string& report) {
+    if (trial < 1) trial = 1;
+    char line[160];
+    report.clear();
+    auto time_shape = [&](const Shape& sh, double* ms) -> int {
+      int rc = set_shape(sh);
+      if (rc) return rc;
+      std::vector<double> km(kNumStages);
+      long long v = 0;
+      if ((rc = profile(1, flush_bytes, km.data(), &v))) return rc;  // first launches: untimed
+      if ((rc = profile(trial, flush_bytes, km.data(), &v))) return rc;
+      double t = 0;
+      for (double x : km) t += x;
+      *ms = t / trial;
+      std::snprintf(line, sizeof(line), "narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d: %.4f ms\n",
+                    sh.narrow_k, sh.acc_tile, sh.cl_tile, sh.un_warps, *ms);
+      report += line;
+      return LG_OK;
+    };
+    Shape best = shape;
+    double best_ms = 0;
+    int rc = time_shape(best, &best_ms);
+    if (rc) return rc;
+    auto consider = [&](Shape cand) -> int {
+      double ms = 0;
+      int r = time_shape(cand, &ms);
+      if (r) return r;
+      if (ms < best_ms) { best_ms = ms; best = cand; }
+      return LG_OK;
+    };
+    // narrow / wide split: one candidate per distinct set of narrow chains
+    std::vector<double> mu(C);
+    for (int c = 0; c < C; ++c) mu[c] = endpoints_per_site(c);
+    std::vector<int> seen;
+    auto n_below = [&](double k) { int n = 0; for (double m : mu) n += m < k; return n; };
+    seen.push_back(n_below(best.narrow_k));
+    for (double k : {0.0, 4.0, 8.0, 16.0, 32.0, 64.0, 128.0, 256.0, 1e300}) {
+      const int nb = n_below(k);
+      if (std::find(seen.begin(), seen.end(), nb) != seen.end()) continue;
+      seen.push_back(nb);
+      Shape c = best;
+      c.narrow_k = k;
+      if ((rc = consider(c))) return rc;
+    }
+    for (int t : {512, 1024, 2048}) {
+      if (t == best.acc_tile) continue;
+      Shape c = best; c.acc_tile = t;
+      if ((rc = consider(c))) return rc;
+    }
+    for (int t : {2048, 4096, 8192}) {
+      if (t == best.cl_tile) continue;
+      Shape c = best; c.cl_tile = t;
+      if ((rc = consider(c))) return rc;
+    }
+    for (int w : {4, 8, 16}) {
+      if (w == best.un_warps) continue;
+      Shape c = best; c.un_warps = w;
+      if ((rc = consider(c))) return rc;
+    }
+    std::snprintf(line, sizeof(line), "chosen: narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d (%.4f ms)\n",
+                  best.narrow_k, best.acc_tile, best.cl_tile, best.un_warps, best_ms);
+    report += line;
+    return set_shape(best);
   }
 
   void consume(int rows) {
@@ -620,10 +812,10 @@ struct Engine {
     Arena A = arena();
     k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A, 0);
     scan(d_site_cnt.p, d_sbase.p, N, &d_ctl.p->ns_total, ns_cap, 1, 0);
-    k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A);
-    k_union<<<grid_for(2 * nops + N, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
+    k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A, nullptr, N);
+    k_union<><<<grid_for(2 * nops + N, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
     k_compress<<<grid_for(2 * nops + N, 256), 256, 0, st>>>(A);
-    g_launches += 4;
+    g_launches += 7;
     LG_CUDA(cudaGetLastError());
     LG_CUDA(cudaStreamSynchronize(st));
     LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
@@ -687,6 +879,7 @@ struct Engine {
     k_repack_count<<<grid_for(N, 256), 256, 0, st>>>(A, dmap.p, old.d_off_cnt.p, dcnt.p);
     LG_CUDA(cudaMemsetAsync(d_ctl.p, 0, sizeof(int), st));
     scan(dcnt.p, dbase.p, N, &d_ctl.p->ns_total, 0x7FFFFFFF, 0, 0);
+    g_launches += 3;
     LG_CUDA(cudaMemcpyAsync(d_off_cnt.p, dcnt.p, N * sizeof(int), cudaMemcpyDeviceToDevice, st));
     int total = 0;
     LG_CUDA(cudaMemcpyAsync(&total, dbase.p + N, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -697,7 +890,7 @@ struct Engine {
     }
     k_repack_copy<<<grid_for((long long)N * 32, 256), 256, 0, st>>>(A, dmap.p, old.d_spin0.p,
         old.d_off_base.p, old.d_stime.p, old.d_sdir.p, dbase.p);
-    g_launches += 5;
+    g_launches += 2;
     LG_CUDA(cudaGetLastError());
     LG_CUDA(cudaStreamSynchronize(st));
     return LG_OK;
@@ -710,7 +903,7 @@ struct Engine {
     hch[c].flip_coef = spec[c].dchain.flip_coef;
     LG_CUDA(cudaMemcpy(d_ch.p + c, &hch[c], sizeof(DChain), cudaMemcpyHostToDevice));
     acc[c] = ChainAcc();
-    return LG_OK;
+    return set_shape(shape);  // the chain's narrow / wide class depends on beta
   }
 };
 
@@ -905,6 +1098,54 @@ int lg_batch_stats(const lg_batch* b, int64_t* total_sites, int64_t* site_sweeps
   return LG_OK;
 }
 
+
+static void shape_out(const Shape& s, lg_shape* out) {
+  if (!out) return;
+  out->narrow_k = s.narrow_k;
+  out->acc_tile = s.acc_tile;
+  out->cl_tile = s.cl_tile;
+  out->union_warps = s.un_warps;
+  out->reserved = 0;
+}
+
+static int autotune_engine(Engine& e, int trial, size_t flush_bytes, lg_shape* chosen, char* report,
+                           size_t report_len) {
+  std::string rep;
+  int rc = e.autotune(trial, flush_bytes, rep);
+  if (report && report_len) std::snprintf(report, report_len, "%s", rep.c_str());
+  if (rc) return rc;
+  shape_out(e.shape, chosen);
+  return LG_OK;
+}
+
+int lg_autotune(lg_chain* c, int trial_sweeps, size_t flush_bytes, lg_shape* chosen, char* report,
+                size_t report_len) {
+  if (!c || trial_sweeps < 1) return lg_fail(LG_EINVAL, "bad argument");
+  if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_autotune on a batch member; use lg_batch_autotune");
+  return autotune_engine(*c->eng, trial_sweeps, flush_bytes, chosen, report, report_len);
+}
+
+int lg_batch_autotune(lg_batch* b, int trial_sweeps, size_t flush_bytes, lg_shape* chosen,
+                      char* report, size_t report_len) {
+  if (!b || trial_sweeps < 1) return lg_fail(LG_EINVAL, "bad argument");
+  return autotune_engine(*b->eng, trial_sweeps, flush_bytes, chosen, report, report_len);
+}
+
+int lg_batch_get_shape(const lg_batch* b, lg_shape* out) {
+  if (!b || !out) return lg_fail(LG_EINVAL, "null argument");
+  shape_out(b->eng->shape, out);
+  return LG_OK;
+}
+
+int lg_batch_set_shape(lg_batch* b, const lg_shape* in) {
+  if (!b || !in) return lg_fail(LG_EINVAL, "null argument");
+  Shape s;
+  s.narrow_k = in->narrow_k;
+  s.acc_tile = in->acc_tile;
+  s.cl_tile = in->cl_tile;
+  s.un_warps = in->union_warps;
+  return b->eng->set_shape(s);
+}
 
 int lg_time_sweeps(lg_chain* c, int64_t n, size_t flush_bytes, float* ms) {
   if (!c || n < 0 || !ms) return lg_fail(LG_EINVAL, "bad argument");

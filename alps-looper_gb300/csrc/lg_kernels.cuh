@@ -237,7 +237,8 @@ __device__ __forceinline__ int count_lt(const uint64_t* T, int n, uint64_t t) {
 
 // The vertex count n of a bond is known once its proposals are drawn, so the warp claims its
 // range of n vertices (claim_vertices) before it writes the list there: one pass, no scan.
-__global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
+// The warps run over `sites` (nullptr: every site of the arena, in order).
+__global__ void __launch_bounds__(INS_WARPS * 32, 6) k_insert(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
   __shared__ uint64_t offS[INS_WARPS][INS_CAP];
   __shared__ uint8_t dirS[INS_WARPS][INS_CAP];
@@ -248,7 +249,8 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
   const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < A.N; s += warps) {
+  for (int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; si < nsites; si += warps) {
+    const int s = sites ? sites[si] : si;
     const int j0 = A.inc_off[s];
     const int z = A.inc_off[s + 1] - j0;
     if (!A.ch_active[A.site_chain[s]]) {
@@ -365,6 +367,40 @@ __global__ void __launch_bounds__(INS_WARPS * 32) k_insert(Arena A) {
         }
       }
       __syncwarp();
+    }
+  }
+}
+
+// Thread-per-bond form for chains with few operators per bond, where a warp per site would idle:
+// the 32 bonds of a warp count their vertices, claim one range with a single atomic add (a warp
+// prefix sum places each bond), and write their lists.
+__global__ void __launch_bounds__(256) k_insert_narrow(Arena A, const int* bonds, int nb) {
+  if (A.ctl->err) return;
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * blockDim.x;        // a multiple of 32
+  const int nround = (nb + 31) & ~31;               // same trip count for every lane of a warp
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nround; i += stride) {
+    const bool ok = i < nb;
+    const int b = ok ? bonds[i] : 0;
+    int n = 0;
+    if (ok && A.ch_active[A.bond_chain[b]]) n = insert_bond_serial<false>(A, b, 0);
+    int incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total) base = atomicAdd(&A.ctl->nv_alloc, (unsigned long long)total);
+    base = __shfl_sync(0xFFFFFFFFu, base, 31);
+    const bool room = base + (unsigned long long)total <= (unsigned long long)A.ctl->nv_cap;
+    if (!room && lane == 31) atomicExch(&A.ctl->err, ERR_OVERFLOW);
+    if (ok) {
+      const int at = room ? (int)(base + (unsigned long long)(incl - n)) : 0;
+      A.bond_cnt[b] = n;
+      A.bond_ptr[b] = at;
+      if (room && n) insert_bond_serial<true>(A, b, at);
     }
   }
 }
@@ -569,14 +605,15 @@ __device__ void merge_site_serial(Arena& A, int s) {
   if (k > 0) A.parent[base + k] = base;
 }
 
-__global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A) {
+__global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
   __shared__ uint64_t sT[MERGE_WARPS][MERGE_CAP];   // staged times, list by list
   __shared__ uint8_t sC[MERGE_WARPS][MERGE_CAP];    // staged codes
   __shared__ uint16_t mE[MERGE_WARPS][MERGE_CAP];   // merged order -> staged index
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < A.N; s += warps) {
+  for (int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; si < nsites; si += warps) {
+    const int s = sites ? sites[si] : si;
     const int j0 = A.inc_off[s];
     const int z = A.inc_off[s + 1] - j0;
     const int base = A.sbase[s];
@@ -670,6 +707,18 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A) {
   }
 }
 
+// Thread-per-site form of the merge for sites with few endpoints.
+__global__ void __launch_bounds__(256) k_merge_narrow(Arena A, const int* sites, int nsites) {
+  if (A.ctl->err) return;
+  LG_GRID_STRIDE(i, nsites) {
+    const int s = sites[i];
+    const int c = A.site_chain[s];
+    if (s == A.ch[c].site_off) A.ch_slot_off[c] = A.sbase[s];
+    if (s == A.N - 1) A.ch_slot_off[A.C] = A.sbase[s + 1];
+    merge_site_serial(A, s);
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // Lock-free union-find on segments.  Roots are hooked larger-index -> smaller-index with
 // atomicCAS, so the root of every cluster is its smallest segment index whatever the order of
@@ -708,18 +757,19 @@ __device__ __forceinline__ bool uf_union(int* P, int a, int b) {
 // segments of a chunk, about half of them, are compacted so that every lane makes the unions of
 // one vertex.  Neighbouring warps so work on neighbouring sites, whatever order the vertex
 // ranges were claimed in, which keeps the union-find trees of concurrently running blocks local.
-constexpr int UN_WARPS = 8;
+constexpr int UN_WARPS = 8;   // default warps per block
 constexpr int UN_CHUNK = 64;
 
-__global__ void __launch_bounds__(UN_WARPS * 32) k_union(Arena A) {
+template <int WARPS = UN_WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_union(Arena A) {
   if (A.ctl->err) return;
-  __shared__ int pend[UN_WARPS][UN_CHUNK];
+  __shared__ int pend[WARPS][UN_CHUNK];
   const int ns = A.ctl->ns_total;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
-  const long long stride = (long long)gridDim.x * UN_WARPS * UN_CHUNK;
+  const long long stride = (long long)gridDim.x * WARPS * UN_CHUNK;
   bool ok = true;
-  for (long long c0 = ((long long)blockIdx.x * UN_WARPS + w) * UN_CHUNK; c0 < ns; c0 += stride) {
+  for (long long c0 = ((long long)blockIdx.x * WARPS + w) * UN_CHUNK; c0 < ns; c0 += stride) {
     const int x0 = (int)c0 + lane, x1 = x0 + 32;
     const bool s0 = x0 < ns && (A.sinfo[x0] & SI_SRC);
     const bool s1 = x1 < ns && (A.sinfo[x1] & SI_SRC);
@@ -778,22 +828,13 @@ __global__ void __launch_bounds__(256) k_compress(Arena A) {
 constexpr int ACC_TILE = 1024;
 constexpr int ACC_HASH = 1024;   // power of two
 
-__device__ __forceinline__ unsigned long long group_sum_u48(unsigned mask, unsigned long long v) {
-  unsigned long long s = 0;
-#pragma unroll
-  for (int q = 0; q < 3; ++q) {
-    const unsigned limb = (unsigned)((v >> (16 * q)) & 0xFFFFull);
-    s += (unsigned long long)__reduce_add_sync(mask, limb) << (16 * q);
-  }
-  return s;
-}
-
+template <int TILE = ACC_TILE>
 __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
   if (A.ctl->err) return;
   __shared__ int hkey[ACC_HASH];
   __shared__ unsigned long long hval[ACC_HASH * 4];
   const int ns = A.ctl->ns_total;
-  const int ntiles = (ns + ACC_TILE - 1) / ACC_TILE;
+  const int ntiles = (ns + TILE - 1) / TILE;
   const int lane = threadIdx.x & 31;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     for (int i = threadIdx.x; i < ACC_HASH; i += blockDim.x) {
@@ -801,8 +842,8 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
       hval[4 * i] = hval[4 * i + 1] = hval[4 * i + 2] = hval[4 * i + 3] = 0ull;
     }
     __syncthreads();
-    const int t0 = tile * ACC_TILE;
-    constexpr int PER = ACC_TILE / 256;  // segments per thread (blockDim.x == 256)
+    const int t0 = tile * TILE;
+    constexpr int PER = TILE / 256;  // segments per thread (blockDim.x == 256)
     int xs[PER], par[PER];
     uint8_t info[PER];
     uint64_t ta[PER], tb[PER];
@@ -868,34 +909,6 @@ __device__ __forceinline__ void atomic_add_u128(unsigned long long* p, u128 v) {
   const unsigned long long old = atomicAdd(p, v.lo);
   const unsigned long long carry = (old + v.lo < old) ? 1ull : 0ull;
   if (v.hi + carry) atomicAdd(p + 1, v.hi + carry);
-}
-
-__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
-  unsigned long long s = 0;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const unsigned limb = (unsigned)((v >> (16 * q)) & 0xFFFFull);
-    s += (unsigned long long)__reduce_add_sync(0xFFFFFFFFu, limb) << (16 * q);
-  }
-  return s;
-}
-
-__device__ __forceinline__ u128 warp_sum_u128(u128 v) {
-  u128 s = {0, 0};
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const unsigned long long w = q < 4 ? v.lo : v.hi;
-    const unsigned limb = (unsigned)((w >> (16 * (q & 3))) & 0xFFFFull);
-    const unsigned long long t = __reduce_add_sync(0xFFFFFFFFu, limb);
-    const int sh = 16 * q;
-    // add t << sh into s (t < 2^21)
-    unsigned long long lo_add = sh < 64 ? (t << sh) : 0ull;
-    unsigned long long hi_add = sh == 0 ? 0ull : (sh < 64 ? (t >> (64 - sh)) : (t << (sh - 64)));
-    const unsigned long long nlo = s.lo + lo_add;
-    s.hi += hi_add + (nlo < s.lo ? 1ull : 0ull);
-    s.lo = nlo;
-  }
-  return s;
 }
 
 __device__ __forceinline__ int chain_of_segment(const Arena& A, int x) {
@@ -996,26 +1009,73 @@ __device__ __forceinline__ void record_atomics(const Arena& A, int c, const Root
   for (int i = 0; i < 8; ++i) if (R.w[i].lo | R.w[i].hi) atomic_add_u128(row + kRecW[i], R.w[i]);
 }
 
+// Sum of a u64 over the lanes of `grp` (16-bit limbs, exact).
+__device__ __forceinline__ unsigned long long group_sum_u64(unsigned grp, unsigned long long v) {
+  unsigned long long s = 0;
+#pragma unroll
+  for (int l = 0; l < 4; ++l)
+    s += (unsigned long long)__reduce_add_sync(grp, (unsigned)((v >> (16 * l)) & 0xFFFFull)) << (16 * l);
+  return s;
+}
+
+__device__ __forceinline__ u128 group_sum_u128(unsigned grp, u128 v) {
+  u128 s = {0, 0};
+#pragma unroll
+  for (int l = 0; l < 8; ++l) {
+    const unsigned long long w = l < 4 ? v.lo : v.hi;
+    const unsigned long long t = __reduce_add_sync(grp, (unsigned)((w >> (16 * (l & 3))) & 0xFFFFull));
+    const int sh = 16 * l;
+    u128 add;
+    add.lo = sh < 64 ? (t << sh) : 0ull;
+    add.hi = sh == 0 ? 0ull : (sh < 64 ? (t >> (64 - sh)) : (t << (sh - 64)));
+    add_u128(s, add);
+  }
+  return s;
+}
+
+// Adds every lane's root sums into its chain's record (c < 0: nothing).  Lanes of the same chain
+// are reduced first, so that a chain takes one set of atomics per warp rather than per root.
+// Warp-collective: every lane calls it.
+__device__ __forceinline__ void record_by_chain(const Arena& A, int c, const RootSums& R) {
+  const unsigned grp = __match_any_sync(0xFFFFFFFFu, c);
+  if (c < 0) return;
+  if (__popc(grp) == 1) { record_atomics(A, c, R); return; }
+  const bool leader = (threadIdx.x & 31) == __ffs(grp) - 1;
+  unsigned long long* row = rec_row(A, c);
+#pragma unroll
+  for (int i = 0; i < 10; ++i) {
+    const unsigned long long v = group_sum_u64(grp, R.q[i]);
+    if (leader && v) atomicAdd(row + kRecQ[i], v);
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const u128 v = group_sum_u128(grp, R.w[i]);
+    if (leader && (v.lo | v.hi)) atomic_add_u128(row + kRecW[i], v);
+  }
+}
+
 // Per cluster root: flip decision (path_integral.C:780-803) and the exact per-sweep sums of the
 // improved estimator collector (susceptibility.h:182-198), cluster count (:774-778), field
 // energy (:852-859) and the normal time-integrated magnetisations (susceptibility.h:283-297).
-// Each block handles tiles of CL_TILE consecutive segments; a tile inside one chain is reduced
-// in registers and shared memory (16-bit limbs, exact) and adds to the record once.
+// Each block handles one tile of TILE consecutive segments.  A tile inside one chain is reduced
+// in registers and shared memory (16-bit limbs, exact) and adds to the record once; a tile that
+// spans chains reduces each warp's roots per chain (record_by_chain).
 constexpr int CL_TILE = 4096;
 constexpr int CL_THREADS = 256;
 
+template <int TILE = CL_TILE>
 __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
   if (A.ctl->err) return;
   __shared__ unsigned limbs[CL_THREADS / 32][NLIMB];
   __shared__ unsigned long long tot[NLIMB];
-  __shared__ int roots[CL_TILE];
+  __shared__ int roots[TILE];
   __shared__ int nroots;
   const int ns = A.ctl->ns_total;
-  const int ntiles = (ns + CL_TILE - 1) / CL_TILE;
+  const int ntiles = (ns + TILE - 1) / TILE;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int t0 = tile * CL_TILE;
-    const int t1 = min(t0 + CL_TILE, ns);
+    const int t0 = tile * TILE;
+    const int t1 = min(t0 + TILE, ns);
     if (threadIdx.x == 0) nroots = 0;
     __syncthreads();
     // compact this tile's roots so that every lane works on one
@@ -1031,37 +1091,47 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
     __syncthreads();
     const int nr = nroots;
     const int cf = chain_of_segment(A, t0), cl = chain_of_segment(A, t1 - 1);
-    const bool uniform = cf == cl;
-    RootSums acc;
-#pragma unroll
-    for (int i = 0; i < 10; ++i) acc.q[i] = 0;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) acc.w[i] = {0, 0};
     // software-pipelined: the next root's class sums are loaded while this one is processed
     int i = threadIdx.x;
     int x = i < nr ? roots[i] : 0;
     RootClass cur = i < nr ? load_root_class(A, x) : RootClass{};
-    while (i < nr) {
-      const int inext = i + blockDim.x;
-      const int xnext = inext < nr ? roots[inext] : 0;
-      RootClass nxt = inext < nr ? load_root_class(A, xnext) : RootClass{};
-      if (uniform) {
-        root_sums(A, x, cf, cur, acc);
-      } else {
+    if (cf != cl) {
+      // the tile spans chains: per-chain warp reductions (same trip count for every thread)
+      const int iters = (nr + (int)blockDim.x - 1) / (int)blockDim.x;
+      for (int it = 0; it < iters; ++it) {
+        const int inext = i + blockDim.x;
+        const int xnext = inext < nr ? roots[inext] : 0;
+        RootClass nxt = inext < nr ? load_root_class(A, xnext) : RootClass{};
         RootSums R;
 #pragma unroll
         for (int k = 0; k < 10; ++k) R.q[k] = 0;
 #pragma unroll
         for (int k = 0; k < 8; ++k) R.w[k] = {0, 0};
-        const int c = chain_of_segment(A, x);
-        root_sums(A, x, c, cur, R);
-        record_atomics(A, c, R);
+        int c = -1;
+        if (i < nr) {
+          c = chain_of_segment(A, x);
+          root_sums(A, x, c, cur, R);
+        }
+        record_by_chain(A, c, R);
+        i = inext;
+        x = xnext;
+        cur = nxt;
       }
-      i = inext;
-      x = xnext;
-      cur = nxt;
-    }
-    if (uniform) {
+    } else {
+      RootSums acc;
+#pragma unroll
+      for (int k = 0; k < 10; ++k) acc.q[k] = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) acc.w[k] = {0, 0};
+      while (i < nr) {
+        const int inext = i + blockDim.x;
+        const int xnext = inext < nr ? roots[inext] : 0;
+        RootClass nxt = inext < nr ? load_root_class(A, xnext) : RootClass{};
+        root_sums(A, x, cf, cur, acc);
+        i = inext;
+        x = xnext;
+        cur = nxt;
+      }
 #pragma unroll
       for (int i = 0; i < 10; ++i)
 #pragma unroll
@@ -1134,11 +1204,12 @@ __global__ void __launch_bounds__(256) k_flip_vertex(Arena A) {
 // the start of the site's segment range: this is the next sweep's off-diagonal list.  Every
 // lane reads its chunk before any lane writes, and a kept endpoint never moves forward, so the
 // in-place compaction reads no overwritten slot.
-__global__ void __launch_bounds__(256) k_site_end(Arena A) {
+__global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
-  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < A.N; s += warps) {
+  for (int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; si < nsites; si += warps) {
+    const int s = sites ? sites[si] : si;
     const int base = A.sbase[s];
     const int k = A.sbase[s + 1] - base - 1;
     if (lane == 0 && A.flip[A.parent[base]]) A.spin0[s] ^= 1u;
@@ -1164,6 +1235,29 @@ __global__ void __launch_bounds__(256) k_site_end(Arena A) {
       __syncwarp();
     }
     if (lane == 0) { A.off_base[s] = base; A.off_cnt[s] = n; }
+  }
+}
+
+// Thread-per-site form of k_site_end for sites with few endpoints (kept entries never move
+// forward, so the in-place compaction reads no overwritten slot).
+__global__ void __launch_bounds__(256) k_site_end_narrow(Arena A, const int* sites, int nsites) {
+  if (A.ctl->err) return;
+  LG_GRID_STRIDE(i, nsites) {
+    const int s = sites[i];
+    const int base = A.sbase[s];
+    const int k = A.sbase[s + 1] - base - 1;
+    if (A.flip[A.parent[base]]) A.spin0[s] ^= 1u;
+    int n = 0;
+    for (int j = 1; j <= k; ++j) {
+      const int x = base + j;
+      if (A.vnew[A.svert[x]]) {
+        A.stime[base + n] = A.stime[x];
+        A.sdir[base + n] = A.sdir[x];
+        ++n;
+      }
+    }
+    A.off_base[s] = base;
+    A.off_cnt[s] = n;
   }
 }
 

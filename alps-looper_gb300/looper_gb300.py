@@ -61,6 +61,16 @@ class Result(ctypes.Structure):
                 ("sweeps", ctypes.c_uint64), ("sites", ctypes.c_int64), ("obs", Obs)]
 
 
+class Shape(ctypes.Structure):
+    """Launch shape of an arena (lg_shape): changes speed only, never a result."""
+    _fields_ = [("narrow_k", ctypes.c_double), ("acc_tile", ctypes.c_int), ("cl_tile", ctypes.c_int),
+                ("union_warps", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+    def as_dict(self):
+        return {"narrow_k": self.narrow_k, "acc_tile": self.acc_tile, "cl_tile": self.cl_tile,
+                "union_warps": self.union_warps}
+
+
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
                 ("rejected", ctypes.c_uint64), ("rebuilds", ctypes.c_uint64),
@@ -112,6 +122,10 @@ def lib():
             "lg_batch_time_sweeps": (ctypes.c_int, [vp, i64, ctypes.c_size_t, vp]),
             "lg_profile_sweeps": (ctypes.c_int, [vp, i64, ctypes.c_size_t, vp, vp]),
             "lg_batch_profile_sweeps": (ctypes.c_int, [vp, i64, ctypes.c_size_t, vp, vp]),
+            "lg_autotune": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_size_t, vp, vp, ctypes.c_size_t]),
+            "lg_batch_autotune": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_size_t, vp, vp, ctypes.c_size_t]),
+            "lg_batch_get_shape": (ctypes.c_int, [vp, vp]),
+            "lg_batch_set_shape": (ctypes.c_int, [vp, vp]),
             "lg_num_kernels": (ctypes.c_int, []),
             "lg_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
             "lg_server_config_default": (None, [vp]),
@@ -218,6 +232,13 @@ def _profile(fn, h, n, flush_bytes):
     return dict(zip(names, out.tolist())), v.value
 
 
+def _autotune(fn, h, trial, flush_bytes):
+    sh = Shape()
+    buf = ctypes.create_string_buffer(8192)
+    check(fn(h, int(trial), int(flush_bytes), ctypes.byref(sh), buf, 8192))
+    return sh.as_dict(), buf.value.decode()
+
+
 class LoopWorker:
     """One chain: looper's "loop; path integral" worker on the GPU."""
 
@@ -288,6 +309,10 @@ class LoopWorker:
     def profile_sweeps(self, n, flush_bytes=0):
         """Per-stage device time (ms, summed over n sweeps) and operators processed."""
         return _profile(lib().lg_profile_sweeps, self._h, n, flush_bytes)
+
+    def autotune(self, trial_sweeps=4, flush_bytes=0):
+        """Pick the fastest launch shape for this chain; returns (shape dict, report text)."""
+        return _autotune(lib().lg_autotune, self._h, trial_sweeps, flush_bytes)
 
     # ---- test seams ----
     def num_sites(self):
@@ -362,6 +387,24 @@ class Batch:
 
     def profile_sweeps(self, n, flush_bytes=0):
         return _profile(lib().lg_batch_profile_sweeps, self._h, n, flush_bytes)
+
+    def autotune(self, trial_sweeps=4, flush_bytes=0):
+        """Pick the fastest launch shape; returns (shape dict, report text)."""
+        return _autotune(lib().lg_batch_autotune, self._h, trial_sweeps, flush_bytes)
+
+    @property
+    def shape(self):
+        sh = Shape()
+        check(lib().lg_batch_get_shape(self._h, ctypes.byref(sh)))
+        return sh.as_dict()
+
+    @shape.setter
+    def shape(self, d):
+        sh = Shape()
+        check(lib().lg_batch_get_shape(self._h, ctypes.byref(sh)))
+        for k, v in d.items():
+            setattr(sh, k, v)
+        check(lib().lg_batch_set_shape(self._h, ctypes.byref(sh)))
 
     def chain(self, i) -> LoopWorker:
         h = lib().lg_batch_chain(self._h, i)

@@ -195,6 +195,36 @@ int lg_batch_stats(const lg_batch* b, int64_t* total_sites, int64_t* site_sweeps
 /* Access one chain of a batch through the single-chain test seams. */
 lg_chain* lg_batch_chain(lg_batch* b, int i);
 
+/* ---- launch shapes and the autotuner (no counterpart in the reference) ---------------------
+ * The shape of an arena's sweep launches.  No shape changes any result (trajectories, records
+ * and observables are bit-identical under every shape); it only changes speed.
+ *   narrow_k     chains whose expected endpoints per site, 2 beta W N_bonds / N, are below this
+ *                run their insertion, merge and list compaction with a thread per bond / site;
+ *                the others with a warp per site (0: all warp, a huge value: all thread)
+ *   acc_tile     segments per CTA of the cluster-sum accumulation: 512, 1024 or 2048
+ *   cl_tile      segments per CTA of the cluster flip / estimator kernel: 2048, 4096 or 8192
+ *   union_warps  warps per CTA of the union-find kernel: 4, 8 or 16 */
+typedef struct lg_shape {
+  double narrow_k;
+  int acc_tile;
+  int cl_tile;
+  int union_warps;
+  int reserved;
+} lg_shape;
+
+/* Autotuner: times trial_sweeps sweeps per candidate shape (device events, flush_bytes of L2
+ * flush before each sweep) and keeps the fastest shape, searching the narrow/wide split first,
+ * then each tile size.  The timed sweeps are the chains' own sweeps and count as done.
+ * chosen (may be NULL) receives the shape kept; report (may be NULL) a line per candidate. */
+int lg_batch_autotune(lg_batch* b, int trial_sweeps, size_t flush_bytes, lg_shape* chosen,
+                      char* report, size_t report_len);
+/* The same for a single chain created with lg_create. */
+int lg_autotune(lg_chain* c, int trial_sweeps, size_t flush_bytes, lg_shape* chosen, char* report,
+                size_t report_len);
+int lg_batch_get_shape(const lg_batch* b, lg_shape* out);
+/* Fix the shape by hand (LG_EINVAL for values outside the lists above). */
+int lg_batch_set_shape(lg_batch* b, const lg_shape* in);
+
 /* ---- request server: continuous batching over one device arena ---------------------------
  * Serving form of the worker (no counterpart in the reference, whose scheduler runs one
  * worker per clone; see path_integral.C:872-876 for the worker it batches).  Requests (lg_params)

@@ -1,0 +1,115 @@
+"""Launch shapes and the autotuner change speed only, never a result.
+
+A shape picks, per arena, which chains run insertion / merge / list compaction with a thread per
+bond or site ("narrow") instead of a warp per site, and the CTA sizes of the union-find, cluster
+sum and cluster flip kernels.  Every shape must give the same trajectories and the same exact
+per-sweep sums, so the arena below (chains of mixed lattices, temperatures, anisotropy and field,
+all smaller than one k_cluster tile so that the per-chain reductions of tiles spanning chains are
+exercised) is run under several shapes and compared bit for bit.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lg():
+    import build as b
+    b.build()
+    import looper_gb300 as m
+    return m
+
+
+MODELS = [
+    dict(LATTICE="chain", L=32, BETA=3.0),
+    dict(LATTICE="square", L=8, BETA=1.0),
+    dict(LATTICE="square", L=12, BETA=8.0, h=0.2),
+    dict(LATTICE="cubic", L=4, BETA=2.0, Jxy=1.0, Jz=0.5, h=0.3),
+    dict(LATTICE="square", L=16, BETA=0.5),
+    dict(LATTICE="chain", L=64, BETA=16.0, Jxy=1.0, Jz=1.5),
+]
+
+SHAPES = [
+    dict(narrow_k=0.0),                                           # every chain warp-per-site
+    dict(narrow_k=1e300),                                         # every chain thread-per-site
+    dict(narrow_k=10.0, acc_tile=512, cl_tile=2048, union_warps=4),
+    dict(narrow_k=32.0, acc_tile=2048, cl_tile=8192, union_warps=16),
+]
+
+
+def _params(lg):
+    return [lg.make_params(SEED=31 + i, INITIAL_SPINS="random", SWEEPS=4096, THERMALIZATION=0, **m)
+            for i, m in enumerate(MODELS)]
+
+
+def _snapshot(b):
+    out = []
+    for i in range(len(b)):
+        spins, bonds, times = b.chain(i).state()
+        out.append((spins, bonds, times, b.observables(i)))
+    return out
+
+
+def _assert_same(a, b):
+    assert len(a) == len(b)
+    for (s0, b0, t0, o0), (s1, b1, t1, o1) in zip(a, b):
+        np.testing.assert_array_equal(s0, s1)
+        np.testing.assert_array_equal(b0, b1)
+        np.testing.assert_array_equal(t0.view(np.uint64), t1.view(np.uint64))
+        for k, v in o0.items():
+            v1 = o1[k]
+            if isinstance(v, float) and np.isnan(v):
+                assert np.isnan(v1), k
+            else:
+                assert v == v1, k
+
+
+def test_every_shape_gives_the_same_trajectories(lg):
+    ref = None
+    for sh in SHAPES:
+        b = lg.Batch(_params(lg))
+        b.shape = sh
+        got = b.shape
+        for k, v in sh.items():
+            assert got[k] == v
+        b.run(40)
+        snap = _snapshot(b)
+        b.close()
+        if ref is None:
+            ref = snap
+        else:
+            _assert_same(ref, snap)
+
+
+def test_bad_shape_is_rejected(lg):
+    b = lg.Batch(_params(lg)[:2])
+    with pytest.raises(lg.LoopError) as e:
+        b.shape = dict(acc_tile=300)
+    assert e.value.code == -1
+    b.close()
+
+
+def test_autotune_keeps_the_trajectory(lg):
+    b1 = lg.Batch(_params(lg))
+    shape, report = b1.autotune(trial_sweeps=2)
+    assert "chosen:" in report
+    assert shape["acc_tile"] in (512, 1024, 2048) and shape["cl_tile"] in (2048, 4096, 8192)
+    assert shape["union_warps"] in (4, 8, 16)
+    total_sites, site_sweeps = b1.stats()
+    done = site_sweeps // total_sites
+    assert done >= 2
+    b1.run(10)
+    b2 = lg.Batch(_params(lg))
+    b2.run(done + 10)
+    _assert_same(_snapshot(b1), _snapshot(b2))
+    b1.close()
+    b2.close()
+
+
+def test_single_chain_autotune(lg):
+    w = lg.LoopWorker(lg.make_params(LATTICE="square", L=16, BETA=4.0, SEED=5, SWEEPS=4096,
+                                     THERMALIZATION=0))
+    shape, report = w.autotune(trial_sweeps=1)
+    assert report.count("ms") >= 2
+    w.close()
