@@ -71,12 +71,14 @@ struct DBuf {
 
 // Launch shape of an arena's sweep.  No choice here changes a result: every variant computes the
 // same vertices, segments, clusters and exact sums.
-//   narrow_k  chains whose expected endpoints per site (2 beta W N_b / N) are below this use the
-//             thread-per-bond / thread-per-site kernels, the others a warp per site
+//   insert_k  chains whose expected endpoints per site (2 beta W N_b / N) are below this insert
+//             with a thread per bond, the others with a warp per site
+//   narrow_k  the same split for the merge and the list compaction (thread / warp per site)
 //   acc_tile  segments per block in k_accumulate (512, 1024, 2048)
 //   cl_tile   segments per block in k_cluster (2048, 4096, 8192)
 //   un_warps  warps per block in k_union (4, 8, 16)
 struct Shape {
+  double insert_k = 32.0;
   double narrow_k = 32.0;
   int acc_tile = 1024;
   int cl_tile = 4096;
@@ -119,9 +121,10 @@ struct Engine {
   int rec_rows = 64;
   // site / bond classes of the current shape (nullptr list: all sites, in order)
   Shape shape;
-  DBuf<int> d_wide_sites, d_narrow_sites, d_narrow_bonds;
-  const int* wide_list = nullptr;
-  int n_wide = 0, n_narrow = 0, n_narrow_b = 0;
+  DBuf<int> d_wide_sites, d_narrow_sites, d_ins_sites, d_narrow_bonds;
+  const int* wide_list = nullptr;   // merge / compaction, warp per site
+  const int* ins_list = nullptr;    // insertion, warp per site
+  int n_wide = 0, n_narrow = 0, n_ins = 0, n_narrow_b = 0;
   int sweep_launches = 0;         // kernel launches of one sweep
   cudaStream_t st2 = nullptr;     // the narrow kernels run beside the wide ones
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -256,7 +259,7 @@ struct Engine {
     long long cap = (long long)(1.3 * est) + 4096;
     LG_CUDA(cudaMemset(d_ctl.p, 0, sizeof(Ctl)));
     if ((rc = alloc_dynamic(cap, false))) return rc;
-    if ((rc = set_shape(shape))) return rc;
+    if ((rc = set_shape(default_shape()))) return rc;
     // initial spins (one launch per distinct init mode)
     Arena A = arena();
     int random = spec.empty() ? 0 : spec[0].init_spins;
@@ -313,6 +316,27 @@ struct Engine {
     return LG_OK;
   }
 
+  // Starting shape before any tuning.  An arena of few sites is latency-bound: a warp per site
+  // gives the shortest critical path there, whatever the temperature.  A large arena fills the
+  // GPU either way, and its low-temperature-density chains do better with a thread per bond or
+  // site (thresholds from autotuning the 512-chain mixed arena).  Tiles shrink until the grid
+  // has at least two blocks per SM.
+  Shape default_shape() const {
+    Shape s;
+    if (N < 131072) {
+      s.insert_k = 0.0;
+      s.narrow_k = 0.0;
+    } else {
+      s.insert_k = 64.0;
+      s.narrow_k = 16.0;
+    }
+    const long long goal = 2ll * nsm;
+    s.acc_tile = ns_cap / 1024 >= goal ? 1024 : 512;
+    s.cl_tile = ns_cap / 4096 >= goal ? 4096 : 2048;
+    s.un_warps = 8;
+    return s;
+  }
+
   // Expected endpoints per site of chain c: the narrow / wide criterion.
   double endpoints_per_site(int c) const {
     const ChainSpec& s = spec[c];
@@ -323,32 +347,44 @@ struct Engine {
   int set_shape(const Shape& sh) {
     if (!(sh.acc_tile == 512 || sh.acc_tile == 1024 || sh.acc_tile == 2048) ||
         !(sh.cl_tile == 2048 || sh.cl_tile == 4096 || sh.cl_tile == 8192) ||
-        !(sh.un_warps == 4 || sh.un_warps == 8 || sh.un_warps == 16) || !(sh.narrow_k >= 0))
+        !(sh.un_warps == 4 || sh.un_warps == 8 || sh.un_warps == 16) || !(sh.narrow_k >= 0) ||
+        !(sh.insert_k >= 0))
       return lg_fail(LG_EINVAL, "bad launch shape");
-    std::vector<int> ws, nsl, nbl;
+    std::vector<int> ws, nsl, is, nbl;
     for (int c = 0; c < C; ++c) {
-      const bool narrow = endpoints_per_site(c) < sh.narrow_k;
-      for (int i = 0; i < spec[c].N; ++i) (narrow ? nsl : ws).push_back(hch[c].site_off + i);
-      if (narrow)
+      const double mu = endpoints_per_site(c);
+      const bool narrow = mu < sh.narrow_k, narrow_ins = mu < sh.insert_k;
+      for (int i = 0; i < spec[c].N; ++i) {
+        (narrow ? nsl : ws).push_back(hch[c].site_off + i);
+        if (!narrow_ins) is.push_back(hch[c].site_off + i);
+      }
+      if (narrow_ins)
         for (int b = 0; b < spec[c].NB; ++b) nbl.push_back(hch[c].bond_off + b);
     }
     int rc;
+    auto upload = [&](DBuf<int>& d, const std::vector<int>& h) -> int {
+      int r = d.alloc(std::max<size_t>(h.size(), 1));
+      if (r) return r;
+      if (!h.empty())
+        LG_CUDA(cudaMemcpy(d.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+      return LG_OK;
+    };
     n_wide = (int)ws.size();
     n_narrow = (int)nsl.size();
+    n_ins = (int)is.size();
     n_narrow_b = (int)nbl.size();
+    // a list covering every site in order is passed as nullptr (no indirection)
     wide_list = nullptr;
-    if (n_narrow > 0 && n_wide > 0) {
-      if ((rc = d_wide_sites.alloc(n_wide))) return rc;
-      LG_CUDA(cudaMemcpy(d_wide_sites.p, ws.data(), n_wide * sizeof(int), cudaMemcpyHostToDevice));
+    ins_list = nullptr;
+    if (n_wide > 0 && n_wide < N) {
+      if ((rc = upload(d_wide_sites, ws))) return rc;
       wide_list = d_wide_sites.p;
     }
-    if (n_narrow > 0) {
-      if ((rc = d_narrow_sites.alloc(n_narrow)) || (rc = d_narrow_bonds.alloc(std::max(n_narrow_b, 1))))
-        return rc;
-      LG_CUDA(cudaMemcpy(d_narrow_sites.p, nsl.data(), n_narrow * sizeof(int), cudaMemcpyHostToDevice));
-      if (n_narrow_b)
-        LG_CUDA(cudaMemcpy(d_narrow_bonds.p, nbl.data(), n_narrow_b * sizeof(int), cudaMemcpyHostToDevice));
+    if (n_ins > 0 && n_ins < N) {
+      if ((rc = upload(d_ins_sites, is))) return rc;
+      ins_list = d_ins_sites.p;
     }
+    if ((rc = upload(d_narrow_sites, nsl)) || (rc = upload(d_narrow_bonds, nbl))) return rc;
     shape = sh;
     drop_graph();
     return LG_OK;
@@ -387,19 +423,18 @@ struct Engine {
     Ctl* ctl = d_ctl.p;
     int launches = 0;
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
-    const bool both = n_wide > 0 && n_narrow > 0;
-    cudaStream_t sn = both ? st2 : st;
-    auto fork = [&]() { if (both) { cudaEventRecord(ev_fork, st); cudaStreamWaitEvent(st2, ev_fork, 0); } };
+    bool both = false;
+    auto fork = [&](bool b) { both = b; if (b) { cudaEventRecord(ev_fork, st); cudaStreamWaitEvent(st2, ev_fork, 0); } };
     auto join = [&]() { if (both) { cudaEventRecord(ev_join, st2); cudaStreamWaitEvent(st, ev_join, 0); } };
     k_begin<<<grid_for((long long)C * REC_WORDS, 256), 256, 0, st>>>(A);
     ++launches;
-    fork();
-    if (n_wide) {
-      k_insert<<<grid_for((long long)n_wide * 32, INS_WARPS * 32, 16), INS_WARPS * 32, 0, st>>>(A, wide_list, n_wide);
+    fork(n_ins > 0 && n_narrow_b > 0);
+    if (n_ins) {
+      k_insert<<<grid_for((long long)n_ins * 32, INS_WARPS * 32, 16), INS_WARPS * 32, 0, st>>>(A, ins_list, n_ins);
       ++launches;
     }
     if (n_narrow_b) {
-      k_insert_narrow<<<grid_for(n_narrow_b, 256, 16), 256, 0, sn>>>(A, d_narrow_bonds.p, n_narrow_b);
+      k_insert_narrow<<<grid_for(n_narrow_b, 256, 16), 256, 0, both ? st2 : st>>>(A, d_narrow_bonds.p, n_narrow_b);
       ++launches;
     }
     join();
@@ -407,13 +442,13 @@ struct Engine {
     k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A, 1);
     scan(d_site_cnt.p, d_sbase.p, N, &ctl->ns_total, ns_cap, 1, 0, ev ? ev + 1 : nullptr);
     launches += 4;
-    fork();
+    fork(n_wide > 0 && n_narrow > 0);
     if (n_wide) {
       k_merge<<<grid_for((long long)n_wide * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A, wide_list, n_wide);
       ++launches;
     }
     if (n_narrow) {
-      k_merge_narrow<<<grid_for(n_narrow, 256, 16), 256, 0, sn>>>(A, d_narrow_sites.p, n_narrow);
+      k_merge_narrow<<<grid_for(n_narrow, 256, 16), 256, 0, both ? st2 : st>>>(A, d_narrow_sites.p, n_narrow);
       ++launches;
     }
     join();
@@ -443,13 +478,13 @@ struct Engine {
     k_flip_vertex<<<(nv_cap + 255) / 256, 256, 0, st>>>(A);
     mark(6);
     launches += 4;
-    fork();
+    fork(n_wide > 0 && n_narrow > 0);
     if (n_wide) {
       k_site_end<<<grid_for((long long)n_wide * 32, 256, 16), 256, 0, st>>>(A, wide_list, n_wide);
       ++launches;
     }
     if (n_narrow) {
-      k_site_end_narrow<<<grid_for(n_narrow, 256, 16), 256, 0, sn>>>(A, d_narrow_sites.p, n_narrow);
+      k_site_end_narrow<<<grid_for(n_narrow, 256, 16), 256, 0, both ? st2 : st>>>(A, d_narrow_sites.p, n_narrow);
       ++launches;
     }
     join();
@@ -595,8 +630,8 @@ struct Engine {
       double t = 0;
       for (double x : km) t += x;
       *ms = t / trial;
-      std::snprintf(line, sizeof(line), "narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d: %.4f ms\n",
-                    sh.narrow_k, sh.acc_tile, sh.cl_tile, sh.un_warps, *ms);
+      std::snprintf(line, sizeof(line), "insert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d: %.4f ms\n",
+                    sh.insert_k, sh.narrow_k, sh.acc_tile, sh.cl_tile, sh.un_warps, *ms);
       report += line;
       return LG_OK;
     };
@@ -616,13 +651,23 @@ struct Engine {
     for (int c = 0; c < C; ++c) mu[c] = endpoints_per_site(c);
     std::vector<int> seen;
     auto n_below = [&](double k) { int n = 0; for (double m : mu) n += m < k; return n; };
+    const double ks[] = {0.0, 4.0, 8.0, 16.0, 32.0, 64.0, 128.0, 256.0, 1e300};
     seen.push_back(n_below(best.narrow_k));
-    for (double k : {0.0, 4.0, 8.0, 16.0, 32.0, 64.0, 128.0, 256.0, 1e300}) {
+    for (double k : ks) {
       const int nb = n_below(k);
       if (std::find(seen.begin(), seen.end(), nb) != seen.end()) continue;
       seen.push_back(nb);
       Shape c = best;
       c.narrow_k = k;
+      if ((rc = consider(c))) return rc;
+    }
+    seen.assign(1, n_below(best.insert_k));
+    for (double k : ks) {
+      const int nb = n_below(k);
+      if (std::find(seen.begin(), seen.end(), nb) != seen.end()) continue;
+      seen.push_back(nb);
+      Shape c = best;
+      c.insert_k = k;
       if ((rc = consider(c))) return rc;
     }
     for (int t : {512, 1024, 2048}) {
@@ -640,8 +685,8 @@ struct Engine {
       Shape c = best; c.un_warps = w;
       if ((rc = consider(c))) return rc;
     }
-    std::snprintf(line, sizeof(line), "chosen: narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d (%.4f ms)\n",
-                  best.narrow_k, best.acc_tile, best.cl_tile, best.un_warps, best_ms);
+    std::snprintf(line, sizeof(line), "chosen: insert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d (%.4f ms)\n",
+                  best.insert_k, best.narrow_k, best.acc_tile, best.cl_tile, best.un_warps, best_ms);
     report += line;
     return set_shape(best);
   }
@@ -1101,6 +1146,7 @@ int lg_batch_stats(const lg_batch* b, int64_t* total_sites, int64_t* site_sweeps
 
 static void shape_out(const Shape& s, lg_shape* out) {
   if (!out) return;
+  out->insert_k = s.insert_k;
   out->narrow_k = s.narrow_k;
   out->acc_tile = s.acc_tile;
   out->cl_tile = s.cl_tile;
@@ -1140,6 +1186,7 @@ int lg_batch_get_shape(const lg_batch* b, lg_shape* out) {
 int lg_batch_set_shape(lg_batch* b, const lg_shape* in) {
   if (!b || !in) return lg_fail(LG_EINVAL, "null argument");
   Shape s;
+  s.insert_k = in->insert_k;
   s.narrow_k = in->narrow_k;
   s.acc_tile = in->acc_tile;
   s.cl_tile = in->cl_tile;

@@ -749,6 +749,7 @@ __device__ __forceinline__ bool uf_union(int* P, int a, int b) {
   return false;
 }
 
+
 // reconnect (graph_impl.h:280-295) in segment form: g = 0 joins the two lower legs and the two
 // upper legs; g = 1 joins lower-left with upper-right and lower-right with upper-left; frozen
 // graphs (g & 2) join all four legs.
@@ -763,7 +764,9 @@ constexpr int UN_CHUNK = 64;
 template <int WARPS = UN_WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_union(Arena A) {
   if (A.ctl->err) return;
-  __shared__ int pend[WARPS][UN_CHUNK];
+  __shared__ int pend[WARPS][UN_CHUNK];   // source-side segment a
+  __shared__ int pb[WARPS][UN_CHUNK];     // target-side segment b of the same vertex
+  __shared__ uint8_t pg[WARPS][UN_CHUNK]; // graph
   const int ns = A.ctl->ns_total;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
@@ -771,27 +774,30 @@ __global__ void __launch_bounds__(WARPS * 32) k_union(Arena A) {
   bool ok = true;
   for (long long c0 = ((long long)blockIdx.x * WARPS + w) * UN_CHUNK; c0 < ns; c0 += stride) {
     const int x0 = (int)c0 + lane, x1 = x0 + 32;
-    const bool s0 = x0 < ns && (A.sinfo[x0] & SI_SRC);
-    const bool s1 = x1 < ns && (A.sinfo[x1] & SI_SRC);
+    // segment info and vertex of both halves of the chunk in one round trip, then the target
+    // leg of the source-side ones
+    const uint8_t i0 = x0 < ns ? A.sinfo[x0] : 0;
+    const uint8_t i1 = x1 < ns ? A.sinfo[x1] : 0;
+    const int v0 = x0 < ns ? A.svert[x0] : 0;
+    const int v1 = x1 < ns ? A.svert[x1] : 0;
+    const bool s0 = (i0 & SI_SRC) != 0, s1 = (i1 & SI_SRC) != 0;
+    const int b0 = s0 ? A.vslot[2 * v0 + 1] : 0;
+    const int b1 = s1 ? A.vslot[2 * v1 + 1] : 0;
     const unsigned m0 = __ballot_sync(0xFFFFFFFFu, s0), m1 = __ballot_sync(0xFFFFFFFFu, s1);
     const int n0 = __popc(m0), tot = n0 + __popc(m1);
-    if (s0) pend[w][__popc(m0 & lt)] = x0;
-    if (s1) pend[w][n0 + __popc(m1 & lt)] = x1;
+    if (s0) { const int q = __popc(m0 & lt); pend[w][q] = x0; pb[w][q] = b0; pg[w][q] = i0 >> SI_GSHIFT; }
+    if (s1) { const int q = n0 + __popc(m1 & lt); pend[w][q] = x1; pb[w][q] = b1; pg[w][q] = i1 >> SI_GSHIFT; }
     __syncwarp();
     for (int j = lane; j < tot; j += 32) {
-      const int a = pend[w][j];
-      const int g = A.sinfo[a] >> SI_GSHIFT;
-      const int b = A.vslot[2 * A.svert[a] + 1];
-      if (g & 2) {
-        ok &= uf_union(A.parent, a - 1, b - 1);
-        ok &= uf_union(A.parent, a, b);
-        ok &= uf_union(A.parent, a - 1, a);
-      } else if (g == 0) {
-        ok &= uf_union(A.parent, a - 1, b - 1);
-        ok &= uf_union(A.parent, a, b);
+      const int a = pend[w][j], b = pb[w][j], g = pg[w][j];
+      int* P = A.parent;
+      if (g == 1) {
+        ok &= uf_union(P, a - 1, b);
+        ok &= uf_union(P, b - 1, a);
       } else {
-        ok &= uf_union(A.parent, a - 1, b);
-        ok &= uf_union(A.parent, b - 1, a);
+        ok &= uf_union(P, a - 1, b - 1);
+        ok &= uf_union(P, a, b);
+        if (g & 2) ok &= uf_union(P, a - 1, a);
       }
     }
     __syncwarp();

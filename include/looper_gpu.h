@@ -198,13 +198,15 @@ lg_chain* lg_batch_chain(lg_batch* b, int i);
 /* ---- launch shapes and the autotuner (no counterpart in the reference) ---------------------
  * The shape of an arena's sweep launches.  No shape changes any result (trajectories, records
  * and observables are bit-identical under every shape); it only changes speed.
- *   narrow_k     chains whose expected endpoints per site, 2 beta W N_bonds / N, are below this
- *                run their insertion, merge and list compaction with a thread per bond / site;
- *                the others with a warp per site (0: all warp, a huge value: all thread)
+ *   insert_k     chains whose expected endpoints per site, 2 beta W N_bonds / N, are below this
+ *                insert operators with a thread per bond, the others with a warp per site
+ *                (0: all warp, a huge value: all thread)
+ *   narrow_k     the same split for the per-site merge and list compaction
  *   acc_tile     segments per CTA of the cluster-sum accumulation: 512, 1024 or 2048
  *   cl_tile      segments per CTA of the cluster flip / estimator kernel: 2048, 4096 or 8192
  *   union_warps  warps per CTA of the union-find kernel: 4, 8 or 16 */
 typedef struct lg_shape {
+  double insert_k;
   double narrow_k;
   int acc_tile;
   int cl_tile;
@@ -213,8 +215,8 @@ typedef struct lg_shape {
 } lg_shape;
 
 /* Autotuner: times trial_sweeps sweeps per candidate shape (device events, flush_bytes of L2
- * flush before each sweep) and keeps the fastest shape, searching the narrow/wide split first,
- * then each tile size.  The timed sweeps are the chains' own sweeps and count as done.
+ * flush before each sweep) and keeps the fastest shape, searching the merge split, then the
+ * insertion split, then each tile size.  The timed sweeps are the chains' own sweeps and count as done.
  * chosen (may be NULL) receives the shape kept; report (may be NULL) a line per candidate. */
 int lg_batch_autotune(lg_batch* b, int trial_sweeps, size_t flush_bytes, lg_shape* chosen,
                       char* report, size_t report_len);

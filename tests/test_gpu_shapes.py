@@ -31,10 +31,10 @@ MODELS = [
 ]
 
 SHAPES = [
-    dict(narrow_k=0.0),                                           # every chain warp-per-site
-    dict(narrow_k=1e300),                                         # every chain thread-per-site
-    dict(narrow_k=10.0, acc_tile=512, cl_tile=2048, union_warps=4),
-    dict(narrow_k=32.0, acc_tile=2048, cl_tile=8192, union_warps=16),
+    dict(insert_k=0.0, narrow_k=0.0),                             # every chain warp-per-site
+    dict(insert_k=1e300, narrow_k=1e300),                         # every chain thread-per-site
+    dict(insert_k=1e300, narrow_k=10.0, acc_tile=512, cl_tile=2048, union_warps=4),
+    dict(insert_k=10.0, narrow_k=32.0, acc_tile=2048, cl_tile=8192, union_warps=16),
 ]
 
 
