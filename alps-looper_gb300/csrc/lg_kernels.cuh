@@ -224,15 +224,26 @@ constexpr int INS_WARPS = 4;
 constexpr int INS_CAP = 128;      // staged off-diagonal endpoints per site
 constexpr int INS_ACC = 128;      // staged accepted proposals per bond
 
+// Entries of the sorted T[0, n) that are <= t (INCL) or < t.  The probe steps are powers of two
+// from the largest one <= n down, so the trip count depends on n only: lanes searching lists of
+// the same length never diverge.
+template <bool INCL>
+__device__ __forceinline__ int count_before(const uint64_t* T, int n, uint64_t t) {
+  int pos = 0;
+  for (int step = n ? 1 << (31 - __clz(n)) : 0; step > 0; step >>= 1) {
+    const int np = pos + step;
+    if (np <= n) {
+      const uint64_t v = T[np - 1];
+      if (INCL ? v <= t : v < t) pos = np;
+    }
+  }
+  return pos;
+}
 __device__ __forceinline__ int count_le(const uint64_t* T, int n, uint64_t t) {
-  int a = 0, b = n;
-  while (a < b) { const int m = (a + b) >> 1; if (T[m] <= t) a = m + 1; else b = m; }
-  return a;
+  return count_before<true>(T, n, t);
 }
 __device__ __forceinline__ int count_lt(const uint64_t* T, int n, uint64_t t) {
-  int a = 0, b = n;
-  while (a < b) { const int m = (a + b) >> 1; if (T[m] < t) a = m + 1; else b = m; }
-  return a;
+  return count_before<false>(T, n, t);
 }
 
 // The vertex count n of a bond is known once its proposals are drawn, so the warp claims its
@@ -530,18 +541,10 @@ __global__ void k_site_count(Arena A, int from_claims) {
 constexpr int MERGE_WARPS = 4;
 constexpr int MERGE_CAP = 384;
 
-// number of entries of list [lo, hi) ordered before key (t, dg); `inclusive` counts equal keys
-__device__ __forceinline__ int merge_count(const uint64_t* T, const uint8_t* Cd, int lo, int hi,
-                                           uint64_t t, uint8_t dg, bool inclusive) {
-  int a = lo, b = hi;
-  while (a < b) {
-    const int m = (a + b) >> 1;
-    const uint64_t tm = T[m];
-    const uint8_t dm = (uint8_t)(~Cd[m] & 1u);
-    const bool before = tm < t || (tm == t && (dm < dg || (inclusive && dm == dg)));
-    if (before) a = m + 1; else b = m;
-  }
-  return a - lo;
+// Merge key of an endpoint: (time bits << 1) | diagonal.  Times are FP64 bit patterns of values
+// in [0, 1), below 2^62, so the key fits; key order is (time, off-diagonal first).
+__device__ __forceinline__ uint64_t merge_key(uint64_t t, uint8_t code) {
+  return (t << 1) | (uint64_t)(~code & 1u);
 }
 
 __device__ void merge_site_serial(Arena& A, int s) {
@@ -607,7 +610,7 @@ __device__ void merge_site_serial(Arena& A, int s) {
 
 __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
-  __shared__ uint64_t sT[MERGE_WARPS][MERGE_CAP];   // staged times, list by list
+  __shared__ uint64_t sK[MERGE_WARPS][MERGE_CAP];   // staged merge keys, list by list
   __shared__ uint8_t sC[MERGE_WARPS][MERGE_CAP];    // staged codes
   __shared__ uint16_t mE[MERGE_WARPS][MERGE_CAP];   // merged order -> staged index
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -645,23 +648,27 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
 #pragma unroll
     for (int d = 0; d < MAXZ; ++d) {
       for (int i = lane; i < off[d + 1] - off[d]; i += 32) {
-        sT[w][off[d] + i] = A.vtime[ptr[d] + i];
-        sC[w][off[d] + i] = A.vcode[ptr[d] + i];
+        const uint8_t c = A.vcode[ptr[d] + i];
+        sK[w][off[d] + i] = merge_key(A.vtime[ptr[d] + i], c);
+        sC[w][off[d] + i] = c;
       }
     }
     __syncwarp();
-    // merged rank of every endpoint
+    // merged rank of every endpoint: its place in its own list plus, for every other list, the
+    // entries ordered before it (equal keys of an earlier list count as before).  Every lane
+    // searches every list (the own list too, whose count it then ignores), so the warp does not
+    // diverge on the list index.
     for (int e = lane; e < k; e += 32) {
       int d = 0;
 #pragma unroll
       for (int q = 1; q < MAXZ; ++q) if (e >= off[q]) d = q;
-      const uint64_t t = sT[w][e];
-      const uint8_t dg = (uint8_t)(~sC[w][e] & 1u);
+      const uint64_t key = sK[w][e];
       int r = 0;
 #pragma unroll
-      for (int q = 0; q < MAXZ; ++q) {
-        if (q == d) r += e - off[q];
-        else if (off[q + 1] > off[q]) r += merge_count(sT[w], sC[w], off[q], off[q + 1], t, dg, q < d);
+      for (int q = 0; q < MAXZ; ++q) {  // lists q >= z are empty
+        // keys are below 2^63, so key + 1 does not wrap: "< key + 1" is "<= key"
+        const int c = count_before<false>(sK[w] + off[q], off[q + 1] - off[q], key + (q < d ? 1u : 0u));
+        r += q == d ? e - off[q] : c;
       }
       mE[w][r] = (uint16_t)e;
     }
@@ -693,7 +700,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
         const int v = pd + (e - od);
         const int x = base + 1 + r;
         const uint8_t side = A.inc_side[j0 + d];
-        A.stime[x] = sT[w][e];
+        A.stime[x] = sK[w][e] >> 1;
         A.sinfo[x] = (uint8_t)(spin | gneg | (r == k - 1 ? SI_LAST : 0) | (side == 0 ? SI_SRC : 0) |
                                ((cd >> 1) << SI_GSHIFT));
         A.svert[x] = v;
