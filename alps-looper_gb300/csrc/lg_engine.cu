@@ -639,11 +639,12 @@ struct Engine {
     double best_ms = 0;
     int rc = time_shape(best, &best_ms);
     if (rc) return rc;
+    // a candidate must beat the kept shape by 2%, so that timing noise does not move the shape
     auto consider = [&](Shape cand) -> int {
       double ms = 0;
       int r = time_shape(cand, &ms);
       if (r) return r;
-      if (ms < best_ms) { best_ms = ms; best = cand; }
+      if (ms < 0.98 * best_ms) { best_ms = ms; best = cand; }
       return LG_OK;
     };
     // narrow / wide split: one candidate per distinct set of narrow chains
@@ -1177,6 +1178,28 @@ int lg_batch_autotune(lg_batch* b, int trial_sweeps, size_t flush_bytes, lg_shap
   return autotune_engine(*b->eng, trial_sweeps, flush_bytes, chosen, report, report_len);
 }
 
+static int set_shape_engine(Engine& e, const lg_shape* in) {
+  Shape s;
+  s.insert_k = in->insert_k;
+  s.narrow_k = in->narrow_k;
+  s.acc_tile = in->acc_tile;
+  s.cl_tile = in->cl_tile;
+  s.un_warps = in->union_warps;
+  return e.set_shape(s);
+}
+
+int lg_get_shape(const lg_chain* c, lg_shape* out) {
+  if (!c || !out) return lg_fail(LG_EINVAL, "null argument");
+  shape_out(c->eng->shape, out);
+  return LG_OK;
+}
+
+int lg_set_shape(lg_chain* c, const lg_shape* in) {
+  if (!c || !in) return lg_fail(LG_EINVAL, "null argument");
+  if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_set_shape on a batch member; use lg_batch_set_shape");
+  return set_shape_engine(*c->eng, in);
+}
+
 int lg_batch_get_shape(const lg_batch* b, lg_shape* out) {
   if (!b || !out) return lg_fail(LG_EINVAL, "null argument");
   shape_out(b->eng->shape, out);
@@ -1185,13 +1208,7 @@ int lg_batch_get_shape(const lg_batch* b, lg_shape* out) {
 
 int lg_batch_set_shape(lg_batch* b, const lg_shape* in) {
   if (!b || !in) return lg_fail(LG_EINVAL, "null argument");
-  Shape s;
-  s.insert_k = in->insert_k;
-  s.narrow_k = in->narrow_k;
-  s.acc_tile = in->acc_tile;
-  s.cl_tile = in->cl_tile;
-  s.un_warps = in->union_warps;
-  return b->eng->set_shape(s);
+  return set_shape_engine(*b->eng, in);
 }
 
 int lg_time_sweeps(lg_chain* c, int64_t n, size_t flush_bytes, float* ms) {

@@ -127,6 +127,8 @@ def lib():
             "lg_batch_autotune": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_size_t, vp, vp, ctypes.c_size_t]),
             "lg_batch_get_shape": (ctypes.c_int, [vp, vp]),
             "lg_batch_set_shape": (ctypes.c_int, [vp, vp]),
+            "lg_get_shape": (ctypes.c_int, [vp, vp]),
+            "lg_set_shape": (ctypes.c_int, [vp, vp]),
             "lg_num_kernels": (ctypes.c_int, []),
             "lg_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
             "lg_server_config_default": (None, [vp]),
@@ -314,6 +316,20 @@ class LoopWorker:
     def autotune(self, trial_sweeps=4, flush_bytes=0):
         """Pick the fastest launch shape for this chain; returns (shape dict, report text)."""
         return _autotune(lib().lg_autotune, self._h, trial_sweeps, flush_bytes)
+
+    @property
+    def shape(self):
+        sh = Shape()
+        check(lib().lg_get_shape(self._h, ctypes.byref(sh)))
+        return sh.as_dict()
+
+    @shape.setter
+    def shape(self, d):
+        sh = Shape()
+        check(lib().lg_get_shape(self._h, ctypes.byref(sh)))
+        for k, v in d.items():
+            setattr(sh, k, v)
+        check(lib().lg_set_shape(self._h, ctypes.byref(sh)))
 
     # ---- test seams ----
     def num_sites(self):

@@ -316,8 +316,12 @@ def run_ours(args, dist, ws, rank, local):
     lg.lib()
     w = lg.LoopWorker(_params(lg, seed=SEED + 7919 * rank))
     w.run(PRE_THERM // 2)
-    # launch shape chosen by the autotuner on the chain's own pre-thermalization sweeps
-    shape, _ = w.autotune(2, FLUSH_BYTES)
+    if args.shape == "auto":
+        # launch shape chosen by the autotuner on the chain's own pre-thermalization sweeps
+        shape, _ = w.autotune(2, FLUSH_BYTES)
+    else:
+        w.shape = json.loads(args.shape)  # a fixed shape (e.g. to profile the tuned one)
+        shape = w.shape
     w.run(PRE_THERM // 2)
     w.time_sweeps(max(3, args.warmup), FLUSH_BYTES)
     clk = Clocks(local) if rank == 0 else None
@@ -452,6 +456,9 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=16)
     ap.add_argument("--batched-therm", type=int, default=128)
     ap.add_argument("--served-requests", type=int, default=48)
+    ap.add_argument("--shape", default="auto",
+                    help='launch shape of the headline chain: "auto" (autotuned) or a JSON dict '
+                         'of lg_shape fields')
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = _rank_info()

@@ -216,7 +216,8 @@ typedef struct lg_shape {
 
 /* Autotuner: times trial_sweeps sweeps per candidate shape (device events, flush_bytes of L2
  * flush before each sweep) and keeps the fastest shape, searching the merge split, then the
- * insertion split, then each tile size.  The timed sweeps are the chains' own sweeps and count as done.
+ * insertion split, then each tile size; a candidate replaces the kept shape only when it is at
+ * least 2% faster.  The timed sweeps are the chains' own sweeps and count as done.
  * chosen (may be NULL) receives the shape kept; report (may be NULL) a line per candidate. */
 int lg_batch_autotune(lg_batch* b, int trial_sweeps, size_t flush_bytes, lg_shape* chosen,
                       char* report, size_t report_len);
@@ -226,6 +227,9 @@ int lg_autotune(lg_chain* c, int trial_sweeps, size_t flush_bytes, lg_shape* cho
 int lg_batch_get_shape(const lg_batch* b, lg_shape* out);
 /* Fix the shape by hand (LG_EINVAL for values outside the lists above). */
 int lg_batch_set_shape(lg_batch* b, const lg_shape* in);
+/* The same for a single chain created with lg_create. */
+int lg_get_shape(const lg_chain* c, lg_shape* out);
+int lg_set_shape(lg_chain* c, const lg_shape* in);
 
 /* ---- request server: continuous batching over one device arena ---------------------------
  * Serving form of the worker (no counterpart in the reference, whose scheduler runs one

@@ -113,3 +113,22 @@ def test_single_chain_autotune(lg):
     shape, report = w.autotune(trial_sweeps=1)
     assert report.count("ms") >= 2
     w.close()
+
+
+def test_single_chain_shape_roundtrip(lg):
+    w = lg.LoopWorker(lg.make_params(LATTICE="cubic", L=4, BETA=2.0, SEED=9, SWEEPS=4096,
+                                     THERMALIZATION=0))
+    w.shape = dict(insert_k=1e300, narrow_k=1e300, acc_tile=512, cl_tile=2048, union_warps=16)
+    sh = w.shape
+    assert sh["acc_tile"] == 512 and sh["cl_tile"] == 2048 and sh["union_warps"] == 16
+    w.run(5)
+    spins_a, bonds_a, times_a = w.state()
+    w.close()
+    v = lg.LoopWorker(lg.make_params(LATTICE="cubic", L=4, BETA=2.0, SEED=9, SWEEPS=4096,
+                                     THERMALIZATION=0))
+    v.run(5)
+    spins_b, bonds_b, times_b = v.state()
+    v.close()
+    np.testing.assert_array_equal(spins_a, spins_b)
+    np.testing.assert_array_equal(bonds_a, bonds_b)
+    np.testing.assert_array_equal(times_a.view(np.uint64), times_b.view(np.uint64))
