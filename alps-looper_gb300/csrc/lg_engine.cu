@@ -6,10 +6,12 @@
 // run in chunks; after each chunk the exact per-sweep records come back to the host, which turns
 // them into the reference's observables with a rebinning accumulator.
 //
-// A sweep that would overflow the vertex capacity is detected on the device by the insertion
-// pass, before any persistent state is touched; the engine then grows the buffers to the demand
-// it counted and replays that sweep with the same random numbers, so capacity never changes a
-// trajectory.
+// Vertices are claimed from regions: every run of consecutive sites of a chain (about 4096
+// expected vertices) has its own slot range and claim counter, so that claims do not contend on
+// one address.  A sweep that would overflow a region is detected on the device by the insertion
+// pass, before any persistent state is touched; the engine then grows the regions that
+// overflowed to the demand they counted and replays that sweep with the same random numbers, so
+// capacity never changes a trajectory.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -119,6 +121,13 @@ struct Engine {
 
   int nv_cap = 0, ns_cap = 0;
   int rec_rows = 64;
+  // vertex regions (see the file comment)
+  int R = 0;
+  std::vector<int> h_site_region;
+  std::vector<long long> h_region_cap;
+  long long region_total = 0;
+  DBuf<int> d_site_region, d_region_base;
+  DBuf<unsigned long long> d_region_fill;
   // site / bond classes of the current shape (nullptr list: all sites, in order)
   Shape shape;
   DBuf<int> d_wide_sites, d_narrow_sites, d_ins_sites, d_narrow_bonds;
@@ -156,6 +165,8 @@ struct Engine {
     A.spin0 = d_spin0.p; A.off_base = d_off_base.p; A.off_cnt = d_off_cnt.p;
     A.bond_cnt = d_bond_cnt.p; A.bond_ptr = d_bond_ptr.p; A.site_cnt = d_site_cnt.p;
     A.sbase = d_sbase.p;
+    A.R = R; A.site_region = d_site_region.p; A.region_base = d_region_base.p;
+    A.region_fill = d_region_fill.p;
     A.vtime = d_vtime.p; A.vcode = d_vcode.p; A.vnew = d_vnew.p; A.vslot = d_vslot.p;
     A.stime = d_stime.p; A.sinfo = d_sinfo.p; A.svert = d_svert.p; A.sdir = d_sdir.p;
     A.parent = d_parent.p; A.flip = d_flip.p; A.cls = d_cls.p; A.cnt0 = d_cnt0.p;
@@ -253,12 +264,10 @@ struct Engine {
     std::vector<uint32_t> sw(C);
     for (int c = 0; c < C; ++c) sw[c] = (uint32_t)spec[c].mcs;
     LG_CUDA(cudaMemcpy(d_sweep.p, sw.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    // per-sweep buffers from the expected operator count
-    double est = 0;
-    for (auto& s : spec) est += s.expected_vertices();
-    long long cap = (long long)(1.3 * est) + 4096;
+    // vertex regions and per-sweep buffers from the expected operator count
     LG_CUDA(cudaMemset(d_ctl.p, 0, sizeof(Ctl)));
-    if ((rc = alloc_dynamic(cap, false))) return rc;
+    if ((rc = build_regions())) return rc;
+    if ((rc = alloc_dynamic(region_total, false))) return rc;
     if ((rc = set_shape(default_shape()))) return rc;
     // initial spins (one launch per distinct init mode)
     Arena A = arena();
@@ -277,9 +286,73 @@ struct Engine {
     return LG_OK;
   }
 
-  // (Re)allocate the per-sweep buffers for cap vertices; with keep, preserve the persistent
-  // off-diagonal lists that live at the front of each site's segment range.
+  // Vertex regions: each chain's sites in runs of S consecutive sites, S chosen so that a region
+  // expects about 4096 vertices; a region's capacity is 1.3 times its expectation plus slack.
+  int build_regions() {
+    h_site_region.assign(N, 0);
+    h_region_cap.clear();
+    for (int c = 0; c < C; ++c) {
+      const int n = spec[c].N;
+      const double per_site = n ? spec[c].expected_vertices() / n : 0.0;
+      int S = per_site > 0 ? (int)std::ceil(4096.0 / per_site) : 1024;
+      S = std::min(std::max(S, 8), 1024);
+      for (int i0 = 0; i0 < n; i0 += S) {
+        const int m = std::min(S, n - i0);
+        const double e = per_site * m;
+        long long cap = (long long)std::ceil(1.3 * e + 8.0 * std::sqrt(e)) + 32;
+        cap = (cap + 7) & ~7ll;
+        for (int i = 0; i < m; ++i) h_site_region[hch[c].site_off + i0 + i] = (int)h_region_cap.size();
+        h_region_cap.push_back(cap);
+      }
+    }
+    R = (int)h_region_cap.size();
+    int rc;
+    if ((rc = d_site_region.alloc(N)) || (rc = d_region_fill.alloc(R))) return rc;
+    LG_CUDA(cudaMemcpy(d_site_region.p, h_site_region.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    return layout_regions();
+  }
+
+  // Region slot ranges from the capacities.
+  int layout_regions() {
+    std::vector<int> base(R + 1, 0);
+    long long tot = 0;
+    for (int r = 0; r < R; ++r) {
+      base[r] = (int)tot;
+      tot += h_region_cap[r];
+      if (tot > (1ll << 30) - N) return lg_fail(LG_EBUDGET, "vertex capacity %lld too large", tot);
+    }
+    base[R] = (int)tot;
+    region_total = tot;
+    int rc = d_region_base.alloc(R + 1);
+    if (rc) return rc;
+    LG_CUDA(cudaMemcpy(d_region_base.p, base.data(), (R + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    drop_graph();
+    return LG_OK;
+  }
+
+  // After an overflowing sweep: grow every region whose demand passed its capacity.
+  int grow_regions() {
+    std::vector<unsigned long long> fill(R);
+    LG_CUDA(cudaMemcpy(fill.data(), d_region_fill.p, R * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    bool grew = false;
+    for (int r = 0; r < R; ++r) {
+      if ((long long)fill[r] <= h_region_cap[r]) continue;
+      const long long need = (long long)std::min<unsigned long long>(fill[r], 1ull << 40);
+      h_region_cap[r] = ((long long)(1.25 * need) + 64 + 7) & ~7ll;
+      grew = true;
+    }
+    if (!grew)  // no region reported a shortage: grow them all, so that the replay progresses
+      for (auto& c : h_region_cap) c = ((long long)(1.25 * c) + 64 + 7) & ~7ll;
+    int rc = layout_regions();
+    if (rc) return rc;
+    return alloc_dynamic(region_total, true);
+  }
+
+  // (Re)allocate the per-sweep buffers for cap vertices (at least the regions' total); with keep,
+  // preserve the persistent off-diagonal lists that live at the front of each site's segment
+  // range.
   int alloc_dynamic(long long cap, bool keep) {
+    cap = std::max(cap, region_total);
     if (cap > (1ll << 30) - N) return lg_fail(LG_EBUDGET, "vertex capacity %lld too large", cap);
     int new_nv = (int)cap;
     int new_ns = 2 * new_nv + N;
@@ -426,7 +499,7 @@ struct Engine {
     bool both = false;
     auto fork = [&](bool b) { both = b; if (b) { cudaEventRecord(ev_fork, st); cudaStreamWaitEvent(st2, ev_fork, 0); } };
     auto join = [&]() { if (both) { cudaEventRecord(ev_join, st2); cudaStreamWaitEvent(st, ev_join, 0); } };
-    k_begin<<<grid_for((long long)C * REC_WORDS, 256), 256, 0, st>>>(A);
+    k_begin<<<grid_for(std::max<long long>((long long)C * REC_WORDS, R), 256), 256, 0, st>>>(A);
     ++launches;
     fork(n_ins > 0 && n_narrow_b > 0);
     if (n_ins) {
@@ -439,7 +512,7 @@ struct Engine {
     }
     join();
     mark(0);
-    k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A, 1);
+    k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
     scan(d_site_cnt.p, d_sbase.p, N, &ctl->ns_total, ns_cap, 1, 0, ev ? ev + 1 : nullptr);
     launches += 4;
     fork(n_wide > 0 && n_narrow > 0);
@@ -475,7 +548,7 @@ struct Engine {
       else k_cluster<4096><<<g, CL_THREADS, 0, st>>>(A);
     }
     mark(5);
-    k_flip_vertex<<<(nv_cap + 255) / 256, 256, 0, st>>>(A);
+    k_flip_vertex<<<(ns_cap + 511) / 512, 256, 0, st>>>(A);  // one 64-segment chunk per warp
     mark(6);
     launches += 4;
     fork(n_wide > 0 && n_narrow > 0);
@@ -556,9 +629,8 @@ struct Engine {
       if (hc.err == ERR_ITERCAP)
         return lg_fail(LG_EITERCAP, "union-find iteration cap hit");
       if (hc.err == ERR_OVERFLOW) {
-        long long need = std::max<long long>((long long)std::min<unsigned long long>(hc.nv_alloc, 1ull << 40), nv_cap);
         LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
-        rc = alloc_dynamic((long long)(need * 1.25) + 4096, true);
+        rc = grow_regions();
         if (rc) return rc;
       } else {
         LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
@@ -599,7 +671,7 @@ struct Engine {
         LG_CUDA(cudaEventElapsedTime(&t, ev[k - 1], ev[k]));
         kernel_ms[k] += t;
       }
-      verts += hc.nv_total;
+      verts += (hc.ns_total - N) / 2;  // every vertex adds a segment at each of its two sites
       hrec.resize((size_t)C * REC_WORDS);
       LG_CUDA(cudaMemcpy(hrec.data(), d_rec.p, hrec.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
       consume(1);
@@ -856,7 +928,7 @@ struct Engine {
     hc.nv_total = (int)nops; hc.nv_cap = nv_cap; hc.ns_cap = ns_cap;
     LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
     Arena A = arena();
-    k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A, 0);
+    k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
     scan(d_site_cnt.p, d_sbase.p, N, &d_ctl.p->ns_total, ns_cap, 1, 0);
     k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A, nullptr, N);
     k_union<><<<grid_for(2 * nops + N, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);

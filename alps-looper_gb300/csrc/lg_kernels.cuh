@@ -20,9 +20,11 @@
 // Memory layout (HBM, struct of arrays, 32-bit indices):
 //   sites    spin0[N] u8, off_base[N], off_cnt[N]     persistent between sweeps
 //   bonds    s0/s1[NB], chain[NB], dir0[NB] u8         static
-//   vertices (one contiguous time-ordered range per bond: bond_ptr[b], bond_cnt[b]; the ranges
-//            are claimed in whatever order the warps finish, which changes no result: cluster
-//            roots are segment indices and every sum is an exact integer)
+//   vertices (one contiguous time-ordered range per bond: bond_ptr[b], bond_cnt[b], claimed
+//            from the vertex region of the bond's source site; a region serves a run of
+//            consecutive sites and has its own claim counter, so claims do not contend.  The
+//            order of claims changes no result: cluster roots are segment indices and every sum
+//            is an exact integer.  Regions keep unused slots at their ends.)
 //            vtime u64 (FP64 bits), vcode u8 = g<<1|offdiag, vnew u8,
 //            vslot[2] i32 (segment of the leg on source / target site)
 //   segments (site-major CSR by sbase, k_s+1 per site, bottom segment first) stime u64,
@@ -37,8 +39,9 @@
 namespace lg {
 
 // sinfo bits
-// SI_SRC: the segment starts at the source-side leg of its vertex; bits 5-6: the vertex's graph
-enum : uint8_t { SI_SPIN = 1, SI_GNEG = 2, SI_FIRST = 4, SI_LAST = 8, SI_SRC = 16 };
+// SI_SRC: the segment starts at the source-side leg of its vertex; bits 5-6: the vertex's graph;
+// SI_OFF: the vertex is off-diagonal
+enum : uint8_t { SI_SPIN = 1, SI_GNEG = 2, SI_FIRST = 4, SI_LAST = 8, SI_SRC = 16, SI_OFF = 128 };
 constexpr int SI_GSHIFT = 5;
 
 struct Arena {
@@ -65,6 +68,13 @@ struct Arena {
   // per-sweep
   int* bond_cnt;           // NB: vertices of the bond this sweep
   int* bond_ptr;           // NB(+1): first vertex of the bond's range
+  // vertex regions: site s claims from region site_region[s], whose slots are
+  // [region_base[r], region_base[r+1]); region_fill[r] counts the claims (the whole demand,
+  // also past the end of the region)
+  int R;
+  const int* site_region;
+  const int* region_base;
+  unsigned long long* region_fill;
   int* site_cnt;           // N
   int* sbase;              // N+1
   uint64_t* vtime;
@@ -93,10 +103,10 @@ __device__ __forceinline__ unsigned long long* rec_row(const Arena& A, int c) {
 // ---------------------------------------------------------------------------------------------
 __global__ void k_begin(Arena A) {
   if (A.ctl->err) return;
-  if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl->nv_alloc = 0ull;
   LG_GRID_STRIDE(i, A.C * REC_WORDS) {
     A.rec[(size_t)A.ctl->step * A.C * REC_WORDS + i] = 0ull;
   }
+  LG_GRID_STRIDE(r, A.R) A.region_fill[r] = 0ull;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -110,9 +120,12 @@ __global__ void k_begin(Arena A) {
 // and draw a new graph with probability v0/(v0+v1) for g = 0 (graph_impl.h:323-327).  Old
 // diagonal operators are dropped (path_integral.C:515-518).
 // The output list is time ordered; at equal times off-diagonal operators come first.
-// Returns the number of vertices; with WRITE the list is stored from vertex out0 on.
-template <bool WRITE>
-__device__ int insert_bond_serial(const Arena& A, int b, int out0) {
+// Returns the number of vertices; with WRITE the list is stored from vertex out0 on.  Without
+// WRITE, a LOCAL > 0 keeps the first LOCAL vertices in the caller's buffers lt / lc (thread-local
+// memory), so that a short list needs no second walk.
+template <bool WRITE, int LOCAL = 0>
+__device__ int insert_bond_serial(const Arena& A, int b, int out0, uint64_t* lt = nullptr,
+                                  uint8_t* lc = nullptr) {
   {
     const int c = A.bond_chain[b];
     const DChain ch = A.ch[c];
@@ -157,13 +170,18 @@ __device__ int insert_bond_serial(const Arena& A, int b, int out0) {
         if (t0 == TIME_INF) break;
         p0 ^= 1u;
         if (A.sdir[i0] == own) {
-          if (WRITE) {
+          if (WRITE || LOCAL) {
             if ((ordinal & 3u) == 0) ro = philox(ch.seed, sweep, bl, TAG_OFFDIAG, ordinal >> 2);
             const uint32_t w = (ordinal & 3u) == 0 ? ro.x : (ordinal & 3u) == 1 ? ro.y
                              : (ordinal & 3u) == 2 ? ro.z : ro.w;
             const uint32_t g = ((uint64_t)w < ch.Poff) ? 0u : 1u;
-            A.vtime[out] = t0;
-            A.vcode[out] = (uint8_t)((g << 1) | 1u);
+            if (WRITE) {
+              A.vtime[out] = t0;
+              A.vcode[out] = (uint8_t)((g << 1) | 1u);
+            } else if (out - out0 < LOCAL) {
+              lt[out - out0] = t0;
+              lc[out - out0] = (uint8_t)((g << 1) | 1u);
+            }
           }
           ++ordinal;
           ++out;
@@ -179,6 +197,9 @@ __device__ int insert_bond_serial(const Arena& A, int b, int out0) {
           if (WRITE) {
             A.vtime[out] = tp;
             A.vcode[out] = (uint8_t)(gp << 1);
+          } else if (LOCAL && out - out0 < LOCAL) {
+            lt[out - out0] = tp;
+            lc[out - out0] = (uint8_t)(gp << 1);
           }
           ++out;
         }
@@ -189,25 +210,27 @@ __device__ int insert_bond_serial(const Arena& A, int b, int out0) {
   }
 }
 
-// Claims n vertices for bond b; returns the first, or -1 (and flags the sweep) when the vertex
-// buffers are too small.  The claim is made even then, so that nv_alloc ends at the demand.
-__device__ __forceinline__ int claim_vertices(const Arena& A, int b, int n) {
+// Claims n vertices for bond b from region r; returns the first, or -1 (and flags the sweep)
+// when the region is full.  The claim is counted even then, so that region_fill ends at the
+// region's demand.
+__device__ __forceinline__ int claim_vertices(const Arena& A, int b, int n, int r) {
   if (n == 0) { A.bond_cnt[b] = 0; A.bond_ptr[b] = 0; return 0; }
-  const unsigned long long at = atomicAdd(&A.ctl->nv_alloc, (unsigned long long)n);
+  const unsigned long long at = atomicAdd(A.region_fill + r, (unsigned long long)n);
+  const int base = A.region_base[r];
   A.bond_cnt[b] = n;
-  if (at + (unsigned long long)n > (unsigned long long)A.ctl->nv_cap) {
+  if (at + (unsigned long long)n > (unsigned long long)(A.region_base[r + 1] - base)) {
     A.bond_ptr[b] = 0;
     atomicExch(&A.ctl->err, ERR_OVERFLOW);
     return -1;
   }
-  A.bond_ptr[b] = (int)at;
-  return (int)at;
+  A.bond_ptr[b] = base + (int)at;
+  return base + (int)at;
 }
 
 // One-thread insertion of bond b: count, claim, write (the same list as the warp form).
 __device__ void insert_bond_alone(const Arena& A, int b) {
   const int n = insert_bond_serial<false>(A, b, 0);
-  const int at = claim_vertices(A, b, n);
+  const int at = claim_vertices(A, b, n, A.site_region[A.bond_s0[b]]);
   if (at >= 0) insert_bond_serial<true>(A, b, at);
 }
 
@@ -355,7 +378,7 @@ __global__ void __launch_bounds__(INS_WARPS * 32, 6) k_insert(Arena A, const int
       }
       const int n = nacc + nown;
       int out0 = 0;
-      if (lane == 0) out0 = claim_vertices(A, b, n);
+      if (lane == 0) out0 = claim_vertices(A, b, n, A.site_region[s]);
       out0 = __shfl_sync(0xFFFFFFFFu, out0, 0);
       if (out0 >= 0 && nacc > INS_ACC) {
         // more accepted proposals than the staging holds: the one-thread form writes the list
@@ -384,7 +407,10 @@ __global__ void __launch_bounds__(INS_WARPS * 32, 6) k_insert(Arena A, const int
 
 // Thread-per-bond form for chains with few operators per bond, where a warp per site would idle:
 // the 32 bonds of a warp count their vertices, claim one range with a single atomic add (a warp
-// prefix sum places each bond), and write their lists.
+// prefix sum places each bond), and write their lists.  A list of up to INS_LOCAL vertices is
+// kept in thread-local memory by the counting walk; longer ones are walked again to write them.
+constexpr int INS_LOCAL = 16;
+
 __global__ void __launch_bounds__(256) k_insert_narrow(Arena A, const int* bonds, int nb) {
   if (A.ctl->err) return;
   const int lane = threadIdx.x & 31;
@@ -394,24 +420,43 @@ __global__ void __launch_bounds__(256) k_insert_narrow(Arena A, const int* bonds
     const bool ok = i < nb;
     const int b = ok ? bonds[i] : 0;
     int n = 0;
-    if (ok && A.ch_active[A.bond_chain[b]]) n = insert_bond_serial<false>(A, b, 0);
+    uint64_t lt[INS_LOCAL];
+    uint8_t lc[INS_LOCAL];
+    if (ok && A.ch_active[A.bond_chain[b]]) n = insert_bond_serial<false, INS_LOCAL>(A, b, 0, lt, lc);
+    // the bonds of a warp are consecutive, so their regions form runs of lanes: a segmented
+    // prefix sum over each run, and one claim per run by its last lane
+    const int r = ok ? A.site_region[A.bond_s0[b]] : 0x7FFFFFFF;
+    const int rprev = __shfl_up_sync(0xFFFFFFFFu, r, 1);
+    const unsigned heads = __ballot_sync(0xFFFFFFFFu, lane == 0 || r != rprev);
+    const int seg0 = 31 - __clz(heads & (0xFFFFFFFFu >> (31 - lane)));
+    const unsigned later = lane == 31 ? 0u : heads & (0xFFFFFFFEu << lane);
+    const int seg1 = later ? __ffs(later) - 2 : 31;
     int incl = n;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-      if (lane >= o) incl += y;
+      if (lane - o >= seg0) incl += y;
     }
-    const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    unsigned long long base = 0;
-    if (lane == 31 && total) base = atomicAdd(&A.ctl->nv_alloc, (unsigned long long)total);
-    base = __shfl_sync(0xFFFFFFFFu, base, 31);
-    const bool room = base + (unsigned long long)total <= (unsigned long long)A.ctl->nv_cap;
-    if (!room && lane == 31) atomicExch(&A.ctl->err, ERR_OVERFLOW);
+    const int total = __shfl_sync(0xFFFFFFFFu, incl, seg1);
+    unsigned long long fill = 0;
+    if (lane == seg1 && ok && total) fill = atomicAdd(A.region_fill + r, (unsigned long long)total);
+    fill = __shfl_sync(0xFFFFFFFFu, fill, seg1);
+    bool room = true;
+    int base = 0;
     if (ok) {
-      const int at = room ? (int)(base + (unsigned long long)(incl - n)) : 0;
+      base = A.region_base[r];
+      room = fill + (unsigned long long)total <= (unsigned long long)(A.region_base[r + 1] - base);
+      if (!room && lane == seg1) atomicExch(&A.ctl->err, ERR_OVERFLOW);
+    }
+    if (ok) {
+      const int at = room ? base + (int)fill + (incl - n) : 0;
       A.bond_cnt[b] = n;
       A.bond_ptr[b] = at;
-      if (room && n) insert_bond_serial<true>(A, b, at);
+      if (room && n && n <= INS_LOCAL) {
+        for (int j = 0; j < n; ++j) { A.vtime[at + j] = lt[j]; A.vcode[at + j] = lc[j]; }
+      } else if (room && n) {
+        insert_bond_serial<true>(A, b, at);
+      }
     }
   }
 }
@@ -515,11 +560,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const int* in, int*
 }
 
 // ---------------------------------------------------------------------------------------------
-// Per site: number of segments.  In a sweep (from_claims) the vertex total is also taken from
-// the insertion's claims; the labelling paths set it themselves.
-__global__ void k_site_count(Arena A, int from_claims) {
+// Per site: number of segments.
+__global__ void k_site_count(Arena A) {
   if (A.ctl->err) return;
-  if (from_claims && blockIdx.x == 0 && threadIdx.x == 0) A.ctl->nv_total = (int)A.ctl->nv_alloc;
   LG_GRID_STRIDE(s, A.N) {
     int k = 1;
     for (int j = A.inc_off[s]; j < A.inc_off[s + 1]; ++j) k += A.bond_cnt[A.inc[j]];
@@ -599,7 +642,7 @@ __device__ void merge_site_serial(Arena& A, int s) {
     if (code & 1u) spin ^= 1u;
     A.stime[x] = bt;
     A.sinfo[x] = (uint8_t)(spin | gneg | (j == k ? SI_LAST : 0) | (sd == 0 ? SI_SRC : 0) |
-                           ((code >> 1) << SI_GSHIFT));
+                           ((code >> 1) << SI_GSHIFT) | ((code & 1u) ? SI_OFF : 0));
     A.svert[x] = v;
     A.sdir[x] = (uint8_t)best;
     A.parent[x] = x;
@@ -702,7 +745,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
         const uint8_t side = A.inc_side[j0 + d];
         A.stime[x] = sK[w][e] >> 1;
         A.sinfo[x] = (uint8_t)(spin | gneg | (r == k - 1 ? SI_LAST : 0) | (side == 0 ? SI_SRC : 0) |
-                               ((cd >> 1) << SI_GSHIFT));
+                               ((cd >> 1) << SI_GSHIFT) | ((cd & 1u) ? SI_OFF : 0));
         A.svert[x] = v;
         A.sdir[x] = (uint8_t)d;
         A.parent[x] = (r == k - 1) ? base : x;  // closure: top segment joins the bottom one
@@ -792,8 +835,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_union(Arena A) {
     const int b1 = s1 ? A.vslot[2 * v1 + 1] : 0;
     const unsigned m0 = __ballot_sync(0xFFFFFFFFu, s0), m1 = __ballot_sync(0xFFFFFFFFu, s1);
     const int n0 = __popc(m0), tot = n0 + __popc(m1);
-    if (s0) { const int q = __popc(m0 & lt); pend[w][q] = x0; pb[w][q] = b0; pg[w][q] = i0 >> SI_GSHIFT; }
-    if (s1) { const int q = n0 + __popc(m1 & lt); pend[w][q] = x1; pb[w][q] = b1; pg[w][q] = i1 >> SI_GSHIFT; }
+    if (s0) { const int q = __popc(m0 & lt); pend[w][q] = x0; pb[w][q] = b0; pg[w][q] = (i0 >> SI_GSHIFT) & 3; }
+    if (s1) { const int q = n0 + __popc(m1 & lt); pend[w][q] = x1; pb[w][q] = b1; pg[w][q] = (i1 >> SI_GSHIFT) & 3; }
     __syncwarp();
     for (int j = lane; j < tot; j += 32) {
       const int a = pend[w][j], b = pb[w][j], g = pg[w][j];
@@ -848,7 +891,6 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
   __shared__ unsigned long long hval[ACC_HASH * 4];
   const int ns = A.ctl->ns_total;
   const int ntiles = (ns + TILE - 1) / TILE;
-  const int lane = threadIdx.x & 31;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     for (int i = threadIdx.x; i < ACC_HASH; i += blockDim.x) {
       hkey[i] = -1;
@@ -1194,21 +1236,43 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
 }
 
 // Per vertex: flip the operator type when its two clusters flip differently
-// (path_integral.C:815-818; loop_0/loop_1 of graph_impl.h:489-494 in segment form).
+// (path_integral.C:815-818; loop_0/loop_1 of graph_impl.h:489-494 in segment form).  Like
+// k_union, the warps run over chunks of 64 segments and the source-side segments of a chunk are
+// compacted so that every lane handles one vertex (the vertex regions have unused slots, so
+// vertices are not enumerated directly).  The graph and the off-diagonal flag come with the
+// segment info.
 __global__ void __launch_bounds__(256) k_flip_vertex(Arena A) {
   if (A.ctl->err) return;
-  const int nv = A.ctl->nv_total;
-  LG_GRID_STRIDE(v, nv) {
-    const int a = A.vslot[2 * v], b = A.vslot[2 * v + 1];
-    const uint8_t code = A.vcode[v];
-    const int g = code >> 1;
-    uint8_t t = 0;
-    if (!(g & 2)) {
-      const int l = A.parent[a - 1];
-      const int o = (g == 0) ? A.parent[a] : A.parent[b - 1];
-      t = A.flip[l] ^ A.flip[o];
+  __shared__ int pend[8][UN_CHUNK];
+  __shared__ uint8_t pinf[8][UN_CHUNK];
+  const int ns = A.ctl->ns_total;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const long long stride = (long long)gridDim.x * 8 * UN_CHUNK;
+  for (long long c0 = ((long long)blockIdx.x * 8 + w) * UN_CHUNK; c0 < ns; c0 += stride) {
+    const int x0 = (int)c0 + lane, x1 = x0 + 32;
+    const uint8_t i0 = x0 < ns ? A.sinfo[x0] : 0;
+    const uint8_t i1 = x1 < ns ? A.sinfo[x1] : 0;
+    const bool s0 = (i0 & SI_SRC) != 0, s1 = (i1 & SI_SRC) != 0;
+    const unsigned m0 = __ballot_sync(0xFFFFFFFFu, s0), m1 = __ballot_sync(0xFFFFFFFFu, s1);
+    const int n0 = __popc(m0), tot = n0 + __popc(m1);
+    if (s0) { const int q = __popc(m0 & lt); pend[w][q] = x0; pinf[w][q] = i0; }
+    if (s1) { const int q = n0 + __popc(m1 & lt); pend[w][q] = x1; pinf[w][q] = i1; }
+    __syncwarp();
+    for (int j = lane; j < tot; j += 32) {
+      const int a = pend[w][j];
+      const uint8_t info = pinf[w][j];
+      const int v = A.svert[a];
+      const int g = (info >> SI_GSHIFT) & 3;
+      uint8_t t = 0;
+      if (!(g & 2)) {
+        const int l = A.parent[a - 1];
+        const int o = (g == 0) ? A.parent[a] : A.parent[A.vslot[2 * v + 1] - 1];
+        t = A.flip[l] ^ A.flip[o];
+      }
+      A.vnew[v] = (uint8_t)(((info & SI_OFF) ? 1u : 0u) ^ t);
     }
-    A.vnew[v] = (uint8_t)((code & 1u) ^ t);
+    __syncwarp();
   }
 }
 

@@ -284,7 +284,7 @@ extern "C" int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_
   static_scan(A.bond_cnt, A.bond_ptr, nb, &ctl->nv_total, partial, ctl, st);
   if (nv > 0) ks_scatter<<<grid_of(nv, 256), 256, 0, st>>>(A, d_bonds, nv, fill);
   ks_sort_bonds<<<grid_of(nb, 128), 128, 0, st>>>(A, d_graphs, v_of_input);
-  k_site_count<<<grid_of(n, 256), 256, 0, st>>>(A, 0);
+  k_site_count<<<grid_of(n, 256), 256, 0, st>>>(A);
   static_scan(A.site_cnt, A.sbase, n, &ctl->ns_total, partial, ctl, st);
   k_merge<<<grid_of((long long)n * 32, MERGE_WARPS * 32), MERGE_WARPS * 32, 0, st>>>(A, nullptr, n);
   if (nv > 0) k_union<><<<grid_of(ns, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);

@@ -39,9 +39,7 @@ struct Ctl {
   uint32_t step;     // record row of the current sweep
   int nv_cap;
   int ns_cap;
-  // vertex slots claimed by the insertion pass; 64-bit so that it counts the whole demand of a
-  // sweep that overflows nv_cap (the engine grows to it and replays the sweep)
-  unsigned long long nv_alloc;
+  int pad[2];
 };
 
 }  // namespace lg
