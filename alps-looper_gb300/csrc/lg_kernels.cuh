@@ -774,21 +774,26 @@ __global__ void __launch_bounds__(256) k_merge_narrow(Arena A, const int* sites,
 // atomicCAS, so the root of every cluster is its smallest segment index whatever the order of
 // the unions (the deterministic unify of union_find.h:231-233,270-273).  Finds halve paths with
 // plain stores: a store only ever replaces a non-root's parent by one of its ancestors.
-__device__ __forceinline__ int uf_find(int* P, int x) {
+// uf_find with the first parent read, p = P[x], already made by the caller.
+__device__ __forceinline__ int uf_find_from(int* P, int x, int p) {
   while (true) {
-    const int p = __ldcg(P + x);
     if (p == x) return x;
     const int gp = __ldcg(P + p);
     if (gp == p) return p;
     P[x] = gp;
     x = gp;
+    p = __ldcg(P + x);
   }
 }
 
+// The first parent reads of both finds are issued together (one round trip instead of two when
+// both nodes are roots).  Hooks always go from a larger to a smaller index, so parent pointers
+// decrease along every path and no interleaving of unions can close a cycle.
 __device__ __forceinline__ bool uf_union(int* P, int a, int b) {
   for (int it = 0; it < ITER_CAP; ++it) {
-    a = uf_find(P, a);
-    b = uf_find(P, b);
+    const int pa = __ldcg(P + a), pb = __ldcg(P + b);
+    a = uf_find_from(P, a, pa);
+    b = uf_find_from(P, b, pb);
     if (a == b) return true;
     const int lo = a < b ? a : b, hi = a < b ? b : a;
     const int old = atomicCAS(P + hi, hi, lo);
@@ -930,7 +935,9 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
         unsigned h = ((unsigned)r * 2654435761u) >> 22;  // 10-bit hash
         bool done = false;
         for (int probe = 0; probe < 32; ++probe) {
-          const int k = atomicCAS(hkey + h, -1, r);
+          // a slot's key never changes once set: read it first, CAS only an empty one
+          int k = hkey[h];
+          if (k == -1) k = atomicCAS(hkey + h, -1, r);
           if (k == -1 || k == r) { atomicAdd(hval + 4 * h + q, len); done = true; break; }
           h = (h + 1) & (ACC_HASH - 1);
         }
