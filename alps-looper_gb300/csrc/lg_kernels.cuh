@@ -590,6 +590,37 @@ __device__ __forceinline__ uint64_t merge_key(uint64_t t, uint8_t code) {
   return (t << 1) | (uint64_t)(~code & 1u);
 }
 
+// One two-way merge by a warp (merge path).  X (nx keys at XK) goes before Y (ny keys at YK) at
+// equal keys.  Indices travel with the keys: XI[i], or xb + i when XI is null (the same for Y).
+// Each lane takes a contiguous chunk of the output, finds where its chunk starts in X and Y by
+// one binary search along its diagonal (the co-rank), then merges the chunk sequentially.
+__device__ __forceinline__ void warp_merge2(const uint64_t* XK, const uint16_t* XI, int xb, int nx,
+                                            const uint64_t* YK, const uint16_t* YI, int yb, int ny,
+                                            uint64_t* OK, uint16_t* OI, int lane) {
+  const int n = nx + ny;
+  const int per = (n + 31) >> 5;
+  const int d0 = min(lane * per, n), d1 = min(d0 + per, n);
+  if (d0 >= d1) return;
+  int lo = max(0, d0 - ny), hi = min(d0, nx);
+  while (lo < hi) {  // smallest i with Y[d0 - i - 1] < X[i]
+    const int i = (lo + hi) >> 1;
+    if (XK[i] <= YK[d0 - i - 1]) lo = i + 1; else hi = i;
+  }
+  int i = lo, j = d0 - lo;
+  for (int d = d0; d < d1; ++d) {
+    const bool tx = j >= ny || (i < nx && XK[i] <= YK[j]);
+    if (tx) {
+      OK[d] = XK[i];
+      OI[d] = XI ? XI[i] : (uint16_t)(xb + i);
+      ++i;
+    } else {
+      OK[d] = YK[j];
+      OI[d] = YI ? YI[j] : (uint16_t)(yb + j);
+      ++j;
+    }
+  }
+}
+
 __device__ void merge_site_serial(Arena& A, int s) {
   const int j0 = A.inc_off[s];
   const int z = A.inc_off[s + 1] - j0;
@@ -655,7 +686,9 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
   if (A.ctl->err) return;
   __shared__ uint64_t sK[MERGE_WARPS][MERGE_CAP];   // staged merge keys, list by list
   __shared__ uint8_t sC[MERGE_WARPS][MERGE_CAP];    // staged codes
-  __shared__ uint16_t mE[MERGE_WARPS][MERGE_CAP];   // merged order -> staged index
+  __shared__ uint16_t sI[MERGE_WARPS][MERGE_CAP];   // staged index of the keys in sK (levels >= 2)
+  __shared__ uint64_t mK[MERGE_WARPS][MERGE_CAP];   // merge output (keys)
+  __shared__ uint16_t mI[MERGE_WARPS][MERGE_CAP];   // merge output (staged indices)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; si < nsites; si += warps) {
@@ -697,25 +730,58 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
       }
     }
     __syncwarp();
-    // merged rank of every endpoint: its place in its own list plus, for every other list, the
-    // entries ordered before it (equal keys of an earlier list count as before).  Every lane
-    // searches every list (the own list too, whose count it then ignores), so the warp does not
-    // diverge on the list index.
-    for (int e = lane; e < k; e += 32) {
-      int d = 0;
+    // merge the incident lists pairwise, level by level (lists in index order, earlier list
+    // first at equal keys: the order (time, off-diagonal first, list)), ping-ponging between sK
+    // and mK; the final keys and staged indices end in fK / fI
+    int rs[MAXZ], rn[MAXZ];
 #pragma unroll
-      for (int q = 1; q < MAXZ; ++q) if (e >= off[q]) d = q;
-      const uint64_t key = sK[w][e];
-      int r = 0;
+    for (int q = 0; q < MAXZ; ++q) { rs[q] = off[q]; rn[q] = off[q + 1] - off[q]; }
+    int nr = z;
+    uint64_t* curK = sK[w];
+    const uint16_t* curI = nullptr;  // level 0: the index of a key is its position
+    bool in_m = false;
 #pragma unroll
-      for (int q = 0; q < MAXZ; ++q) {  // lists q >= z are empty
-        // keys are below 2^63, so key + 1 does not wrap: "< key + 1" is "<= key"
-        const int c = count_before<false>(sK[w] + off[q], off[q + 1] - off[q], key + (q < d ? 1u : 0u));
-        r += q == d ? e - off[q] : c;
+    for (int level = 0; level < 3; ++level) {
+      if (nr <= 1) break;
+      uint64_t* nK = in_m ? sK[w] : mK[w];
+      uint16_t* nI = in_m ? sI[w] : mI[w];
+      int ns2[MAXZ], nn2[MAXZ];
+      int o = 0, nn = 0;
+#pragma unroll
+      for (int p = 0; p < MAXZ; p += 2) {
+        if (p + 1 < nr) {
+          warp_merge2(curK + rs[p], curI ? curI + rs[p] : nullptr, rs[p], rn[p],
+                      curK + rs[p + 1], curI ? curI + rs[p + 1] : nullptr, rs[p + 1], rn[p + 1],
+                      nK + o, nI + o, lane);
+          ns2[p >> 1] = o; nn2[p >> 1] = rn[p] + rn[p + 1];
+          o += rn[p] + rn[p + 1];
+          ++nn;
+        } else if (p < nr) {  // an odd run out: copied
+          for (int i = lane; i < rn[p]; i += 32) {
+            nK[o + i] = curK[rs[p] + i];
+            nI[o + i] = curI ? curI[rs[p] + i] : (uint16_t)(rs[p] + i);
+          }
+          ns2[p >> 1] = o; nn2[p >> 1] = rn[p];
+          o += rn[p];
+          ++nn;
+        }
       }
-      mE[w][r] = (uint16_t)e;
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < MAXZ / 2; ++q) { rs[q] = ns2[q]; rn[q] = nn2[q]; }
+      nr = nn;
+      curK = nK;
+      curI = nI;
+      in_m = !in_m;
     }
-    __syncwarp();
+    if (!curI) {  // a single list: its indices are its positions
+      for (int i = lane; i < k; i += 32) { mK[w][i] = sK[w][i]; mI[w][i] = (uint16_t)i; }
+      __syncwarp();
+      curK = mK[w];
+      curI = mI[w];
+    }
+    const uint64_t* fK = curK;
+    const uint16_t* fI = curI;
     // segments: prefix XOR of off-diagonal flags gives each segment's spin
     const uint8_t gneg = A.gauge[s] < 0 ? SI_GNEG : 0;
     uint32_t carry = A.spin0[s];
@@ -729,7 +795,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
     for (int r0 = 0; r0 < k; r0 += 32) {
       const int r = r0 + lane;
       const bool ok = r < k;
-      const int e = ok ? mE[w][r] : 0;
+      const int e = ok ? fI[r] : 0;
       const uint8_t cd = ok ? sC[w][e] : 0;
       const unsigned ball = __ballot_sync(0xFFFFFFFFu, ok && (cd & 1u));
       const uint32_t spin = carry ^ (__popc(ball & (0xFFFFFFFFu >> (31 - lane))) & 1u);
@@ -743,7 +809,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
         const int v = pd + (e - od);
         const int x = base + 1 + r;
         const uint8_t side = A.inc_side[j0 + d];
-        A.stime[x] = sK[w][e] >> 1;
+        A.stime[x] = fK[r] >> 1;
         A.sinfo[x] = (uint8_t)(spin | gneg | (r == k - 1 ? SI_LAST : 0) | (side == 0 ? SI_SRC : 0) |
                                ((cd >> 1) << SI_GSHIFT) | ((cd & 1u) ? SI_OFF : 0));
         A.svert[x] = v;
