@@ -135,6 +135,7 @@ struct Engine {
   const int* ins_list = nullptr;    // insertion, warp per site
   int n_wide = 0, n_narrow = 0, n_ins = 0, n_narrow_b = 0;
   int sweep_launches = 0;         // kernel launches of one sweep
+  int merge_cap = MERGE_CAP;      // k_merge staging capacity per warp (see set_merge_cap)
   cudaStream_t st2 = nullptr;     // the narrow kernels run beside the wide ones
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaStream_t st = nullptr;
@@ -268,6 +269,7 @@ struct Engine {
     LG_CUDA(cudaMemset(d_ctl.p, 0, sizeof(Ctl)));
     if ((rc = build_regions())) return rc;
     if ((rc = alloc_dynamic(region_total, false))) return rc;
+    set_merge_cap();
     if ((rc = set_shape(default_shape()))) return rc;
     // initial spins (one launch per distinct init mode)
     Arena A = arena();
@@ -410,6 +412,19 @@ struct Engine {
     return s;
   }
 
+  // k_merge stages a site's endpoints in shared memory up to merge_cap of them (larger sites take
+  // the one-thread merge).  The capacity follows the arena's largest expected endpoint count per
+  // site with a wide margin, so that small arenas keep k_merge's shared memory (and so its
+  // occupancy) small.
+  void set_merge_cap() {
+    double mu = 0;
+    for (int c = 0; c < C; ++c) mu = std::max(mu, endpoints_per_site(c));
+    int cap = (int)std::ceil(1.6 * mu + 6.0 * std::sqrt(mu) + 32.0);
+    cap = (cap + 31) & ~31;
+    merge_cap = std::min(std::max(cap, 64), MERGE_CAP);
+    drop_graph();
+  }
+
   // Expected endpoints per site of chain c: the narrow / wide criterion.
   double endpoints_per_site(int c) const {
     const ChainSpec& s = spec[c];
@@ -517,7 +532,8 @@ struct Engine {
     launches += 4;
     fork(n_wide > 0 && n_narrow > 0);
     if (n_wide) {
-      k_merge<<<grid_for((long long)n_wide * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A, wide_list, n_wide);
+      k_merge<<<grid_for((long long)n_wide * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32,
+                MERGE_WARPS * merge_smem_per_warp(merge_cap), st>>>(A, wide_list, n_wide, merge_cap);
       ++launches;
     }
     if (n_narrow) {
@@ -930,7 +946,8 @@ struct Engine {
     Arena A = arena();
     k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
     scan(d_site_cnt.p, d_sbase.p, N, &d_ctl.p->ns_total, ns_cap, 1, 0);
-    k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32, 0, st>>>(A, nullptr, N);
+    k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32,
+              MERGE_WARPS * merge_smem_per_warp(MERGE_CAP), st>>>(A, nullptr, N, MERGE_CAP);
     k_union<><<<grid_for(2 * nops + N, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
     k_compress<<<grid_for(2 * nops + N, 256), 256, 0, st>>>(A);
     g_launches += 7;
@@ -1021,6 +1038,7 @@ struct Engine {
     hch[c].flip_coef = spec[c].dchain.flip_coef;
     LG_CUDA(cudaMemcpy(d_ch.p + c, &hch[c], sizeof(DChain), cudaMemcpyHostToDevice));
     acc[c] = ChainAcc();
+    set_merge_cap();
     return set_shape(shape);  // the chain's narrow / wide class depends on beta
   }
 };

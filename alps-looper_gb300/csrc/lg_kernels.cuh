@@ -582,7 +582,9 @@ __global__ void k_site_count(Arena A) {
 // merge), the spins follow from a warp prefix-XOR of the off-diagonal flags in merged order, and
 // the segment arrays are written coalesced.  Sites with more endpoints use the one-thread merge.
 constexpr int MERGE_WARPS = 4;
-constexpr int MERGE_CAP = 384;
+constexpr int MERGE_CAP = 384;        // largest staging capacity per warp
+// shared memory of k_merge per warp for a staging capacity of cap endpoints
+__host__ __device__ constexpr int merge_smem_per_warp(int cap) { return cap * (8 + 8 + 2 + 2 + 1); }
 
 // Merge key of an endpoint: (time bits << 1) | diagonal.  Times are FP64 bit patterns of values
 // in [0, 1), below 2^62, so the key fits; key order is (time, off-diagonal first).
@@ -682,14 +684,20 @@ __device__ void merge_site_serial(Arena& A, int s) {
   if (k > 0) A.parent[base + k] = base;
 }
 
-__global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const int* sites, int nsites) {
+// `cap` (a multiple of 32, at most MERGE_CAP) is the staging capacity per warp, sized by the
+// engine from the arena's largest expected endpoint count per site; the dynamic shared memory is
+// MERGE_WARPS * merge_smem_per_warp(cap) bytes.
+__global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const int* sites, int nsites,
+                                                              int cap) {
   if (A.ctl->err) return;
-  __shared__ uint64_t sK[MERGE_WARPS][MERGE_CAP];   // staged merge keys, list by list
-  __shared__ uint8_t sC[MERGE_WARPS][MERGE_CAP];    // staged codes
-  __shared__ uint16_t sI[MERGE_WARPS][MERGE_CAP];   // staged index of the keys in sK (levels >= 2)
-  __shared__ uint64_t mK[MERGE_WARPS][MERGE_CAP];   // merge output (keys)
-  __shared__ uint16_t mI[MERGE_WARPS][MERGE_CAP];   // merge output (staged indices)
+  extern __shared__ __align__(16) unsigned char merge_smem[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned char* wb = merge_smem + (size_t)w * merge_smem_per_warp(cap);
+  uint64_t* const wsK = reinterpret_cast<uint64_t*>(wb);              // staged merge keys, list by list
+  uint64_t* const wmK = wsK + cap;                                    // merge output (keys)
+  uint16_t* const wsI = reinterpret_cast<uint16_t*>(wmK + cap);       // index of the keys in sK (levels >= 2)
+  uint16_t* const wmI = wsI + cap;                                    // merge output (staged indices)
+  uint8_t* const wsC = reinterpret_cast<uint8_t*>(wmI + cap);         // staged codes
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; si < nsites; si += warps) {
     const int s = sites ? sites[si] : si;
@@ -702,7 +710,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
       if (s == A.ch[c].site_off) A.ch_slot_off[c] = base;
       if (s == A.N - 1) A.ch_slot_off[A.C] = base + k + 1;
     }
-    if (k > MERGE_CAP) {
+    if (k > cap) {
       if (lane == 0) merge_site_serial(A, s);
       __syncwarp();
       continue;
@@ -725,26 +733,47 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
     for (int d = 0; d < MAXZ; ++d) {
       for (int i = lane; i < off[d + 1] - off[d]; i += 32) {
         const uint8_t c = A.vcode[ptr[d] + i];
-        sK[w][off[d] + i] = merge_key(A.vtime[ptr[d] + i], c);
-        sC[w][off[d] + i] = c;
+        wsK[off[d] + i] = merge_key(A.vtime[ptr[d] + i], c);
+        wsC[off[d] + i] = c;
       }
     }
     __syncwarp();
-    // merge the incident lists pairwise, level by level (lists in index order, earlier list
-    // first at equal keys: the order (time, off-diagonal first, list)), ping-ponging between sK
-    // and mK; the final keys and staged indices end in fK / fI
+    // The merged order is (time, off-diagonal first, list).  Up to 32 endpoints: every lane
+    // takes one and computes its rank directly (its place in its own list plus, per other list,
+    // the entries before it; equal keys of an earlier list count as before).  More: the lists
+    // are merged pairwise, level by level, in list order (warp_merge2), ping-ponging between sK
+    // and mK.  Either way the final keys and staged indices end in fK / fI.
+    if (k <= 32) {
+      uint64_t key = 0;
+      int r = 0;
+      if (lane < k) {
+        int d = 0;
+#pragma unroll
+        for (int q = 1; q < MAXZ; ++q) if (lane >= off[q]) d = q;
+        key = wsK[lane];
+#pragma unroll
+        for (int q = 0; q < MAXZ; ++q) {  // lists q >= z are empty
+          // keys are below 2^63, so "< key + 1" is "<= key"
+          const int c = count_before<false>(wsK + off[q], off[q + 1] - off[q], key + (q < d ? 1u : 0u));
+          r += q == d ? lane - off[q] : c;
+        }
+      }
+      __syncwarp();
+      if (lane < k) { wmK[r] = key; wmI[r] = (uint16_t)lane; }
+      __syncwarp();
+    }
     int rs[MAXZ], rn[MAXZ];
 #pragma unroll
     for (int q = 0; q < MAXZ; ++q) { rs[q] = off[q]; rn[q] = off[q + 1] - off[q]; }
-    int nr = z;
-    uint64_t* curK = sK[w];
-    const uint16_t* curI = nullptr;  // level 0: the index of a key is its position
-    bool in_m = false;
+    int nr = k <= 32 ? 1 : z;
+    uint64_t* curK = k <= 32 ? wmK : wsK;
+    const uint16_t* curI = k <= 32 ? wmI : nullptr;  // level 0: the index of a key is its position
+    bool in_m = k <= 32;
 #pragma unroll
     for (int level = 0; level < 3; ++level) {
       if (nr <= 1) break;
-      uint64_t* nK = in_m ? sK[w] : mK[w];
-      uint16_t* nI = in_m ? sI[w] : mI[w];
+      uint64_t* nK = in_m ? wsK : wmK;
+      uint16_t* nI = in_m ? wsI : wmI;
       int ns2[MAXZ], nn2[MAXZ];
       int o = 0, nn = 0;
 #pragma unroll
@@ -775,10 +804,10 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
       in_m = !in_m;
     }
     if (!curI) {  // a single list: its indices are its positions
-      for (int i = lane; i < k; i += 32) { mK[w][i] = sK[w][i]; mI[w][i] = (uint16_t)i; }
+      for (int i = lane; i < k; i += 32) { wmK[i] = wsK[i]; wmI[i] = (uint16_t)i; }
       __syncwarp();
-      curK = mK[w];
-      curI = mI[w];
+      curK = wmK;
+      curI = wmI;
     }
     const uint64_t* fK = curK;
     const uint16_t* fI = curI;
@@ -796,7 +825,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
       const int r = r0 + lane;
       const bool ok = r < k;
       const int e = ok ? fI[r] : 0;
-      const uint8_t cd = ok ? sC[w][e] : 0;
+      const uint8_t cd = ok ? wsC[e] : 0;
       const unsigned ball = __ballot_sync(0xFFFFFFFFu, ok && (cd & 1u));
       const uint32_t spin = carry ^ (__popc(ball & (0xFFFFFFFFu >> (31 - lane))) & 1u);
       if (ok) {
