@@ -33,7 +33,7 @@ using namespace lg;
 // timed stages of one sweep, in launch order (an event is recorded after each stage)
 static const int kNumStages = 8;
 static const char* kStageNames[kNumStages] = {
-    "k_begin+k_insert", "k_site_count+scan(sites)", "k_merge", "k_union", "k_accumulate",
+    "k_insert", "k_site_count+scan(sites)", "k_merge", "k_union", "k_accumulate",
     "k_cluster", "k_flip_vertex", "k_site_end+k_end"};
 
 static std::atomic<uint64_t> g_launches{0};
@@ -171,7 +171,7 @@ struct Engine {
     A.vtime = d_vtime.p; A.vcode = d_vcode.p; A.vnew = d_vnew.p; A.vslot = d_vslot.p;
     A.stime = d_stime.p; A.sinfo = d_sinfo.p; A.svert = d_svert.p; A.sdir = d_sdir.p;
     A.parent = d_parent.p; A.flip = d_flip.p; A.cls = d_cls.p; A.cnt0 = d_cnt0.p;
-    A.rec = d_rec.p; A.ctl = d_ctl.p;
+    A.rec = d_rec.p; A.ctl = d_ctl.p; A.rec_rows = rec_rows;
     return A;
   }
 
@@ -249,6 +249,7 @@ struct Engine {
         (rc = d_sbase.alloc(N + 1)) || (rc = d_ctl.alloc(1)))
       return rc;
     int maxparts = std::max((NB + SCAN_TILE - 1) / SCAN_TILE, (N + SCAN_TILE - 1) / SCAN_TILE);
+    maxparts = std::max(maxparts, (N + SITE_SCAN_BLOCK - 1) / SITE_SCAN_BLOCK);  // k_site_blocks
     if ((rc = d_partial.alloc(maxparts + 1))) return rc;
     LG_CUDA(cudaMemcpy(d_ch.p, hch.data(), C * sizeof(DChain), cudaMemcpyHostToDevice));
     LG_CUDA(cudaMemcpy(d_bond_s0.p, h_bond_s0.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
@@ -332,6 +333,15 @@ struct Engine {
     return LG_OK;
   }
 
+  // A sweep starts with its record row and the region claim counters at zero; k_end leaves them
+  // so for the next sweep.  This sets them up for the record row the host resets the counter to
+  // (row 0), after a chunk, a failed sweep or a reallocation.
+  int clear_sweep_state() {
+    if (d_rec.p) LG_CUDA(cudaMemsetAsync(d_rec.p, 0, (size_t)C * REC_WORDS * sizeof(unsigned long long), st));
+    if (R) LG_CUDA(cudaMemsetAsync(d_region_fill.p, 0, (size_t)R * sizeof(unsigned long long), st));
+    return LG_OK;
+  }
+
   // After an overflowing sweep: grow every region whose demand passed its capacity.
   int grow_regions() {
     std::vector<unsigned long long> fill(R);
@@ -383,6 +393,7 @@ struct Engine {
     }
     nv_cap = new_nv;
     ns_cap = new_ns;
+    if ((rc = clear_sweep_state())) return rc;
     Ctl hc;
     LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
     hc.nv_cap = nv_cap; hc.ns_cap = ns_cap;
@@ -508,14 +519,11 @@ struct Engine {
   // beside the wide ones (a fork and a join in the captured graph).
   void enqueue_sweep(cudaEvent_t* ev = nullptr) {
     Arena A = arena();
-    Ctl* ctl = d_ctl.p;
     int launches = 0;
     auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
     bool both = false;
     auto fork = [&](bool b) { both = b; if (b) { cudaEventRecord(ev_fork, st); cudaStreamWaitEvent(st2, ev_fork, 0); } };
     auto join = [&]() { if (both) { cudaEventRecord(ev_join, st2); cudaStreamWaitEvent(st, ev_join, 0); } };
-    k_begin<<<grid_for(std::max<long long>((long long)C * REC_WORDS, R), 256), 256, 0, st>>>(A);
-    ++launches;
     fork(n_ins > 0 && n_narrow_b > 0);
     if (n_ins) {
       k_insert<<<grid_for((long long)n_ins * 32, INS_WARPS * 32, 16), INS_WARPS * 32, 0, st>>>(A, ins_list, n_ins);
@@ -527,9 +535,17 @@ struct Engine {
     }
     join();
     mark(0);
-    k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
-    scan(d_site_cnt.p, d_sbase.p, N, &ctl->ns_total, ns_cap, 1, 0, ev ? ev + 1 : nullptr);
-    launches += 4;
+    if (N <= SITE_SCAN_MAX) {
+      const int g = (N + SITE_SCAN_BLOCK - 1) / SITE_SCAN_BLOCK;
+      k_site_blocks<<<g, SITE_SCAN_BLOCK, 0, st>>>(A, d_partial.p);
+      k_site_offsets<<<g, SITE_SCAN_BLOCK, 0, st>>>(A, d_partial.p);
+      launches += 2;
+    } else {
+      k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
+      scan(d_site_cnt.p, d_sbase.p, N, &d_ctl.p->ns_total, ns_cap, 1, 0);
+      launches += 4;
+    }
+    mark(1);
     fork(n_wide > 0 && n_narrow > 0);
     if (n_wide) {
       k_merge<<<grid_for((long long)n_wide * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32,
@@ -577,10 +593,9 @@ struct Engine {
       ++launches;
     }
     join();
-    k_end<<<grid_for(C, 128), 128, 0, st>>>(A);
-    k_step<<<1, 1, 0, st>>>(ctl);
+    k_end<<<1, 1024, 0, st>>>(A);
     mark(7);
-    launches += 2;
+    launches += 1;
     sweep_launches = launches;
     g_launches += launches;
   }
@@ -651,6 +666,7 @@ struct Engine {
       } else {
         LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
       }
+      if ((rc = clear_sweep_state())) return rc;
       n -= done;
     }
     return LG_OK;
@@ -694,6 +710,7 @@ struct Engine {
       Ctl z = hc;
       z.step = 0;
       LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
+      if (int rc = clear_sweep_state()) return rc;
       --n;
     }
     *vertices = verts;

@@ -2,7 +2,6 @@
 //
 // One sweep of every chain in the arena (path_integral.C:355-864) is this kernel sequence:
 //
-//   k_begin          zero this sweep's measurement records                   (:472-479 reset)
 //   k_insert         per bond: new operator string (time, graph, type), written at a vertex
 //                    range claimed with one atomic add; capacity check          (:403-577)
 //   k_site_count     per site: number of segments = 1 + incident vertices
@@ -15,7 +14,8 @@
 //   k_cluster        per root: flip coin, improved / field sums -> records     (:739-803)
 //   k_flip_vertex    per vertex: new diagonal/off-diagonal type               (:805-818)
 //   k_site_end       per site: spin flip, compacted off-diagonal list         (:822-823)
-//   k_end            per chain: operator count, sweep counter
+//   k_end            per chain: operator count, sweep counter; clears the next sweep's record
+//                    row and claim counters                                    (:472-479 reset)
 //
 // Memory layout (HBM, struct of arrays, 32-bit indices):
 //   sites    spin0[N] u8, off_base[N], off_cnt[N]     persistent between sweeps
@@ -91,6 +91,7 @@ struct Arena {
   unsigned int* cnt0;       // 4 per segment
   unsigned long long* rec;  // [rows][C][REC_WORDS]
   Ctl* ctl;
+  int rec_rows;             // rows of rec
 };
 
 #define LG_GRID_STRIDE(i, n) \
@@ -101,13 +102,8 @@ __device__ __forceinline__ unsigned long long* rec_row(const Arena& A, int c) {
 }
 
 // ---------------------------------------------------------------------------------------------
-__global__ void k_begin(Arena A) {
-  if (A.ctl->err) return;
-  LG_GRID_STRIDE(i, A.C * REC_WORDS) {
-    A.rec[(size_t)A.ctl->step * A.C * REC_WORDS + i] = 0ull;
-  }
-  LG_GRID_STRIDE(r, A.R) A.region_fill[r] = 0ull;
-}
+// (A sweep starts with its record row and the region claim counters at zero: k_end of the previous
+// sweep clears them, the host when it resets the record row counter.)
 
 // ---------------------------------------------------------------------------------------------
 // Insertion / removal of operators for one bond (path_integral.C:484-566).
@@ -560,14 +556,59 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const int* in, int*
 }
 
 // ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ int site_segments(const Arena& A, int s) {
+  int k = 1;
+  for (int j = A.inc_off[s]; j < A.inc_off[s + 1]; ++j) k += A.bond_cnt[A.inc[j]];
+  return k;
+}
+
+// Segment offsets of an arena of at most SITE_SCAN_MAX sites in two launches.  k_site_blocks:
+// one site per thread, the block's total into partial[block].  k_site_offsets: every block scans
+// the (at most 1024) block totals for its own offset, then its sites; the last block writes the
+// total, ns_total, and checks it against ns_cap.
+constexpr int SITE_SCAN_BLOCK = 1024;
+constexpr int SITE_SCAN_MAX = SITE_SCAN_BLOCK * SITE_SCAN_BLOCK;
+
+__global__ void __launch_bounds__(SITE_SCAN_BLOCK) k_site_blocks(Arena A, int* partial) {
+  if (A.ctl->err) return;
+  __shared__ int sw[32];
+  const int s = blockIdx.x * SITE_SCAN_BLOCK + threadIdx.x;
+  int k = 0;
+  if (s < A.N) {
+    k = site_segments(A, s);
+    A.site_cnt[s] = k;
+  }
+  int tot;
+  block_exclusive_scan(k, sw, &tot);
+  if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(SITE_SCAN_BLOCK) k_site_offsets(Arena A, const int* partial) {
+  if (A.ctl->err) return;
+  __shared__ int sw[32];
+  __shared__ int base;
+  const int nparts = gridDim.x;
+  const int pv = (int)threadIdx.x < nparts ? partial[threadIdx.x] : 0;
+  int ptot;
+  const int pex = block_exclusive_scan(pv, sw, &ptot);
+  if ((int)threadIdx.x == (int)blockIdx.x) base = pex;
+  __syncthreads();
+  const int s = blockIdx.x * SITE_SCAN_BLOCK + threadIdx.x;
+  const int k = s < A.N ? A.site_cnt[s] : 0;
+  int tot;
+  const int ex = block_exclusive_scan(k, sw, &tot);
+  if (s < A.N) A.sbase[s] = base + ex;
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+    A.sbase[A.N] = ptot;
+    A.ctl->ns_total = ptot;
+    if (ptot > A.ctl->ns_cap) A.ctl->err = ERR_OVERFLOW;
+  }
+}
+
 // Per site: number of segments.
 __global__ void k_site_count(Arena A) {
   if (A.ctl->err) return;
-  LG_GRID_STRIDE(s, A.N) {
-    int k = 1;
-    for (int j = A.inc_off[s]; j < A.inc_off[s + 1]; ++j) k += A.bond_cnt[A.inc[j]];
-    A.site_cnt[s] = k;
-  }
+  LG_GRID_STRIDE(s, A.N) A.site_cnt[s] = site_segments(A, s);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1440,19 +1481,24 @@ __global__ void __launch_bounds__(256) k_site_end_narrow(Arena A, const int* sit
   }
 }
 
-__global__ void k_end(Arena A) {
+// One block: per chain the operator count and the sweep counter; then the next sweep's record
+// row (if the chunk has one) and the region claim counters are cleared, and the record row
+// counter advances.
+__global__ void __launch_bounds__(1024) k_end(Arena A) {
   if (A.ctl->err) return;
-  LG_GRID_STRIDE(c, A.C) {
+  const uint32_t step = A.ctl->step;
+  for (int c = threadIdx.x; c < A.C; c += blockDim.x) {
     // every vertex adds one segment at each of its two sites
     const int nv = (A.ch_slot_off[c + 1] - A.ch_slot_off[c] - A.ch[c].nsites) / 2;
     rec_row(A, c)[R_NOP] = (unsigned long long)nv;
     A.ch_sweep[c] += 1u;
   }
-}
-
-__global__ void k_step(Ctl* ctl) {
-  if (ctl->err) return;
-  ctl->step += 1u;
+  if ((int)step + 1 < A.rec_rows)
+    for (int i = threadIdx.x; i < A.C * REC_WORDS; i += blockDim.x)
+      A.rec[((size_t)step + 1) * A.C * REC_WORDS + i] = 0ull;
+  for (int r = threadIdx.x; r < A.R; r += blockDim.x) A.region_fill[r] = 0ull;
+  __syncthreads();
+  if (threadIdx.x == 0) A.ctl->step = step + 1u;
 }
 
 // Moving chains into a new arena: site s of the new arena takes the state of site map[s] of
