@@ -223,8 +223,8 @@ def run_batched(lg, steps, therm, plain_sample=16):
     for i in idx:
         w = lg.LoopWorker(ps[i])
         w.run(min(therm, 64))
-        w.autotune(1, FLUSH_BYTES)  # the plain path at its own best launch shape
-        m = w.time_sweeps(max(4, steps // 4), FLUSH_BYTES)
+        w.autotune(2, FLUSH_BYTES)  # the plain path at its own best launch shape
+        m = w.time_sweeps(max(16, steps), FLUSH_BYTES)
         t_p += float(m.mean()) / 1e3
         s_p += ps[i].L * ps[i].L
         w.close()
@@ -292,10 +292,10 @@ def run_served(lg, n_requests, plain_sample=12):
         p = reqs[i][1]
         w = lg.LoopWorker(p)
         w.run(4)
-        w.autotune(1)  # the plain path at its own best launch shape
+        w.autotune(2)  # the plain path at its own best launch shape
         t1 = time.perf_counter()
-        w.run(16)
-        per = (time.perf_counter() - t1) / 16
+        w.run(32)
+        per = (time.perf_counter() - t1) / 32
         total_sweeps = p.sweeps + (p.sweeps >> 3)
         t_plain += per * total_sweeps
         w_plain += p.L ** p.lattice * total_sweeps
