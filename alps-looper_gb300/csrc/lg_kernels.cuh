@@ -268,7 +268,7 @@ __device__ __forceinline__ int count_lt(const uint64_t* T, int n, uint64_t t) {
 // The vertex count n of a bond is known once its proposals are drawn, so the warp claims its
 // range of n vertices (claim_vertices) before it writes the list there: one pass, no scan.
 // The warps run over `sites` (nullptr: every site of the arena, in order).
-__global__ void __launch_bounds__(INS_WARPS * 32, 6) k_insert(Arena A, const int* sites, int nsites) {
+__global__ void __launch_bounds__(INS_WARPS * 32, 7) k_insert(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
   __shared__ uint64_t offS[INS_WARPS][INS_CAP];
   __shared__ uint8_t dirS[INS_WARPS][INS_CAP];
