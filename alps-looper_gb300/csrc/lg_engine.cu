@@ -93,12 +93,12 @@ struct Engine {
   std::vector<ChainAcc> acc;
   int C = 0, N = 0, NB = 0;
   std::vector<DChain> hch;
-  std::vector<int> h_bond_s0, h_bond_s1, h_inc_off, h_inc;
+  std::vector<int> h_bond_s0, h_bond_s1, h_inc_off, h_inc, h_inc_nbr;
   std::vector<uint8_t> h_inc_side, h_bond_dir0;
   std::vector<int> h_site_chain, h_bond_chain;
 
   DBuf<DChain> d_ch;
-  DBuf<int> d_bond_s0, d_bond_s1, d_bond_chain, d_inc_off, d_inc, d_site_chain;
+  DBuf<int> d_bond_s0, d_bond_s1, d_bond_chain, d_inc_off, d_inc, d_inc_nbr, d_site_chain;
   DBuf<uint8_t> d_bond_dir0, d_inc_side;
   DBuf<int8_t> d_gauge;
   DBuf<uint32_t> d_sweep;
@@ -161,7 +161,10 @@ struct Engine {
     A.ch = d_ch.p; A.C = C; A.N = N; A.NB = NB;
     A.bond_s0 = d_bond_s0.p; A.bond_s1 = d_bond_s1.p; A.bond_chain = d_bond_chain.p;
     A.bond_dir0 = d_bond_dir0.p; A.inc_off = d_inc_off.p; A.inc = d_inc.p;
-    A.inc_side = d_inc_side.p; A.gauge = d_gauge.p; A.site_chain = d_site_chain.p;
+    A.inc_side = d_inc_side.p; A.inc_nbr = d_inc_nbr.p; A.gauge = d_gauge.p;
+    A.site_chain = d_site_chain.p;
+    A.all_active = 1;
+    for (uint8_t a : h_active) A.all_active &= a ? 1 : 0;
     A.ch_sweep = d_sweep.p; A.ch_slot_off = d_ch_slot_off.p; A.ch_active = d_active.p;
     A.spin0 = d_spin0.p; A.off_base = d_off_base.p; A.off_cnt = d_off_cnt.p;
     A.bond_cnt = d_bond_cnt.p; A.bond_ptr = d_bond_ptr.p; A.site_cnt = d_site_cnt.p;
@@ -223,13 +226,14 @@ struct Engine {
     }
     h_inc.assign(h_inc_off[N], 0);
     h_inc_side.assign(h_inc_off[N], 0);
+    h_inc_nbr.assign(h_inc_off[N], 0);
     std::vector<int> fill(N, 0);
     for (int b = 0; b < NB; ++b) {
       int a = h_bond_s0[b], t = h_bond_s1[b];
       int ia = h_inc_off[a] + fill[a]++;
-      h_inc[ia] = b; h_inc_side[ia] = 0;
+      h_inc[ia] = b; h_inc_side[ia] = 0; h_inc_nbr[ia] = t;
       int it = h_inc_off[t] + fill[t]++;
-      h_inc[it] = b; h_inc_side[it] = 1;
+      h_inc[it] = b; h_inc_side[it] = 1; h_inc_nbr[it] = a;
     }
     // bonds were visited in ascending order, so each site's list is ascending already
     for (int b = 0; b < NB; ++b) {
@@ -241,6 +245,7 @@ struct Engine {
     if ((rc = d_ch.alloc(C)) || (rc = d_bond_s0.alloc(NB)) || (rc = d_bond_s1.alloc(NB)) ||
         (rc = d_bond_chain.alloc(NB)) || (rc = d_bond_dir0.alloc(NB)) ||
         (rc = d_inc_off.alloc(N + 1)) || (rc = d_inc.alloc(h_inc.size())) ||
+        (rc = d_inc_nbr.alloc(h_inc.size())) ||
         (rc = d_inc_side.alloc(h_inc.size())) || (rc = d_gauge.alloc(N)) ||
         (rc = d_site_chain.alloc(N)) || (rc = d_sweep.alloc(C)) || (rc = d_active.alloc(C)) ||
         (rc = d_ch_slot_off.alloc(C + 1)) || (rc = d_spin0.alloc(N)) ||
@@ -259,6 +264,7 @@ struct Engine {
     LG_CUDA(cudaMemcpy(d_inc_off.p, h_inc_off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice));
     LG_CUDA(cudaMemcpy(d_inc.p, h_inc.data(), h_inc.size() * sizeof(int), cudaMemcpyHostToDevice));
     LG_CUDA(cudaMemcpy(d_inc_side.p, h_inc_side.data(), h_inc_side.size(), cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_inc_nbr.p, h_inc_nbr.data(), h_inc_nbr.size() * sizeof(int), cudaMemcpyHostToDevice));
     LG_CUDA(cudaMemcpy(d_gauge.p, h_gauge.data(), N, cudaMemcpyHostToDevice));
     LG_CUDA(cudaMemcpy(d_site_chain.p, h_site_chain.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     h_active.assign(C, 1);
@@ -999,7 +1005,10 @@ struct Engine {
 
   // Retire (or re-enable) a chain: a retired chain inserts no operators and costs almost nothing.
   int set_active(int c, bool on) {
+    const bool was_all = std::all_of(h_active.begin(), h_active.end(), [](uint8_t a) { return a != 0; });
     h_active[c] = on ? 1 : 0;
+    const bool all = std::all_of(h_active.begin(), h_active.end(), [](uint8_t a) { return a != 0; });
+    if (all != was_all) drop_graph();  // the arena's all_active flag is a launch parameter
     LG_CUDA(cudaMemcpyAsync(d_active.p + c, &h_active[c], 1, cudaMemcpyHostToDevice, st));
     LG_CUDA(cudaStreamSynchronize(st));
     return LG_OK;

@@ -55,11 +55,13 @@ struct Arena {
   const int* inc_off;      // N+1
   const int* inc;          // incident bonds of each site, ascending
   const uint8_t* inc_side; // 0: site is the bond's source, 1: target
+  const int* inc_nbr;      // the bond's other site
   const int8_t* gauge;     // N
   const int* site_chain;   // N
   // per-chain mutable
   uint32_t* ch_sweep;      // C
   const uint8_t* ch_active;  // C: 0 = retired chain (inserts nothing; its state is dropped)
+  int all_active;            // no chain retired: ch_active need not be read
   int* ch_slot_off;        // C+1 (this sweep)
   // persistent site state
   uint8_t* spin0;
@@ -281,32 +283,42 @@ __global__ void __launch_bounds__(INS_WARPS * 32, 7) k_insert(Arena A, const int
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; si < nsites; si += warps) {
     const int s = sites ? sites[si] : si;
+    // everything the site's bonds need, loaded up front: lane d < z holds incidence d and, for a
+    // bond s owns, the partner site's list and spin
     const int j0 = A.inc_off[s];
     const int z = A.inc_off[s + 1] - j0;
-    if (!A.ch_active[A.site_chain[s]]) {
-      if (lane == 0)
-        for (int d = 0; d < z; ++d)
-          if (A.inc_side[j0 + d] == 0) { A.bond_cnt[A.inc[j0 + d]] = 0; A.bond_ptr[A.inc[j0 + d]] = 0; }
-      continue;
-    }
+    const int c = A.site_chain[s];
+    const int reg = A.site_region[s];
     const int ns_off = A.off_cnt[s];
     const int sb = A.off_base[s];
+    const uint32_t ps0 = A.spin0[s];
+    int my_b = 0, my_t = 0, my_side = 1, my_nt = 0, my_tb = 0;
+    uint32_t my_pt = 0;
+    if (lane < z) {
+      my_b = A.inc[j0 + lane];
+      my_side = A.inc_side[j0 + lane];
+      my_t = A.inc_nbr[j0 + lane];
+      if (my_side == 0) { my_nt = A.off_cnt[my_t]; my_tb = A.off_base[my_t]; my_pt = A.spin0[my_t]; }
+    }
+    if (!A.all_active && !A.ch_active[c]) {
+      if (lane < z && my_side == 0) { A.bond_cnt[my_b] = 0; A.bond_ptr[my_b] = 0; }
+      continue;
+    }
     const bool s_fits = ns_off <= INS_CAP;
     if (s_fits) {
       for (int i = lane; i < ns_off; i += 32) { offS[w][i] = A.stime[sb + i]; dirS[w][i] = A.sdir[sb + i]; }
     }
-    const uint32_t ps0 = A.spin0[s];
     for (int d = 0; d < z; ++d) {
-      if (A.inc_side[j0 + d] != 0) continue;  // bonds owned by s: s is the source
-      const int b = A.inc[j0 + d];
-      const int t = A.bond_s1[b];
-      const int nt_off = A.off_cnt[t];
+      if (__shfl_sync(0xFFFFFFFFu, my_side, d) != 0) continue;  // bonds owned by s: s is the source
+      const int b = __shfl_sync(0xFFFFFFFFu, my_b, d);
+      const int nt_off = __shfl_sync(0xFFFFFFFFu, my_nt, d);
+      const int tb_ = __shfl_sync(0xFFFFFFFFu, my_tb, d);
+      const uint32_t pt0 = __shfl_sync(0xFFFFFFFFu, my_pt, d);
       if (!s_fits || nt_off > INS_CAP) {
         if (lane == 0) insert_bond_alone(A, b);
         __syncwarp();
         continue;
       }
-      const int tb_ = A.off_base[t];
       __syncwarp();
       for (int i = lane; i < nt_off; i += 32) offT[w][i] = A.stime[tb_ + i];
       // own off-diagonal operators of bond b, in time order
@@ -319,11 +331,9 @@ __global__ void __launch_bounds__(INS_WARPS * 32, 7) k_insert(Arena A, const int
         nown += __popc(ball);
       }
       __syncwarp();
-      const int c = A.bond_chain[b];
       const DChain ch = A.ch[c];
       const uint32_t sweep = A.ch_sweep[c];
       const uint32_t bl = (uint32_t)(b - ch.bond_off);
-      const uint32_t pt0 = A.spin0[t];
       // diagonal proposals, 32 at a time
       int nacc = 0;
       bool more = ch.inv_rate > 0.0f;
@@ -374,7 +384,7 @@ __global__ void __launch_bounds__(INS_WARPS * 32, 7) k_insert(Arena A, const int
       }
       const int n = nacc + nown;
       int out0 = 0;
-      if (lane == 0) out0 = claim_vertices(A, b, n, A.site_region[s]);
+      if (lane == 0) out0 = claim_vertices(A, b, n, reg);
       out0 = __shfl_sync(0xFFFFFFFFu, out0, 0);
       if (out0 >= 0 && nacc > INS_ACC) {
         // more accepted proposals than the staging holds: the one-thread form writes the list
@@ -418,7 +428,8 @@ __global__ void __launch_bounds__(256) k_insert_narrow(Arena A, const int* bonds
     int n = 0;
     uint64_t lt[INS_LOCAL];
     uint8_t lc[INS_LOCAL];
-    if (ok && A.ch_active[A.bond_chain[b]]) n = insert_bond_serial<false, INS_LOCAL>(A, b, 0, lt, lc);
+    if (ok && (A.all_active || A.ch_active[A.bond_chain[b]]))
+      n = insert_bond_serial<false, INS_LOCAL>(A, b, 0, lt, lc);
     // the bonds of a warp are consecutive, so their regions form runs of lanes: a segmented
     // prefix sum over each run, and one claim per run by its last lane
     const int r = ok ? A.site_region[A.bond_s0[b]] : 0x7FFFFFFF;
