@@ -1040,13 +1040,18 @@ template <int TILE = ACC_TILE>
 __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
   if (A.ctl->err) return;
   __shared__ int hkey[ACC_HASH];
-  __shared__ unsigned long long hval[ACC_HASH * 4];
+  // class sums of the hash entries as two 32-bit words: 32-bit shared-memory atomics are
+  // single instructions, 64-bit ones are not.  hhi counts every wrap of hlo once, whatever the
+  // order of the additions, so hhi * 2^32 + hlo is the exact sum (below 2^50 per tile).
+  __shared__ unsigned hlo[ACC_HASH * 4];
+  __shared__ unsigned hhi[ACC_HASH * 4];
   const int ns = A.ctl->ns_total;
   const int ntiles = (ns + TILE - 1) / TILE;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     for (int i = threadIdx.x; i < ACC_HASH; i += blockDim.x) {
       hkey[i] = -1;
-      hval[4 * i] = hval[4 * i + 1] = hval[4 * i + 2] = hval[4 * i + 3] = 0ull;
+      hlo[4 * i] = hlo[4 * i + 1] = hlo[4 * i + 2] = hlo[4 * i + 3] = 0u;
+      hhi[4 * i] = hhi[4 * i + 1] = hhi[4 * i + 2] = hhi[4 * i + 3] = 0u;
     }
     __syncthreads();
     const int t0 = tile * TILE;
@@ -1085,7 +1090,14 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
           // a slot's key never changes once set: read it first, CAS only an empty one
           int k = hkey[h];
           if (k == -1) k = atomicCAS(hkey + h, -1, r);
-          if (k == -1 || k == r) { atomicAdd(hval + 4 * h + q, len); done = true; break; }
+          if (k == -1 || k == r) {
+            const unsigned lo = (unsigned)len, hi = (unsigned)(len >> 32);
+            const unsigned old = atomicAdd(hlo + 4 * h + q, lo);
+            const unsigned carry = (old + lo < old) ? 1u : 0u;
+            if (hi + carry) atomicAdd(hhi + 4 * h + q, hi + carry);
+            done = true;
+            break;
+          }
           h = (h + 1) & (ACC_HASH - 1);
         }
         if (!done) atomicAdd(A.cls + 4 * (size_t)r + q, len);
@@ -1097,7 +1109,7 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
       if (k >= 0) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          const unsigned long long v = hval[4 * i + q];
+          const unsigned long long v = ((unsigned long long)hhi[4 * i + q] << 32) | hlo[4 * i + q];
           if (v) atomicAdd(A.cls + 4 * (size_t)k + q, v);
         }
       }
