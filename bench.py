@@ -211,7 +211,7 @@ def run_batched(lg, steps, therm, plain_sample=16):
     b = lg.Batch(ps)
     b.run(therm // 2)
     # launch shapes chosen by the autotuner on the arena's own (thermalization) sweeps
-    shape, report = b.autotune(2, FLUSH_BYTES)
+    shape, report = b.autotune(4, FLUSH_BYTES)
     b.run(therm - therm // 2)
     b.time_sweeps(3, FLUSH_BYTES)
     ms = b.time_sweeps(steps, FLUSH_BYTES)
@@ -318,7 +318,7 @@ def run_ours(args, dist, ws, rank, local):
     w.run(PRE_THERM // 2)
     if args.shape == "auto":
         # launch shape chosen by the autotuner on the chain's own pre-thermalization sweeps
-        shape, _ = w.autotune(2, FLUSH_BYTES)
+        shape, _ = w.autotune(8, FLUSH_BYTES)
     else:
         w.shape = json.loads(args.shape)  # a fixed shape (e.g. to profile the tuned one)
         shape = w.shape
