@@ -91,6 +91,7 @@ struct Shape {
 struct Engine {
   std::vector<ChainSpec> spec;
   std::vector<ChainAcc> acc;
+  std::vector<int> acc_of_chain;   // the accumulator chain c's measurements go to (exchange MC)
   int C = 0, N = 0, NB = 0;
   std::vector<DChain> hch;
   std::vector<int> h_bond_s0, h_bond_s1, h_inc_off, h_inc, h_inc_nbr;
@@ -183,6 +184,8 @@ struct Engine {
     spec = specs;
     C = (int)spec.size();
     acc.assign(C, ChainAcc());
+    acc_of_chain.resize(C);
+    for (int c = 0; c < C; ++c) acc_of_chain[c] = c;
     int dev = 0;
     LG_CUDA(cudaGetDevice(&dev));
     cudaDeviceProp prop;
@@ -811,7 +814,7 @@ struct Engine {
         if (keep_records && c == 0) kept.insert(kept.end(), rec, rec + REC_WORDS);
         s.last_nop = rec[R_NOP];
         if (s.mcs >= (uint64_t)s.therm && s.mcs < (uint64_t)(s.therm + s.sweeps))
-          acc[c].push(s, rec);
+          acc[acc_of_chain[c]].push(s, rec);
         ++s.mcs;
       }
     }
@@ -1053,6 +1056,23 @@ struct Engine {
         old.d_off_base.p, old.d_stime.p, old.d_sdir.p, dbase.p);
     g_launches += 2;
     LG_CUDA(cudaGetLastError());
+    LG_CUDA(cudaStreamSynchronize(st));
+    return LG_OK;
+  }
+
+  // Exchange of temperatures between chains c1 and c2 (same model): their inverse temperatures
+  // and the device parameters that depend on them trade places.  The launch shape, the graph and
+  // the accumulators stay (the caller re-points acc_of_chain); a region that then overflows
+  // grows on the next sweep as usual.
+  int swap_beta(int c1, int c2) {
+    const double b1 = spec[c1].beta, b2 = spec[c2].beta;
+    int rc;
+    if ((rc = spec[c1].set_beta(b2)) || (rc = spec[c2].set_beta(b1))) return rc;
+    for (int c : {c1, c2}) {
+      hch[c].inv_rate = spec[c].dchain.inv_rate;
+      hch[c].flip_coef = spec[c].dchain.flip_coef;
+      LG_CUDA(cudaMemcpyAsync(d_ch.p + c, &hch[c], sizeof(DChain), cudaMemcpyHostToDevice, st));
+    }
     LG_CUDA(cudaStreamSynchronize(st));
     return LG_OK;
   }
@@ -1363,3 +1383,6 @@ const char* lg_kernel_name(int k) { return (k >= 0 && k < kNumStages) ? kStageNa
 
 // Request server with continuous batching over one arena.
 #include "lg_server.cu"
+
+// Exchange Monte Carlo over a ladder of temperatures in one arena.
+#include "lg_exchange.cu"

@@ -131,6 +131,13 @@ def lib():
             "lg_set_shape": (ctypes.c_int, [vp, vp]),
             "lg_num_kernels": (ctypes.c_int, []),
             "lg_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
+            "lg_exchange_chain_seed": (u64, [u64, ctypes.c_int]),
+            "lg_exchange_create": (ctypes.c_int, [vp, ctypes.c_int, vp, vp]),
+            "lg_exchange_destroy": (ctypes.c_int, [vp]),
+            "lg_exchange_run": (ctypes.c_int, [vp, i64, ctypes.c_int]),
+            "lg_exchange_observables": (ctypes.c_int, [vp, ctypes.c_int, vp]),
+            "lg_exchange_state": (ctypes.c_int, [vp, vp, vp, vp]),
+            "lg_exchange_chain": (vp, [vp, ctypes.c_int]),
             "lg_server_config_default": (None, [vp]),
             "lg_request_bytes": (ctypes.c_double, [vp]),
             "lg_server_create": (ctypes.c_int, [vp, vp]),
@@ -428,6 +435,59 @@ class Batch:
         if not h:
             raise IndexError(i)
         return LoopWorker(self.params[i], _handle=h, _owner=self)
+
+
+class Exchange:
+    """Exchange Monte Carlo (parallel tempering) over a ladder of inverse temperatures."""
+
+    def __init__(self, params: Params, betas):
+        self.params = params
+        self.betas = [float(b) for b in betas]
+        arr = (ctypes.c_double * len(self.betas))(*self.betas)
+        h = ctypes.c_void_p()
+        check(lib().lg_exchange_create(ctypes.byref(params), len(self.betas), arr, ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().lg_exchange_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, nsweeps: int, interval: int = 1):
+        check(lib().lg_exchange_run(self._h, int(nsweeps), int(interval)))
+
+    def observables(self, t):
+        o = Obs()
+        check(lib().lg_exchange_observables(self._h, int(t), ctypes.byref(o)))
+        return _obs_dict(o)
+
+    def state(self):
+        """(chain_of_temp, attempts, accepts) as numpy arrays."""
+        n = len(self.betas)
+        cot = np.zeros(n, dtype=np.int32)
+        att = np.zeros(max(n - 1, 1), dtype=np.uint64)
+        acc = np.zeros(max(n - 1, 1), dtype=np.uint64)
+        check(lib().lg_exchange_state(self._h, _p(cot), _p(att), _p(acc)))
+        return cot, att[:n - 1], acc[:n - 1]
+
+    def chain(self, c) -> "LoopWorker":
+        h = lib().lg_exchange_chain(self._h, int(c))
+        if not h:
+            raise IndexError(c)
+        p = Params.from_buffer_copy(self.params)
+        p.seed = chain_seed(self.params.seed, c)
+        return LoopWorker(p, _handle=h, _owner=self)
+
+
+def chain_seed(seed: int, i: int) -> int:
+    """SEED of chain i of an exchange ladder created with SEED = seed."""
+    return int(lib().lg_exchange_chain_seed(int(seed), int(i)))
 
 
 def request_bytes(params: Params) -> float:

@@ -231,6 +231,29 @@ int lg_batch_set_shape(lg_batch* b, const lg_shape* in);
 int lg_get_shape(const lg_chain* c, lg_shape* out);
 int lg_set_shape(lg_chain* c, const lg_shape* in);
 
+/* ---- exchange Monte Carlo (parallel tempering) over a temperature ladder ------------------
+ * Replaces ALPS parapack's exchange worker around loop_worker (path_integral.C:874-875), with
+ * the worker's hooks weight_parameter() = operator count n and log_weight(n, beta) = n log beta
+ * (path_integral.C:98-109).  Temperature t of the ladder betas[0..n) runs as one chain of a
+ * single arena (SEED of chain i: lg_exchange_chain_seed(SEED, i)).  Every `interval` sweeps the
+ * neighbouring temperatures (t, t+1), t even and t odd in alternate steps, try to swap with
+ * probability min(1, exp((n_i - n_j)(log beta_{t+1} - log beta_t))); a swap exchanges the two
+ * chains' inverse temperatures.  Observables are accumulated per temperature. */
+typedef struct lg_exchange lg_exchange;
+uint64_t lg_exchange_chain_seed(uint64_t seed, int i);
+int lg_exchange_create(const lg_params* p, int nbeta, const double* betas, lg_exchange** out);
+int lg_exchange_destroy(lg_exchange* x);
+/* nsweeps sweeps of every temperature, with an exchange step every `interval` sweeps (counted
+ * across calls). */
+int lg_exchange_run(lg_exchange* x, int64_t nsweeps, int interval);
+/* Observables at temperature index t (the sweeps measured there, whichever chain held it). */
+int lg_exchange_observables(lg_exchange* x, int t, lg_obs* out);
+/* chain_of_temp[nbeta]; attempts / accepts[nbeta - 1] per neighbouring pair (any may be NULL). */
+int lg_exchange_state(const lg_exchange* x, int32_t* chain_of_temp, uint64_t* attempts,
+                      uint64_t* accepts);
+/* Chain c of the ladder through the single-chain test seams (its state, records). */
+lg_chain* lg_exchange_chain(lg_exchange* x, int c);
+
 /* ---- request server: continuous batching over one device arena ---------------------------
  * Serving form of the worker (no counterpart in the reference, whose scheduler runs one
  * worker per clone; see path_integral.C:872-876 for the worker it batches).  Requests (lg_params)
