@@ -95,12 +95,12 @@ struct Engine {
   int C = 0, N = 0, NB = 0;
   std::vector<DChain> hch;
   std::vector<int> h_bond_s0, h_bond_s1, h_inc_off, h_inc, h_inc_nbr;
-  std::vector<uint8_t> h_inc_side, h_bond_dir0;
+  std::vector<uint8_t> h_inc_side, h_bond_dir0, h_inc_dir;
   std::vector<int> h_site_chain, h_bond_chain;
 
   DBuf<DChain> d_ch;
   DBuf<int> d_bond_s0, d_bond_s1, d_bond_chain, d_inc_off, d_inc, d_inc_nbr, d_site_chain;
-  DBuf<uint8_t> d_bond_dir0, d_inc_side;
+  DBuf<uint8_t> d_bond_dir0, d_inc_side, d_inc_dir;
   DBuf<int8_t> d_gauge;
   DBuf<uint32_t> d_sweep;
   DBuf<uint8_t> d_active;
@@ -116,7 +116,7 @@ struct Engine {
   DBuf<uint8_t> d_sinfo, d_sdir, d_flip;
   DBuf<int> d_svert, d_parent;
   DBuf<unsigned long long> d_cls;
-  DBuf<unsigned int> d_cnt0;
+  DBuf<RootKW> d_rkw;
   DBuf<unsigned long long> d_rec;
   DBuf<Ctl> d_ctl;
 
@@ -174,7 +174,7 @@ struct Engine {
     A.region_fill = d_region_fill.p;
     A.vtime = d_vtime.p; A.vcode = d_vcode.p; A.vnew = d_vnew.p; A.vslot = d_vslot.p;
     A.stime = d_stime.p; A.sinfo = d_sinfo.p; A.svert = d_svert.p; A.sdir = d_sdir.p;
-    A.parent = d_parent.p; A.flip = d_flip.p; A.cls = d_cls.p; A.cnt0 = d_cnt0.p;
+    A.parent = d_parent.p; A.flip = d_flip.p; A.cls = d_cls.p; A.rkw = d_rkw.p; A.inc_dir = d_inc_dir.p;
     A.rec = d_rec.p; A.ctl = d_ctl.p; A.rec_rows = rec_rows;
     return A;
   }
@@ -230,13 +230,16 @@ struct Engine {
     h_inc.assign(h_inc_off[N], 0);
     h_inc_side.assign(h_inc_off[N], 0);
     h_inc_nbr.assign(h_inc_off[N], 0);
+    h_inc_dir.assign(h_inc_off[N], 0);
     std::vector<int> fill(N, 0);
     for (int b = 0; b < NB; ++b) {
       int a = h_bond_s0[b], t = h_bond_s1[b];
+      const int c = h_bond_chain[b];
+      const uint8_t dir = (uint8_t)((b - hch[c].bond_off) % spec[c].dim);  // bond = site*dim + d
       int ia = h_inc_off[a] + fill[a]++;
-      h_inc[ia] = b; h_inc_side[ia] = 0; h_inc_nbr[ia] = t;
+      h_inc[ia] = b; h_inc_side[ia] = 0; h_inc_nbr[ia] = t; h_inc_dir[ia] = dir;
       int it = h_inc_off[t] + fill[t]++;
-      h_inc[it] = b; h_inc_side[it] = 1; h_inc_nbr[it] = a;
+      h_inc[it] = b; h_inc_side[it] = 1; h_inc_nbr[it] = a; h_inc_dir[it] = dir;
     }
     // bonds were visited in ascending order, so each site's list is ascending already
     for (int b = 0; b < NB; ++b) {
@@ -248,7 +251,7 @@ struct Engine {
     if ((rc = d_ch.alloc(C)) || (rc = d_bond_s0.alloc(NB)) || (rc = d_bond_s1.alloc(NB)) ||
         (rc = d_bond_chain.alloc(NB)) || (rc = d_bond_dir0.alloc(NB)) ||
         (rc = d_inc_off.alloc(N + 1)) || (rc = d_inc.alloc(h_inc.size())) ||
-        (rc = d_inc_nbr.alloc(h_inc.size())) ||
+        (rc = d_inc_nbr.alloc(h_inc.size())) || (rc = d_inc_dir.alloc(h_inc.size())) ||
         (rc = d_inc_side.alloc(h_inc.size())) || (rc = d_gauge.alloc(N)) ||
         (rc = d_site_chain.alloc(N)) || (rc = d_sweep.alloc(C)) || (rc = d_active.alloc(C)) ||
         (rc = d_ch_slot_off.alloc(C + 1)) || (rc = d_spin0.alloc(N)) ||
@@ -268,6 +271,7 @@ struct Engine {
     LG_CUDA(cudaMemcpy(d_inc.p, h_inc.data(), h_inc.size() * sizeof(int), cudaMemcpyHostToDevice));
     LG_CUDA(cudaMemcpy(d_inc_side.p, h_inc_side.data(), h_inc_side.size(), cudaMemcpyHostToDevice));
     LG_CUDA(cudaMemcpy(d_inc_nbr.p, h_inc_nbr.data(), h_inc_nbr.size() * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(cudaMemcpy(d_inc_dir.p, h_inc_dir.data(), h_inc_dir.size(), cudaMemcpyHostToDevice));
     LG_CUDA(cudaMemcpy(d_gauge.p, h_gauge.data(), N, cudaMemcpyHostToDevice));
     LG_CUDA(cudaMemcpy(d_site_chain.p, h_site_chain.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     h_active.assign(C, 1);
@@ -390,12 +394,12 @@ struct Engine {
         (rc = d_vslot.alloc(2 * (size_t)new_nv)) || (rc = d_stime.alloc(new_ns)) ||
         (rc = d_sinfo.alloc(new_ns)) || (rc = d_svert.alloc(new_ns)) || (rc = d_sdir.alloc(new_ns)) ||
         (rc = d_parent.alloc(new_ns)) || (rc = d_flip.alloc(new_ns)) ||
-        (rc = d_cls.alloc(4 * (size_t)new_ns)) || (rc = d_cnt0.alloc(4 * (size_t)new_ns)) ||
+        (rc = d_cls.alloc(4 * (size_t)new_ns)) || (rc = d_rkw.alloc((size_t)new_ns)) ||
         (rc = d_rec.alloc((size_t)rec_rows * C * REC_WORDS)))
       return rc;
     // cluster class sums must start at zero (k_cluster clears what it consumes)
     LG_CUDA(cudaMemset(d_cls.p, 0, 4 * (size_t)new_ns * sizeof(unsigned long long)));
-    LG_CUDA(cudaMemset(d_cnt0.p, 0, 4 * (size_t)new_ns * sizeof(unsigned int)));
+    LG_CUDA(cudaMemset(d_rkw.p, 0, (size_t)new_ns * sizeof(RootKW)));
     if (keep) {
       LG_CUDA(cudaMemcpy(d_stime.p, old_t.p, keep_n * sizeof(uint64_t), cudaMemcpyDeviceToDevice));
       LG_CUDA(cudaMemcpy(d_sdir.p, old_d.p, keep_n, cudaMemcpyDeviceToDevice));

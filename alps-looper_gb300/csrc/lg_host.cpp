@@ -237,6 +237,16 @@ void record_values(const ChainSpec& s, const uint64_t* r, double* v) {
   v[RAW_E2] = ene * ene - nop / (beta * beta);                     // energy.h:83
   v[RAW_NC] = (double)r[R_NC];
   v[RAW_NOP] = nop;
+  // Stiffness (stiffness.h:116-160): sum over directions of (winding/2)^2 / (beta dim); the
+  // improved estimator sums the clusters' squared windings, the normal one squares the total
+  const double dim = (double)s.dim;
+  if (s.improved) {
+    v[RAW_STIFF] = (double)r[R_WSQ] / 4 / (beta * dim);
+  } else {
+    double w2 = 0;
+    for (int d = 0; d < 3; ++d) w2 += i64(r[R_W0 + d]) * i64(r[R_W0 + d]) / 4;
+    v[RAW_STIFF] = w2 / (beta * dim);
+  }
   const double t80 = std::ldexp(1.0, -80), t40 = std::ldexp(1.0, -40);
   if (s.improved) {                                                // susceptibility.h:200-254
     const double m2 = (double)r[R_M0SQ] / 4, m4 = u128d(r, R_M0Q) / 16;
@@ -360,6 +370,7 @@ void ChainAcc::report(const ChainSpec& s, lg_obs* out) const {
   put(LG_OBS_GEN_SUSCEPTIBILITY, raw[RAW_GCHI], 1.0);
   put(LG_OBS_NUM_CLUSTERS, raw[RAW_NC], 1.0);
   put(LG_OBS_NUM_OPERATORS, raw[RAW_NOP], 1.0);
+  put(LG_OBS_STIFFNESS, raw[RAW_STIFF], 1.0);
   // evaluators: energy.h:89-101, susceptibility.h:340-374
   double m, e;
   jackknife2(raw[RAW_E], raw[RAW_E2], [&](double a, double b) { return beta * beta * (b - a * a) / V; }, &m, &e);
@@ -380,7 +391,7 @@ extern "C" const char* lg_obs_name(int i) {
       "Staggered Magnetization^2", "Staggered Magnetization^4", "Staggered Susceptibility",
       "Generalized Magnetization^2", "Generalized Susceptibility", "Number of Clusters",
       "Number of Operators", "Binder Ratio of Magnetization",
-      "Binder Ratio of Staggered Magnetization"};
+      "Binder Ratio of Staggered Magnetization", "Stiffness"};
   return (i >= 0 && i < LG_NUM_OBS) ? names[i] : "";
 }
 

@@ -43,7 +43,7 @@ struct BinAcc {
 
 enum {
   RAW_E = 0, RAW_E2, RAW_M, RAW_ABSM, RAW_M2, RAW_M4, RAW_CHI, RAW_SM2, RAW_SM4, RAW_SCHI,
-  RAW_GM2, RAW_GCHI, RAW_NC, RAW_NOP, NUM_RAW
+  RAW_GM2, RAW_GCHI, RAW_NC, RAW_NOP, RAW_STIFF, NUM_RAW
 };
 
 struct ChainAcc {

@@ -44,6 +44,16 @@ namespace lg {
 enum : uint8_t { SI_SPIN = 1, SI_GNEG = 2, SI_FIRST = 4, SI_LAST = 8, SI_SRC = 16, SI_OFF = 128 };
 constexpr int SI_GSHIFT = 5;
 
+// What k_accumulate gathers for a cluster besides its class lengths, stored at its root's
+// segment index (32 bytes, read by k_cluster with the lengths as two requests): the tau = 0
+// count of each (spin, gauge sign) class and the winding per lattice direction.  The lengths
+// stay in their own array: the counts of a giant cluster's bottom segments and the tiles'
+// length flushes then contend on different lines.
+struct RootKW {
+  unsigned K[4];
+  int W[4];
+};
+
 struct Arena {
   // static
   const DChain* ch;
@@ -56,6 +66,7 @@ struct Arena {
   const int* inc;          // incident bonds of each site, ascending
   const uint8_t* inc_side; // 0: site is the bond's source, 1: target
   const int* inc_nbr;      // the bond's other site
+  const uint8_t* inc_dir;  // the bond's lattice direction (nullptr: 0)
   const int8_t* gauge;     // N
   const int* site_chain;   // N
   // per-chain mutable
@@ -89,8 +100,8 @@ struct Arena {
   uint8_t* sdir;
   int* parent;
   uint8_t* flip;
-  unsigned long long* cls;  // 4 per segment
-  unsigned int* cnt0;       // 4 per segment
+  unsigned long long* cls;  // 4 per segment (used at roots): time-integrated class lengths
+  RootKW* rkw;              // per segment (used at roots): tau = 0 class counts, winding
   unsigned long long* rec;  // [rows][C][REC_WORDS]
   Ctl* ctl;
   int rec_rows;             // rows of rec
@@ -729,7 +740,7 @@ __device__ void merge_site_serial(Arena& A, int s) {
     A.sinfo[x] = (uint8_t)(spin | gneg | (j == k ? SI_LAST : 0) | (sd == 0 ? SI_SRC : 0) |
                            ((code >> 1) << SI_GSHIFT) | ((code & 1u) ? SI_OFF : 0));
     A.svert[x] = v;
-    A.sdir[x] = (uint8_t)best;
+    A.sdir[x] = (uint8_t)(best | (A.inc_dir ? A.inc_dir[j0 + best] << 3 : 0));
     A.parent[x] = x;
     A.vslot[2 * v + sd] = x;
   }
@@ -894,7 +905,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
         A.sinfo[x] = (uint8_t)(spin | gneg | (r == k - 1 ? SI_LAST : 0) | (side == 0 ? SI_SRC : 0) |
                                ((cd >> 1) << SI_GSHIFT) | ((cd & 1u) ? SI_OFF : 0));
         A.svert[x] = v;
-        A.sdir[x] = (uint8_t)d;
+        A.sdir[x] = (uint8_t)(d | (A.inc_dir ? A.inc_dir[j0 + d] << 3 : 0));
         A.parent[x] = (r == k - 1) ? base : x;  // closure: top segment joins the bottom one
         A.vslot[2 * v + side] = x;
       }
@@ -1015,9 +1026,10 @@ __global__ void __launch_bounds__(256) k_compress(Arena A) {
     int p = A.parent[r];
     while (p != r) { r = p; p = A.parent[r]; }
     A.parent[x] = r;
-    if (r == x) {
+    if (r == x && A.rkw) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) { A.cls[4 * (size_t)x + q] = 0ull; A.cnt0[4 * (size_t)x + q] = 0u; }
+      for (int q = 0; q < 4; ++q) A.cls[4 * (size_t)x + q] = 0ull;
+      A.rkw[x] = RootKW{};
     }
   }
 }
@@ -1045,6 +1057,10 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
   // order of the additions, so hhi * 2^32 + hlo is the exact sum (below 2^50 per tile).
   __shared__ unsigned hlo[ACC_HASH * 4];
   __shared__ unsigned hhi[ACC_HASH * 4];
+  // winding sums of the hash entries: w0 + 65536 w1 in hwa, w2 in hwb (a tile's sums stay
+  // within +-2 TILE, so both fields of hwa decode exactly)
+  __shared__ int hwa[ACC_HASH];
+  __shared__ int hwb[ACC_HASH];
   const int ns = A.ctl->ns_total;
   const int ntiles = (ns + TILE - 1) / TILE;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -1052,12 +1068,13 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
       hkey[i] = -1;
       hlo[4 * i] = hlo[4 * i + 1] = hlo[4 * i + 2] = hlo[4 * i + 3] = 0u;
       hhi[4 * i] = hhi[4 * i + 1] = hhi[4 * i + 2] = hhi[4 * i + 3] = 0u;
+      hwa[i] = hwb[i] = 0;
     }
     __syncthreads();
     const int t0 = tile * TILE;
     constexpr int PER = TILE / 256;  // segments per thread (blockDim.x == 256)
     int xs[PER], par[PER];
-    uint8_t info[PER];
+    uint8_t info[PER], info1[PER], dir[PER], dir1[PER];
     uint64_t ta[PER], tb[PER];
     // issue every load of this thread's segments first, then walk and add
 #pragma unroll
@@ -1067,8 +1084,12 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
       if (x < ns) {
         par[j] = A.parent[x];
         info[j] = A.sinfo[x];
+        dir[j] = A.sdir[x];
         ta[j] = A.stime[x];
-        tb[j] = (info[j] & SI_LAST) ? 0ull : A.stime[x + 1];
+        const bool last = info[j] & SI_LAST;
+        tb[j] = last ? 0ull : A.stime[x + 1];
+        info1[j] = last ? 0 : A.sinfo[x + 1];
+        dir1[j] = last ? 0 : A.sdir[x + 1];
       }
     }
 #pragma unroll
@@ -1082,8 +1103,17 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
       const int64_t hi = (info[j] & SI_LAST) ? ((int64_t)1 << 40) : bits_fix40(tb[j]);
       const unsigned long long len = (unsigned long long)(hi - lo);
       const int q = (info[j] & SI_SPIN) * 2 + ((info[j] & SI_GNEG) ? 1 : 0);
-      if (info[j] & SI_FIRST) atomicAdd(A.cnt0 + 4 * (size_t)r + q, 1u);
-      if (len) {
+      if (info[j] & SI_FIRST) atomicAdd(&A.rkw[r].K[q], 1u);
+      // winding (stiffness.h:82-130 through improved_accumulator::begin_b / end_b): at the
+      // source-side leg of a non-frozen bond vertex, the segment starting there loses (1-2c) e_d
+      // and the segment ending there gains (1-2c) e_d, c being the segment's spin and d the
+      // bond's direction (carried in sdir bits 3-4)
+      int w[3] = {0, 0, 0};
+      const int sg = (info[j] & SI_SPIN) ? -1 : 1;
+      if ((info[j] & SI_SRC) && !((info[j] >> SI_GSHIFT) & 2)) w[dir[j] >> 3] -= sg;
+      if ((info1[j] & SI_SRC) && !((info1[j] >> SI_GSHIFT) & 2)) w[dir1[j] >> 3] += sg;
+      const bool wnz = (w[0] | w[1] | w[2]) != 0;
+      if (len || wnz) {
         unsigned h = ((unsigned)r * 2654435761u) >> 22;  // 10-bit hash
         bool done = false;
         for (int probe = 0; probe < 32; ++probe) {
@@ -1091,16 +1121,25 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
           int k = hkey[h];
           if (k == -1) k = atomicCAS(hkey + h, -1, r);
           if (k == -1 || k == r) {
-            const unsigned lo = (unsigned)len, hi = (unsigned)(len >> 32);
-            const unsigned old = atomicAdd(hlo + 4 * h + q, lo);
-            const unsigned carry = (old + lo < old) ? 1u : 0u;
-            if (hi + carry) atomicAdd(hhi + 4 * h + q, hi + carry);
+            if (len) {
+              const unsigned lo = (unsigned)len, hi = (unsigned)(len >> 32);
+              const unsigned old = atomicAdd(hlo + 4 * h + q, lo);
+              const unsigned carry = (old + lo < old) ? 1u : 0u;
+              if (hi + carry) atomicAdd(hhi + 4 * h + q, hi + carry);
+            }
+            if (w[0] | w[1]) atomicAdd(hwa + h, w[0] + 65536 * w[1]);
+            if (w[2]) atomicAdd(hwb + h, w[2]);
             done = true;
             break;
           }
           h = (h + 1) & (ACC_HASH - 1);
         }
-        if (!done) atomicAdd(A.cls + 4 * (size_t)r + q, len);
+        if (!done) {
+          if (len) atomicAdd(A.cls + 4 * (size_t)r + q, len);
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            if (w[d]) atomicAdd(&A.rkw[r].W[d], w[d]);
+        }
       }
     }
     __syncthreads();
@@ -1112,6 +1151,12 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
           const unsigned long long v = ((unsigned long long)hhi[4 * i + q] << 32) | hlo[4 * i + q];
           if (v) atomicAdd(A.cls + 4 * (size_t)k + q, v);
         }
+        const int wa = hwa[i];
+        const int w0 = ((wa + 32768) & 0xFFFF) - 32768;
+        const int w1 = (wa - w0) / 65536;
+        if (w0) atomicAdd(&A.rkw[k].W[0], w0);
+        if (w1) atomicAdd(&A.rkw[k].W[1], w1);
+        if (hwb[i]) atomicAdd(&A.rkw[k].W[2], hwb[i]);
       }
     }
     __syncthreads();
@@ -1142,14 +1187,17 @@ __device__ __forceinline__ int chain_of_segment(const Arena& A, int x) {
 }
 
 // The 18 per-sweep sums a cluster root contributes to its chain's record.
+constexpr int NQ = 14;  // u64 sums of a root
 struct RootSums {
-  unsigned long long q[10];  // R_NC, R_M0, R_SM0, R_M0SQ, R_N0SQ, R_SM0SQ, R_SN0SQ, R_FLD, R_MA, R_SMA
+  unsigned long long q[NQ];  // R_NC, R_M0, R_SM0, R_M0SQ, R_N0SQ, R_SM0SQ, R_SN0SQ, R_FLD, R_MA, R_SMA,
+                             // R_WSQ, R_W0, R_W1, R_W2
   u128 w[8];                 // R_M0Q, R_N0Q, R_SM0Q, R_SN0Q, R_LSQ, R_MSQ, R_SLSQ, R_SMSQ
 };
-__device__ __constant__ int kRecQ[10] = {R_NC, R_M0, R_SM0, R_M0SQ, R_N0SQ, R_SM0SQ, R_SN0SQ,
-                                         R_FLD, R_MA, R_SMA};
+__device__ __constant__ int kRecQ[NQ] = {R_NC, R_M0, R_SM0, R_M0SQ, R_N0SQ, R_SM0SQ, R_SN0SQ,
+                                         R_FLD, R_MA, R_SMA, R_WSQ, R_W0, R_W1, R_W2};
 __device__ __constant__ int kRecW[8] = {R_M0Q, R_N0Q, R_SM0Q, R_SN0Q, R_LSQ, R_MSQ, R_SLSQ, R_SMSQ};
-constexpr int NLIMB = 10 * 4 + 8 * 8;  // 16-bit limbs of the sums
+constexpr int QLIMB = NQ * 4;            // 16-bit limbs of the u64 sums
+constexpr int NLIMB = QLIMB + 8 * 8;      // and of the u128 ones
 
 __device__ __forceinline__ void add_u128(u128& a, u128 b) {
   const unsigned long long lo = a.lo + b.lo;
@@ -1157,16 +1205,19 @@ __device__ __forceinline__ void add_u128(u128& a, u128 b) {
   a.lo = lo;
 }
 
-// The eight class integers of a root (four time-integrated length sums, four tau = 0 counts).
-struct RootClass { unsigned long long S[4]; unsigned K[4]; };
+// The class integers of a root: four time-integrated length sums, four tau = 0 counts, and the
+// winding per direction.
+struct RootClass { unsigned long long S[4]; unsigned K[4]; int Wd[3]; };
 
 __device__ __forceinline__ RootClass load_root_class(const Arena& A, int x) {
   RootClass rc;
   const ulonglong2* S = reinterpret_cast<const ulonglong2*>(A.cls + 4 * (size_t)x);
   const ulonglong2 a = S[0], b = S[1];
   rc.S[0] = a.x; rc.S[1] = a.y; rc.S[2] = b.x; rc.S[3] = b.y;
-  const uint4 k = *reinterpret_cast<const uint4*>(A.cnt0 + 4 * (size_t)x);
+  const uint4 k = *reinterpret_cast<const uint4*>(A.rkw[x].K);
   rc.K[0] = k.x; rc.K[1] = k.y; rc.K[2] = k.z; rc.K[3] = k.w;
+  const int4 wd = *reinterpret_cast<const int4*>(A.rkw[x].W);
+  rc.Wd[0] = wd.x; rc.Wd[1] = wd.y; rc.Wd[2] = wd.z;
   return rc;
 }
 
@@ -1178,7 +1229,8 @@ __device__ __forceinline__ void root_sums(const Arena& A, int x, int c, const Ro
   ulonglong2* S = reinterpret_cast<ulonglong2*>(A.cls + 4 * (size_t)x);
   S[0] = make_ulonglong2(0ull, 0ull);
   S[1] = make_ulonglong2(0ull, 0ull);
-  *reinterpret_cast<uint4*>(A.cnt0 + 4 * (size_t)x) = make_uint4(0u, 0u, 0u, 0u);
+  *reinterpret_cast<uint4*>(A.rkw[x].K) = make_uint4(0u, 0u, 0u, 0u);
+  *reinterpret_cast<int4*>(A.rkw[x].W) = make_int4(0, 0, 0, 0);
   const long long s0 = (long long)rcl.S[0], s1 = (long long)rcl.S[1], s2 = (long long)rcl.S[2],
                   s3 = (long long)rcl.S[3];
   const long long k0 = rcl.K[0], k1 = rcl.K[1], k2 = rcl.K[2], k3 = rcl.K[3];
@@ -1215,6 +1267,12 @@ __device__ __forceinline__ void root_sums(const Arena& A, int x, int c, const Ro
   R.q[7] += (unsigned long long)(f ? -Ms : Ms);
   R.q[8] += (unsigned long long)Ms;
   R.q[9] += (unsigned long long)SMs;
+  // winding (stiffness.h collector: sum over clusters of the squared winding per direction)
+  R.q[10] += (unsigned long long)((long long)rcl.Wd[0] * rcl.Wd[0] + (long long)rcl.Wd[1] * rcl.Wd[1] +
+                                  (long long)rcl.Wd[2] * rcl.Wd[2]);
+  R.q[11] += (unsigned long long)(long long)rcl.Wd[0];
+  R.q[12] += (unsigned long long)(long long)rcl.Wd[1];
+  R.q[13] += (unsigned long long)(long long)rcl.Wd[2];
   const unsigned long long L = ab(s0 + s1 + s2 + s3), SL = ab(s0 - s1 + s2 - s3);
   add_u128(R.w[4], mul64(L, L));
   add_u128(R.w[5], mul64(ab(Ms), ab(Ms)));
@@ -1225,7 +1283,7 @@ __device__ __forceinline__ void root_sums(const Arena& A, int x, int c, const Ro
 __device__ __forceinline__ void record_atomics(const Arena& A, int c, const RootSums& R) {
   unsigned long long* row = rec_row(A, c);
 #pragma unroll
-  for (int i = 0; i < 10; ++i) if (R.q[i]) atomicAdd(row + kRecQ[i], R.q[i]);
+  for (int i = 0; i < NQ; ++i) if (R.q[i]) atomicAdd(row + kRecQ[i], R.q[i]);
 #pragma unroll
   for (int i = 0; i < 8; ++i) if (R.w[i].lo | R.w[i].hi) atomic_add_u128(row + kRecW[i], R.w[i]);
 }
@@ -1264,7 +1322,7 @@ __device__ __forceinline__ void record_by_chain(const Arena& A, int c, const Roo
   const bool leader = (threadIdx.x & 31) == __ffs(grp) - 1;
   unsigned long long* row = rec_row(A, c);
 #pragma unroll
-  for (int i = 0; i < 10; ++i) {
+  for (int i = 0; i < NQ; ++i) {
     const unsigned long long v = group_sum_u64(grp, R.q[i]);
     if (leader && v) atomicAdd(row + kRecQ[i], v);
   }
@@ -1325,7 +1383,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
         RootClass nxt = inext < nr ? load_root_class(A, xnext) : RootClass{};
         RootSums R;
 #pragma unroll
-        for (int k = 0; k < 10; ++k) R.q[k] = 0;
+        for (int k = 0; k < NQ; ++k) R.q[k] = 0;
 #pragma unroll
         for (int k = 0; k < 8; ++k) R.w[k] = {0, 0};
         int c = -1;
@@ -1341,7 +1399,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
     } else {
       RootSums acc;
 #pragma unroll
-      for (int k = 0; k < 10; ++k) acc.q[k] = 0;
+      for (int k = 0; k < NQ; ++k) acc.q[k] = 0;
 #pragma unroll
       for (int k = 0; k < 8; ++k) acc.w[k] = {0, 0};
       while (i < nr) {
@@ -1354,7 +1412,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
         cur = nxt;
       }
 #pragma unroll
-      for (int i = 0; i < 10; ++i)
+      for (int i = 0; i < NQ; ++i)
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
           const unsigned v = __reduce_add_sync(0xFFFFFFFFu, (unsigned)((acc.q[i] >> (16 * l)) & 0xFFFFull));
@@ -1366,7 +1424,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
         for (int l = 0; l < 8; ++l) {
           const unsigned long long wv = l < 4 ? acc.w[i].lo : acc.w[i].hi;
           const unsigned v = __reduce_add_sync(0xFFFFFFFFu, (unsigned)((wv >> (16 * (l & 3))) & 0xFFFFull));
-          if (lane == 0) limbs[wid][40 + 8 * i + l] = v;
+          if (lane == 0) limbs[wid][QLIMB + 8 * i + l] = v;
         }
       __syncthreads();
       for (int j = threadIdx.x; j < NLIMB; j += blockDim.x) {
@@ -1375,18 +1433,18 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
         tot[j] = sum;
       }
       __syncthreads();
-      if (threadIdx.x < 18) {
+      if (threadIdx.x < NQ + 8) {
         unsigned long long* row = rec_row(A, cf);
         const int i = threadIdx.x;
-        if (i < 10) {
+        if (i < NQ) {
           unsigned long long v = 0;
           for (int l = 0; l < 4; ++l) v += tot[4 * i + l] << (16 * l);
           if (v) atomicAdd(row + kRecQ[i], v);
         } else {
-          const int k = i - 10;
+          const int k = i - NQ;
           u128 v = {0, 0};
           for (int l = 0; l < 8; ++l) {
-            const unsigned long long t = tot[40 + 8 * k + l];
+            const unsigned long long t = tot[QLIMB + 8 * k + l];
             const int sh = 16 * l;
             u128 add;
             add.lo = sh < 64 ? (t << sh) : 0ull;
@@ -1465,7 +1523,7 @@ __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int
       if (j <= k) {
         const int x = base + j;
         keep = A.vnew[A.svert[x]] != 0;
-        if (keep) { t = A.stime[x]; d = A.sdir[x]; }
+        if (keep) { t = A.stime[x]; d = A.sdir[x] & 7; }  // the list keeps the incidence index
       }
       const unsigned ball = __ballot_sync(0xFFFFFFFFu, keep);
       __syncwarp();
@@ -1495,7 +1553,7 @@ __global__ void __launch_bounds__(256) k_site_end_narrow(Arena A, const int* sit
       const int x = base + j;
       if (A.vnew[A.svert[x]]) {
         A.stime[base + n] = A.stime[x];
-        A.sdir[base + n] = A.sdir[x];
+        A.sdir[base + n] = A.sdir[x] & 7;  // the list keeps the incidence index
         ++n;
       }
     }

@@ -16,10 +16,12 @@ enum : int { ERR_OVERFLOW = 1, ERR_ITERCAP = 2 };
 //   *SQ  sum over clusters of squares        *Q   sum of 4th powers (u128: lo, hi)
 //   LSQ/MSQ/SLSQ/SMSQ  sum of squared time-integrated size / magnetisation (2^-40 units, u128)
 //   FLD  sum_c (flipped ? -M_c : M_c)        MA / SMA  sum of time-integrated (staggered) M
+//   WSQ  sum over clusters and directions of the cluster winding squared
+//   W0..W2  total winding per direction (signed)
 enum : int {
   R_NOP = 0, R_NC, R_M0, R_SM0, R_M0SQ, R_N0SQ, R_SM0SQ, R_SN0SQ,
   R_M0Q = 8, R_N0Q = 10, R_SM0Q = 12, R_SN0Q = 14, R_LSQ = 16, R_MSQ = 18, R_SLSQ = 20,
-  R_SMSQ = 22, R_FLD = 24, R_MA = 25, R_SMA = 26
+  R_SMSQ = 22, R_FLD = 24, R_MA = 25, R_SMA = 26, R_WSQ = 27, R_W0 = 28, R_W1 = 29, R_W2 = 30
 };
 
 struct DChain {

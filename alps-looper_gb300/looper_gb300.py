@@ -23,7 +23,7 @@ CHAIN, SQUARE, CUBIC = 1, 2, 3
 LATTICES = {"chain lattice": CHAIN, "chain": CHAIN, "square lattice": SQUARE, "square": SQUARE,
             "simple cubic lattice": CUBIC, "cubic": CUBIC}
 RECORD_WORDS = 32
-NUM_OBS = 18
+NUM_OBS = 19
 
 ERRORS = {0: "LG_OK", -1: "LG_EINVAL", -2: "LG_ENOMEM", -3: "LG_EDEVICE", -4: "LG_EUNSUPPORTED",
           -5: "LG_EITERCAP", -6: "LG_EBUDGET", -7: "LG_ECORRUPT", -8: "LG_ENOTREADY"}

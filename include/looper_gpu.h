@@ -79,7 +79,7 @@ int lg_params_parse(const char* text, lg_params* p);
 
 /* ---- observables -------------------------------------------------------------------------
  * Names follow the reference's ObservableSet entries (energy.h:79-84, susceptibility.h:200-254
- * and :303-335, path_integral.C:832-861) and the evaluators (energy.h:89-101,
+ * and :303-335, stiffness.h:77-78, path_integral.C:832-861) and the evaluators (energy.h:89-101,
  * susceptibility.h:340-374).  With the improved estimator (no field) the (Staggered)
  * Magnetization^2/^4 and Susceptibility entries are the improved ones; with a field they are
  * the normal estimators. */
@@ -102,6 +102,7 @@ enum {
   LG_OBS_NUM_OPERATORS,              /* operator count n_v (weight_parameter)     */
   LG_OBS_BINDER,                     /* "Binder Ratio of Magnetization"           */
   LG_OBS_STAG_BINDER,                /* "Binder Ratio of Staggered Magnetization" */
+  LG_OBS_STIFFNESS,                  /* "Stiffness" (stiffness.h:116-160)        */
   LG_NUM_OBS
 };
 

@@ -300,6 +300,8 @@ enum {
   R_SLSQ_LO, R_SLSQ_HI, R_SMSQ_LO, R_SMSQ_HI,
   R_FLD,                                   // sum_c (flip ? -M_c : M_c)   (2^-40 units)
   R_MA, R_SMA,                             // sum over all segments of (1-2c) len, gauge*(1-2c) len
+  R_WSQ,                                   // sum over clusters and directions of winding^2
+  R_W0, R_W1, R_W2,                        // total winding per direction (signed)
   R_WORDS = 32
 };
 
@@ -466,6 +468,12 @@ struct chain_t {
     std::vector<int64_t> key(nc, INT64_MAX);
     std::vector<int64_t> L(nc, 0), M(nc, 0), SL(nc, 0), SM(nc, 0);
     std::vector<int64_t> n0(nc, 0), m0(nc, 0), sn0(nc, 0), sm0(nc, 0);
+    // winding of each cluster per direction (stiffness.h:82-130): the improved accumulator calls
+    // end_bs / begin_bs for the source-site legs of every non-frozen bond vertex
+    // (measurement.h improved_accumulator::end_b / begin_b, path_integral.C:697-709).  The lower
+    // leg's cluster gains (1-2c) e_d with c the spin before the vertex, the upper leg's cluster
+    // loses (1-2c') e_d with c' the spin after; d is the bond's direction (bond = site*dim + d).
+    std::vector<int64_t> wind((size_t)nc * 3, 0);
     int64_t MA = 0, SMA = 0, M0tot = 0, SM0tot = 0;
     for (int s = 0; s < N; ++s) {
       int c = spins[s];
@@ -485,6 +493,14 @@ struct chain_t {
           tnext = (int64_t)1 << 40;
         }
         int cl = frag.id[fr];
+        if (j < (int)ep[s].size()) {
+          const op_t& o = nops[ep[s][j]];
+          if (lat.s0[o.bond] == s && !(o.g & 2)) {
+            const int d = o.bond % lat.dim;
+            wind[(size_t)cl * 3 + d] += 1 - 2 * c;                          // end_bs
+            wind[(size_t)frag.id[nextfr] * 3 + d] -= 1 - 2 * nextc;          // begin_bs
+          }
+        }
         int64_t segidx = base[s] + j;
         if (segidx < key[cl]) key[cl] = segidx;
         int64_t len = tnext - tprev;
@@ -535,6 +551,11 @@ struct chain_t {
       add128(rec.data(), R_SLSQ_LO, sq(SL[cl]));
       add128(rec.data(), R_SMSQ_LO, sq(SM[cl]));
       fld += flip[cl] ? -M[cl] : M[cl];
+      for (int d = 0; d < 3; ++d) {
+        const int64_t w = wind[(size_t)cl * 3 + d];
+        rec[R_WSQ] += (uint64_t)(w * w);
+        rec[R_W0 + d] += (uint64_t)w;
+      }
     }
     rec[R_FLD] = (uint64_t)fld;
     rec[R_MA] = (uint64_t)MA;
