@@ -781,6 +781,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
     // stage the incident lists: list d occupies [off[d], off[d+1])
     int off[MAXZ + 1];
     int ptr[MAXZ];
+    uint8_t sdv[MAXZ];  // per list: the segment's sdir value (incidence | direction << 3) | side << 7
     off[0] = 0;
 #pragma unroll
     for (int d = 0; d < MAXZ; ++d) {
@@ -788,8 +789,9 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
         const int b = A.inc[j0 + d];
         ptr[d] = A.bond_ptr[b];
         off[d + 1] = off[d] + A.bond_cnt[b];
+        sdv[d] = (uint8_t)(d | (A.inc_dir ? A.inc_dir[j0 + d] << 3 : 0) | (A.inc_side[j0 + d] << 7));
       } else {
-        ptr[d] = 0; off[d + 1] = off[d];
+        ptr[d] = 0; off[d + 1] = off[d]; sdv[d] = 0;
       }
     }
 #pragma unroll
@@ -896,16 +898,17 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
 #pragma unroll
         for (int q = 1; q < MAXZ; ++q) if (e >= off[q]) d = q;
         int pd = 0, od = 0;
+        uint8_t sv = 0;
 #pragma unroll
-        for (int q = 0; q < MAXZ; ++q) if (q == d) { pd = ptr[q]; od = off[q]; }
+        for (int q = 0; q < MAXZ; ++q) if (q == d) { pd = ptr[q]; od = off[q]; sv = sdv[q]; }
         const int v = pd + (e - od);
         const int x = base + 1 + r;
-        const uint8_t side = A.inc_side[j0 + d];
+        const uint8_t side = sv >> 7;
         A.stime[x] = fK[r] >> 1;
         A.sinfo[x] = (uint8_t)(spin | gneg | (r == k - 1 ? SI_LAST : 0) | (side == 0 ? SI_SRC : 0) |
                                ((cd >> 1) << SI_GSHIFT) | ((cd & 1u) ? SI_OFF : 0));
         A.svert[x] = v;
-        A.sdir[x] = (uint8_t)(d | (A.inc_dir ? A.inc_dir[j0 + d] << 3 : 0));
+        A.sdir[x] = (uint8_t)(sv & 0x7F);
         A.parent[x] = (r == k - 1) ? base : x;  // closure: top segment joins the bottom one
         A.vslot[2 * v + side] = x;
       }
