@@ -239,6 +239,44 @@ def run_batched(lg, steps, therm, plain_sample=16):
             "shape": shape, "autotune_candidates": report.count(" ms\n") - 1}
 
 
+def replica_params(lg, n=64):
+    """64 replicas of the S=1/2 XXZ model on a periodic 24^3 simple-cubic lattice (13824
+    sites), Jxy = 1, Jz = 0.5, uniform field h = 0.3, beta = 8, seeds 1000..1063."""
+    return [lg.make_params(LATTICE="cubic", L=24, BETA=8.0, Jxy=1.0, Jz=0.5, h=0.3,
+                           SEED=1000 + i, SWEEPS=1 << 13, THERMALIZATION=1 << 10,
+                           INITIAL_SPINS="random")
+            for i in range(n)]
+
+
+def run_replicas(lg, steps, therm, plain_sample=4):
+    """The 64 field replicas in one arena vs the plain path on a sample of them."""
+    ps = replica_params(lg)
+    sites = sum(p.L ** 3 for p in ps)
+    b = lg.Batch(ps)
+    b.run(therm // 2)
+    shape, _ = b.autotune(2, FLUSH_BYTES)
+    b.run(therm - therm // 2)
+    b.time_sweeps(3, FLUSH_BYTES)
+    ms = b.time_sweeps(steps, FLUSH_BYTES)
+    t_b = float(ms.sum()) / 1e3
+    t_p, s_p = 0.0, 0
+    for i in range(plain_sample):
+        w = lg.LoopWorker(ps[i])
+        w.run(min(therm, 64))
+        w.autotune(2, FLUSH_BYTES)
+        m = w.time_sweeps(max(8, steps), FLUSH_BYTES)
+        t_p += float(m.mean()) / 1e3
+        s_p += ps[i].L ** 3
+        w.close()
+    b.close()
+    return {"workload": "64 replicas, XXZ Jxy=1 Jz=0.5 h=0.3 on a 24^3 cubic lattice, beta=8, "
+                        "seeds 1000..1063 (%d sites)" % sites,
+            "value": steps * sites / t_b, "unit": UNIT, "ms_per_sweep": t_b * 1e3 / steps,
+            "steps": steps, "thermalization_sweeps": therm,
+            "plain_value": s_p / t_p, "plain_sample_replicas": plain_sample,
+            "speedup_vs_plain": (steps * sites / t_b) / (s_p / t_p), "shape": shape}
+
+
 def served_requests(lg, n=4096, seed=2024):
     """The served stream: Poisson arrivals at 200/s; lattice uniform over {chain L in [32,4096],
     square L in [8,96], cubic L in [6,24]} (L rounded up to even: odd periodic lattices with an
@@ -378,6 +416,9 @@ def run_ours(args, dist, ws, rank, local):
     batched = None
     if rank == 0 and args.batched_steps > 0:
         batched = run_batched(lg, args.batched_steps, args.batched_therm)
+    replicas = None
+    if rank == 0 and args.replica_steps > 0:
+        replicas = run_replicas(lg, args.replica_steps, args.replica_therm)
     served = None
     if rank == 0 and args.served_requests > 0:
         served = run_served(lg, args.served_requests)
@@ -396,6 +437,7 @@ def run_ours(args, dist, ws, rank, local):
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
         "clocks": clocks,
         "batched": batched,
+        "replicas_field": replicas,
         "served": served,
         "observables": {"Energy Density": obs["Energy Density"][0],
                         "sweeps_measured": int(obs["count"]),
@@ -455,6 +497,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--batched-steps", type=int, default=16)
     ap.add_argument("--batched-therm", type=int, default=128)
+    ap.add_argument("--replica-steps", type=int, default=8)
+    ap.add_argument("--replica-therm", type=int, default=32)
     ap.add_argument("--served-requests", type=int, default=48)
     ap.add_argument("--shape", default="auto",
                     help='launch shape of the headline chain: "auto" (autotuned) or a JSON dict '
