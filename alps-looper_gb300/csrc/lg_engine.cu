@@ -31,10 +31,10 @@
 using namespace lg;
 
 // timed stages of one sweep, in launch order (an event is recorded after each stage)
-static const int kNumStages = 8;
+static const int kNumStages = 7;
 static const char* kStageNames[kNumStages] = {
-    "k_insert", "k_site_count+scan(sites)", "k_merge", "k_union|k_tile",
-    "k_accumulate|k_union_ext", "k_fix", "k_cluster", "k_site_end+k_end"};
+    "k_insert", "k_site_count+scan(sites)", "k_merge", "k_union", "k_accumulate", "k_cluster",
+    "k_site_end+k_end"};
 
 static std::atomic<uint64_t> g_launches{0};
 static thread_local std::string g_err;
@@ -79,16 +79,12 @@ struct DBuf {
 //   acc_tile  segments per block in k_accumulate (512, 1024, 2048)
 //   cl_tile   segments per block in k_cluster (2048, 4096, 8192)
 //   un_warps  warps per block in k_union (4, 8, 16)
-//   tile_cap  0: union-find and cluster sums by k_union + k_accumulate over all segments;
-//             2048, 4096, 8192: by k_tile over lattice patches of up to that many segments in
-//             shared memory, then k_union_ext + k_fix for what crosses the patches
 struct Shape {
   double insert_k = 32.0;
   double narrow_k = 32.0;
   int acc_tile = 1024;
   int cl_tile = 4096;
   int un_warps = 8;
-  int tile_cap = 0;
 };
 
 // ----------------------------------------------------------------------------------------------
@@ -123,9 +119,6 @@ struct Engine {
   DBuf<RootKW> d_rkw;
   DBuf<unsigned long long> d_rec;
   DBuf<Ctl> d_ctl;
-  // tile union-find: static tiles of the current shape, per-sweep lists
-  int ntiles = 0;
-  DBuf<int> d_tile_run_off, d_run_lo, d_run_hi, d_ovf, d_ext, d_hook;
 
   int nv_cap = 0, ns_cap = 0;
   int rec_rows = 64;
@@ -183,8 +176,6 @@ struct Engine {
     A.stime = d_stime.p; A.sinfo = d_sinfo.p; A.svert = d_svert.p; A.sdir = d_sdir.p;
     A.parent = d_parent.p; A.flip = d_flip.p; A.cls = d_cls.p; A.rkw = d_rkw.p; A.inc_dir = d_inc_dir.p;
     A.rec = d_rec.p; A.ctl = d_ctl.p; A.rec_rows = rec_rows;
-    A.ntiles = ntiles; A.tile_run_off = d_tile_run_off.p; A.run_lo = d_run_lo.p;
-    A.run_hi = d_run_hi.p; A.ext = d_ext.p; A.hook = d_hook.p; A.ovf = d_ovf.p;
     return A;
   }
 
@@ -204,13 +195,6 @@ struct Engine {
     LG_CUDA(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
     LG_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     LG_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
-    LG_CUDA(cudaFuncSetAttribute(k_tile<2048, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 tile_smem_bytes<2048>()));
-    LG_CUDA(cudaFuncSetAttribute(k_tile<4096, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 tile_smem_bytes<4096>()));
-    LG_CUDA(cudaFuncSetAttribute(k_tile<8192, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 tile_smem_bytes<8192>()));
-    LG_CUDA(cudaFuncSetAttribute(k_fix, cudaFuncAttributeMaxDynamicSharedMemorySize, FIX_SMEM));
     // static tables
     long long nsite = 0, nbond = 0;
     for (auto& s : spec) { nsite += s.N; nbond += s.NB; }
@@ -411,7 +395,6 @@ struct Engine {
         (rc = d_sinfo.alloc(new_ns)) || (rc = d_svert.alloc(new_ns)) || (rc = d_sdir.alloc(new_ns)) ||
         (rc = d_parent.alloc(new_ns)) || (rc = d_flip.alloc(new_ns)) ||
         (rc = d_cls.alloc(4 * (size_t)new_ns)) || (rc = d_rkw.alloc((size_t)new_ns)) ||
-        (rc = d_ext.alloc(new_nv)) || (rc = d_hook.alloc(new_ns)) ||
         (rc = d_rec.alloc((size_t)rec_rows * C * REC_WORDS)))
       return rc;
     // cluster class sums must start at zero (k_cluster clears what it consumes)
@@ -450,7 +433,6 @@ struct Engine {
     s.acc_tile = ns_cap / 1024 >= goal ? 1024 : 512;
     s.cl_tile = ns_cap / 4096 >= goal ? 4096 : 2048;
     s.un_warps = 8;
-    s.tile_cap = 0;
     return s;
   }
 
@@ -478,8 +460,7 @@ struct Engine {
     if (!(sh.acc_tile == 512 || sh.acc_tile == 1024 || sh.acc_tile == 2048) ||
         !(sh.cl_tile == 2048 || sh.cl_tile == 4096 || sh.cl_tile == 8192) ||
         !(sh.un_warps == 4 || sh.un_warps == 8 || sh.un_warps == 16) || !(sh.narrow_k >= 0) ||
-        !(sh.insert_k >= 0) ||
-        !(sh.tile_cap == 0 || sh.tile_cap == 2048 || sh.tile_cap == 4096 || sh.tile_cap == 8192))
+        !(sh.insert_k >= 0))
       return lg_fail(LG_EINVAL, "bad launch shape");
     std::vector<int> ws, nsl, is, nbl;
     for (int c = 0; c < C; ++c) {
@@ -516,94 +497,8 @@ struct Engine {
       ins_list = d_ins_sites.p;
     }
     if ((rc = upload(d_narrow_sites, nsl)) || (rc = upload(d_narrow_bonds, nbl))) return rc;
-    if ((rc = build_tiles(sh.tile_cap))) return rc;
     shape = sh;
     drop_graph();
-    return LG_OK;
-  }
-
-  // Expected segments of chain c per sweep (sites plus two per operator): the last sweep's
-  // operator count once there is one, else about 1.2 beta W N_b operators (the Heisenberg
-  // antiferromagnet's ratio of operators to diagonal proposals).
-  double expected_segments(int c) const {
-    const ChainSpec& s = spec[c];
-    const double nop = s.last_nop ? (double)s.last_nop : 1.2 * s.beta * s.W * s.NB;
-    return s.N + 2.0 * nop;
-  }
-
-  // Tiles of the tile union-find for capacity cap (segments in shared memory): a tile aims at
-  // 55% of cap.  A chain expected to fit in that share is one run, and consecutive such chains
-  // share a tile.  A larger chain is cut into patches: runs of p sites on a chain, p x p (x p)
-  // blocks of a square (cubic) lattice, one run per row of the patch, at most TILE_MAXR runs.
-  // Runs of a tile ascend in site order; adjacent ones are merged.
-  int build_tiles(int cap) {
-    ntiles = 0;
-    if (cap == 0) return LG_OK;
-    std::vector<int> off{0}, lo, hi;
-    const double target = 0.55 * cap;
-    double pend = 0;
-    int pend_runs = 0;
-    auto add_run = [&](int a, int b) {
-      if (pend_runs && hi.back() == a) { hi.back() = b; return; }
-      lo.push_back(a); hi.push_back(b); ++pend_runs;
-    };
-    auto close = [&]() {
-      if (pend_runs) off.push_back((int)lo.size());
-      pend_runs = 0; pend = 0;
-    };
-    for (int c = 0; c < C; ++c) {
-      const ChainSpec& sp = spec[c];
-      const int so = hch[c].site_off, n = sp.N, L = sp.L;
-      const double es = expected_segments(c);
-      if (es <= target) {
-        if (pend + es > target || pend_runs >= TILE_MAXR) close();
-        add_run(so, so + n);
-        pend += es;
-        continue;
-      }
-      close();
-      const double per_site = es / n;
-      const long long want = std::max(1ll, (long long)(target / per_site));
-      if (sp.dim == 1) {
-        const int p = (int)std::min<long long>(want, n);
-        for (int i0 = 0; i0 < n; i0 += p) { add_run(so + i0, so + std::min(i0 + p, n)); close(); }
-      } else if (sp.dim == 2) {
-        int py = std::max(1, (int)std::floor(std::sqrt((double)want)));
-        py = std::min(std::min(py, L), TILE_MAXR);
-        const int px = (int)std::min<long long>(L, std::max(1ll, want / py));
-        for (int y0 = 0; y0 < L; y0 += py)
-          for (int x0 = 0; x0 < L; x0 += px) {
-            for (int y = y0; y < std::min(y0 + py, L); ++y)
-              add_run(so + y * L + x0, so + y * L + std::min(x0 + px, L));
-            close();
-          }
-      } else {
-        int pz = std::max(1, (int)std::floor(std::cbrt((double)want)));
-        pz = std::min(std::min(pz, L), 8);
-        const int py = std::min(pz, TILE_MAXR / pz);
-        const int px = (int)std::min<long long>(L, std::max(1ll, want / ((long long)py * pz)));
-        for (int z0 = 0; z0 < L; z0 += pz)
-          for (int y0 = 0; y0 < L; y0 += py)
-            for (int x0 = 0; x0 < L; x0 += px) {
-              for (int z = z0; z < std::min(z0 + pz, L); ++z)
-                for (int y = y0; y < std::min(y0 + py, L); ++y)
-                  add_run(so + (z * L + y) * L + x0, so + (z * L + y) * L + std::min(x0 + px, L));
-              close();
-            }
-      }
-    }
-    close();
-    ntiles = (int)off.size() - 1;
-    for (int t = 0; t < ntiles; ++t)
-      if (off[t + 1] - off[t] > TILE_MAXR || off[t + 1] <= off[t])
-        return lg_fail(LG_EINVAL, "internal: tile %d has %d runs", t, off[t + 1] - off[t]);
-    int rc;
-    if ((rc = d_tile_run_off.alloc(off.size())) || (rc = d_run_lo.alloc(lo.size())) ||
-        (rc = d_run_hi.alloc(hi.size())) || (rc = d_ovf.alloc(ntiles)))
-      return rc;
-    LG_CUDA(cudaMemcpy(d_tile_run_off.p, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_run_lo.p, lo.data(), lo.size() * sizeof(int), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_run_hi.p, hi.data(), hi.size() * sizeof(int), cudaMemcpyHostToDevice));
     return LG_OK;
   }
 
@@ -676,42 +571,29 @@ struct Engine {
     }
     join();
     mark(2);
-    const int tc = shape.tile_cap;
-    if (tc == 0) {
-      {
-        const int w = shape.un_warps, per = w * UN_CHUNK;
-        const int g = (ns_cap + per - 1) / per;  // one chunk per warp: no straggler tail
-        if (w == 4) k_union<4><<<g, 4 * 32, 0, st>>>(A);
-        else if (w == 16) k_union<16><<<g, 16 * 32, 0, st>>>(A);
-        else k_union<8><<<g, 8 * 32, 0, st>>>(A);
-      }
-      mark(3);
-      {
-        const int t = shape.acc_tile, g = (ns_cap + t - 1) / t;  // one tile per block
-        if (t == 512) k_accumulate<512><<<g, 256, 0, st>>>(A);
-        else if (t == 2048) k_accumulate<2048><<<g, 256, 0, st>>>(A);
-        else k_accumulate<1024><<<g, 256, 0, st>>>(A);
-      }
-      mark(4);
-      launches += 2;
-    } else {
-      if (tc == 2048) k_tile<2048, 256><<<ntiles, 256, tile_smem_bytes<2048>(), st>>>(A);
-      else if (tc == 8192) k_tile<8192, 1024><<<ntiles, 1024, tile_smem_bytes<8192>(), st>>>(A);
-      else k_tile<4096, 512><<<ntiles, 512, tile_smem_bytes<4096>(), st>>>(A);
-      mark(3);
-      k_union_ext<<<nsm * 8, 256, 0, st>>>(A);
-      mark(4);
-      k_fix<<<nsm, FIX_THREADS, FIX_SMEM, st>>>(A);
-      launches += 3;
+    {
+      const int w = shape.un_warps, per = w * UN_CHUNK;
+      const int g = (ns_cap + per - 1) / per;  // one chunk per warp: no straggler tail
+      if (w == 4) k_union<4><<<g, 4 * 32, 0, st>>>(A);
+      else if (w == 16) k_union<16><<<g, 16 * 32, 0, st>>>(A);
+      else k_union<8><<<g, 8 * 32, 0, st>>>(A);
     }
-    mark(5);
+    mark(3);
+    {
+      const int t = shape.acc_tile, g = (ns_cap + t - 1) / t;  // one tile per block
+      if (t == 512) k_accumulate<512><<<g, 256, 0, st>>>(A);
+      else if (t == 2048) k_accumulate<2048><<<g, 256, 0, st>>>(A);
+      else k_accumulate<1024><<<g, 256, 0, st>>>(A);
+    }
+    mark(4);
+    launches += 2;
     {
       const int t = shape.cl_tile, g = (ns_cap + t - 1) / t;  // one tile per block
       if (t == 2048) k_cluster<2048><<<g, CL_THREADS, 0, st>>>(A);
       else if (t == 8192) k_cluster<8192><<<g, CL_THREADS, 0, st>>>(A);
       else k_cluster<4096><<<g, CL_THREADS, 0, st>>>(A);
     }
-    mark(6);
+    mark(5);
     launches += 1;
     fork(n_wide > 0 && n_narrow > 0);
     if (n_wide) {
@@ -724,7 +606,7 @@ struct Engine {
     }
     join();
     k_end<<<1, 1024, 0, st>>>(A);
-    mark(7);
+    mark(6);
     launches += 1;
     sweep_launches = launches;
     g_launches += launches;
@@ -787,7 +669,6 @@ struct Engine {
       Ctl z = hc;
       z.step = 0;
       z.err = 0;
-      z.ext_n = z.hook_n = z.ovf_n = 0;
       if (hc.err == ERR_ITERCAP)
         return lg_fail(LG_EITERCAP, "union-find iteration cap hit");
       if (hc.err == ERR_OVERFLOW) {
@@ -866,8 +747,8 @@ struct Engine {
       double t = 0;
       for (double x : km) t += x;
       *ms = t / trial;
-      std::snprintf(line, sizeof(line), "insert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d tile_cap=%d: %.4f ms\n",
-                    sh.insert_k, sh.narrow_k, sh.acc_tile, sh.cl_tile, sh.un_warps, sh.tile_cap, *ms);
+      std::snprintf(line, sizeof(line), "insert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d: %.4f ms\n",
+                    sh.insert_k, sh.narrow_k, sh.acc_tile, sh.cl_tile, sh.un_warps, *ms);
       report += line;
       return LG_OK;
     };
@@ -907,13 +788,8 @@ struct Engine {
       c.insert_k = k;
       if ((rc = consider(c))) return rc;
     }
-    for (int t : {0, 2048, 4096, 8192}) {
-      if (t == best.tile_cap) continue;
-      Shape c = best; c.tile_cap = t;
-      if ((rc = consider(c))) return rc;
-    }
     for (int t : {512, 1024, 2048}) {
-      if (best.tile_cap != 0 || t == best.acc_tile) continue;
+      if (t == best.acc_tile) continue;
       Shape c = best; c.acc_tile = t;
       if ((rc = consider(c))) return rc;
     }
@@ -923,12 +799,12 @@ struct Engine {
       if ((rc = consider(c))) return rc;
     }
     for (int w : {4, 8, 16}) {
-      if (best.tile_cap != 0 || w == best.un_warps) continue;
+      if (w == best.un_warps) continue;
       Shape c = best; c.un_warps = w;
       if ((rc = consider(c))) return rc;
     }
-    std::snprintf(line, sizeof(line), "chosen: insert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d tile_cap=%d (%.4f ms)\n",
-                  best.insert_k, best.narrow_k, best.acc_tile, best.cl_tile, best.un_warps, best.tile_cap, best_ms);
+    std::snprintf(line, sizeof(line), "chosen: insert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d (%.4f ms)\n",
+                  best.insert_k, best.narrow_k, best.acc_tile, best.cl_tile, best.un_warps, best_ms);
     report += line;
     return set_shape(best);
   }
@@ -1415,7 +1291,7 @@ static void shape_out(const Shape& s, lg_shape* out) {
   out->acc_tile = s.acc_tile;
   out->cl_tile = s.cl_tile;
   out->union_warps = s.un_warps;
-  out->tile_cap = s.tile_cap;
+  out->reserved = 0;
 }
 
 static int autotune_engine(Engine& e, int trial, size_t flush_bytes, lg_shape* chosen, char* report,
@@ -1448,7 +1324,6 @@ static int set_shape_engine(Engine& e, const lg_shape* in) {
   s.acc_tile = in->acc_tile;
   s.cl_tile = in->cl_tile;
   s.un_warps = in->union_warps;
-  s.tile_cap = in->tile_cap;
   return e.set_shape(s);
 }
 

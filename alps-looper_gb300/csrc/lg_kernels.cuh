@@ -10,10 +10,6 @@
 //                    temporal closure                                          (:584-589)
 //   k_union          per vertex: lock-free unions of its four legs            (graph_impl.h:280-295)
 //   k_accumulate     per segment: parent := root, length into the root's class sums (:650-737)
-//     or, by lattice patches in shared memory (the tile union-find):
-//   k_tile           per patch: unions of its own vertices, cluster sums per local root
-//   k_union_ext      per vertex crossing patches: global unions; hooked roots listed
-//   k_fix            per hooked root: its sums to the final root
 //   k_cluster        per root: flip coin, improved / field sums -> records     (:739-803)
 //   k_site_end       per site: spin flip; new vertex types from the flips of the clusters
 //                    below and above each endpoint; compacted off-diagonal list (:805-823)
@@ -107,15 +103,6 @@ struct Arena {
   unsigned long long* rec;  // [rows][C][REC_WORDS]
   Ctl* ctl;
   int rec_rows;             // rows of rec
-  // tile union-find (k_tile): tile t is the site runs [tile_run_off[t], tile_run_off[t+1]), run
-  // i the sites [run_lo[i], run_hi[i]); runs of a tile ascend and do not overlap
-  int ntiles;
-  const int* tile_run_off;
-  const int* run_lo;
-  const int* run_hi;
-  int* ext;                 // source-side segments of vertices left to k_union_ext
-  int* hook;                // roots hooked by k_union_ext
-  int* ovf;                 // tiles handled without shared memory
 };
 
 #define LG_GRID_STRIDE(i, n) \
@@ -976,7 +963,6 @@ __device__ __forceinline__ bool uf_union(int* P, int a, int b) {
   return false;
 }
 
-
 // reconnect (graph_impl.h:280-295) in segment form: g = 0 joins the two lower legs and the two
 // upper legs; g = 1 joins lower-left with upper-right and lower-right with upper-left; frozen
 // graphs (g & 2) join all four legs.
@@ -1132,12 +1118,28 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
         dir1[j] = last ? 0 : A.sdir[x + 1];
       }
     }
+    // root walks of this thread's segments in lockstep (their parent reads in flight together)
+    int rt[PER];
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      rt[j] = xs[j];
+      if (xs[j] >= ns) par[j] = xs[j];
+    }
+    for (int it = 0; it < ITER_CAP; ++it) {
+      unsigned moved = 0;
+#pragma unroll
+      for (int j = 0; j < PER; ++j)
+        if (par[j] != rt[j]) { rt[j] = par[j]; moved |= 1u << j; }
+      if (!moved) break;
+#pragma unroll
+      for (int j = 0; j < PER; ++j)
+        if (moved & (1u << j)) par[j] = A.parent[rt[j]];
+    }
 #pragma unroll
     for (int j = 0; j < PER; ++j) {
       const int x = xs[j];
       if (x >= ns) continue;
-      int r = x, p = par[j];
-      while (p != r) { r = p; p = A.parent[r]; }
+      const int r = rt[j];
       if (r != x) A.parent[x] = r;
       const SegContrib sc = seg_contrib(info[j], info1[j], ta[j], tb[j], dir[j], dir1[j]);
       const unsigned long long len = sc.len;
@@ -1491,496 +1493,8 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
   }
 }
 
-// ---------------------------------------------------------------------------------------------
-// Tile union-find: the unions and the cluster sums of k_union + k_accumulate, done first inside
-// patches of the lattice in shared memory.
-//
-// A tile is a set of whole sites (runs of consecutive sites: a patch of a square or cubic
-// lattice is one run per row, a small chain is one run), so its segments are a few contiguous
-// ranges of the site-major segment arrays.  Local index = rank of the global index inside the
-// tile, so local order is global order and the smallest local index of a local cluster is its
-// smallest global index.  k_tile:
-//   1. stages the segment infos and the union-find init (k_merge's temporal closure) of its
-//      segments in shared memory;
-//   2. unites the legs of every vertex whose two sites lie in the tile (the reconnect of
-//      k_union, graph_impl.h:280-295) with shared-memory CAS hooking, larger index to smaller;
-//      a vertex with a site outside the tile goes to the ext list (a frozen vertex still joins its
-//      own two legs here);
-//   3. writes parent := local root for every segment;
-//   4. sums every segment's length, tau = 0 count and winding (seg_contrib) into its local root,
-//      in shared memory, and stores the sums at the local root's slot.
-// k_union_ext then unites the legs of the listed vertices in global memory (hooks by global
-// index, so every cluster's root is still its smallest segment) and lists every root it hooks;
-// k_fix folds each hooked root's sums into its final root.  k_cluster finishes the path
-// compression.  A tile whose segments do not fit in shared memory sends all its vertices to the
-// ext list and its segments' sums to k_fix.  Every sum is an exact integer, so the result equals
-// k_union + k_accumulate bit for bit.
-constexpr int TILE_MAXR = 64;   // site runs per tile
-constexpr int TILE_ACC = 10;    // words per local root: class sums lo[4], hi[4], winding wa, wb
-
-template <int CAP>
-__host__ __device__ constexpr int tile_smem_bytes() {
-  return CAP * 4 + (CAP / 2) * (TILE_ACC * 4 + 4) + CAP;
-}
-
-// Shared-memory find (volatile reads: other threads hook concurrently) with path halving.
-__device__ __forceinline__ int sm_find(volatile int* P, int x) {
-  while (true) {
-    const int p = P[x];
-    if (p == x) return x;
-    const int gp = P[p];
-    if (gp == p) return p;
-    P[x] = gp;
-    x = gp;
-  }
-}
-
-__device__ __forceinline__ bool sm_union(int* P, int a, int b) {
-  volatile int* V = P;
-  for (int it = 0; it < ITER_CAP; ++it) {
-    a = sm_find(V, a);
-    b = sm_find(V, b);
-    if (a == b) return true;
-    const int lo = a < b ? a : b, hi = a < b ? b : a;
-    const int old = atomicCAS(P + hi, hi, lo);
-    if (old == hi) return true;
-    a = lo;
-    b = old;
-  }
-  return false;
-}
-
-// Largest i in [0, n) with key[i] <= v (key ascending, key[0] <= v).
-__device__ __forceinline__ int run_of(const int* key, int n, int v) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (key[mid] <= v) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
-// Appends v (where `want`) to list[*count ...], one atomic per warp.  Warp-collective.
-__device__ __forceinline__ void warp_append(int* list, int* count, bool want, int v) {
-  const unsigned ball = __ballot_sync(0xFFFFFFFFu, want);
-  if (!ball) return;
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(ball) - 1;
-  int base = 0;
-  if (lane == leader) base = atomicAdd(count, __popc(ball));
-  base = __shfl_sync(0xFFFFFFFFu, base, leader);
-  if (want) list[base + __popc(ball & ((1u << lane) - 1u))] = v;
-}
-
-template <int CAP, int THREADS>
-__global__ void __launch_bounds__(THREADS) k_tile(Arena A) {
-  if (A.ctl->err) return;
-  constexpr int RCAP = CAP / 2;          // local roots with shared-memory sums
-  constexpr int PER = CAP / THREADS;     // segments per thread
-  extern __shared__ __align__(16) unsigned char tile_smem[];
-  int* P = reinterpret_cast<int*>(tile_smem);                    // [CAP] local parents
-  unsigned* acc = reinterpret_cast<unsigned*>(P + CAP);          // [RCAP][TILE_ACC]
-  int* gidx = reinterpret_cast<int*>(acc + RCAP * TILE_ACC);     // [RCAP] root's global index
-  uint8_t* inf = reinterpret_cast<uint8_t*>(gidx + RCAP);        // [CAP] segment infos
-  __shared__ int rg0[TILE_MAXR];       // first global segment of each run
-  __shared__ int rl0[TILE_MAXR + 1];   // first local index of each run
-  __shared__ int s_w0, s_nroots;
-  const int tid = threadIdx.x, lane = tid & 31;
-  const int t = blockIdx.x;
-  const int q0 = A.tile_run_off[t], nr = A.tile_run_off[t + 1] - q0;
-  // run extents and their prefix (nr <= 64: warps 0 and 1)
-  if (tid < TILE_MAXR) {
-    int cnt = 0;
-    if (tid < nr) {
-      const int g0 = A.sbase[A.run_lo[q0 + tid]];
-      rg0[tid] = g0;
-      cnt = A.sbase[A.run_hi[q0 + tid]] - g0;
-    }
-    int v = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xFFFFFFFFu, v, o);
-      if (lane >= o) v += y;
-    }
-    if (tid == 31) s_w0 = v;
-    rl0[tid + 1] = v;
-  }
-  if (tid == 0) { rl0[0] = 0; s_nroots = 0; }
-  __syncthreads();
-  if (tid >= 32 && tid < TILE_MAXR) rl0[tid + 1] += s_w0;
-  __syncthreads();
-  const int n = rl0[nr];
-  if (n > CAP) {
-    // too large for shared memory: every vertex to the global pass, every segment to k_fix
-    for (int l0 = 0; l0 < n; l0 += THREADS) {
-      const int l = l0 + tid;
-      int x = 0;
-      bool src = false;
-      if (l < n) {
-        const int r = run_of(rl0, nr, l);
-        x = rg0[r] + (l - rl0[r]);
-        src = (A.sinfo[x] & SI_SRC) != 0;
-      }
-      warp_append(A.ext, &A.ctl->ext_n, src, x);
-    }
-    if (tid == 0) A.ovf[atomicAdd(&A.ctl->ovf_n, 1)] = t;
-    return;
-  }
-  // 1. stage: segment info, local parent (the closure hook of the top segment stays in the run),
-  //    and the target-side leg of every source-side segment
-  int xs[PER], bs[PER];
-  uint8_t fs[PER];
-#pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    const int l = tid + j * THREADS;
-    xs[j] = 0; bs[j] = 0; fs[j] = 0;
-    if (l < n) {
-      const int r = run_of(rl0, nr, l);
-      const int x = rg0[r] + (l - rl0[r]);
-      xs[j] = x;
-      fs[j] = A.sinfo[x];
-      P[l] = l + (A.parent[x] - x);
-      inf[l] = fs[j];
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < PER; ++j)
-    if (fs[j] & SI_SRC) bs[j] = A.svert[xs[j]];
-#pragma unroll
-  for (int j = 0; j < PER; ++j)
-    if (fs[j] & SI_SRC) bs[j] = A.vslot[2 * bs[j] + 1];
-  __syncthreads();
-  // 2. unions of the tile's own vertices; the others to the ext list
-  bool ok = true;
-#pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    const int l = tid + j * THREADS;
-    bool ext = false;
-    if (fs[j] & SI_SRC) {
-      const int b = bs[j];
-      const int g = (fs[j] >> SI_GSHIFT) & 3;
-      const int r = run_of(rg0, nr, b < rg0[0] ? rg0[0] : b);
-      const bool inside = b >= rg0[r] && b - rg0[r] < rl0[r + 1] - rl0[r];
-      if (inside) {
-        const int lb = rl0[r] + (b - rg0[r]);
-        if (g == 1) {
-          ok &= sm_union(P, l - 1, lb);
-          ok &= sm_union(P, lb - 1, l);
-        } else {
-          ok &= sm_union(P, l - 1, lb - 1);
-          ok &= sm_union(P, l, lb);
-          if (g & 2) ok &= sm_union(P, l - 1, l);
-        }
-      } else {
-        if (g & 2) ok &= sm_union(P, l - 1, l);
-        ext = true;
-      }
-    }
-    warp_append(A.ext, &A.ctl->ext_n, ext, xs[j]);
-  }
-  if (!ok) atomicExch(&A.ctl->err, ERR_ITERCAP);
-  __syncthreads();
-  // 3. local roots; parent := local root (global index); roots numbered for the sums
-  int rt[PER];
-#pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    const int l = tid + j * THREADS;
-    rt[j] = -1;
-    if (l < n) {
-      volatile int* V = P;
-      int r = l, p = V[r];
-      while (p != r) { r = p; p = V[r]; }
-      rt[j] = r;
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    const int l = tid + j * THREADS;
-    const bool root = l < n && rt[j] == l;
-    const unsigned ball = __ballot_sync(0xFFFFFFFFu, root);
-    int base = 0;
-    if (ball) {
-      const int leader = __ffs(ball) - 1;
-      if (lane == leader) base = atomicAdd(&s_nroots, __popc(ball));
-      base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    }
-    if (root) {
-      const int rank = base + __popc(ball & ((1u << lane) - 1u));
-      P[l] = ~rank;
-      if (rank < RCAP) gidx[rank] = xs[j];
-      A.parent[xs[j]] = xs[j];
-    } else if (l < n) {
-      const int r = run_of(rl0, nr, rt[j]);
-      A.parent[xs[j]] = rg0[r] + (rt[j] - rl0[r]);
-    }
-  }
-  __syncthreads();
-  const int nroots = s_nroots;
-  const int nacc = nroots < RCAP ? nroots : RCAP;
-  for (int i = tid; i < nacc * TILE_ACC; i += THREADS) acc[i] = 0u;
-  __syncthreads();
-  // 4. segment sums into the local roots
-#pragma unroll
-  for (int j = 0; j < PER; ++j) {
-    const int l = tid + j * THREADS;
-    if (l >= n) continue;
-    const int x = xs[j];
-    const uint8_t info = fs[j];
-    const bool last = info & SI_LAST;
-    const uint8_t info1 = last ? 0 : inf[l + 1];
-    const SegContrib sc = seg_contrib(info, info1, A.stime[x], last ? 0ull : A.stime[x + 1],
-                                      A.sdir[x], last ? 0 : A.sdir[x + 1]);
-    const int rank = ~P[rt[j]];
-    int g = 0;
-    if (rank < RCAP) {
-      g = gidx[rank];
-    } else {
-      const int r = run_of(rl0, nr, rt[j]);
-      g = rg0[r] + (rt[j] - rl0[r]);
-    }
-    if (info & SI_FIRST) atomicAdd(&A.rkw[g].K[sc.q], 1u);
-    if (rank < RCAP) {
-      unsigned* a = acc + rank * TILE_ACC;
-      if (sc.len) {
-        const unsigned lo = (unsigned)sc.len, hi = (unsigned)(sc.len >> 32);
-        const unsigned old = atomicAdd(a + sc.q, lo);
-        const unsigned carry = (old + lo < old) ? 1u : 0u;
-        if (hi + carry) atomicAdd(a + 4 + sc.q, hi + carry);
-      }
-      if (sc.w[0] | sc.w[1]) atomicAdd(reinterpret_cast<int*>(a + 8), sc.w[0] + 65536 * sc.w[1]);
-      if (sc.w[2]) atomicAdd(reinterpret_cast<int*>(a + 9), sc.w[2]);
-    } else {
-      if (sc.len) atomicAdd(A.cls + 4 * (size_t)g + sc.q, sc.len);
-#pragma unroll
-      for (int d = 0; d < 3; ++d)
-        if (sc.w[d]) atomicAdd(&A.rkw[g].W[d], sc.w[d]);
-    }
-  }
-  __syncthreads();
-  // the shared-memory sums to their roots' slots (this tile is their only writer)
-  for (int i = tid; i < nacc; i += THREADS) {
-    const unsigned* a = acc + i * TILE_ACC;
-    const int g = gidx[i];
-    ulonglong2* S = reinterpret_cast<ulonglong2*>(A.cls + 4 * (size_t)g);
-    S[0] = make_ulonglong2(((unsigned long long)a[4] << 32) | a[0], ((unsigned long long)a[5] << 32) | a[1]);
-    S[1] = make_ulonglong2(((unsigned long long)a[6] << 32) | a[2], ((unsigned long long)a[7] << 32) | a[3]);
-    const int wa = (int)a[8];
-    const int w0 = ((wa + 32768) & 0xFFFF) - 32768;
-    const int w1 = (wa - w0) / 65536;
-    *reinterpret_cast<int4*>(A.rkw[g].W) = make_int4(w0, w1, (int)a[9], 0);
-  }
-}
-
-// Global unions of the vertices k_tile left (both legs' sites not in one tile), and the list of
-// the roots they hook.  A frozen vertex also joins its own two legs (needed for the vertices of
-// tiles handled without shared memory; already true for the others).
-__device__ __forceinline__ int uf_union_hook(int* P, int a, int b, bool* ok) {
-  for (int it = 0; it < ITER_CAP; ++it) {
-    const int pa = __ldcg(P + a), pb = __ldcg(P + b);
-    a = uf_find_from(P, a, pa);
-    b = uf_find_from(P, b, pb);
-    if (a == b) return -1;
-    const int lo = a < b ? a : b, hi = a < b ? b : a;
-    const int old = atomicCAS(P + hi, hi, lo);
-    if (old == hi) return hi;
-    a = lo;
-    b = old;
-  }
-  *ok = false;
-  return -1;
-}
-
-__global__ void __launch_bounds__(256) k_union_ext(Arena A) {
-  if (A.ctl->err) return;
-  const int n = A.ctl->ext_n;
-  const int stride = gridDim.x * blockDim.x;
-  bool ok = true;
-  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
-    const int i = i0 + threadIdx.x;
-    int h0 = -1, h1 = -1, h2 = -1;
-    if (i < n) {
-      const int x = A.ext[i];
-      const uint8_t info = A.sinfo[x];
-      const int b = A.vslot[2 * A.svert[x] + 1];
-      const int g = (info >> SI_GSHIFT) & 3;
-      int* P = A.parent;
-      if (g == 1) {
-        h0 = uf_union_hook(P, x - 1, b, &ok);
-        h1 = uf_union_hook(P, b - 1, x, &ok);
-      } else {
-        h0 = uf_union_hook(P, x - 1, b - 1, &ok);
-        h1 = uf_union_hook(P, x, b, &ok);
-        if (g & 2) h2 = uf_union_hook(P, x - 1, x, &ok);
-      }
-    }
-    warp_append(A.hook, &A.ctl->hook_n, h0 >= 0, h0);
-    warp_append(A.hook, &A.ctl->hook_n, h1 >= 0, h1);
-    warp_append(A.hook, &A.ctl->hook_n, h2 >= 0, h2);
-  }
-  if (!ok) atomicExch(&A.ctl->err, ERR_ITERCAP);
-}
-
-__device__ __forceinline__ int uf_root(const int* P, int x) {
-  int p = __ldcg(P + x);
-  while (p != x) { x = p; p = __ldcg(P + x); }
-  return x;
-}
-
-// Every hooked root: parent := final root, and its sums move there.  Many hooked roots of one
-// giant cluster end at the same root, so the moves are combined before they reach global
-// memory: lanes of a warp with the same root are summed (match_any + redux, 16-bit limbs), and
-// each block keeps a shared-memory hash of (root, sums) over its contiguous share of the hook
-// list, flushed with one global atomic per word and entry.  Every segment of a tile handled
-// without shared memory: parent := final root, and its contribution goes there directly.
-constexpr int FIX_THREADS = 1024;
-constexpr int FIX_HASH = 2048;              // entries (power of two)
-constexpr int FIX_WORDS = 16;               // per entry: lo[4], hi[4] class sums, K[4], W[3]
-constexpr int FIX_SMEM = FIX_HASH * (FIX_WORDS + 1) * 4;
-
-__device__ __forceinline__ void fix_flush(const Arena& A, const int* key, const unsigned* val) {
-  for (int e = threadIdx.x; e < FIX_HASH; e += blockDim.x) {
-    const int r = key[e];
-    if (r < 0) continue;
-    const unsigned* v = val + e * FIX_WORDS;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const unsigned long long x = ((unsigned long long)v[4 + q] << 32) | v[q];
-      if (x) atomicAdd(A.cls + 4 * (size_t)r + q, x);
-    }
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (v[8 + q]) atomicAdd(&A.rkw[r].K[q], v[8 + q]);
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-      if (v[12 + d]) atomicAdd(&A.rkw[r].W[d], (int)v[12 + d]);
-  }
-}
-
-__global__ void __launch_bounds__(FIX_THREADS, 1) k_fix(Arena A) {
-  if (A.ctl->err) return;
-  extern __shared__ __align__(16) unsigned char fix_smem[];
-  int* key = reinterpret_cast<int*>(fix_smem);
-  unsigned* val = reinterpret_cast<unsigned*>(key + FIX_HASH);
-  __shared__ int s_used;
-  const int tid = threadIdx.x, lane = tid & 31;
-  const int nh = A.ctl->hook_n;
-  const int per = (nh + (int)gridDim.x - 1) / (int)gridDim.x;
-  const int ib = min(nh, (int)blockIdx.x * per), ie = min(nh, ib + per);
-  for (int e = tid; e < FIX_HASH; e += FIX_THREADS) key[e] = -1;
-  for (int e = tid; e < FIX_HASH * FIX_WORDS; e += FIX_THREADS) val[e] = 0u;
-  if (tid == 0) s_used = 0;
-  __syncthreads();
-  for (int i0 = ib; i0 < ie; i0 += FIX_THREADS) {
-    const int i = i0 + tid;
-    int r = -1;
-    unsigned long long S[4] = {0, 0, 0, 0};
-    unsigned K[4] = {0, 0, 0, 0};
-    int W[3] = {0, 0, 0};
-    if (i < ie) {
-      const int h = A.hook[i];
-      r = uf_root(A.parent, h);
-      A.parent[h] = r;
-      ulonglong2* Sp = reinterpret_cast<ulonglong2*>(A.cls + 4 * (size_t)h);
-      const ulonglong2 s0 = Sp[0], s1 = Sp[1];
-      const uint4 k = *reinterpret_cast<const uint4*>(A.rkw[h].K);
-      const int4 w = *reinterpret_cast<const int4*>(A.rkw[h].W);
-      S[0] = s0.x; S[1] = s0.y; S[2] = s1.x; S[3] = s1.y;
-      K[0] = k.x; K[1] = k.y; K[2] = k.z; K[3] = k.w;
-      W[0] = w.x; W[1] = w.y; W[2] = w.z;
-      const bool any_s = (s0.x | s0.y | s1.x | s1.y) != 0;
-      const bool any_kw = (k.x | k.y | k.z | k.w | (unsigned)w.x | (unsigned)w.y | (unsigned)w.z) != 0;
-      if (any_s) { Sp[0] = make_ulonglong2(0ull, 0ull); Sp[1] = make_ulonglong2(0ull, 0ull); }
-      if (any_kw) A.rkw[h] = RootKW{};
-      if (!any_s && !any_kw) r = -1;  // nothing to move
-    }
-    // lanes with the same root: one sum, added by the group's first lane
-    const unsigned grp = __match_any_sync(0xFFFFFFFFu, r);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) S[q] = group_sum_u64(grp, S[q]);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) K[q] = __reduce_add_sync(grp, K[q]);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) W[d] = (int)__reduce_add_sync(grp, (unsigned)W[d]);
-    if (r >= 0 && lane == __ffs(grp) - 1) {
-      unsigned hsh = ((unsigned)r * 2654435761u) >> (32 - 11);  // 11-bit hash
-      bool done = false;
-      for (int probe = 0; probe < 32; ++probe) {
-        int k = key[hsh];
-        if (k == -1) {
-          k = atomicCAS(key + hsh, -1, r);
-          if (k == -1) { atomicAdd(&s_used, 1); k = r; }
-        }
-        if (k == r) {
-          unsigned* v = val + hsh * FIX_WORDS;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (!S[q]) continue;
-            const unsigned lo = (unsigned)S[q], hi = (unsigned)(S[q] >> 32);
-            const unsigned old = atomicAdd(v + q, lo);
-            const unsigned carry = (old + lo < old) ? 1u : 0u;
-            if (hi + carry) atomicAdd(v + 4 + q, hi + carry);
-          }
-#pragma unroll
-          for (int q = 0; q < 4; ++q) if (K[q]) atomicAdd(v + 8 + q, K[q]);
-#pragma unroll
-          for (int d = 0; d < 3; ++d) if (W[d]) atomicAdd(v + 12 + d, (unsigned)W[d]);
-          done = true;
-          break;
-        }
-        hsh = (hsh + 1) & (FIX_HASH - 1);
-      }
-      if (!done) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) if (S[q]) atomicAdd(A.cls + 4 * (size_t)r + q, S[q]);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) if (K[q]) atomicAdd(&A.rkw[r].K[q], K[q]);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) if (W[d]) atomicAdd(&A.rkw[r].W[d], W[d]);
-      }
-    }
-    __syncthreads();
-    if (s_used > FIX_HASH / 2) {  // block-uniform: flush and clear a filling hash
-      fix_flush(A, key, val);
-      __syncthreads();
-      for (int e = tid; e < FIX_HASH; e += FIX_THREADS) key[e] = -1;
-      for (int e = tid; e < FIX_HASH * FIX_WORDS; e += FIX_THREADS) val[e] = 0u;
-      if (tid == 0) s_used = 0;
-      __syncthreads();
-    }
-  }
-  fix_flush(A, key, val);
-  const int stride = gridDim.x * blockDim.x;
-  const int no = A.ctl->ovf_n;
-  for (int o = 0; o < no; ++o) {
-    const int t = A.ovf[o];
-    for (int q = A.tile_run_off[t]; q < A.tile_run_off[t + 1]; ++q) {
-      const int g0 = A.sbase[A.run_lo[q]], g1 = A.sbase[A.run_hi[q]];
-      for (int x = g0 + blockIdx.x * blockDim.x + threadIdx.x; x < g1; x += stride) {
-        const int r = uf_root(A.parent, x);
-        if (r != x) A.parent[x] = r;
-        const uint8_t info = A.sinfo[x];
-        const bool last = info & SI_LAST;
-        const SegContrib sc = seg_contrib(info, last ? 0 : A.sinfo[x + 1], A.stime[x],
-                                          last ? 0ull : A.stime[x + 1], A.sdir[x],
-                                          last ? 0 : A.sdir[x + 1]);
-        if (info & SI_FIRST) atomicAdd(&A.rkw[r].K[sc.q], 1u);
-        if (sc.len) atomicAdd(A.cls + 4 * (size_t)r + sc.q, sc.len);
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-          if (sc.w[d]) atomicAdd(&A.rkw[r].W[d], sc.w[d]);
-      }
-    }
-  }
-}
-
-// Root of segment x: after k_accumulate every parent is a root; after k_fix a parent is a root or
-// a root hooked by k_union_ext, whose parent is the root.
-__device__ __forceinline__ int seg_root(const int* P, int x) {
-  int p = P[x], q = P[p];
-  while (q != p) { p = q; q = P[p]; }
-  return p;
-}
+// Root of segment x (after k_accumulate every parent is a root).
+__device__ __forceinline__ int seg_root(const int* P, int x) { return P[x]; }
 
 // Per site (one warp each): flip the tau = 0 spin with its bottom segment's cluster
 // (path_integral.C:822-823) and keep, in time order and in place at the start of the site's
@@ -1990,7 +1504,7 @@ __device__ __forceinline__ int seg_root(const int* P, int x) {
 // are the clusters of the segments below and above it: g = 0 joins the two lower legs and the
 // two upper legs, g = 1 crosses them, and a frozen graph has all four legs in one cluster.  So
 // the new type at endpoint x is its old type ^ flip(cluster of x-1) ^ flip(cluster of x), the
-// same at both of its sites.  Every lane reads its chunk before any lane writes, and a kept
+// same at both of its sites.  Every lane reads its step's segments before any lane writes, and a kept
 // endpoint never moves forward, so the in-place compaction reads no overwritten slot.
 __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
@@ -2002,34 +1516,44 @@ __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int
     const int k = A.sbase[s + 1] - base - 1;
     const uint8_t fb = A.flip[seg_root(A.parent, base)];
     if (lane == 0 && fb) A.spin0[s] ^= 1u;
-    uint8_t below = fb;   // flip of the cluster under the chunk's first segment
+    uint8_t below = fb;   // flip of the cluster under the step's first segment
     int n = 0;
-    for (int j0 = 1; j0 <= k; j0 += 32) {
-      const int j = j0 + lane;
-      const int x = base + j;
-      uint8_t fx = 0, info = 0;
-      if (j <= k) {
-        info = A.sinfo[x];
-        fx = A.flip[seg_root(A.parent, x)];
-      }
-      uint8_t fprev = (uint8_t)__shfl_up_sync(0xFFFFFFFFu, (unsigned)fx, 1);
-      if (lane == 0) fprev = below;
-      below = (uint8_t)__shfl_sync(0xFFFFFFFFu, (unsigned)fx, 31);
-      bool keep = false;
-      uint64_t t = 0;
-      uint8_t d = 0;
-      if (j <= k) {
-        keep = (((info & SI_OFF) ? 1u : 0u) ^ fprev ^ fx) != 0;
-        if (keep) { t = A.stime[x]; d = A.sdir[x] & 7; }  // the list keeps the incidence index
-      }
-      const unsigned ball = __ballot_sync(0xFFFFFFFFu, keep);
+    // 64 segments per step (two per lane), every load of the step issued before any use
+    for (int j0 = 1; j0 <= k; j0 += 64) {
+      const int ja = j0 + lane, jb = ja + 32;
+      uint8_t ia = 0, ib = 0, fa = 0, fbb = 0;
+      int pa = 0, pb = 0;
+      if (ja <= k) { ia = A.sinfo[base + ja]; pa = A.parent[base + ja]; }
+      if (jb <= k) { ib = A.sinfo[base + jb]; pb = A.parent[base + jb]; }
+      if (ja <= k) fa = A.flip[pa];
+      if (jb <= k) fbb = A.flip[pb];
+      uint8_t prev_a = (uint8_t)__shfl_up_sync(0xFFFFFFFFu, (unsigned)fa, 1);
+      uint8_t prev_b = (uint8_t)__shfl_up_sync(0xFFFFFFFFu, (unsigned)fbb, 1);
+      const uint8_t top_a = (uint8_t)__shfl_sync(0xFFFFFFFFu, (unsigned)fa, 31);
+      if (lane == 0) { prev_a = below; prev_b = top_a; }
+      below = (uint8_t)__shfl_sync(0xFFFFFFFFu, (unsigned)fbb, 31);
+      const bool ka = ja <= k && ((((ia & SI_OFF) ? 1u : 0u) ^ prev_a ^ fa) != 0);
+      const bool kb = jb <= k && ((((ib & SI_OFF) ? 1u : 0u) ^ prev_b ^ fbb) != 0);
+      uint64_t ta = 0, tb = 0;
+      uint8_t da = 0, db = 0;
+      if (ka) { ta = A.stime[base + ja]; da = A.sdir[base + ja] & 7; }  // the list keeps the
+      if (kb) { tb = A.stime[base + jb]; db = A.sdir[base + jb] & 7; }  // incidence index
+      const unsigned balla = __ballot_sync(0xFFFFFFFFu, ka);
+      const unsigned ballb = __ballot_sync(0xFFFFFFFFu, kb);
       __syncwarp();
-      if (keep) {
-        const int pos = n + __popc(ball & ((1u << lane) - 1u));
-        A.stime[base + pos] = t;
-        A.sdir[base + pos] = d;
+      const unsigned lt = (1u << lane) - 1u;
+      if (ka) {
+        const int pos = n + __popc(balla & lt);
+        A.stime[base + pos] = ta;
+        A.sdir[base + pos] = da;
       }
-      n += __popc(ball);
+      n += __popc(balla);
+      if (kb) {
+        const int pos = n + __popc(ballb & lt);
+        A.stime[base + pos] = tb;
+        A.sdir[base + pos] = db;
+      }
+      n += __popc(ballb);
       __syncwarp();
     }
     if (lane == 0) { A.off_base[s] = base; A.off_cnt[s] = n; }
@@ -2079,12 +1603,7 @@ __global__ void __launch_bounds__(1024) k_end(Arena A) {
       A.rec[((size_t)step + 1) * A.C * REC_WORDS + i] = 0ull;
   for (int r = threadIdx.x; r < A.R; r += blockDim.x) A.region_fill[r] = 0ull;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    A.ctl->step = step + 1u;
-    A.ctl->ext_n = 0;
-    A.ctl->hook_n = 0;
-    A.ctl->ovf_n = 0;
-  }
+  if (threadIdx.x == 0) A.ctl->step = step + 1u;
 }
 
 // Moving chains into a new arena: site s of the new arena takes the state of site map[s] of

@@ -29,7 +29,7 @@ double server_now(std::chrono::steady_clock::time_point t0) {
 // tables and persistent state (the figures follow Engine::build / alloc_dynamic).
 double chain_bytes(const ChainSpec& s) {
   const double nv = 1.3 * s.expected_vertices() + 64;
-  const double per_vertex = 21.0 + 2 * (23.0 + 48.0 + 16.0);  // vertex + its 2 segments
+  const double per_vertex = 17.0 + 2 * (19.0 + 48.0 + 16.0);  // vertex + its 2 segments
   const double per_site = 64.0;
   return nv * per_vertex + (double)s.N * per_site + (double)s.NB * 24.0;
 }

@@ -41,12 +41,7 @@ struct Ctl {
   uint32_t step;     // record row of the current sweep
   int nv_cap;
   int ns_cap;
-  // tile union-find lists of the current sweep (cleared by k_end): vertices left for the global
-  // pass, roots that pass hooked, tiles too large for shared memory
-  int ext_n;
-  int hook_n;
-  int ovf_n;
-  int pad[3];
+  int pad[2];
 };
 
 }  // namespace lg

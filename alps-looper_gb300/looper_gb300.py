@@ -65,12 +65,11 @@ class Shape(ctypes.Structure):
     """Launch shape of an arena (lg_shape): changes speed only, never a result."""
     _fields_ = [("insert_k", ctypes.c_double), ("narrow_k", ctypes.c_double),
                 ("acc_tile", ctypes.c_int), ("cl_tile", ctypes.c_int),
-                ("union_warps", ctypes.c_int), ("tile_cap", ctypes.c_int)]
+                ("union_warps", ctypes.c_int), ("reserved", ctypes.c_int)]
 
     def as_dict(self):
         return {"insert_k": self.insert_k, "narrow_k": self.narrow_k, "acc_tile": self.acc_tile,
-                "cl_tile": self.cl_tile, "union_warps": self.union_warps,
-                "tile_cap": self.tile_cap}
+                "cl_tile": self.cl_tile, "union_warps": self.union_warps}
 
 
 class ServerStats(ctypes.Structure):

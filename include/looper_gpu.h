@@ -205,17 +205,14 @@ lg_chain* lg_batch_chain(lg_batch* b, int i);
  *   narrow_k     the same split for the per-site merge and list compaction
  *   acc_tile     segments per CTA of the cluster-sum accumulation: 512, 1024 or 2048
  *   cl_tile      segments per CTA of the cluster flip / estimator kernel: 2048, 4096 or 8192
- *   union_warps  warps per CTA of the union-find kernel: 4, 8 or 16
- *   tile_cap     0: union-find and cluster sums over all segments in global memory (acc_tile and
- *                union_warps apply); 2048, 4096 or 8192: first inside lattice patches of up to
- *                that many segments in shared memory, then globally for what crosses patches */
+ *   union_warps  warps per CTA of the union-find kernel: 4, 8 or 16 */
 typedef struct lg_shape {
   double insert_k;
   double narrow_k;
   int acc_tile;
   int cl_tile;
   int union_warps;
-  int tile_cap;
+  int reserved;
 } lg_shape;
 
 /* Autotuner: times trial_sweeps sweeps per candidate shape (device events, flush_bytes of L2

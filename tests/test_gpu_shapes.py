@@ -1,9 +1,8 @@
 """Launch shapes and the autotuner change speed only, never a result.
 
 A shape picks, per arena, which chains run insertion / merge / list compaction with a thread per
-bond or site ("narrow") instead of a warp per site, the CTA sizes of the union-find, cluster
-sum and cluster flip kernels, and whether the union-find and cluster sums run first inside
-lattice patches in shared memory (tile_cap > 0) or over all segments in global memory.  Every shape must give the same trajectories and the same exact
+bond or site ("narrow") instead of a warp per site, and the CTA sizes of the union-find, cluster
+sum and cluster flip kernels.  Every shape must give the same trajectories and the same exact
 per-sweep sums, so the arena below (chains of mixed lattices, temperatures, anisotropy and field,
 all smaller than one k_cluster tile so that the per-chain reductions of tiles spanning chains are
 exercised) is run under several shapes and compared bit for bit.
@@ -32,12 +31,10 @@ MODELS = [
 ]
 
 SHAPES = [
-    dict(insert_k=0.0, narrow_k=0.0, tile_cap=0),                 # every chain warp-per-site
-    dict(insert_k=1e300, narrow_k=1e300, tile_cap=2048),          # every chain thread-per-site
-    dict(insert_k=1e300, narrow_k=10.0, acc_tile=512, cl_tile=2048, union_warps=4, tile_cap=0),
-    dict(insert_k=10.0, narrow_k=32.0, acc_tile=2048, cl_tile=8192, union_warps=16, tile_cap=0),
-    dict(insert_k=10.0, narrow_k=10.0, tile_cap=4096),
-    dict(insert_k=0.0, narrow_k=1e300, cl_tile=2048, tile_cap=8192),
+    dict(insert_k=0.0, narrow_k=0.0),                             # every chain warp-per-site
+    dict(insert_k=1e300, narrow_k=1e300),                         # every chain thread-per-site
+    dict(insert_k=1e300, narrow_k=10.0, acc_tile=512, cl_tile=2048, union_warps=4),
+    dict(insert_k=10.0, narrow_k=32.0, acc_tile=2048, cl_tile=8192, union_warps=16),
 ]
 
 
@@ -90,9 +87,6 @@ def test_bad_shape_is_rejected(lg):
     with pytest.raises(lg.LoopError) as e:
         b.shape = dict(acc_tile=300)
     assert e.value.code == -1
-    with pytest.raises(lg.LoopError) as e:
-        b.shape = dict(tile_cap=1000)
-    assert e.value.code == -1
     b.close()
 
 
@@ -101,7 +95,7 @@ def test_autotune_keeps_the_trajectory(lg):
     shape, report = b1.autotune(trial_sweeps=2)
     assert "chosen:" in report
     assert shape["acc_tile"] in (512, 1024, 2048) and shape["cl_tile"] in (2048, 4096, 8192)
-    assert shape["union_warps"] in (4, 8, 16) and shape["tile_cap"] in (0, 2048, 4096, 8192)
+    assert shape["union_warps"] in (4, 8, 16)
     total_sites, site_sweeps = b1.stats()
     done = site_sweeps // total_sites
     assert done >= 2
