@@ -119,6 +119,11 @@ struct Engine {
   DBuf<RootKW> d_rkw;
   DBuf<unsigned long long> d_rec;
   DBuf<Ctl> d_ctl;
+  // spin correlations: k_corr work tiles and the per-chunk exact sums (arena site indexed)
+  int n_corr_tiles = 0, corr_smem = 0;
+  DBuf<int2> d_corr_tiles;
+  DBuf<long long> d_corr_disp, d_corr_origin;
+  std::vector<long long> h_corr;
 
   int nv_cap = 0, ns_cap = 0;
   int rec_rows = 64;
@@ -176,6 +181,7 @@ struct Engine {
     A.stime = d_stime.p; A.sinfo = d_sinfo.p; A.svert = d_svert.p; A.sdir = d_sdir.p;
     A.parent = d_parent.p; A.flip = d_flip.p; A.cls = d_cls.p; A.rkw = d_rkw.p; A.inc_dir = d_inc_dir.p;
     A.rec = d_rec.p; A.ctl = d_ctl.p; A.rec_rows = rec_rows;
+    A.corr_tiles = d_corr_tiles.p; A.corr_disp = d_corr_disp.p; A.corr_origin = d_corr_origin.p;
     return A;
   }
 
@@ -195,6 +201,7 @@ struct Engine {
     LG_CUDA(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
     LG_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     LG_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    LG_CUDA(cudaFuncSetAttribute(k_corr, cudaFuncAttributeMaxDynamicSharedMemorySize, CORR_SMEM));
     // static tables
     long long nsite = 0, nbond = 0;
     for (auto& s : spec) { nsite += s.N; nbond += s.NB; }
@@ -281,6 +288,7 @@ struct Engine {
     LG_CUDA(cudaMemcpy(d_sweep.p, sw.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice));
     // vertex regions and per-sweep buffers from the expected operator count
     LG_CUDA(cudaMemset(d_ctl.p, 0, sizeof(Ctl)));
+    if ((rc = build_corr())) return rc;
     if ((rc = build_regions())) return rc;
     if ((rc = alloc_dynamic(region_total, false))) return rc;
     set_merge_cap();
@@ -299,6 +307,35 @@ struct Engine {
         LG_CUDA(cudaMemcpyAsync(d_spin0.p + hch[c].site_off, sp.data(), sp.size(), cudaMemcpyHostToDevice, st));
       }
     LG_CUDA(cudaStreamSynchronize(st));
+    return LG_OK;
+  }
+
+  // Spin correlation work (k_corr): one tile per CORR_THREADS entries of every chain that
+  // measures correlations or the structure factor; zeroed sum arrays.
+  int build_corr() {
+    std::vector<int2> tiles;
+    bool disp = false, orig = false;
+    int maxn = 0;
+    for (int c = 0; c < C; ++c) {
+      const DChain& d = hch[c];
+      if (!d.corr_disp && d.corr_origin < 0) continue;
+      disp |= d.corr_disp != 0;
+      orig |= d.corr_origin >= 0;
+      maxn = std::max(maxn, d.nsites);
+      for (int r0 = 0; r0 < d.nsites; r0 += CORR_THREADS) tiles.push_back(make_int2(c, r0));
+    }
+    n_corr_tiles = (int)tiles.size();
+    corr_smem = maxn <= CORR_SMEM ? maxn : 0;
+    if (!n_corr_tiles) return LG_OK;
+    int rc;
+    if ((rc = d_corr_tiles.alloc(tiles.size())) || (rc = d_corr_disp.alloc(disp ? N : 0)) ||
+        (rc = d_corr_origin.alloc(orig ? N : 0)))
+      return rc;
+    LG_CUDA(cudaMemcpy(d_corr_tiles.p, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    if (disp) LG_CUDA(cudaMemset(d_corr_disp.p, 0, (size_t)N * sizeof(long long)));
+    if (orig) LG_CUDA(cudaMemset(d_corr_origin.p, 0, (size_t)N * sizeof(long long)));
+    if (!disp) d_corr_disp.n = 0;
+    if (!orig) d_corr_origin.n = 0;
     return LG_OK;
   }
 
@@ -605,6 +642,10 @@ struct Engine {
       ++launches;
     }
     join();
+    if (n_corr_tiles) {
+      k_corr<<<n_corr_tiles, CORR_THREADS, corr_smem, st>>>(A);
+      ++launches;
+    }
     k_end<<<1, 1024, 0, st>>>(A);
     mark(6);
     launches += 1;
@@ -660,7 +701,7 @@ struct Engine {
       if (done > 0) {
         hrec.resize((size_t)done * C * REC_WORDS);
         LG_CUDA(cudaMemcpy(hrec.data(), d_rec.p, hrec.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
-        consume(done);
+        if ((rc = consume(done))) return rc;
         if (ms)
           for (int i = 0; i < done; ++i)
             LG_CUDA(cudaEventElapsedTime(&ms[done_total + i], ev[2 * i], ev[2 * i + 1]));
@@ -718,7 +759,7 @@ struct Engine {
       verts += (hc.ns_total - N) / 2;  // every vertex adds a segment at each of its two sites
       hrec.resize((size_t)C * REC_WORDS);
       LG_CUDA(cudaMemcpy(hrec.data(), d_rec.p, hrec.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
-      consume(1);
+      if (int rc = consume(1)) return rc;
       Ctl z = hc;
       z.step = 0;
       LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
@@ -809,18 +850,43 @@ struct Engine {
     return set_shape(best);
   }
 
-  void consume(int rows) {
+  // Host side of a finished chunk of `rows` sweeps: records into the accumulators, then the
+  // chunk's correlation sums (k_corr adds only measurement sweeps) into the vector accumulators.
+  int consume(int rows) {
+    std::vector<int64_t> measured(n_corr_tiles ? C : 0, 0);
     for (int r = 0; r < rows; ++r) {
       for (int c = 0; c < C; ++c) {
         const uint64_t* rec = hrec.data() + ((size_t)r * C + c) * REC_WORDS;
         ChainSpec& s = spec[c];
         if (keep_records && c == 0) kept.insert(kept.end(), rec, rec + REC_WORDS);
         s.last_nop = rec[R_NOP];
-        if (s.mcs >= (uint64_t)s.therm && s.mcs < (uint64_t)(s.therm + s.sweeps))
+        if (s.mcs >= (uint64_t)s.therm && s.mcs < (uint64_t)(s.therm + s.sweeps)) {
           acc[acc_of_chain[c]].push(s, rec);
+          if (n_corr_tiles) ++measured[c];
+        }
         ++s.mcs;
       }
     }
+    if (!n_corr_tiles) return LG_OK;
+    bool any = false;
+    for (int64_t m : measured) any |= m > 0;
+    if (!any) return LG_OK;
+    for (int which = 0; which < 2; ++which) {
+      DBuf<long long>& d = which ? d_corr_origin : d_corr_disp;
+      if (!d.n) continue;
+      h_corr.resize(N);
+      LG_CUDA(cudaMemcpy(h_corr.data(), d.p, (size_t)N * sizeof(long long), cudaMemcpyDeviceToHost));
+      LG_CUDA(cudaMemsetAsync(d.p, 0, (size_t)N * sizeof(long long), st));
+      for (int c = 0; c < C; ++c) {
+        const bool on = which ? hch[c].corr_origin >= 0 : hch[c].corr_disp != 0;
+        if (!on || !measured[c]) continue;
+        ChainAcc& a = acc[acc_of_chain[c]];
+        (which ? a.corr_origin : a.corr_disp)
+            .add_chunk(reinterpret_cast<const int64_t*>(h_corr.data()) + hch[c].site_off, hch[c].nsites,
+                       measured[c]);
+      }
+    }
+    return LG_OK;
   }
 
   // ---- state access (test seams, checkpoints) ----
@@ -1158,6 +1224,120 @@ double lg_progress(const lg_chain* c) {
 int lg_observables(lg_chain* c, lg_obs* out) {
   if (!c || !out) return lg_fail(LG_EINVAL, "null argument");
   c->eng->acc[c->index].report(c->eng->spec[c->index], out);
+  return LG_OK;
+}
+
+// Real part of the discrete Fourier transform sum_r e^{i k.r} f(r) over a periodic L^dim grid
+// (site order x fastest), one dimension at a time: O(N L dim).
+static void grid_dft(int dim, int L, const std::vector<double>& f, std::vector<double>& out) {
+  const int N = (int)f.size();
+  std::vector<double> re(f), im(N, 0.0), tr(N), ti(N);
+  std::vector<double> cs(L), sn(L);
+  for (int t = 0; t < L; ++t) {
+    const double a = 2.0 * M_PI * (double)t / (double)L;
+    cs[t] = std::cos(a);
+    sn[t] = std::sin(a);
+  }
+  int stride = 1;
+  for (int d = 0; d < dim; ++d) {
+    for (int i = 0; i < N; ++i) {
+      const int x = (i / stride) % L, base = i - x * stride;
+      double sr = 0, si = 0;
+      for (int y = 0; y < L; ++y) {  // k_x = x, r_x = y: phase 2 pi x y / L
+        const int t = (int)(((long long)x * y) % L);
+        const double vr = re[base + y * stride], vi = im[base + y * stride];
+        sr += vr * cs[t] - vi * sn[t];
+        si += vr * sn[t] + vi * cs[t];
+      }
+      tr[i] = sr;
+      ti[i] = si;
+    }
+    re.swap(tr);
+    im.swap(ti);
+    stride *= L;
+  }
+  out = re;
+}
+
+int lg_correlations(lg_chain* c, int kind, double* mean, double* err) {
+  if (!c || !mean) return lg_fail(LG_EINVAL, "null argument");
+  const Engine& e = *c->eng;
+  const ChainSpec& s = e.spec[c->index];
+  const ChainAcc& a = e.acc[c->index];
+  const int N = s.N;
+  std::vector<double> m, er;
+  if (kind == LG_CORR_SPIN || kind == LG_CORR_STAGGERED) {
+    if (!s.measure_corr) return lg_fail(LG_EINVAL, "the chain does not measure correlations");
+    if (kind == LG_CORR_STAGGERED && !s.bipartite)
+      return lg_fail(LG_EINVAL, "staggered correlations need a bipartite lattice");
+    const bool origin = s.corr_origin >= 0;
+    (origin ? a.corr_origin : a.corr_disp).mean_err(m, er);
+    if ((int)m.size() != N) { m.assign(N, NAN); er.assign(N, NAN); }
+    // correlation.h:243-264: 1/4 (1-2s)(1-2s'), times 1/N pairs per displacement without origin
+    const double f = origin ? 0.25 : 0.25 / N;
+    for (int i = 0; i < N; ++i) {
+      double g = 1.0;
+      if (kind == LG_CORR_STAGGERED)
+        g = origin ? (double)(s.gauge[s.corr_origin] * s.gauge[i]) : (double)s.gauge[i] * s.gauge[0];
+      mean[i] = f * g * m[i];
+      if (err) err[i] = f * er[i];
+    }
+    return LG_OK;
+  }
+  if (kind == LG_SFAC) {
+    if (!s.measure_sfac) return lg_fail(LG_EINVAL, "the chain does not measure the structure factor");
+    // S(k) = 1/N |sum_s (1/2 - s_s) e^{ik.r_s}|^2 (correlation.h:268-281) = sum_r e^{ik.r} C(r)
+    // with C(r) = 1/(4N) sum_i m_i m_{i+r}: the transform of the all-pairs sums, per sweep and so
+    // for the mean and for every bin mean
+    const VecAcc& v = a.corr_disp;
+    if ((int)v.sum.size() != N || v.count <= 0) {
+      for (int i = 0; i < N; ++i) { mean[i] = NAN; if (err) err[i] = NAN; }
+      return LG_OK;
+    }
+    std::vector<double> f(N), out;
+    for (int i = 0; i < N; ++i) f[i] = 0.25 * (double)v.sum[i] / (double)v.count / N;
+    grid_dft(s.dim, s.L, f, out);
+    for (int i = 0; i < N; ++i) mean[i] = out[i];
+    if (err) {
+      // bins merged into at most 32 groups for the error
+      const size_t B = v.bins.size();
+      const size_t G = std::min<size_t>(B, 32);
+      std::vector<double> var(N, 0.0);
+      int64_t tot = 0;
+      if (G >= 2) {
+        for (size_t g = 0; g < G; ++g) {
+          const size_t k0 = g * B / G, k1 = (g + 1) * B / G;
+          int64_t cnt = 0;
+          std::vector<double> fb(N, 0.0);
+          for (size_t k = k0; k < k1; ++k) {
+            cnt += v.bin_count[k];
+            for (int i = 0; i < N; ++i) fb[i] += (double)v.bins[k][i];
+          }
+          for (int i = 0; i < N; ++i) fb[i] = 0.25 * fb[i] / (double)cnt / N;
+          grid_dft(s.dim, s.L, fb, out);
+          for (int i = 0; i < N; ++i) var[i] += (double)cnt * (out[i] - mean[i]) * (out[i] - mean[i]);
+          tot += cnt;
+        }
+        for (int i = 0; i < N; ++i) err[i] = std::sqrt(var[i] / (double)tot / (double)(G - 1));
+      } else {
+        for (int i = 0; i < N; ++i) err[i] = NAN;
+      }
+    }
+    return LG_OK;
+  }
+  return lg_fail(LG_EINVAL, "unknown correlation kind %d", kind);
+}
+
+int lg_correlation_sums(lg_chain* c, int which, int64_t* sums, int64_t* nsweeps) {
+  if (!c || !sums) return lg_fail(LG_EINVAL, "null argument");
+  const Engine& e = *c->eng;
+  const ChainSpec& s = e.spec[c->index];
+  const ChainAcc& a = e.acc[c->index];
+  const bool on = which == 0 ? e.hch[c->index].corr_disp != 0 : e.hch[c->index].corr_origin >= 0;
+  if (which < 0 || which > 1 || !on) return lg_fail(LG_EINVAL, "the chain does not keep these sums");
+  const VecAcc& v = which ? a.corr_origin : a.corr_disp;
+  for (int i = 0; i < s.N; ++i) sums[i] = (int)v.sum.size() == s.N ? v.sum[i] : 0;
+  if (nsweeps) *nsweeps = v.count;
   return LG_OK;
 }
 

@@ -30,6 +30,15 @@ extern "C" void lg_params_default(lg_params* p) {
   p->seed = 29833;
   p->init_spins = 0;
   p->disable_improved_estimator = 0;
+  p->measure_correlations = 0;
+  p->measure_structure_factor = 0;
+  p->initial_site = -1;
+}
+
+static bool parse_bool(const std::string& v, int* out) {
+  if (v == "1" || v == "true" || v == "True" || v == "TRUE") { *out = 1; return true; }
+  if (v == "0" || v == "false" || v == "False" || v == "FALSE") { *out = 0; return true; }
+  return false;
 }
 
 static std::string trim(std::string s) {
@@ -117,6 +126,14 @@ extern "C" int lg_params_parse(const char* text, lg_params* p) {
       else return lg_fail(LG_EINVAL, "INITIAL_SPINS must be up or random");
     } else if (key == "DISABLE_IMPROVED_ESTIMATOR") {
       p->disable_improved_estimator = (val == "0" || val == "false") ? 0 : 1;
+    } else if (key == "MEASURE[Correlations]") {
+      if (!parse_bool(val, &p->measure_correlations))
+        return lg_fail(LG_EINVAL, "MEASURE[Correlations] must be true or false");
+    } else if (key == "MEASURE[Structure Factor]") {
+      if (!parse_bool(val, &p->measure_structure_factor))
+        return lg_fail(LG_EINVAL, "MEASURE[Structure Factor] must be true or false");
+    } else if (key == "INITIAL_SITE") {
+      double d; rc = num(&d); p->initial_site = (int)d;
     }
     if (rc) return rc;
   }
@@ -206,7 +223,65 @@ int ChainSpec::init(const lg_params& p) {
   const double s01 = v[0] + v[1];
   dchain.Poff = prob32(s01 > 0 ? v[0] / s01 : 1.0);
   dchain.field = field ? 1 : 0;
+  // correlations (correlation.h:62-110): the structure factor needs the all-pairs sums; the
+  // correlations use them too unless INITIAL_SITE picks one origin
+  if (p.initial_site >= N)
+    return lg_fail(LG_EINVAL, "INITIAL_SITE %d out of range (%d sites)", p.initial_site, N);
+  measure_corr = p.measure_correlations != 0;
+  measure_sfac = p.measure_structure_factor != 0;
+  corr_origin = (measure_corr && p.initial_site >= 0) ? p.initial_site : -1;
+  dchain.dim = dim;
+  dchain.L = L;
+  dchain.corr_disp = (measure_sfac || (measure_corr && corr_origin < 0)) ? 1 : 0;
+  dchain.corr_origin = corr_origin;
+  dchain.corr_from = (uint32_t)std::min<int64_t>(therm, 0xFFFFFFFFll);
+  dchain.corr_to = (uint32_t)std::min<int64_t>(therm + sweeps, 0xFFFFFFFFll);
   return set_beta(b);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Vector observables: exact integer sums per chunk of sweeps, rebinned
+// ---------------------------------------------------------------------------------------------
+void VecAcc::add_chunk(const int64_t* s, int n, int64_t sweeps) {
+  if (sweeps <= 0) return;
+  if ((int)sum.size() != n) { sum.assign(n, 0); bins.clear(); bin_count.clear(); count = 0; }
+  std::vector<int64_t> b(s, s + n);
+  for (int i = 0; i < n; ++i) sum[i] += s[i];
+  count += sweeps;
+  bins.push_back(std::move(b));
+  bin_count.push_back(sweeps);
+  if (bins.size() >= 128) {  // merge neighbouring bins: at most 64 remain
+    std::vector<std::vector<int64_t>> nb;
+    std::vector<int64_t> nc;
+    for (size_t k = 0; k + 1 < bins.size(); k += 2) {
+      std::vector<int64_t> m = bins[k];
+      for (int i = 0; i < n; ++i) m[i] += bins[k + 1][i];
+      nb.push_back(std::move(m));
+      nc.push_back(bin_count[k] + bin_count[k + 1]);
+    }
+    if (bins.size() % 2) { nb.push_back(bins.back()); nc.push_back(bin_count.back()); }
+    bins.swap(nb);
+    bin_count.swap(nc);
+  }
+}
+
+// Mean per sweep and the standard error from the spread of the bin means (count-weighted).
+void VecAcc::mean_err(std::vector<double>& mean, std::vector<double>& err) const {
+  const int n = (int)sum.size();
+  mean.assign(n, NAN);
+  err.assign(n, NAN);
+  if (count <= 0) return;
+  for (int i = 0; i < n; ++i) mean[i] = (double)sum[i] / (double)count;
+  const size_t B = bins.size();
+  if (B < 2) return;
+  for (int i = 0; i < n; ++i) {
+    double v = 0;
+    for (size_t k = 0; k < B; ++k) {
+      const double d = (double)bins[k][i] / (double)bin_count[k] - mean[i];
+      v += (double)bin_count[k] * d * d;
+    }
+    err[i] = std::sqrt(v / (double)count / (double)(B - 1));
+  }
 }
 
 int ChainSpec::set_beta(double b) {

@@ -23,6 +23,8 @@ struct ChainSpec {
   uint64_t last_nop = 0;
   int init_spins = 0;
   bool field = false, improved = true;
+  bool measure_corr = false, measure_sfac = false;
+  int corr_origin = -1;
   lg::DChain dchain{};
 
   int init(const lg_params& p);
@@ -46,8 +48,21 @@ enum {
   RAW_GM2, RAW_GCHI, RAW_NC, RAW_NOP, RAW_STIFF, NUM_RAW
 };
 
+// Exact integer sums of a vector observable over chunks of sweeps, kept as up to 128 bins
+// (neighbouring bins merge when full).
+struct VecAcc {
+  std::vector<int64_t> sum;
+  int64_t count = 0;
+  std::vector<std::vector<int64_t>> bins;
+  std::vector<int64_t> bin_count;
+  void add_chunk(const int64_t* s, int n, int64_t sweeps);
+  void mean_err(std::vector<double>& mean, std::vector<double>& err) const;
+};
+
 struct ChainAcc {
   BinAcc raw[NUM_RAW];
+  VecAcc corr_disp;    // sum_i m_i m_{i+r} per displacement r
+  VecAcc corr_origin;  // m_o m_j per site j
   void push(const ChainSpec& s, const uint64_t* rec);
   void report(const ChainSpec& s, lg_obs* out) const;
 };

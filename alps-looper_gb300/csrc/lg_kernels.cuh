@@ -103,6 +103,11 @@ struct Arena {
   unsigned long long* rec;  // [rows][C][REC_WORDS]
   Ctl* ctl;
   int rec_rows;             // rows of rec
+  // spin correlations (k_corr): work tiles (chain, first entry) and the exact sums per chain
+  // entry (arena site index), added over the measured sweeps of the current chunk
+  const int2* corr_tiles;
+  long long* corr_disp;     // sum_i m_i m_{i+r}, entry r of the chain
+  long long* corr_origin;   // m_o m_j, entry j of the chain
 };
 
 #define LG_GRID_STRIDE(i, n) \
@@ -1584,6 +1589,53 @@ __global__ void __launch_bounds__(256) k_site_end_narrow(Arena A, const int* sit
     A.off_base[s] = base;
     A.off_cnt[s] = n;
   }
+}
+
+// Spin correlations from the tau = 0 spins after the flips (the normal estimator of
+// correlation.h:222-266, which reads `spins` at commit time).  One block per tile of
+// CORR_THREADS entries of one chain; the chain's spins are staged in shared memory (up to
+// CORR_SMEM sites; larger chains read them from global memory).  Entry r of the all-pairs sums
+// is sum_i m_i m_{i+r} over every site i, i + r taken with periodic wrap per dimension and
+// m = 1 - 2 s, an exact integer; with an origin o, entry j adds m_o m_j.  Only sweeps in the
+// chain's measurement window [corr_from, corr_to) are added.
+constexpr int CORR_THREADS = 256;
+constexpr int CORR_SMEM = 64 * 1024;
+
+__global__ void __launch_bounds__(CORR_THREADS) k_corr(Arena A) {
+  if (A.ctl->err) return;
+  extern __shared__ uint8_t corr_sp[];
+  const int2 tl = A.corr_tiles[blockIdx.x];
+  const int c = tl.x;
+  const DChain ch = A.ch[c];
+  const uint32_t sw = A.ch_sweep[c];
+  if (sw < ch.corr_from || sw >= ch.corr_to) return;
+  const int N = ch.nsites, so = ch.site_off, L = ch.L;
+  const uint8_t* sp = A.spin0 + so;
+  if (N <= CORR_SMEM) {
+    for (int i = threadIdx.x; i < N; i += CORR_THREADS) corr_sp[i] = A.spin0[so + i];
+    __syncthreads();
+    sp = corr_sp;
+  }
+  const int r = tl.y + threadIdx.x;
+  if (r >= N) return;
+  if (ch.corr_origin >= 0)
+    A.corr_origin[so + r] += (sp[ch.corr_origin] == sp[r]) ? 1 : -1;
+  if (!ch.corr_disp) return;
+  const int rx = r % L, ry = ch.dim > 1 ? (r / L) % L : 0, rz = ch.dim > 2 ? r / (L * L) : 0;
+  const int Ly = ch.dim > 1 ? L : 1, Lz = ch.dim > 2 ? L : 1;
+  int sum = 0;
+  for (int z = 0; z < Lz; ++z) {
+    const int jz = z + rz < Lz ? z + rz : z + rz - Lz;
+    for (int y = 0; y < Ly; ++y) {
+      const int jy = y + ry < Ly ? y + ry : y + ry - Ly;
+      const uint8_t* row = sp + (z * Ly + y) * L;
+      const uint8_t* jrow = sp + (jz * Ly + jy) * L;
+      int x = 0;
+      for (; x + rx < L; ++x) sum += row[x] == jrow[x + rx] ? 1 : -1;
+      for (; x < L; ++x) sum += row[x] == jrow[x + rx - L] ? 1 : -1;
+    }
+  }
+  A.corr_disp[so + r] += sum;
 }
 
 // One block: per chain the operator count and the sweep counter; then the next sweep's record

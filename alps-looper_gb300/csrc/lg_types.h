@@ -32,6 +32,11 @@ struct DChain {
   int field;
   int site_off, nsites;
   int bond_off, nbonds;
+  // spin correlations (correlation.h): all-pairs sums per displacement (corr_disp) and/or the
+  // products with site corr_origin (>= 0), added for sweeps in [corr_from, corr_to)
+  int dim, L;
+  int corr_disp, corr_origin;
+  uint32_t corr_from, corr_to;
 };
 
 struct Ctl {

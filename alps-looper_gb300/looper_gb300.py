@@ -41,7 +41,9 @@ class Params(ctypes.Structure):
                 ("Jxy", ctypes.c_double), ("h", ctypes.c_double),
                 ("force_scatter", ctypes.c_double), ("sweeps", ctypes.c_uint64),
                 ("thermalization", ctypes.c_int64), ("seed", ctypes.c_uint64),
-                ("init_spins", ctypes.c_int), ("disable_improved_estimator", ctypes.c_int)]
+                ("init_spins", ctypes.c_int), ("disable_improved_estimator", ctypes.c_int),
+                ("measure_correlations", ctypes.c_int), ("measure_structure_factor", ctypes.c_int),
+                ("initial_site", ctypes.c_int)]
 
 
 class Obs(ctypes.Structure):
@@ -103,6 +105,8 @@ def lib():
             "lg_save": (ctypes.c_int, [vp, vp, vp]),
             "lg_load": (ctypes.c_int, [vp, vp, ctypes.c_size_t]),
             "lg_set_beta": (ctypes.c_int, [vp, ctypes.c_double]),
+            "lg_correlations": (ctypes.c_int, [vp, ctypes.c_int, vp, vp]),
+            "lg_correlation_sums": (ctypes.c_int, [vp, ctypes.c_int, vp, vp]),
             "lg_weight_parameter": (ctypes.c_double, [vp]),
             "lg_log_weight": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
             "lg_last_error": (ctypes.c_int, [vp, ctypes.c_size_t]),
@@ -176,13 +180,15 @@ def _p(a):
 def make_params(**kw) -> Params:
     """Parameters with the worker's key names: LATTICE, L, T, BETA, J, Jz, Jxy, h, SWEEPS,
     THERMALIZATION, SEED, FORCE_SCATTER, INITIAL_SPINS, DISABLE_IMPROVED_ESTIMATOR (lower-case
-    aliases accepted)."""
+    aliases accepted), and the correlation switches MEASURE_CORRELATIONS (MEASURE[Correlations]),
+    MEASURE_STRUCTURE_FACTOR (MEASURE[Structure Factor]) and INITIAL_SITE."""
     p = Params()
     lib().lg_params_default(ctypes.byref(p))
     for k, v in kw.items():
         key = k.upper() if k.upper() in ("LATTICE", "BETA", "SWEEPS", "THERMALIZATION", "SEED",
                                          "FORCE_SCATTER", "INITIAL_SPINS",
-                                         "DISABLE_IMPROVED_ESTIMATOR") else k
+                                         "DISABLE_IMPROVED_ESTIMATOR", "MEASURE_CORRELATIONS",
+                                         "MEASURE_STRUCTURE_FACTOR", "INITIAL_SITE") else k
         if key == "LATTICE":
             p.lattice = LATTICES[v] if isinstance(v, str) else int(v)
         elif key == "L":
@@ -205,6 +211,12 @@ def make_params(**kw) -> Params:
             p.init_spins = 1 if v in ("random", 1, True) else 0
         elif key == "DISABLE_IMPROVED_ESTIMATOR":
             p.disable_improved_estimator = 1 if v else 0
+        elif key in ("MEASURE_CORRELATIONS", "MEASURE[Correlations]"):
+            p.measure_correlations = 1 if v else 0
+        elif key in ("MEASURE_STRUCTURE_FACTOR", "MEASURE[Structure Factor]"):
+            p.measure_structure_factor = 1 if v else 0
+        elif key == "INITIAL_SITE":
+            p.initial_site = int(v)
         else:
             raise KeyError(k)
     return p
@@ -279,6 +291,29 @@ class LoopWorker:
 
     def run(self, nsweeps: int = 1):
         check(lib().lg_run(self._h, int(nsweeps)))
+
+    CORR_KINDS = {"Spin Correlations": 0, "Staggered Spin Correlations": 1,
+                  "Spin Structure Factor": 2}
+
+    def correlations(self, kind="Spin Correlations"):
+        """(mean, error) arrays of N entries: "Spin Correlations", "Staggered Spin Correlations"
+        (entry i = displacement, or the site with INITIAL_SITE, of site index i) or "Spin
+        Structure Factor" (entry i = momentum 2 pi (x, y, z) / L of site index i)."""
+        k = self.CORR_KINDS[kind] if isinstance(kind, str) else int(kind)
+        n = self.num_sites()
+        mean = np.zeros(n)
+        err = np.zeros(n)
+        check(lib().lg_correlations(self._h, k, _p(mean), _p(err)))
+        return mean, err
+
+    def correlation_sums(self, which=0):
+        """Exact integer sums over the measured sweeps (which = 0: sum_i m_i m_{i+r} per
+        displacement r; 1: m_o m_j per site j for INITIAL_SITE o) and the sweep count."""
+        n = self.num_sites()
+        out = np.zeros(n, dtype=np.int64)
+        ns = ctypes.c_int64()
+        check(lib().lg_correlation_sums(self._h, int(which), _p(out), ctypes.byref(ns)))
+        return out, ns.value
 
     def is_thermalized(self) -> bool:
         return bool(lib().lg_is_thermalized(self._h))

@@ -64,6 +64,9 @@ typedef struct lg_params {
   uint64_t seed;                  /* SEED                                                        */
   int init_spins;                 /* 0: all up (path_integral.C:225), 1: iid from the seed      */
   int disable_improved_estimator; /* DISABLE_IMPROVED_ESTIMATOR                                  */
+  int measure_correlations;       /* MEASURE[Correlations] (correlation.h:66), default 0        */
+  int measure_structure_factor;   /* MEASURE[Structure Factor] (correlation.h:68), default 0    */
+  int initial_site;               /* INITIAL_SITE (correlation.h:87); < 0: all pairs (default)  */
 } lg_params;
 
 /* Fill defaults: chain, L=8, T=0.2, J=1, Jz=Jxy=NaN, h=0, SWEEPS=65536 (montecarlo.h:41),
@@ -73,7 +76,8 @@ void lg_params_default(lg_params* p);
 /* Parse ALPS-style "KEY = value" lines (';' or newline separated, '#' comments) into *p.
  * Keys: LATTICE ("chain lattice" | "square lattice" | "simple cubic lattice"), L, T, BETA, J,
  * Jz, Jxy, h, FORCE_SCATTER, SWEEPS, THERMALIZATION, SEED, INITIAL_SPINS ("up" | "random"),
- * DISABLE_IMPROVED_ESTIMATOR.  Unknown keys are ignored, as ALPS does for keys a worker does not
+ * DISABLE_IMPROVED_ESTIMATOR, MEASURE[Correlations], MEASURE[Structure Factor], INITIAL_SITE.
+ * Unknown keys are ignored, as ALPS does for keys a worker does not
  * read.  Returns LG_EINVAL with a message on a malformed value. */
 int lg_params_parse(const char* text, lg_params* p);
 
@@ -139,6 +143,28 @@ int lg_save(lg_chain* c, void* buf, size_t* size);
 int lg_load(lg_chain* c, const void* buf, size_t size);
 /* Exchange Monte Carlo hooks (path_integral.C:97-109). */
 int lg_set_beta(lg_chain* c, double beta);
+
+/* ---- spin correlations and structure factor (correlation.h:38-300) ------------------------
+ * The reference's normal estimator of looper::correlation, measured from the tau = 0 spins at
+ * the end of every measurement sweep (normal_estimator::collector::commit, correlation.h:
+ * 222-296).  A chain measures them when created with measure_correlations or
+ * measure_structure_factor.  Entry i of the N-entry vectors:
+ *   LG_CORR_SPIN       "Spin Correlations": the displacement with site index i, i.e.
+ *                      (x, y, z) = (i % L, (i / L) % L, i / L^2), averaged over all pairs
+ *                      (correlation.h:248-264, multiplicity 1/N); with INITIAL_SITE o, the pair
+ *                      (o, site i) (:236-247).  Value 1/4 <(1 - 2 s_a)(1 - 2 s_b)>.
+ *   LG_CORR_STAGGERED  "Staggered Spin Correlations": the same times the gauges of both sites.
+ *   LG_SFAC            "Spin Structure Factor" (:268-281): momentum k = 2 pi (x, y, z) / L with
+ *                      each component taken into (-pi, pi]; the Fourier transform of the
+ *                      all-pairs correlations (needs measure_structure_factor).
+ * mean and err (err may be NULL) receive N doubles; err is the binning error over the bins of
+ * up to 64 sweeps (the record chunks).  LG_EINVAL if the chain does not measure that kind. */
+enum { LG_CORR_SPIN = 0, LG_CORR_STAGGERED = 1, LG_SFAC = 2 };
+int lg_correlations(lg_chain* c, int kind, double* mean, double* err);
+/* Test seam: the exact integer sums behind the correlations.  which = 0: sums[r] over the
+ * measured sweeps of sum_i m_i m_{i+r} (all pairs, m = 1 - 2 s); which = 1: of m_o m_r (with
+ * INITIAL_SITE o).  N entries; *nsweeps receives the number of measured sweeps. */
+int lg_correlation_sums(lg_chain* c, int which, int64_t* sums, int64_t* nsweeps);
 double lg_weight_parameter(lg_chain* c);
 double lg_log_weight(double gw, double beta);
 /* Message of the last failure on this thread. */

@@ -13,6 +13,9 @@ diag.C:159-293:
   * Magnetization^2, ^4 of M = sum Sz                              (static_average4, :405-420)
   * Susceptibility = Kubo integral of M / Z / V                    (dynamic_average2, :421-424)
   * Staggered Magnetization^2 / Susceptibility with gauge (+1/-1)  (:433-462)
+  * Spin Correlations <Sz_0 Sz_r> per displacement r (site order) and the Spin Structure Factor
+    sum_r e^{ik.r} <Sz_0 Sz_r>, the exact values behind looper's correlation estimator
+    (correlation.h:222-281)
 
 The Kubo integral (dynamic_average2, diag.C:245-293) is evaluated within each sector, which is
 exact because both M and the staggered magnetization are diagonal in the Sz basis.
@@ -79,14 +82,16 @@ def thermal(dim: int, L: int, T: float, jxy: float = 1.0, jz: float = 1.0, h: fl
         H[np.arange(dimn), np.arange(dimn)] -= h * m
         ev, U = np.linalg.eigh(H)
         ms = sz @ gauge
-        sectors.append((ev, U, m, ms))
+        szz = sz[:, :1] * sz  # Sz_0 Sz_r per basis state
+        sectors.append((ev, U, m, ms, szz))
         e_min = min(e_min, ev[0])
 
     Z = E1 = E2 = 0.0
     M2 = M4 = Ms2 = Ms4 = 0.0
     M1 = 0.0
     chi = chis = 0.0
-    for ev, U, m, ms in sectors:
+    corr = np.zeros(N)
+    for ev, U, m, ms, szz in sectors:
         w = np.exp(-beta * (ev - e_min))
         Z += w.sum()
         E1 += (ev * w).sum()
@@ -98,11 +103,17 @@ def thermal(dim: int, L: int, T: float, jxy: float = 1.0, jz: float = 1.0, h: fl
         M4 += (w * (P.T @ m ** 4)).sum()
         Ms2 += (w * (P.T @ ms ** 2)).sum()
         Ms4 += (w * (P.T @ ms ** 4)).sum()
+        corr += (P.T @ szz).T @ w
         chi += _kubo(beta, ev, U, m, w, e_min)
         chis += _kubo(beta, ev, U, ms, w, e_min)
     E1 /= Z
     E2 /= Z
+    corr /= Z
+    sfac = np.real(np.fft.ifftn(corr.reshape((L,) * dim)) * N).reshape(-1)
     return {
+        "Spin Correlations": corr,
+        "Staggered Spin Correlations": corr * gauge * gauge[0],
+        "Spin Structure Factor": sfac,
         "Energy": E1,
         "Energy Density": E1 / vol,
         "Specific Heat": beta ** 2 * (E2 - E1 ** 2) / vol,

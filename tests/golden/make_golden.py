@@ -3,7 +3,8 @@
 Sources:
   * standalone/loop.op            -> standalone_loop_op.json   (deterministic standalone run)
   * test/union_find.op            -> union_find_op.json        (100 unions + full listing)
-  * loop.op (diag + PI blocks)    -> loop_op.json              (known answers, L=4 chains)
+  * loop.op (diag + PI blocks)    -> loop_op.json              (known answers, L=4 chains,
+                                                                  with the correlation vectors)
   * oracle (philox mode) configs  -> uf_labels.json            (cluster-construction configs)
     labelled by the reference's own looper/union_find.h, compiled in place by oracle/Makefile
     (oracle/_ref/uf_deterministic, oracle/_ref/uf_weighted).
@@ -55,6 +56,28 @@ def _block(lines, start, keys):
     return vals
 
 
+VECTORS = ["Spin Correlations", "Staggered Spin Correlations", "Spin Structure Factor"]
+
+
+def _vectors(lines, start):
+    """Vector observables of the block starting at `start`: name -> [[label, mean, error]...]
+    from the "Entry[label]: mean +/- error" lines after the name line."""
+    out = {}
+    cur = None
+    for ln in lines[start:]:
+        if ln.startswith("[input parameters]"):
+            break
+        if ln in VECTORS:
+            cur = out.setdefault(ln, [])
+            continue
+        m = re.match(r"Entry\[(.*)\]: (\S+) \+/- (\S+);", ln)
+        if m and cur is not None:
+            cur.append([m.group(1), float(m.group(2)), float(m.group(3))])
+        elif not ln.startswith("Entry[") and not ln.startswith("    bin"):
+            cur = None
+    return out
+
+
 def loop_op(ref):
     lines = open(os.path.join(ref, "loop.op")).read().splitlines()
     keys = ["Energy", "Specific Heat", "Magnetization^2", "Susceptibility",
@@ -80,9 +103,13 @@ def loop_op(ref):
         jz = re.findall(r"Jz = ([^;]+);", h)
         jxy = re.findall(r"Jxy = ([^;]+);", h)
         vals = _block(lines, i + 1, keys)
-        out.append({"algorithm": alg, "L": 4, "T": float(T[-1]),
-                    "jz": float(jz[-1]) if jz else 1.0, "jxy": float(jxy[-1]) if jxy else 1.0,
-                    "values": vals})
+        entry = {"algorithm": alg, "L": 4, "T": float(T[-1]),
+                 "jz": float(jz[-1]) if jz else 1.0, "jxy": float(jxy[-1]) if jxy else 1.0,
+                 "values": vals}
+        vec = _vectors(lines, i + 1)
+        if vec:
+            entry["vectors"] = vec
+        out.append(entry)
     return out
 
 

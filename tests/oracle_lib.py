@@ -248,3 +248,25 @@ def specific_heat(obs, beta, N, nbins=64):
     c = beta ** 2 * (e2b.mean() - eb.mean() ** 2) / N
     err = np.sqrt((nbins - 1) / nbins * ((jk - jk.mean()) ** 2).sum())
     return float(c), float(err)
+
+
+def correlation_sums(spins, dim, L, origin=-1):
+    """The exact integer behind looper's spin-correlation normal estimator for one tau = 0
+    configuration (correlation.h:222-266, before the 1/4 and multiplicity factors): with m = 1 - 2s,
+    entry r = x + L y + L^2 z is sum_i m_i m_{i+r} over all sites i (periodic displacement), or,
+    for an origin o, m_o m_r."""
+    m = 1 - 2 * np.asarray(spins, dtype=np.int64)
+    if origin >= 0:
+        return m[origin] * m
+    g = m.reshape((L,) * dim)  # axes (z, y, x): site = x + L y + L^2 z
+    out = np.zeros_like(g)
+    for idx in np.ndindex(*g.shape):
+        out[idx] = int((g * np.roll(g, tuple(-i for i in idx), axis=tuple(range(dim)))).sum())
+    return out.reshape(-1)
+
+
+def structure_factor(corr, dim, L):
+    """sum_r e^{ik.r} C(r) over the periodic grid (site order), k = 2 pi (x, y, z) / L: the
+    spin structure factor of correlation.h:268-281 from the displacement correlations."""
+    c = np.asarray(corr, dtype=np.float64).reshape((L,) * dim)
+    return np.real(np.fft.ifftn(c) * c.size).reshape(-1)

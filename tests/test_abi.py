@@ -55,6 +55,16 @@ def test_params_parse_alps_keys(lg):
     assert p.h == 0.3 and p.Jz == 0.5 and math.isnan(p.Jxy) and p.init_spins == 1
 
 
+def test_params_parse_correlation_switches(lg):
+    p = lg.make_params()
+    assert p.measure_correlations == 0 and p.measure_structure_factor == 0 and p.initial_site == -1
+    p = lg.parse_params("MEASURE[Correlations] = true; MEASURE[Structure Factor] = 1;\n"
+                        "INITIAL_SITE = 3")
+    assert p.measure_correlations == 1 and p.measure_structure_factor == 1 and p.initial_site == 3
+    with pytest.raises(lg.LoopError):
+        lg.parse_params("MEASURE[Correlations] = maybe")
+
+
 def test_params_parse_rejects_bad_values(lg):
     with pytest.raises(lg.LoopError) as e:
         lg.parse_params("L = abc")

@@ -93,6 +93,38 @@ def test_ed_matches_golden(golden):
             assert r[k] == pytest.approx(v, rel=2e-5, abs=2e-6), k
 
 
+def test_ed_correlations_agree_with_reference_path_integral(golden):
+    # loop.op: "loop; path integral" with MEASURE[Correlations] / MEASURE[Structure Factor],
+    # S=1/2 Heisenberg chain L=4, T=0.5, 4096 sweeps: the exact correlations must lie within
+    # 3 sigma of the reference's binned Monte Carlo values
+    blk = [b for b in golden("loop_op.json") if "vectors" in b]
+    assert len(blk) == 1
+    b = blk[0]
+    r = orc.ed.thermal(1, b["L"], b["T"], jxy=b["jxy"], jz=b["jz"])
+    for name, entries in b["vectors"].items():
+        assert len(entries) == 4
+        for (label, mean, err), exact in zip(entries, r[name]):
+            assert abs(mean - exact) <= 3 * err + 1e-6, (name, label, mean, err, exact)
+
+
+def test_correlation_sums_restatement():
+    # all up: every product is +1; a Neel state on an even chain: (-1)^r; the origin form
+    up = np.zeros(16, dtype=np.int32)
+    assert orc.correlation_sums(up, 2, 4).tolist() == [16] * 16
+    neel = np.array([i % 2 for i in range(8)], dtype=np.int32)
+    assert orc.correlation_sums(neel, 1, 8).tolist() == [8 * (-1) ** r for r in range(8)]
+    assert orc.correlation_sums(neel, 1, 8, origin=3).tolist() == [-(-1) ** j for j in range(8)]
+    rng = np.random.default_rng(3)
+    s = rng.integers(0, 2, size=27)
+    c = orc.correlation_sums(s, 3, 3)
+    m = 1 - 2 * s
+    assert c[0] == 27 and c[1 + 3 * 2] == sum(
+        m[x + 3 * y + 9 * z] * m[(x + 1) % 3 + 3 * ((y + 2) % 3) + 9 * z]
+        for x in range(3) for y in range(3) for z in range(3))
+    # the structure factor at k = 0 is the sum of the correlations
+    assert orc.structure_factor(c, 3, 3)[0] == pytest.approx(c.sum())
+
+
 def _check_vs_ed(dim, L, T, jxy, jz, h, therm, sweeps, seed, keys):
     beta = 1.0 / T
     o = orc.Oracle(dim, L, beta, jxy, jz, h, seed=seed)
