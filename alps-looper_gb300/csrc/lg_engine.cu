@@ -121,6 +121,7 @@ struct Engine {
   DBuf<Ctl> d_ctl;
   // spin correlations: k_corr work tiles and the per-chunk exact sums (arena site indexed)
   int n_corr_tiles = 0, corr_smem = 0;
+  bool any_spin_s = false;   // some chain has S > 1/2: k_boundary closes its sites
   DBuf<int2> d_corr_tiles;
   DBuf<long long> d_corr_disp, d_corr_origin;
   std::vector<long long> h_corr;
@@ -242,7 +243,9 @@ struct Engine {
     for (int b = 0; b < NB; ++b) {
       int a = h_bond_s0[b], t = h_bond_s1[b];
       const int c = h_bond_chain[b];
-      const uint8_t dir = (uint8_t)((b - hch[c].bond_off) % spec[c].dim);  // bond = site*dim + d
+      // bond = (site*dim + d) * spin2^2 + virtual pair
+      const int q = spec[c].spin2 * spec[c].spin2;
+      const uint8_t dir = (uint8_t)(((b - hch[c].bond_off) / q) % spec[c].dim);
       int ia = h_inc_off[a] + fill[a]++;
       h_inc[ia] = b; h_inc_side[ia] = 0; h_inc_nbr[ia] = t; h_inc_dir[ia] = dir;
       int it = h_inc_off[t] + fill[t]++;
@@ -289,6 +292,8 @@ struct Engine {
     // vertex regions and per-sweep buffers from the expected operator count
     LG_CUDA(cudaMemset(d_ctl.p, 0, sizeof(Ctl)));
     if ((rc = build_corr())) return rc;
+    any_spin_s = false;
+    for (int c = 0; c < C; ++c) any_spin_s |= spec[c].spin2 > 1;
     if ((rc = build_regions())) return rc;
     if ((rc = alloc_dynamic(region_total, false))) return rc;
     set_merge_cap();
@@ -607,6 +612,10 @@ struct Engine {
       ++launches;
     }
     join();
+    if (any_spin_s) {
+      k_boundary<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
+      ++launches;
+    }
     mark(2);
     {
       const int w = shape.un_warps, per = w * UN_CHUNK;
@@ -712,6 +721,11 @@ struct Engine {
       z.err = 0;
       if (hc.err == ERR_ITERCAP)
         return lg_fail(LG_EITERCAP, "union-find iteration cap hit");
+      if (hc.err == ERR_BOUNDARY) {
+        LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
+        clear_sweep_state();
+        return lg_fail(LG_EINVAL, "spin-S configuration not periodic in imaginary time");
+      }
       if (hc.err == ERR_OVERFLOW) {
         LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
         rc = grow_regions();
@@ -1457,7 +1471,7 @@ int lg_batch_observables(lg_batch* b, int chain, lg_obs* out) {
 }
 int lg_batch_stats(const lg_batch* b, int64_t* total_sites, int64_t* site_sweeps) {
   long long ts = 0, ss = 0;
-  for (auto& s : b->eng->spec) { ts += s.N; ss += (long long)s.N * (long long)s.mcs; }
+  for (auto& s : b->eng->spec) { ts += s.volume; ss += (long long)s.volume * (long long)s.mcs; }
   if (total_sites) *total_sites = ts;
   if (site_sweeps) *site_sweeps = ss;
   return LG_OK;

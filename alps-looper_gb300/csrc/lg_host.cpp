@@ -33,6 +33,7 @@ extern "C" void lg_params_default(lg_params* p) {
   p->measure_correlations = 0;
   p->measure_structure_factor = 0;
   p->initial_site = -1;
+  p->spin2 = 1;
 }
 
 static bool parse_bool(const std::string& v, int* out) {
@@ -134,6 +135,14 @@ extern "C" int lg_params_parse(const char* text, lg_params* p) {
         return lg_fail(LG_EINVAL, "MEASURE[Structure Factor] must be true or false");
     } else if (key == "INITIAL_SITE") {
       double d; rc = num(&d); p->initial_site = (int)d;
+    } else if (key == "local_S") {
+      double d; rc = num(&d);
+      if (!rc) {
+        const double t = 2 * d;
+        if (!(t >= 1) || std::fabs(t - std::round(t)) > 1e-9)
+          return lg_fail(LG_EINVAL, "local_S must be a positive multiple of 1/2");
+        p->spin2 = (int)std::round(t);
+      }
     }
     if (rc) return rc;
   }
@@ -157,23 +166,35 @@ int ChainSpec::init(const lg_params& p) {
   if (p.L < 2) return lg_fail(LG_EINVAL, "L must be >= 2 (got %d)", p.L);
   dim = p.lattice;
   L = p.L;
+  spin2 = p.spin2 >= 1 ? p.spin2 : 1;
+  if (spin2 > 8) return lg_fail(LG_EUNSUPPORTED, "local_S = %d/2 > 4 is not supported", spin2);
   long long n = 1;
   for (int i = 0; i < dim; ++i) n *= L;
-  if (n > (1ll << 22)) return lg_fail(LG_EBUDGET, "%lld sites exceed the per-chain limit of 2^22", n);
-  N = (int)n;
-  NB = N * dim;
+  if (n * spin2 > (1ll << 22))
+    return lg_fail(LG_EBUDGET, "%lld sites exceed the per-chain limit of 2^22", n * spin2);
+  // spin S = spin2/2: spin2 virtual spin-1/2 sites per real site (v = site*spin2 + a) and the
+  // spin2^2 virtual bonds between the virtual sites of a real bond's two ends
+  // (b = rbond*spin2^2 + a*spin2 + a'), as looper's virtual graph (lattice.h); every virtual site
+  // has its real site's gauge
+  volume = (int)n;
+  N = (int)n * spin2;
+  const int q = spin2 * spin2;
+  NB = (int)n * dim * q;
   s0.resize(NB); s1.resize(NB); gauge.resize(N);
-  for (int s = 0; s < N; ++s) {
+  for (int s = 0; s < (int)n; ++s) {
     int x[3] = {0, 0, 0}, r = s, par = 0;
     for (int i = 0; i < dim; ++i) { x[i] = r % L; r /= L; par += x[i]; }
-    gauge[s] = (par % 2 == 0) ? 1 : -1;
+    for (int a = 0; a < spin2; ++a) gauge[s * spin2 + a] = (par % 2 == 0) ? 1 : -1;
     for (int i = 0; i < dim; ++i) {
       int y[3] = {x[0], x[1], x[2]};
       y[i] = (y[i] + 1) % L;
       int t = 0;
       for (int j = dim - 1; j >= 0; --j) t = t * L + y[j];
-      s0[s * dim + i] = s;
-      s1[s * dim + i] = t;
+      for (int a = 0; a < spin2; ++a)
+        for (int a2 = 0; a2 < spin2; ++a2) {
+          s0[(s * dim + i) * q + a * spin2 + a2] = s * spin2 + a;
+          s1[(s * dim + i) * q + a * spin2 + a2] = t * spin2 + a2;
+        }
     }
   }
   bipartite = (L % 2 == 0);
@@ -225,13 +246,16 @@ int ChainSpec::init(const lg_params& p) {
   dchain.field = field ? 1 : 0;
   // correlations (correlation.h:62-110): the structure factor needs the all-pairs sums; the
   // correlations use them too unless INITIAL_SITE picks one origin
-  if (p.initial_site >= N)
-    return lg_fail(LG_EINVAL, "INITIAL_SITE %d out of range (%d sites)", p.initial_site, N);
+  if (p.initial_site >= volume)
+    return lg_fail(LG_EINVAL, "INITIAL_SITE %d out of range (%d sites)", p.initial_site, volume);
+  if (spin2 > 1 && (p.measure_correlations || p.measure_structure_factor))
+    return lg_fail(LG_EUNSUPPORTED, "correlations are measured for S = 1/2 only");
   measure_corr = p.measure_correlations != 0;
   measure_sfac = p.measure_structure_factor != 0;
   corr_origin = (measure_corr && p.initial_site >= 0) ? p.initial_site : -1;
   dchain.dim = dim;
   dchain.L = L;
+  dchain.spin2 = spin2;
   dchain.corr_disp = (measure_sfac || (measure_corr && corr_origin < 0)) ? 1 : 0;
   dchain.corr_origin = corr_origin;
   dchain.corr_from = (uint32_t)std::min<int64_t>(therm, 0xFFFFFFFFll);
@@ -304,7 +328,7 @@ static double i64(uint64_t x) { return (double)(int64_t)x; }
 static double u128d(const uint64_t* r, int i) { return (double)r[i] + std::ldexp((double)r[i + 1], 64); }
 
 void record_values(const ChainSpec& s, const uint64_t* r, double* v) {
-  const double beta = s.beta, V = (double)s.N;
+  const double beta = s.beta, V = (double)s.volume;
   const double nop = (double)r[R_NOP];
   double ene = s.energy_offset - nop / beta;                       // path_integral.C:850
   if (s.field) ene += -s.h * i64(r[R_FLD]) * std::ldexp(1.0, -40) / 2;  // :852-859
@@ -420,7 +444,7 @@ static void jackknife2(const BinAcc& A, const BinAcc& B, F f, double* mean, doub
 
 void ChainAcc::report(const ChainSpec& s, lg_obs* out) const {
   std::memset(out, 0, sizeof(*out));
-  const double V = (double)s.N, beta = s.beta;
+  const double V = (double)s.volume, beta = s.beta;
   out->count = (uint64_t)raw[RAW_E].count;
   out->beta = beta;
   out->volume = V;

@@ -11,7 +11,8 @@ int lg_fail(int code, const char* fmt, ...);
 
 // One chain's model, lattice and Monte Carlo schedule, validated from lg_params.
 struct ChainSpec {
-  int dim = 1, L = 0, N = 0, NB = 0;
+  int dim = 1, L = 0, N = 0, NB = 0;   // N, NB: (virtual) sites and bonds of the simulation
+  int spin2 = 1, volume = 0;           // 2S; real sites
   std::vector<int> s0, s1, gauge;
   bool bipartite = true;
   double beta = 1, jxy = 1, jz = 1, h = 0, force_scatter = 0;

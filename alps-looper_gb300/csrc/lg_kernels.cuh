@@ -747,7 +747,8 @@ __device__ void merge_site_serial(Arena& A, int s) {
     A.parent[x] = x;
     A.vslot[2 * v + sd] = x;
   }
-  if (k > 0) A.parent[base + k] = base;
+  // closure (path_integral.C:584-589); spin-S sites close in k_boundary instead
+  if (k > 0 && A.ch[A.site_chain[s]].spin2 <= 1) A.parent[base + k] = base;
 }
 
 // `cap` (a multiple of 32, at most MERGE_CAP) is the staging capacity per warp, sized by the
@@ -881,6 +882,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
     const uint16_t* fI = curI;
     // segments: prefix XOR of off-diagonal flags gives each segment's spin
     const uint8_t gneg = A.gauge[s] < 0 ? SI_GNEG : 0;
+    const bool close = A.ch[c].spin2 <= 1;  // spin-S sites close in k_boundary
     uint32_t carry = A.spin0[s];
     if (lane == 0) {
       A.stime[base] = 0ull;
@@ -912,7 +914,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
                                ((cd >> 1) << SI_GSHIFT) | ((cd & 1u) ? SI_OFF : 0));
         A.svert[x] = v;
         A.sdir[x] = (uint8_t)(sv & 0x7F);
-        A.parent[x] = (r == k - 1) ? base : x;  // closure: top segment joins the bottom one
+        A.parent[x] = (r == k - 1 && close) ? base : x;  // closure: top segment joins the bottom one
         A.vslot[2 * v + side] = x;
       }
       carry ^= __popc(ball) & 1u;
@@ -931,6 +933,35 @@ __global__ void __launch_bounds__(256) k_merge_narrow(Arena A, const int* sites,
     if (s == A.N - 1) A.ch_slot_off[A.C] = A.sbase[s + 1];
     merge_site_serial(A, s);
   }
+}
+
+// Imaginary-time boundary of a spin-S site (spin2 > 1 virtual sites, path_integral.C:590-613 with
+// permutation.h:91-111): the bottom of virtual site a joins the top of virtual site pair[a], and
+// both carry the same spin.  Per spin value c the tops with spin c, in index order, are shuffled
+// by Fisher-Yates: step k (from the last position down; position i swaps with
+// j = floor(w (i+1) / 2^32)) takes Philox word 8c + k of (seed, sweep, real site, TAG_PERM).  The
+// bottoms with spin c, in index order, take the shuffled tops in order.  This is a uniform
+// matching within each spin sector, as the reference's partitioned random shuffle.  False if the
+// two sectors differ in size (a configuration that is not periodic in imaginary time).
+__device__ __forceinline__ bool boundary_pairs(uint64_t seed, uint32_t sweep, uint32_t rs, int spin2,
+                                               const uint8_t* bottom, const uint8_t* top, int* pair) {
+  for (int c = 0; c < 2; ++c) {
+    int T[8], B[8], nt = 0, nb = 0;
+    for (int a = 0; a < spin2; ++a) {
+      if (top[a] == c) T[nt++] = a;
+      if (bottom[a] == c) B[nb++] = a;
+    }
+    if (nt != nb) return false;
+    for (int i = nt - 1, k = 0; i >= 1; --i, ++k) {
+      const int q = 8 * c + k;
+      const rnd4 r = philox(seed, sweep, rs, TAG_PERM, (uint32_t)(q >> 2));
+      const uint32_t w = (q & 3) == 0 ? r.x : (q & 3) == 1 ? r.y : (q & 3) == 2 ? r.z : r.w;
+      const int j = (int)(((uint64_t)w * (uint64_t)(i + 1)) >> 32);
+      const int t = T[i]; T[i] = T[j]; T[j] = t;
+    }
+    for (int k = 0; k < nb; ++k) pair[B[k]] = T[k];
+  }
+  return true;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -966,6 +997,36 @@ __device__ __forceinline__ bool uf_union(int* P, int a, int b) {
     b = old;
   }
   return false;
+}
+
+// One thread per spin-S real site: the boundary pairs are united (uf_union: hooks from the larger
+// segment index to the smaller).  A virtual site without operators has one segment, which is both
+// its bottom and its top and so can be in two pairs; the unions keep both links.  The segments
+// of a real site belong to its thread alone until k_union starts.
+__global__ void __launch_bounds__(256) k_boundary(Arena A) {
+  if (A.ctl->err) return;
+  LG_GRID_STRIDE(s, A.N) {
+    const int c = A.site_chain[s];
+    const int sp2 = A.ch[c].spin2;
+    if (sp2 <= 1) continue;
+    const int loc = s - A.ch[c].site_off;
+    if (loc % sp2) continue;
+    int bot[8], top[8], pair[8];
+    uint8_t bs[8], ts[8];
+    for (int a = 0; a < sp2; ++a) {
+      bot[a] = A.sbase[s + a];
+      top[a] = A.sbase[s + a + 1] - 1;
+      bs[a] = A.spin0[s + a];
+      ts[a] = A.sinfo[top[a]] & SI_SPIN;
+    }
+    if (!boundary_pairs(A.ch[c].seed, A.ch_sweep[c], (uint32_t)(loc / sp2), sp2, bs, ts, pair)) {
+      atomicExch(&A.ctl->err, ERR_BOUNDARY);
+      continue;
+    }
+    bool ok = true;
+    for (int a = 0; a < sp2; ++a) ok &= uf_union(A.parent, bot[a], top[pair[a]]);
+    if (!ok) atomicExch(&A.ctl->err, ERR_ITERCAP);
+  }
 }
 
 // reconnect (graph_impl.h:280-295) in segment form: g = 0 joins the two lower legs and the two

@@ -15,7 +15,9 @@
 namespace lg {
 
 // Stream tags (third Philox counter word).
-enum : uint32_t { TAG_PROPOSAL = 1, TAG_OFFDIAG = 2, TAG_FLIP = 3, TAG_SPIN = 4, TAG_EXCHANGE = 5 };
+enum : uint32_t {
+  TAG_PROPOSAL = 1, TAG_OFFDIAG = 2, TAG_FLIP = 3, TAG_SPIN = 4, TAG_EXCHANGE = 5, TAG_PERM = 6
+};
 
 // Philox4x32-10 (Salmon et al., SC'11): 10 rounds of two 32x32->64 multiplies with the paper's
 // constants, key bumped by the Weyl increments between rounds.

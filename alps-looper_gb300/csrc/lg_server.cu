@@ -70,7 +70,7 @@ struct lg_server {
     res.t_submit = r.t_submit;
     res.t_start = r.t_start;
     res.t_finish = t_now;
-    res.sites = r.spec.N;
+    res.sites = r.spec.volume;
     res.sweeps = (uint64_t)(r.spec.therm + r.spec.sweeps);
     if (obs) res.obs = *obs;
     std::lock_guard<std::mutex> lk(mu);
@@ -173,7 +173,7 @@ struct lg_server {
       }
       long long ss = 0;
       for (size_t c = 0; c < active.size(); ++c)
-        if (!retired[c]) ss += (long long)eng->spec[c].N * cfg.sweeps_per_tick;
+        if (!retired[c]) ss += (long long)eng->spec[c].volume * cfg.sweeps_per_tick;
       {
         std::lock_guard<std::mutex> lk(mu);
         stats.site_sweeps += ss;

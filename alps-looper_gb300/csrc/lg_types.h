@@ -8,7 +8,7 @@ constexpr int MAXZ = 6;                 // largest coordination number (simple c
 constexpr int REC_WORDS = 32;           // uint64 words per sweep record
 constexpr int ITER_CAP = 1 << 22;       // union-find retry cap per union
 
-enum : int { ERR_OVERFLOW = 1, ERR_ITERCAP = 2 };
+enum : int { ERR_OVERFLOW = 1, ERR_ITERCAP = 2, ERR_BOUNDARY = 3 };
 
 // Per-sweep record words: exact integer sums over the clusters of one chain.
 //   NOP  operator count                      NC   cluster count
@@ -37,6 +37,7 @@ struct DChain {
   int dim, L;
   int corr_disp, corr_origin;
   uint32_t corr_from, corr_to;
+  int spin2;                   // 2S: virtual sites per real site (their boundary: k_boundary)
 };
 
 struct Ctl {

@@ -43,7 +43,7 @@ class Params(ctypes.Structure):
                 ("thermalization", ctypes.c_int64), ("seed", ctypes.c_uint64),
                 ("init_spins", ctypes.c_int), ("disable_improved_estimator", ctypes.c_int),
                 ("measure_correlations", ctypes.c_int), ("measure_structure_factor", ctypes.c_int),
-                ("initial_site", ctypes.c_int)]
+                ("initial_site", ctypes.c_int), ("spin2", ctypes.c_int)]
 
 
 class Obs(ctypes.Structure):
@@ -181,7 +181,8 @@ def make_params(**kw) -> Params:
     """Parameters with the worker's key names: LATTICE, L, T, BETA, J, Jz, Jxy, h, SWEEPS,
     THERMALIZATION, SEED, FORCE_SCATTER, INITIAL_SPINS, DISABLE_IMPROVED_ESTIMATOR (lower-case
     aliases accepted), and the correlation switches MEASURE_CORRELATIONS (MEASURE[Correlations]),
-    MEASURE_STRUCTURE_FACTOR (MEASURE[Structure Factor]) and INITIAL_SITE."""
+    MEASURE_STRUCTURE_FACTOR (MEASURE[Structure Factor]) and INITIAL_SITE, and local_S (1/2, 1,
+    3/2: the site spin)."""
     p = Params()
     lib().lg_params_default(ctypes.byref(p))
     for k, v in kw.items():
@@ -217,6 +218,8 @@ def make_params(**kw) -> Params:
             p.measure_structure_factor = 1 if v else 0
         elif key == "INITIAL_SITE":
             p.initial_site = int(v)
+        elif key in ("local_S", "LOCAL_S"):
+            p.spin2 = int(round(2 * float(v)))
         else:
             raise KeyError(k)
     return p
@@ -375,8 +378,9 @@ class LoopWorker:
 
     # ---- test seams ----
     def num_sites(self):
+        """Simulated sites: L^dim, times 2S virtual sites per site for S > 1/2."""
         L = self.params.L
-        return L ** self.params.lattice
+        return L ** self.params.lattice * max(1, self.params.spin2)
 
     def state(self):
         N = self.num_sites()

@@ -67,6 +67,10 @@ typedef struct lg_params {
   int measure_correlations;       /* MEASURE[Correlations] (correlation.h:66), default 0        */
   int measure_structure_factor;   /* MEASURE[Structure Factor] (correlation.h:68), default 0    */
   int initial_site;               /* INITIAL_SITE (correlation.h:87); < 0: all pairs (default)  */
+  int spin2;                      /* 2 local_S: 1 (S=1/2, default), 2 (S=1), 3 (S=3/2); S > 1/2
+                                     runs on 2S virtual spin-1/2 sites per site (lattice.h
+                                     virtual graph) with the random boundary matching of
+                                     path_integral.C:590-613                                    */
 } lg_params;
 
 /* Fill defaults: chain, L=8, T=0.2, J=1, Jz=Jxy=NaN, h=0, SWEEPS=65536 (montecarlo.h:41),
@@ -76,7 +80,8 @@ void lg_params_default(lg_params* p);
 /* Parse ALPS-style "KEY = value" lines (';' or newline separated, '#' comments) into *p.
  * Keys: LATTICE ("chain lattice" | "square lattice" | "simple cubic lattice"), L, T, BETA, J,
  * Jz, Jxy, h, FORCE_SCATTER, SWEEPS, THERMALIZATION, SEED, INITIAL_SPINS ("up" | "random"),
- * DISABLE_IMPROVED_ESTIMATOR, MEASURE[Correlations], MEASURE[Structure Factor], INITIAL_SITE.
+ * DISABLE_IMPROVED_ESTIMATOR, MEASURE[Correlations], MEASURE[Structure Factor], INITIAL_SITE,
+ * local_S (1/2, 1, 3/2).
  * Unknown keys are ignored, as ALPS does for keys a worker does not
  * read.  Returns LG_EINVAL with a message on a malformed value. */
 int lg_params_parse(const char* text, lg_params* p);

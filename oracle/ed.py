@@ -1,7 +1,8 @@
 """Exact diagonalization oracle — test infrastructure only.
 
-Restates the reference's diagonalization worker (diag.C:313-488) for S=1/2 XXZ models with a
-uniform longitudinal field on periodic chain / square / cubic lattices:
+Restates the reference's diagonalization worker (diag.C:313-488) for spin-S XXZ models (S = 1/2
+and, with spin2 = 2S > 1, higher spins: diag.C builds the local spin-S operators the same way)
+with a uniform longitudinal field on periodic chain / square / cubic lattices:
 
     H = sum_<ij> [ Jz Sz_i Sz_j + Jxy/2 (S+_i S-_j + S-_i S+_j) ] - h sum_i Sz_i
 
@@ -44,6 +45,16 @@ def lattice(dim: int, L: int):
     return N, bonds, gauge
 
 
+def _sector_states_s(N: int, spin2: int, tot: int) -> np.ndarray:
+    """Basis states of total (Sz + S) = tot / ... : digits d_i in [0, 2S], sum d_i = tot."""
+    base = spin2 + 1
+    out = []
+    for digits in itertools.product(range(base), repeat=N):
+        if sum(digits) == tot:
+            out.append(sum(d * base ** i for i, d in enumerate(digits)))
+    return np.array(out, dtype=np.int64)
+
+
 def _sector_states(N: int, nup: int) -> np.ndarray:
     states = []
     for ups in itertools.combinations(range(N), nup):
@@ -54,30 +65,50 @@ def _sector_states(N: int, nup: int) -> np.ndarray:
     return np.array(states, dtype=np.int64)
 
 
-def thermal(dim: int, L: int, T: float, jxy: float = 1.0, jz: float = 1.0, h: float = 0.0):
-    """Return a dict of the diag.C observables at temperature T."""
+def thermal(dim: int, L: int, T: float, jxy: float = 1.0, jz: float = 1.0, h: float = 0.0,
+            spin2: int = 1):
+    """Return a dict of the diag.C observables at temperature T (local spin S = spin2 / 2)."""
     beta = 1.0 / T
     N, bonds, gauge = lattice(dim, L)
     vol = float(N)
     sectors = []
     e_min = math.inf
-    for nup in range(N + 1):
-        st = _sector_states(N, nup)
+    S = spin2 / 2.0
+    base = spin2 + 1
+    for nup in range(N * spin2 + 1):
+        st = _sector_states(N, nup) if spin2 == 1 else _sector_states_s(N, spin2, nup)
         dimn = len(st)
         index = {int(v): i for i, v in enumerate(st)}
         H = np.zeros((dimn, dimn))
         sz = np.zeros((dimn, N))
         for i, v in enumerate(st):
-            bits = [(int(v) >> k) & 1 for k in range(N)]  # 1 = up
-            sz[i] = np.array(bits) - 0.5
+            if spin2 == 1:
+                bits = [(int(v) >> k) & 1 for k in range(N)]  # 1 = up
+            else:
+                bits = [(int(v) // base ** k) % base for k in range(N)]
+            sz[i] = np.array(bits) - S
         for (a, b) in bonds:
             H[np.arange(dimn), np.arange(dimn)] += jz * sz[:, a] * sz[:, b]
-            if jxy != 0.0:
+            if jxy == 0.0:
+                continue
+            if spin2 == 1:
                 for i, v in enumerate(st):
                     ba, bb = (int(v) >> a) & 1, (int(v) >> b) & 1
                     if ba != bb:
                         w = int(v) ^ (1 << a) ^ (1 << b)
                         H[index[w], i] += jxy / 2
+            else:
+                # Jxy/2 (S+_a S-_b + S-_a S+_b); S+|m> = sqrt(S(S+1) - m(m+1)) |m+1>
+                for i, v in enumerate(st):
+                    ma, mb = sz[i, a], sz[i, b]
+                    if ma < S and mb > -S:
+                        c = math.sqrt(S * (S + 1) - ma * (ma + 1)) * math.sqrt(S * (S + 1) - mb * (mb - 1))
+                        w = int(v) + base ** a - base ** b
+                        H[index[w], i] += jxy / 2 * c
+                    if ma > -S and mb < S:
+                        c = math.sqrt(S * (S + 1) - ma * (ma - 1)) * math.sqrt(S * (S + 1) - mb * (mb + 1))
+                        w = int(v) - base ** a + base ** b
+                        H[index[w], i] += jxy / 2 * c
         m = sz.sum(axis=1)
         H[np.arange(dimn), np.arange(dimn)] -= h * m
         ev, U = np.linalg.eigh(H)

@@ -71,7 +71,7 @@ static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
 }
 
 // Stream tags (third counter word).
-enum { TAG_PROPOSAL = 1, TAG_OFFDIAG = 2, TAG_FLIP = 3, TAG_SPIN = 4 };
+enum { TAG_PROPOSAL = 1, TAG_OFFDIAG = 2, TAG_FLIP = 3, TAG_SPIN = 4, TAG_PERM = 6 };
 
 static void rng4(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t out[4]) {
   uint32_t c[4] = {c0, c1, c2, c3};
@@ -172,32 +172,71 @@ static int64_t time_fix40(double t) {
 }
 
 // ----------------------------------------------------------------------------------------------
-// Lattice: periodic hypercubic, site = x + L*y + L*L*z, bond = site*dim + d joins site -> site+e_d.
-// gauge = +1 on the even sublattice, -1 on the odd one (lattice.h:601 uses 2*parity-1).
+// Lattice: periodic hypercubic, real site = x + L*y + L*L*z, real bond = site*dim + d joins
+// site -> site+e_d.  gauge = +1 on the even sublattice, -1 on the odd one (lattice.h:601 uses
+// 2*parity-1).  Spin S = spin2/2 > 1/2 is represented by spin2 spin-1/2 virtual sites per real
+// site, v = site*spin2 + a, and every real bond by the spin2^2 virtual bonds between the virtual
+// sites of its two ends, b = rbond*spin2^2 + a*spin2 + a' (the virtual graph of lattice.h); each
+// virtual site has its real site's gauge, each virtual bond its real bond's direction.
 // ----------------------------------------------------------------------------------------------
 struct lattice {
-  int dim = 1, L = 0, N = 0, NB = 0;
-  std::vector<int> s0, s1, gauge;
+  int dim = 1, L = 0, N = 0, NB = 0, NR = 0, spin2 = 1;
+  std::vector<int> s0, s1, gauge, bdir;
   bool bipartite = true;
-  void build(int d, int l) {
-    dim = d; L = l;
-    N = 1; for (int i = 0; i < dim; ++i) N *= L;
-    NB = N * dim;
-    s0.resize(NB); s1.resize(NB); gauge.resize(N);
-    for (int s = 0; s < N; ++s) {
+  void build(int d, int l, int sp2 = 1) {
+    dim = d; L = l; spin2 = sp2;
+    NR = 1; for (int i = 0; i < dim; ++i) NR *= L;
+    N = NR * spin2;
+    const int q = spin2 * spin2;
+    NB = NR * dim * q;
+    s0.resize(NB); s1.resize(NB); gauge.resize(N); bdir.resize(NB);
+    for (int s = 0; s < NR; ++s) {
       int x[3] = {0, 0, 0}, r = s, par = 0;
       for (int i = 0; i < dim; ++i) { x[i] = r % L; r /= L; par += x[i]; }
-      gauge[s] = (par % 2 == 0) ? 1 : -1;
+      for (int a = 0; a < spin2; ++a) gauge[s * spin2 + a] = (par % 2 == 0) ? 1 : -1;
       for (int i = 0; i < dim; ++i) {
         int y[3] = {x[0], x[1], x[2]};
         y[i] = (y[i] + 1) % L;
         int t = 0; for (int j = dim - 1; j >= 0; --j) t = t * L + y[j];
-        s0[s * dim + i] = s; s1[s * dim + i] = t;
+        for (int a = 0; a < spin2; ++a)
+          for (int a2 = 0; a2 < spin2; ++a2) {
+            const int b = (s * dim + i) * q + a * spin2 + a2;
+            s0[b] = s * spin2 + a; s1[b] = t * spin2 + a2; bdir[b] = i;
+          }
       }
     }
     bipartite = (L % 2 == 0);
   }
 };
+
+// Imaginary-time boundary of a real site with spin2 > 1 virtual sites (path_integral.C:590-613,
+// permutation.h:91-111): the bottom of virtual site a joins the top of pair[a], and both carry
+// the same spin.  For each spin value c the tops with spin c, in index order, are shuffled by
+// Fisher-Yates (step i of the shuffle, from the last position down, swaps position i with
+// j = floor(w (i+1) / 2^32)), where step k of sector c takes Philox word 8c + k of the key
+// (seed, sweep, real site, TAG_PERM).  The bottoms with spin c, in index order, take the
+// shuffled tops in order: a uniform matching within each spin sector, like the reference's
+// partitioned random shuffle.  Returns false if the sectors differ in size.
+static bool boundary_matching(uint64_t seed, uint32_t sweep, uint32_t rs, int spin2,
+                              const int* bottom, const int* top, int* pair) {
+  for (int c = 0; c < 2; ++c) {
+    int T[8], B[8], nt = 0, nb = 0;
+    for (int a = 0; a < spin2; ++a) {
+      if (top[a] == c) T[nt++] = a;
+      if (bottom[a] == c) B[nb++] = a;
+    }
+    if (nt != nb) return false;
+    for (int i = nt - 1, k = 0; i >= 1; --i, ++k) {
+      const int q = 8 * c + k;
+      uint32_t w[4];
+      rng4(seed, sweep, rs, TAG_PERM, (uint32_t)(q >> 2), w);
+      const int j = (int)(((uint64_t)w[q & 3] * (uint64_t)(i + 1)) >> 32);
+      const int tmp = T[i]; T[i] = T[j]; T[j] = tmp;
+    }
+    for (int k = 0; k < nb; ++k) pair[B[k]] = T[k];
+  }
+  return true;
+}
 
 // ----------------------------------------------------------------------------------------------
 // Graph weights for one S=1/2 XXZ bond: restates weight_impl.h:282-315 with Jx == Jy == Jxy
@@ -335,6 +374,7 @@ struct chain_t {
   std::vector<int> last_labels;   // reference fragment ids (sites, then g=0 vertices)
   int last_nfrag = 0, last_nc = 0;
   std::vector<uint64_t> records;  // R_WORDS per sweep
+  int status = 0;                 // 1: a boundary had spin sectors of different sizes
 
   void init_derived() {
     double W = bw.W;
@@ -443,8 +483,20 @@ struct chain_t {
       up0.push_back(current[s0]); up1.push_back(current[s1]);
       rank0.push_back(++cnt[s0]); rank1.push_back(++cnt[s1]);
     }
-    // ---- temporal closure (path_integral.C:584-589) ----
-    for (int s = 0; s < N; ++s) frag.unify(s, current[s]);
+    // ---- temporal closure (path_integral.C:582-615) ----
+    if (lat.spin2 == 1) {
+      for (int s = 0; s < N; ++s) frag.unify(s, current[s]);
+    } else {
+      for (int rs = 0; rs < lat.NR; ++rs) {
+        const int off = rs * lat.spin2;
+        int pair[8];
+        if (!boundary_matching(seed, sweep, (uint32_t)rs, lat.spin2, &spins[off], &spins_c[off], pair)) {
+          status = 1;  // not a periodic configuration: each bottom keeps its own top
+          for (int a = 0; a < lat.spin2; ++a) pair[a] = a;
+        }
+        for (int a = 0; a < lat.spin2; ++a) frag.unify(off + a, current[off + pair[a]]);
+      }
+    }
     int nc = frag.set_ids();
 
     last_spins = spins;
@@ -496,7 +548,7 @@ struct chain_t {
         if (j < (int)ep[s].size()) {
           const op_t& o = nops[ep[s][j]];
           if (lat.s0[o.bond] == s && !(o.g & 2)) {
-            const int d = o.bond % lat.dim;
+            const int d = lat.bdir[o.bond];
             wind[(size_t)cl * 3 + d] += 1 - 2 * c;                          // end_bs
             wind[(size_t)frag.id[nextfr] * 3 + d] -= 1 - 2 * nextc;          // begin_bs
           }
@@ -701,11 +753,12 @@ struct orc_params {
   uint64_t seed;
   int random_spins;   // 1: iid spins from the seed; 0: all up
   int deterministic_uf;
+  int spin2;          // 2S: virtual sites per real site
 };
 
 void* orc_create(const orc_params* p) {
   orc::chain_t* c = new orc::chain_t();
-  c->lat.build(p->dim, p->L);
+  c->lat.build(p->dim, p->L, p->spin2 > 1 ? p->spin2 : 1);
   c->bw = orc::make_weight(p->jxy, p->jz, p->force_scatter);
   c->beta = p->beta; c->h = p->h; c->seed = p->seed;
   c->field = (std::fabs(p->h) > 1e-12);
@@ -730,6 +783,7 @@ void orc_sweep(void* h, int n) {
 }
 
 int orc_num_sites(void* h) { return static_cast<orc::chain_t*>(h)->lat.N; }
+int orc_status(void* h) { return static_cast<orc::chain_t*>(h)->status; }
 int orc_num_ops(void* h) { return (int)static_cast<orc::chain_t*>(h)->ops.size(); }
 int orc_num_records(void* h) {
   return (int)(static_cast<orc::chain_t*>(h)->records.size() / orc::R_WORDS);

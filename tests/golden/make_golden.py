@@ -97,15 +97,24 @@ def loop_op(ref):
         lat = re.findall(r'LATTICE = "?([^";]+)"?;', h)
         if not lat or lat[-1] != "chain lattice":
             continue
-        if re.search(r"local_S = 1;", h):
+        # spin-1 blocks are kept when they have no single-ion anisotropy D
+        spin = re.findall(r"local_S = ([^;]+);", h)
+        spin2 = round(2 * eval(spin[-1].replace("/", "/ "))) if spin else 1
+        D = re.findall(r"\nD = ([^;]+);", "\n" + h)
+        if D and float(D[-1]) != 0.0:
             continue
+        L = int(re.findall(r"\nL = ([^;]+);", "\n" + h)[-1])
         T = re.findall(r"\nT = ([^;]+);", "\n" + h)
+        Tv = T[-1].replace("L", str(L))
+        Tf = float(eval(Tv))
         jz = re.findall(r"Jz = ([^;]+);", h)
         jxy = re.findall(r"Jxy = ([^;]+);", h)
         vals = _block(lines, i + 1, keys)
-        entry = {"algorithm": alg, "L": 4, "T": float(T[-1]),
+        entry = {"algorithm": alg, "L": L, "T": Tf,
                  "jz": float(jz[-1]) if jz else 1.0, "jxy": float(jxy[-1]) if jxy else 1.0,
                  "values": vals}
+        if spin2 != 1:
+            entry["spin2"] = spin2
         vec = _vectors(lines, i + 1)
         if vec:
             entry["vectors"] = vec

@@ -52,7 +52,8 @@ class _P(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_int), ("L", ctypes.c_int), ("beta", ctypes.c_double),
                 ("jxy", ctypes.c_double), ("jz", ctypes.c_double), ("h", ctypes.c_double),
                 ("force_scatter", ctypes.c_double), ("seed", ctypes.c_uint64),
-                ("random_spins", ctypes.c_int), ("deterministic_uf", ctypes.c_int)]
+                ("random_spins", ctypes.c_int), ("deterministic_uf", ctypes.c_int),
+                ("spin2", ctypes.c_int)]
 
 
 def _ptr(a):
@@ -66,11 +67,12 @@ class Oracle:
     """One Markov chain in philox mode (the GPU's random source)."""
 
     def __init__(self, dim, L, beta, jxy=1.0, jz=1.0, h=0.0, seed=1, random_spins=True,
-                 force_scatter=0.0, deterministic_uf=False):
+                 force_scatter=0.0, deterministic_uf=False, spin2=1):
         self.dim, self.L, self.beta = dim, L, beta
         self.jxy, self.jz, self.h = jxy, jz, h
+        self.spin2 = spin2
         p = _P(dim, L, beta, jxy, jz, h, force_scatter, seed, 1 if random_spins else 0,
-               1 if deterministic_uf else 0)
+               1 if deterministic_uf else 0, spin2)
         self._h = ctypes.c_void_p(lib().orc_create(ctypes.byref(p)))
         self.N = lib().orc_num_sites(self._h)
 
@@ -87,6 +89,7 @@ class Oracle:
 
     def sweep(self, n=1):
         lib().orc_sweep(self._h, ctypes.c_int(n))
+        assert lib().orc_status(self._h) == 0, "boundary spin sectors differ"
 
     def bonds(self):
         N, bonds, _ = ed.lattice(self.dim, self.L)
@@ -189,12 +192,13 @@ def u128(r, i):
     return r[:, i].astype(np.float64) + r[:, i + 1].astype(np.float64) * 2.0 ** 64
 
 
-def observables(records, dim, L, beta, jxy=1.0, jz=1.0, h=0.0):
+def observables(records, dim, L, beta, jxy=1.0, jz=1.0, h=0.0, spin2=1):
     """Per-sweep observables from oracle records (path_integral.C:827-862; energy.h:76-84;
-    susceptibility.h:200-254 improved / :303-335 normal)."""
+    susceptibility.h:200-254 improved / :303-335 normal).  N is the number of real sites (the
+    volume); a spin-S chain has spin2^2 virtual bonds per real bond."""
     r = records
     N = L ** dim
-    NB = N * dim
+    NB = N * dim * spin2 * spin2
     v, W = weights(jxy, jz)
     offset = NB * W / 2
     nop = r[:, 0].astype(np.float64)

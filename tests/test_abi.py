@@ -65,6 +65,15 @@ def test_params_parse_correlation_switches(lg):
         lg.parse_params("MEASURE[Correlations] = maybe")
 
 
+def test_params_parse_local_spin(lg):
+    assert lg.make_params().spin2 == 1
+    assert lg.parse_params("local_S = 1").spin2 == 2
+    assert lg.parse_params("local_S = 3/2").spin2 == 3
+    assert lg.make_params(local_S=1.5).spin2 == 3
+    with pytest.raises(lg.LoopError):
+        lg.parse_params("local_S = 0.3")
+
+
 def test_params_parse_rejects_bad_values(lg):
     with pytest.raises(lg.LoopError) as e:
         lg.parse_params("L = abc")

@@ -88,16 +88,30 @@ def test_ed_matches_golden(golden):
     for b in golden("loop_op.json"):
         if b["algorithm"] != "diagonalization":
             continue
-        r = orc.ed.thermal(1, b["L"], b["T"], jxy=b["jxy"], jz=b["jz"])
+        r = orc.ed.thermal(1, b["L"], b["T"], jxy=b["jxy"], jz=b["jz"], spin2=b.get("spin2", 1))
         for k, (v, _) in b["values"].items():
             assert r[k] == pytest.approx(v, rel=2e-5, abs=2e-6), k
+
+
+def test_ed_agrees_with_reference_path_integral(golden):
+    # every "loop; path integral" block of loop.op (S=1/2 and S=1 chains) within 3 sigma of ED
+    n = 0
+    for b in golden("loop_op.json"):
+        if b["algorithm"] != "loop; path integral":
+            continue
+        r = orc.ed.thermal(1, b["L"], b["T"], jxy=b["jxy"], jz=b["jz"], spin2=b.get("spin2", 1))
+        for k, (v, e) in b["values"].items():
+            if k in r and k != "Specific Heat":
+                assert abs(v - r[k]) <= 3 * float(e) + 1e-9, (b["T"], b.get("spin2", 1), k, v, e, r[k])
+                n += 1
+    assert n >= 20
 
 
 def test_ed_correlations_agree_with_reference_path_integral(golden):
     # loop.op: "loop; path integral" with MEASURE[Correlations] / MEASURE[Structure Factor],
     # S=1/2 Heisenberg chain L=4, T=0.5, 4096 sweeps: the exact correlations must lie within
     # 3 sigma of the reference's binned Monte Carlo values
-    blk = [b for b in golden("loop_op.json") if "vectors" in b]
+    blk = [b for b in golden("loop_op.json") if "vectors" in b and b.get("spin2", 1) == 1]
     assert len(blk) == 1
     b = blk[0]
     r = orc.ed.thermal(1, b["L"], b["T"], jxy=b["jxy"], jz=b["jz"])
@@ -125,14 +139,14 @@ def test_correlation_sums_restatement():
     assert orc.structure_factor(c, 3, 3)[0] == pytest.approx(c.sum())
 
 
-def _check_vs_ed(dim, L, T, jxy, jz, h, therm, sweeps, seed, keys):
+def _check_vs_ed(dim, L, T, jxy, jz, h, therm, sweeps, seed, keys, spin2=1):
     beta = 1.0 / T
-    o = orc.Oracle(dim, L, beta, jxy, jz, h, seed=seed)
+    o = orc.Oracle(dim, L, beta, jxy, jz, h, seed=seed, spin2=spin2)
     o.sweep(therm)
     o.clear_records()
     o.sweep(sweeps)
-    obs = orc.observables(o.records(), dim, L, beta, jxy, jz, h)
-    ref = orc.ed.thermal(dim, L, T, jxy=jxy, jz=jz, h=h)
+    obs = orc.observables(o.records(), dim, L, beta, jxy, jz, h, spin2=spin2)
+    ref = orc.ed.thermal(dim, L, T, jxy=jxy, jz=jz, h=h, spin2=spin2)
     N = L ** dim
     for k in keys:
         if k == "Specific Heat":
@@ -162,3 +176,15 @@ def test_philox_xxz_field_chain_vs_ed():
 def test_philox_square_vs_ed():
     _check_vs_ed(2, 2, 0.5, 1.0, 1.0, 0.0, 1000, 20000, 10,
                  ["Energy", "Susceptibility", "Staggered Magnetization^2"])
+
+
+def test_philox_spin1_chain_vs_ed():
+    # S = 1 by two virtual spin-1/2 sites per site with the random boundary matching
+    _check_vs_ed(1, 4, 0.5, 1.0, 1.0, 0.0, 1000, 40000, 12,
+                 ["Energy", "Specific Heat", "Susceptibility", "Staggered Magnetization^2",
+                  "Staggered Susceptibility"], spin2=2)
+
+
+def test_philox_spin3half_xxz_field_chain_vs_ed():
+    _check_vs_ed(1, 4, 1.0, 1.0, 0.5, 0.2, 1000, 30000, 13,
+                 ["Energy", "Specific Heat", "Magnetization", "Susceptibility"], spin2=3)
