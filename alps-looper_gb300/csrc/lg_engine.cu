@@ -150,6 +150,7 @@ struct Engine {
   cudaGraphExec_t gexec = nullptr;
   bool use_graph = true;
   int nsm = 148;
+  int stream_priority = 0;   // CUDA stream priority of the arena's streams (0: the default)
   bool keep_records = false;
   std::vector<uint64_t> kept;   // raw records of chain 0 (test seam)
   std::vector<uint64_t> hrec;
@@ -198,8 +199,8 @@ struct Engine {
     cudaDeviceProp prop;
     LG_CUDA(cudaGetDeviceProperties(&prop, dev));
     nsm = prop.multiProcessorCount;
-    LG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    LG_CUDA(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+    LG_CUDA(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, stream_priority));
+    LG_CUDA(cudaStreamCreateWithPriority(&st2, cudaStreamNonBlocking, stream_priority));
     LG_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     LG_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     LG_CUDA(cudaFuncSetAttribute(k_corr, cudaFuncAttributeMaxDynamicSharedMemorySize, CORR_SMEM));

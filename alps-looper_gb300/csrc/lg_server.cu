@@ -1,7 +1,10 @@
-// Request server: continuous batching of simulation requests over one device arena.
+// Request server: continuous batching of simulation requests over device arenas.
 //
-// A server thread owns one Engine holding every active request as a chain.  It runs the arena in
-// ticks of `sweeps_per_tick` sweeps (one CUDA graph launch per sweep).  Between ticks:
+// Requests go to one of `lanes` size classes by their expected operators per sweep.  Each lane
+// has a thread and one Engine holding every active request of its class as a chain, on its own
+// CUDA stream, so the lanes' sweeps run side by side on the GPU and small requests do not wait
+// for the sweeps of large ones.  A lane runs its arena in ticks of `sweeps_per_tick` sweeps (one
+// CUDA graph launch per sweep).  Between ticks:
 //   * chains that reached THERMALIZATION + SWEEPS are retired: their observables become a
 //     result and the chain is masked (it inserts no operators) until the next rebuild;
 //   * queued requests are admitted in arrival order while their estimated device memory fits the
@@ -37,10 +40,11 @@ double chain_bytes(const ChainSpec& s) {
 }  // namespace
 
 struct lg_server {
+  static constexpr int MAX_LANES = 4;
   lg_server_config cfg;
   int device = 0;
+  int nlanes = 1;
   std::chrono::steady_clock::time_point t0;
-  std::thread th;
   std::mutex mu;
   std::condition_variable cv;
   bool stop = false;
@@ -50,18 +54,37 @@ struct lg_server {
     double t_submit, t_start;
     double bytes;
   };
-  std::deque<Req> pending;
+  std::deque<Req> pending[MAX_LANES];   // per lane, in arrival order
   std::vector<lg_result> done;
   uint64_t next_id = 1;
-  // server-thread state
-  std::unique_ptr<Engine> eng;
-  std::vector<Req> active;          // chain c of eng
-  std::vector<bool> retired;
-  double active_bytes = 0;
-  double last_rebuild = -1e30;
+  double active_bytes = 0;              // over all lanes (the admission budget)
   lg_server_stats stats{};
   int fatal = LG_OK;
   std::string fatal_msg;
+  // One lane: an arena of requests of one size class, driven by its own thread on its own CUDA
+  // stream (the Engine's), so lanes run side by side on the GPU and a small request never waits
+  // for the sweeps of a large one.
+  struct Lane {
+    std::unique_ptr<Engine> eng;
+    std::vector<Req> active;          // chain c of eng
+    std::vector<bool> retired;
+    double last_rebuild = -1e30;
+    int priority = 0;                 // CUDA stream priority: smaller size classes go first
+    std::thread th;
+  };
+  Lane lanes[MAX_LANES];
+
+  // Size class of a request: its expected operators per sweep against fixed cut points
+  // (2 lanes: 2^15; 3 lanes: 2^13, 2^17; 4 lanes: 2^12, 2^15, 2^18).
+  int lane_of(const ChainSpec& s) const {
+    if (nlanes <= 1) return 0;
+    const double ev = s.expected_vertices();
+    static const double cut[MAX_LANES - 1][MAX_LANES - 1] = {
+        {32768.0, 0, 0}, {8192.0, 131072.0, 0}, {4096.0, 32768.0, 262144.0}};
+    for (int k = 0; k < nlanes - 1; ++k)
+      if (ev < cut[nlanes - 2][k]) return k;
+    return nlanes - 1;
+  }
 
   void finish(const Req& r, int status, const lg_obs* obs, double t_now) {
     lg_result res{};
@@ -79,15 +102,21 @@ struct lg_server {
     cv.notify_all();
   }
 
-  int rebuild(std::vector<Req>& admit, double t_now) {
+  void fail(int rc) {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!fatal) { fatal = rc; fatal_msg = g_err; }
+    cv.notify_all();
+  }
+
+  int rebuild(Lane& ln, std::vector<Req>& admit, double t_now) {
     std::vector<ChainSpec> specs;
     std::vector<int> from;
     std::vector<Req> nact;
-    for (size_t c = 0; c < active.size(); ++c) {
-      if (retired[c]) continue;
-      specs.push_back(eng->spec[c]);
+    for (size_t c = 0; c < ln.active.size(); ++c) {
+      if (ln.retired[c]) continue;
+      specs.push_back(ln.eng->spec[c]);
       from.push_back((int)c);
-      nact.push_back(active[c]);
+      nact.push_back(ln.active[c]);
     }
     for (auto& r : admit) {
       r.t_start = t_now;
@@ -98,39 +127,45 @@ struct lg_server {
     std::unique_ptr<Engine> ne;
     if (!specs.empty()) {
       ne.reset(new Engine());
+      ne->stream_priority = ln.priority;
       int rc = ne->build(specs);
       if (rc) return rc;
-      if (eng) {
-        rc = ne->adopt(*eng, from);
+      if (ln.eng) {
+        rc = ne->adopt(*ln.eng, from);
         if (rc) return rc;
       }
     }
-    eng = std::move(ne);
-    active = std::move(nact);
-    retired.assign(active.size(), false);
-    stats.rebuilds++;
-    last_rebuild = t_now;
+    ln.eng = std::move(ne);
+    ln.active = std::move(nact);
+    ln.retired.assign(ln.active.size(), false);
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      stats.rebuilds++;
+    }
+    ln.last_rebuild = t_now;
     return LG_OK;
   }
 
-  void loop() {
+  void loop(int k) {
     cudaSetDevice(device);
+    Lane& ln = lanes[k];
+    std::deque<Req>& queue = pending[k];
     while (true) {
       std::vector<Req> admit;
       {
         std::unique_lock<std::mutex> lk(mu);
-        const bool idle = !eng || active.empty();
-        if (idle && pending.empty())
-          cv.wait_for(lk, std::chrono::milliseconds(2), [&] { return stop || !pending.empty(); });
-        if (stop) break;
+        const bool idle = !ln.eng || ln.active.empty();
+        if (idle && queue.empty())
+          cv.wait_for(lk, std::chrono::milliseconds(2), [&] { return stop || fatal || !queue.empty(); });
+        if (stop || fatal) break;
         const double t = server_now(t0);
-        const bool may_rebuild = idle || t - last_rebuild >= cfg.rebuild_interval_s;
-        while (may_rebuild && !pending.empty()) {
-          Req& r = pending.front();
-          const int n_act = (int)active.size() + (int)admit.size();
+        const bool may_rebuild = idle || t - ln.last_rebuild >= cfg.rebuild_interval_s;
+        while (may_rebuild && !queue.empty()) {
+          Req& r = queue.front();
+          const int n_act = (int)ln.active.size() + (int)admit.size();
           if (r.bytes > cfg.budget_bytes) {  // can never fit
             Req bad = r;
-            pending.pop_front();
+            queue.pop_front();
             lk.unlock();
             finish(bad, LG_EBUDGET, nullptr, server_now(t0));
             lk.lock();
@@ -139,59 +174,46 @@ struct lg_server {
           if (active_bytes + r.bytes > cfg.budget_bytes || n_act >= cfg.max_active) break;
           active_bytes += r.bytes;
           admit.push_back(r);
-          pending.pop_front();
+          queue.pop_front();
         }
       }
       const double t = server_now(t0);
       if (!admit.empty()) {
-        int rc = rebuild(admit, t);
-        if (rc) {
-          std::lock_guard<std::mutex> lk(mu);
-          fatal = rc;
-          fatal_msg = g_err;
-          cv.notify_all();
-          break;
-        }
+        int rc = rebuild(ln, admit, t);
+        if (rc) { fail(rc); break; }
       }
-      if (!eng) continue;
+      if (!ln.eng) continue;
       bool any = false;
-      for (size_t c = 0; c < active.size(); ++c) any = any || !retired[c];
+      for (size_t c = 0; c < ln.active.size(); ++c) any = any || !ln.retired[c];
       if (!any) {
-        std::lock_guard<std::mutex> lk(mu);
-        eng.reset();
-        active.clear();
-        retired.clear();
+        ln.eng.reset();
+        ln.active.clear();
+        ln.retired.clear();
         continue;
       }
-      int rc = eng->run(cfg.sweeps_per_tick);
-      if (rc) {
-        std::lock_guard<std::mutex> lk(mu);
-        fatal = rc;
-        fatal_msg = g_err;
-        cv.notify_all();
-        break;
-      }
+      int rc = ln.eng->run(cfg.sweeps_per_tick);
+      if (rc) { fail(rc); break; }
       long long ss = 0;
-      for (size_t c = 0; c < active.size(); ++c)
-        if (!retired[c]) ss += (long long)eng->spec[c].volume * cfg.sweeps_per_tick;
+      for (size_t c = 0; c < ln.active.size(); ++c)
+        if (!ln.retired[c]) ss += (long long)ln.eng->spec[c].volume * cfg.sweeps_per_tick;
       {
         std::lock_guard<std::mutex> lk(mu);
         stats.site_sweeps += ss;
       }
       const double tn = server_now(t0);
-      for (size_t c = 0; c < active.size(); ++c) {
-        if (retired[c]) continue;
-        const ChainSpec& s = eng->spec[c];
-        if (s.mcs < (uint64_t)(s.therm + s.sweeps)) continue;
+      for (size_t c = 0; c < ln.active.size(); ++c) {
+        if (ln.retired[c]) continue;
+        const ChainSpec& sp = ln.eng->spec[c];
+        if (sp.mcs < (uint64_t)(sp.therm + sp.sweeps)) continue;
         lg_obs o;
-        eng->acc[c].report(s, &o);
-        retired[c] = true;
-        eng->set_active((int)c, false);
+        ln.eng->acc[c].report(sp, &o);
+        ln.retired[c] = true;
+        ln.eng->set_active((int)c, false);
         {
           std::lock_guard<std::mutex> lk(mu);
-          active_bytes -= active[c].bytes;
+          active_bytes -= ln.active[c].bytes;
         }
-        finish(active[c], LG_OK, &o, tn);
+        finish(ln.active[c], LG_OK, &o, tn);
       }
     }
   }
@@ -204,6 +226,7 @@ void lg_server_config_default(lg_server_config* c) {
   c->sweeps_per_tick = 16;
   c->rebuild_interval_s = 0.02;
   c->max_active = 4096;
+  c->lanes = 2;
 }
 
 double lg_request_bytes(const lg_params* p) {
@@ -213,13 +236,20 @@ double lg_request_bytes(const lg_params* p) {
 }
 
 int lg_server_create(const lg_server_config* cfg, lg_server** out) {
-  if (!cfg || !out || cfg->sweeps_per_tick < 1 || !(cfg->budget_bytes > 0))
+  if (!cfg || !out || cfg->sweeps_per_tick < 1 || !(cfg->budget_bytes > 0) || cfg->lanes < 1 ||
+      cfg->lanes > lg_server::MAX_LANES)
     return lg_fail(LG_EINVAL, "bad server configuration");
   lg_server* s = new lg_server();
   s->cfg = *cfg;
+  s->nlanes = cfg->lanes;
   s->t0 = std::chrono::steady_clock::now();
   cudaGetDevice(&s->device);
-  s->th = std::thread([s] { s->loop(); });
+  // lane 0 (the smallest requests) gets the greatest stream priority, so that its short sweeps
+  // are scheduled ahead of the long ones of the larger lanes
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess)
+    for (int k = 0; k < s->nlanes; ++k) s->lanes[k].priority = std::min(least, greatest + k);
+  for (int k = 0; k < s->nlanes; ++k) s->lanes[k].th = std::thread([s, k] { s->loop(k); });
   *out = s;
   return LG_OK;
 }
@@ -235,7 +265,7 @@ int lg_server_submit(lg_server* s, const lg_params* p, uint64_t* id) {
   r.id = s->next_id++;
   r.t_submit = server_now(s->t0);
   r.t_start = -1;
-  s->pending.push_back(r);
+  s->pending[s->lane_of(r.spec)].push_back(r);
   s->stats.submitted++;
   if (id) *id = r.id;
   s->cv.notify_all();
@@ -265,7 +295,8 @@ int lg_server_get_stats(lg_server* s, lg_server_stats* out) {
   std::lock_guard<std::mutex> lk(s->mu);
   *out = s->stats;
   out->active_bytes = s->active_bytes;
-  out->queued = (int64_t)s->pending.size();
+  out->queued = 0;
+  for (int k = 0; k < s->nlanes; ++k) out->queued += (int64_t)s->pending[k].size();
   out->elapsed_s = server_now(s->t0);
   return LG_OK;
 }
@@ -277,7 +308,8 @@ int lg_server_destroy(lg_server* s) {
     s->stop = true;
     s->cv.notify_all();
   }
-  if (s->th.joinable()) s->th.join();
+  for (int k = 0; k < s->nlanes; ++k)
+    if (s->lanes[k].th.joinable()) s->lanes[k].th.join();
   delete s;
   return LG_OK;
 }

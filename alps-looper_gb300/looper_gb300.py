@@ -54,7 +54,8 @@ class Obs(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("budget_bytes", ctypes.c_double), ("sweeps_per_tick", ctypes.c_int),
-                ("rebuild_interval_s", ctypes.c_double), ("max_active", ctypes.c_int)]
+                ("rebuild_interval_s", ctypes.c_double), ("max_active", ctypes.c_int),
+                ("lanes", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -538,7 +539,7 @@ class Server:
     """Request server with continuous batching (lg_server_*)."""
 
     def __init__(self, budget_bytes=None, sweeps_per_tick=None, rebuild_interval_s=None,
-                 max_active=None):
+                 max_active=None, lanes=None):
         c = ServerConfig()
         lib().lg_server_config_default(ctypes.byref(c))
         if budget_bytes is not None:
@@ -549,6 +550,8 @@ class Server:
             c.rebuild_interval_s = float(rebuild_interval_s)
         if max_active is not None:
             c.max_active = int(max_active)
+        if lanes is not None:
+            c.lanes = int(lanes)
         h = ctypes.c_void_p()
         check(lib().lg_server_create(ctypes.byref(c), ctypes.byref(h)))
         self._h = h

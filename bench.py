@@ -305,9 +305,9 @@ def served_requests(lg, n=4096, seed=2024):
     return out
 
 
-def run_served(lg, n_requests, plain_sample=12):
+def run_served(lg, n_requests, plain_sample=32, lanes=3):
     reqs = served_requests(lg)[:n_requests]
-    srv = lg.Server(sweeps_per_tick=16, rebuild_interval_s=0.02)
+    srv = lg.Server(sweeps_per_tick=16, rebuild_interval_s=0.02, lanes=lanes)
     t0 = time.perf_counter()
     for t_arr, p in reqs:
         d = t0 + t_arr - time.perf_counter()
@@ -342,7 +342,7 @@ def run_served(lg, n_requests, plain_sample=12):
     q = lambda f: lat[min(len(lat) - 1, int(f * len(lat)))] if lat else None  # noqa: E731
     return {"workload": "served stream: first %d of 4096 Poisson requests (200/s, seed 2024)"
                         % len(reqs),
-            "value": served, "unit": UNIT, "wall_s": wall, "completed": len(ok),
+            "value": served, "unit": UNIT, "wall_s": wall, "completed": len(ok), "lanes": lanes,
             "rejected": int(st["rejected"]), "rebuilds": int(st["rebuilds"]),
             "latency_p50_s": q(0.50), "latency_p99_s": q(0.99),
             "plain_value": plain, "plain_sample_requests": len(idx),
@@ -499,7 +499,7 @@ def main():
     ap.add_argument("--batched-therm", type=int, default=128)
     ap.add_argument("--replica-steps", type=int, default=8)
     ap.add_argument("--replica-therm", type=int, default=32)
-    ap.add_argument("--served-requests", type=int, default=48)
+    ap.add_argument("--served-requests", type=int, default=256)
     ap.add_argument("--shape", default="auto",
                     help='launch shape of the headline chain: "auto" (autotuned) or a JSON dict '
                          'of lg_shape fields')

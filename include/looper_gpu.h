@@ -299,7 +299,10 @@ typedef struct lg_server_config {
   double budget_bytes;       /* device memory budget for admitted requests (default 150e9)    */
   int sweeps_per_tick;       /* sweeps between admission / retirement points (default 16)    */
   double rebuild_interval_s; /* minimum time between arena rebuilds while busy (0.02 s)      */
-  int max_active;            /* maximum chains in the arena (default 4096)                   */
+  int max_active;            /* maximum chains in one lane's arena (default 4096)            */
+  int lanes;                 /* size classes, each with its own arena, host thread and CUDA
+                                stream, run side by side (1..4, default 2): a request goes to
+                                the lane of its expected operators per sweep                   */
 } lg_server_config;
 typedef struct lg_result {
   uint64_t id;

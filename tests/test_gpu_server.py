@@ -1,4 +1,5 @@
-"""Continuous-batching server: every served result equals the same request run alone."""
+"""Continuous-batching server: every served result equals the same request run alone, with one
+arena or with requests spread over size-class lanes that run side by side."""
 import numpy as np
 import pytest
 
@@ -20,15 +21,21 @@ REQS = [
     dict(LATTICE="square", L=16, BETA=8.0, Jxy=1.0, Jz=1.0, h=0.0, SWEEPS=128, THERMALIZATION=16),
     dict(LATTICE="chain", L=200, BETA=1.0, Jxy=1.0, Jz=0.5, h=0.4, SWEEPS=48, THERMALIZATION=6),
     dict(LATTICE="cubic", L=6, BETA=0.7, Jxy=1.0, Jz=1.5, h=0.1, SWEEPS=80, THERMALIZATION=10),
+    # about 3x10^4 operators per sweep: a different size class from the others
+    dict(LATTICE="square", L=32, BETA=16.0, Jxy=1.0, Jz=1.0, h=0.0, SWEEPS=40, THERMALIZATION=8),
 ]
 
 
-def test_served_results_equal_alone(lg):
+@pytest.mark.parametrize("lanes", [1, 3])
+def test_served_results_equal_alone(lg, lanes):
     params = [lg.make_params(SEED=500 + i, INITIAL_SPINS="random", **r) for i, r in enumerate(REQS)]
-    srv = lg.Server(sweeps_per_tick=8, rebuild_interval_s=0.0)
-    ids = []
+    srv = lg.Server(sweeps_per_tick=8, rebuild_interval_s=0.0, lanes=lanes)
     import time
-    for p in params:          # staggered arrivals: admitted into a running arena
+    ids = [srv.submit(params[0])]
+    t_end = time.time() + 60
+    while srv.stats()["rebuilds"] < 1 and time.time() < t_end:  # the first arena exists
+        time.sleep(0.005)
+    for p in params[1:]:      # staggered arrivals: admitted into a running arena
         ids.append(srv.submit(p))
         time.sleep(0.01)
     srv.wait(300)
