@@ -170,3 +170,103 @@ def _kubo(beta, ev, U, d, w, e_min):
     with np.errstate(divide="ignore", invalid="ignore"):
         wij = np.where(np.abs(diff) > 1e-12, -(wn - wm) / diff, beta * wn)
     return float((A2 * wij).sum())
+
+
+def chain_translation(L: int, T: float, jxy: float = 1.0, jz: float = 1.0, h: float = 0.0):
+    """diag.C's thermal averages for the periodic S=1/2 XXZ chain, block-diagonal in total Sz
+    and crystal momentum (the translation eigenbasis |a(k)> = N_a^-1/2 sum_r e^{-ikr} T^r |a> of
+    representatives a), so that L = 16 needs blocks of ~800 states instead of 12870.  Returns the
+    operators that commute with translations: Energy (Density), Specific Heat, Magnetization^2,
+    Susceptibility (= beta <M^2> / V, M conserved), the Spin Correlations <Sz_0 Sz_r> and from them
+    Staggered Magnetization^2 = L sum_r (-1)^r <Sz_0 Sz_r> (L even)."""
+    beta = 1.0 / T
+    full = (1 << L) - 1
+
+    def rot(v):  # translation by one site: bit i -> bit i+1
+        return ((v << 1) | (v >> (L - 1))) & full
+
+    def szz_row(v):  # sum_i Sz_i Sz_{i+r} for every r (diagonal, translation invariant)
+        s = np.array([((v >> i) & 1) - 0.5 for i in range(L)])
+        return np.array([float((s * np.roll(s, -r)).sum()) for r in range(L)])
+
+    levels = []   # (energies, weights over representatives per eigenvector, rep diag values)
+    e_min = math.inf
+    for nup in range(L + 1):
+        reps, per = [], {}
+        for st in _sector_states(L, nup):
+            v = int(st)
+            orbit, w, R = [v], v, 0
+            for r in range(1, L + 1):
+                w = rot(w)
+                if w == v:
+                    R = r
+                    break
+                orbit.append(w)
+            if min(orbit) == v:
+                reps.append(v)
+                per[v] = R
+        idx = {a: i for i, a in enumerate(reps)}
+        # representative and shift of every state of the sector
+        rep_of = {}
+        for a in reps:
+            w = a
+            for l in range(per[a]):
+                rep_of[w] = (a, l)   # T^l a = w, so T^{-l} w = a
+                w = rot(w)
+        diag = np.zeros(len(reps))
+        offd = []   # (i_a, i_b, l): H_j |a> = Jxy/2 T^{-l}... stored as the shift from b to the state
+        for i, a in enumerate(reps):
+            bits = [(a >> k) & 1 for k in range(L)]
+            e = 0.0
+            for k in range(L):
+                b1, b2 = bits[k], bits[(k + 1) % L]
+                e += jz * (b1 - 0.5) * (b2 - 0.5)
+                if b1 != b2 and jxy != 0.0:
+                    w = a ^ (1 << k) ^ (1 << ((k + 1) % L))
+                    b, l = rep_of[w]
+                    offd.append((i, idx[b], l))
+            e -= h * (nup - L / 2.0)
+            diag[i] = e
+        corr_rep = np.array([szz_row(a) for a in reps]) / L if reps else np.zeros((0, L))
+        m2 = (nup - L / 2.0) ** 2
+        for m in range(L):
+            k = 2.0 * math.pi * m / L
+            ok = [i for i, a in enumerate(reps) if (m * per[a]) % L == 0]
+            if not ok:
+                continue
+            pos = {i: j for j, i in enumerate(ok)}
+            H = np.zeros((len(ok), len(ok)), dtype=complex)
+            for j, i in enumerate(ok):
+                H[j, j] = diag[i]
+            for (i, ib, l) in offd:
+                if i in pos and ib in pos:
+                    # H|a(k)> gets jxy/2 e^{-ik l'} sqrt(R_a / R_b) |b(k)>, where T^{l'} w = b, i.e.
+                    # l' = -l (w = T^l b)
+                    ra, rb = per[reps[i]], per[reps[ib]]
+                    H[pos[ib], pos[i]] += jxy / 2 * np.exp(1j * k * l) * math.sqrt(ra / rb)
+            ev, U = np.linalg.eigh(H)
+            P = np.abs(U) ** 2
+            levels.append((ev, P.T @ corr_rep[ok], m2))
+            e_min = min(e_min, ev[0])
+    Z = E1 = E2 = M2 = 0.0
+    corr = np.zeros(L)
+    for ev, cr, m2 in levels:
+        w = np.exp(-beta * (ev - e_min))
+        Z += w.sum()
+        E1 += (w * ev).sum()
+        E2 += (w * ev ** 2).sum()
+        M2 += w.sum() * m2
+        corr += w @ cr
+    E1 /= Z
+    E2 /= Z
+    corr /= Z
+    sign = np.array([(-1.0) ** r for r in range(L)])
+    return {
+        "Energy": E1,
+        "Energy Density": E1 / L,
+        "Specific Heat": beta ** 2 * (E2 - E1 ** 2) / L,
+        "Magnetization^2": M2 / Z,
+        "Susceptibility": beta * M2 / Z / L,
+        "Spin Correlations": corr,
+        "Staggered Magnetization^2": L * float((sign * corr).sum()),
+    }

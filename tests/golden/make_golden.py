@@ -6,6 +6,7 @@ Sources:
   * loop.op (diag + PI blocks)    -> loop_op.json              (known answers, L=4 chains,
                                                                   with the correlation vectors)
   * oracle (philox mode) configs  -> uf_labels.json            (cluster-construction configs)
+  * oracle/ed.py (momentum ED)    -> ed_chain16.json           (exact L=16 chain at T=0.1)
     labelled by the reference's own looper/union_find.h, compiled in place by oracle/Makefile
     (oracle/_ref/uf_deterministic, oracle/_ref/uf_weighted).
 
@@ -182,6 +183,18 @@ def uf_labels():
     return out
 
 
+def ed_chain16():
+    """Exact values for the S=1/2 Heisenberg chain L=16, J=1, T=0.1 (the CPU-runnable chain
+    workload's correctness point), from the momentum-sector restatement of diag.C in
+    oracle/ed.py (about 20 s of CPU, hence stored)."""
+    sys.path.insert(0, os.path.join(os.path.dirname(HERE), "..", "oracle"))
+    import ed
+    r = ed.chain_translation(16, 0.1, 1.0, 1.0, 0.0)
+    return {"L": 16, "T": 0.1, "jxy": 1.0, "jz": 1.0, "h": 0.0,
+            "values": {k: (list(map(float, v)) if hasattr(v, "__len__") else float(v))
+                       for k, v in r.items()}}
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     data = {
@@ -189,6 +202,7 @@ def main():
         "union_find_op.json": union_find(ref),
         "loop_op.json": loop_op(ref),
         "uf_labels.json": uf_labels(),
+        "ed_chain16.json": ed_chain16(),
     }
     for name, obj in data.items():
         with open(os.path.join(HERE, name), "w") as f:

@@ -234,3 +234,19 @@ def test_observables_vs_exact_diagonalization(lg, case):
               "Magnetization^2", "Staggered Magnetization^2"):
         mean, err = obs[k]
         assert abs(mean - ref[k]) <= 3.5 * err + 1e-9, (k, mean, err, ref[k])
+
+
+def test_chain16_vs_exact_diagonalization(lg, golden):
+    # the CPU-runnable chain workload (Heisenberg AF chain, J=1, T=0.1, 2^12 + 2^14 sweeps,
+    # seed 1234, random spins) at L=16, where its correctness point is exact diagonalization
+    g = golden("ed_chain16.json")
+    w = lg.LoopWorker(lg.make_params(LATTICE="chain", L=16, T=0.1, J=1.0, SEED=1234,
+                                     SWEEPS=1 << 14, THERMALIZATION=1 << 12,
+                                     INITIAL_SPINS="random"))
+    w.run((1 << 14) + (1 << 12))
+    obs = w.observables()
+    for k in ("Energy", "Energy Density", "Susceptibility", "Staggered Magnetization^2",
+              "Specific Heat"):
+        mean, err = obs[k]
+        assert abs(mean - g["values"][k]) <= 3.5 * err, (k, mean, err, g["values"][k])
+    w.close()

@@ -188,3 +188,27 @@ def test_philox_spin1_chain_vs_ed():
 def test_philox_spin3half_xxz_field_chain_vs_ed():
     _check_vs_ed(1, 4, 1.0, 1.0, 0.5, 0.2, 1000, 30000, 13,
                  ["Energy", "Specific Heat", "Magnetization", "Susceptibility"], spin2=3)
+
+
+def test_momentum_ed_matches_dense_ed():
+    for (L, T, jxy, jz, h) in [(8, 0.3, 1.0, 0.5, 0.2), (8, 1.0, -1.0, 1.0, 0.0)]:
+        a = orc.ed.thermal(1, L, T, jxy=jxy, jz=jz, h=h)
+        b = orc.ed.chain_translation(L, T, jxy, jz, h)
+        for k in ("Energy", "Specific Heat", "Magnetization^2", "Staggered Magnetization^2"):
+            assert b[k] == pytest.approx(a[k], rel=1e-9, abs=1e-12), k
+        assert np.allclose(b["Spin Correlations"], a["Spin Correlations"], atol=1e-12)
+
+
+def test_philox_chain16_vs_exact_golden(golden):
+    # the CPU-runnable chain workload's correctness point: Heisenberg chain L=16 at T=0.1
+    g = golden("ed_chain16.json")
+    o = orc.Oracle(1, 16, 10.0, 1.0, 1.0, 0.0, seed=1234)
+    o.sweep(1 << 12)
+    o.clear_records()
+    o.sweep(1 << 14)
+    obs = orc.observables(o.records(), 1, 16, 10.0)
+    for k in ("Energy", "Susceptibility", "Staggered Magnetization^2"):
+        m, e = orc.binned(obs[k])
+        assert abs(m - g["values"][k]) <= 3.5 * e, (k, m, e, g["values"][k])
+    m, e = orc.specific_heat(obs, 10.0, 16)
+    assert abs(m - g["values"]["Specific Heat"]) <= 3.5 * e
