@@ -168,6 +168,9 @@ int ChainSpec::init(const lg_params& p) {
   L = p.L;
   spin2 = p.spin2 >= 1 ? p.spin2 : 1;
   if (spin2 > 8) return lg_fail(LG_EUNSUPPORTED, "local_S = %d/2 > 4 is not supported", spin2);
+  if (2 * p.lattice * spin2 > MAXZ)  // incident virtual bonds of a virtual site
+    return lg_fail(LG_EUNSUPPORTED, "local_S = %d/2 on this lattice gives %d incident bonds > %d",
+                   spin2, 2 * p.lattice * spin2, MAXZ);
   long long n = 1;
   for (int i = 0; i < dim; ++i) n *= L;
   if (n * spin2 > (1ll << 22))

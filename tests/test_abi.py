@@ -99,3 +99,22 @@ def test_request_bytes_estimate(lg):
     b = lg.request_bytes(lg.make_params(LATTICE="square", L=128, BETA=64.0))
     assert 1e8 < b < 2e9
     assert lg.request_bytes(lg.make_params(LATTICE="square", L=7, T=1.0)) < 0  # sign problem
+
+
+def test_invalid_models_are_rejected_before_device_work(lg):
+    # lg_create validates the parameters (ChainSpec::init) before touching the GPU, so each of
+    # these returns its status code on a machine without one
+    cases = [
+        (dict(LATTICE="chain", L=1), -1),                                 # LG_EINVAL
+        (dict(LATTICE="chain", L=8, T=-1.0), -1),
+        (dict(LATTICE="cubic", L=162, T=1.0), -6),                        # > 2^22 sites: EBUDGET
+        (dict(LATTICE="square", L=7, T=1.0), -4),                         # sign problem
+        (dict(LATTICE="square", L=8, T=1.0, local_S=1), -4),              # 8 virtual neighbours
+        (dict(LATTICE="chain", L=8, T=1.0, local_S=2.5), -4),             # S > 3/2 on a chain
+        (dict(LATTICE="chain", L=8, T=1.0, local_S=1, MEASURE_CORRELATIONS=True), -4),
+        (dict(LATTICE="chain", L=8, T=1.0, MEASURE_CORRELATIONS=True, INITIAL_SITE=8), -1),
+    ]
+    for kw, code in cases:
+        with pytest.raises(lg.LoopError) as e:
+            lg.LoopWorker(lg.make_params(**kw))
+        assert e.value.code == code, (kw, e.value)

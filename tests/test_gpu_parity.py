@@ -64,6 +64,14 @@ MODELS = {
     "chain12_ferro": dict(dim=1, L=12, beta=5.0, jxy=-1.0, jz=-1.0, h=0.0),
     "chain10_ising": dict(dim=1, L=10, beta=2.0, jxy=0.0, jz=1.0, h=0.0),
     "chain9_ferro_odd": dict(dim=1, L=9, beta=2.0, jxy=-1.0, jz=0.3, h=0.1),
+    # edge cases: the smallest periodic lattices (both bonds of a pair join the same two sites),
+    # a model with no operators at all (only the field acts on single-site clusters), and a
+    # temperature so high that most sweeps have none
+    "chain2_heisenberg": dict(dim=1, L=2, beta=3.0, jxy=1.0, jz=1.0, h=0.0),
+    "square2_xxz": dict(dim=2, L=2, beta=2.0, jxy=1.0, jz=0.5, h=0.0),
+    "cubic2_field": dict(dim=3, L=2, beta=1.0, jxy=1.0, jz=1.0, h=0.1),
+    "chain8_free_spins_field": dict(dim=1, L=8, beta=2.0, jxy=0.0, jz=0.0, h=0.5),
+    "chain16_hot": dict(dim=1, L=16, beta=0.01, jxy=1.0, jz=1.0, h=0.0),
 }
 
 
