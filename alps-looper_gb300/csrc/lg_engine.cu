@@ -720,8 +720,17 @@ struct Engine {
       Ctl z = hc;
       z.step = 0;
       z.err = 0;
-      if (hc.err == ERR_ITERCAP)
-        return lg_fail(LG_EITERCAP, "union-find iteration cap hit");
+      if (hc.err == ERR_ITERCAP) {
+        // the sweep stopped after the merge had overwritten the persistent operator lists, so
+        // the arena's state is lost: the error stays set (every later run reports it) until a
+        // checkpoint is loaded (set_state on a single-chain engine)
+        Ctl zk = hc;
+        zk.step = 0;
+        LG_CUDA(cudaMemcpy(d_ctl.p, &zk, sizeof(Ctl), cudaMemcpyHostToDevice));
+        clear_sweep_state();
+        return lg_fail(LG_EITERCAP, "union-find iteration cap hit; the chain state is lost "
+                                    "(load a checkpoint to continue)");
+      }
       if (hc.err == ERR_BOUNDARY) {
         LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
         clear_sweep_state();
@@ -980,8 +989,24 @@ struct Engine {
     return LG_OK;
   }
 
+  // Union-find retries per union (Ctl::iter_cap): a test seam for the LG_EITERCAP path.
+  int set_iter_cap(int cap) {
+    Ctl hc;
+    LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    hc.iter_cap = cap;
+    LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
+    return LG_OK;
+  }
+
   int set_state(int c, const int32_t* spins, const int32_t* bonds, const double* times, long long n,
                 uint64_t sweep) {
+    if (C == 1) {  // a complete state: a union-find failure (LG_EITERCAP) no longer applies
+      Ctl hc;
+      LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+      hc.err = 0;
+      hc.step = 0;
+      LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
+    }
     const ChainSpec& s = spec[c];
     const int so = hch[c].site_off;
     SiteLists L;
@@ -1409,6 +1434,11 @@ int lg_save(lg_chain* c, void* buf, size_t* size) {
   std::memcpy(buf, blob.data(), blob.size());
   *size = blob.size();
   return LG_OK;
+}
+
+int lg_set_iteration_cap(lg_chain* c, int cap) {
+  if (!c) return lg_fail(LG_EINVAL, "null argument");
+  return c->eng->set_iter_cap(cap);
 }
 
 int lg_load(lg_chain* c, const void* buf, size_t size) {

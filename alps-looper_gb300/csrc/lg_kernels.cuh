@@ -981,11 +981,18 @@ __device__ __forceinline__ int uf_find_from(int* P, int x, int p) {
   }
 }
 
+// The retry cap of the unions of a sweep: Ctl::iter_cap, 0 meaning ITER_CAP; a negative value
+// lets no union run at all (a test seam for the LG_EITERCAP path).
+__device__ __forceinline__ int iter_cap_of(const Ctl* c) {
+  const int v = c->iter_cap;
+  return v < 0 ? 0 : (v == 0 ? ITER_CAP : v);
+}
+
 // The first parent reads of both finds are issued together (one round trip instead of two when
 // both nodes are roots).  Hooks always go from a larger to a smaller index, so parent pointers
 // decrease along every path and no interleaving of unions can close a cycle.
-__device__ __forceinline__ bool uf_union(int* P, int a, int b) {
-  for (int it = 0; it < ITER_CAP; ++it) {
+__device__ __forceinline__ bool uf_union(int* P, int a, int b, int cap = ITER_CAP) {
+  for (int it = 0; it < cap; ++it) {
     const int pa = __ldcg(P + a), pb = __ldcg(P + b);
     a = uf_find_from(P, a, pa);
     b = uf_find_from(P, b, pb);
@@ -1024,7 +1031,8 @@ __global__ void __launch_bounds__(256) k_boundary(Arena A) {
       continue;
     }
     bool ok = true;
-    for (int a = 0; a < sp2; ++a) ok &= uf_union(A.parent, bot[a], top[pair[a]]);
+    const int cap = iter_cap_of(A.ctl);
+    for (int a = 0; a < sp2; ++a) ok &= uf_union(A.parent, bot[a], top[pair[a]], cap);
     if (!ok) atomicExch(&A.ctl->err, ERR_ITERCAP);
   }
 }
@@ -1050,6 +1058,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_union(Arena A) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
   const long long stride = (long long)gridDim.x * WARPS * UN_CHUNK;
+  const int cap = iter_cap_of(A.ctl);
   bool ok = true;
   for (long long c0 = ((long long)blockIdx.x * WARPS + w) * UN_CHUNK; c0 < ns; c0 += stride) {
     const int x0 = (int)c0 + lane, x1 = x0 + 32;
@@ -1071,12 +1080,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_union(Arena A) {
       const int a = pend[w][j], b = pb[w][j], g = pg[w][j];
       int* P = A.parent;
       if (g == 1) {
-        ok &= uf_union(P, a - 1, b);
-        ok &= uf_union(P, b - 1, a);
+        ok &= uf_union(P, a - 1, b, cap);
+        ok &= uf_union(P, b - 1, a, cap);
       } else {
-        ok &= uf_union(P, a - 1, b - 1);
-        ok &= uf_union(P, a, b);
-        if (g & 2) ok &= uf_union(P, a - 1, a);
+        ok &= uf_union(P, a - 1, b - 1, cap);
+        ok &= uf_union(P, a, b, cap);
+        if (g & 2) ok &= uf_union(P, a - 1, a, cap);
       }
     }
     __syncwarp();

@@ -47,7 +47,8 @@ struct Ctl {
   uint32_t step;     // record row of the current sweep
   int nv_cap;
   int ns_cap;
-  int pad[2];
+  int iter_cap;      // union-find retries per union: 0 = ITER_CAP; < 0 = none (test seam)
+  int pad;
 };
 
 }  // namespace lg

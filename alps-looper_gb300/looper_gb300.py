@@ -115,6 +115,7 @@ def lib():
             "lg_set_state": (ctypes.c_int, [vp, vp, vp, vp, i64, u64]),
             "lg_fetch_records": (ctypes.c_int, [vp, vp, i64, vp]),
             "lg_keep_records": (ctypes.c_int, [vp, ctypes.c_int]),
+            "lg_set_iteration_cap": (ctypes.c_int, [vp, ctypes.c_int]),
             "lg_uf_label": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, i64, vp, vp, vp, i64, vp, vp]),
             "lg_uf_label_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, i64, vp, vp, vp, vp, vp, vp]),
             "lg_batch_create": (ctypes.c_int, [ctypes.c_int, vp, vp]),
@@ -318,6 +319,11 @@ class LoopWorker:
         ns = ctypes.c_int64()
         check(lib().lg_correlation_sums(self._h, int(which), _p(out), ctypes.byref(ns)))
         return out, ns.value
+
+    def set_iteration_cap(self, cap: int):
+        """Test seam: union-find retries per union (0: default; < 0: none, forcing
+        LG_EITERCAP)."""
+        check(lib().lg_set_iteration_cap(self._h, int(cap)))
 
     def is_thermalized(self) -> bool:
         return bool(lib().lg_is_thermalized(self._h))

@@ -188,6 +188,11 @@ int lg_set_state(lg_chain* c, const int32_t* spins, const int32_t* bonds, const 
 int lg_fetch_records(lg_chain* c, uint64_t* out, int64_t cap, int64_t* n);
 /* Keep raw records for lg_fetch_records (off by default). */
 int lg_keep_records(lg_chain* c, int on);
+/* Test seam (no counterpart in the reference): the union-find retry cap per union.  0 restores
+ * the default (2^22); a negative value lets no union run, so that the next sweep stops with
+ * LG_EITERCAP.  After LG_EITERCAP the arena's state is lost and every lg_run reports the error
+ * again, until lg_load / lg_set_state restores a single chain's state. */
+int lg_set_iteration_cap(lg_chain* c, int cap);
 
 /* Cluster labels of a given cluster-construction configuration, computed on the GPU by the
  * segment union-find.  The configuration is a time-ordered vertex list (bond, graph 0..3) on a
