@@ -122,6 +122,10 @@ struct Engine {
   // spin correlations: k_corr work tiles and the per-chunk exact sums (arena site indexed)
   int n_corr_tiles = 0, corr_smem = 0;
   bool any_spin_s = false;   // some chain has S > 1/2: k_boundary closes its sites
+  // structural checks between stages (lg_validate_sweeps): the failure counter and first code;
+  // never part of a captured graph
+  int* val_bad = nullptr;
+  bool capturing = false;
   DBuf<int2> d_corr_tiles;
   DBuf<long long> d_corr_disp, d_corr_origin;
   std::vector<long long> h_corr;
@@ -576,7 +580,11 @@ struct Engine {
   void enqueue_sweep(cudaEvent_t* ev = nullptr) {
     Arena A = arena();
     int launches = 0;
-    auto mark = [&](int k) { if (ev) cudaEventRecord(ev[k], st); };
+    auto mark = [&](int k) {
+      if (ev) cudaEventRecord(ev[k], st);
+      if (val_bad && !capturing && (k == 0 || k == 2 || k == 4 || k == 6))
+        k_validate<<<grid_for(std::max(std::max(NB, N), ns_cap), 256, 16), 256, 0, st>>>(arena(), k, val_bad);
+    };
     bool both = false;
     auto fork = [&](bool b) { both = b; if (b) { cudaEventRecord(ev_fork, st); cudaStreamWaitEvent(st2, ev_fork, 0); } };
     auto join = [&]() { if (both) { cudaEventRecord(ev_join, st2); cudaStreamWaitEvent(st, ev_join, 0); } };
@@ -667,7 +675,9 @@ struct Engine {
     if (!use_graph || gexec) return LG_OK;
     LG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     uint64_t before = g_launches.load();
+    capturing = true;
     enqueue_sweep();
+    capturing = false;
     g_launches = before;  // counted when the graph is launched
     LG_CUDA(cudaStreamEndCapture(st, &graph));
     LG_CUDA(cudaGraphInstantiate(&gexec, graph, 0));
@@ -986,6 +996,25 @@ struct Engine {
       LG_CUDA(cudaMemcpy(d_stime.p, t.data(), total * sizeof(uint64_t), cudaMemcpyHostToDevice));
       LG_CUDA(cudaMemcpy(d_sdir.p, d.data(), total, cudaMemcpyHostToDevice));
     }
+    return LG_OK;
+  }
+
+  // n sweeps kernel by kernel with the structural checks of k_validate after insertion, merge,
+  // cluster sums and the end of the sweep.  LG_EDEVICE names the first failed check.
+  int validate(long long n) {
+    DBuf<int> bad;
+    int rc = bad.alloc(2);
+    if (rc) return rc;
+    LG_CUDA(cudaMemset(bad.p, 0, 2 * sizeof(int)));
+    std::vector<double> km(kNumStages);
+    long long v = 0;
+    val_bad = bad.p;
+    rc = profile(n, 0, km.data(), &v);
+    val_bad = nullptr;
+    if (rc) return rc;
+    int hb[2];
+    LG_CUDA(cudaMemcpy(hb, bad.p, sizeof(hb), cudaMemcpyDeviceToHost));
+    if (hb[0]) return lg_fail(LG_EDEVICE, "structural check %d failed (%d failures)", hb[1], hb[0]);
     return LG_OK;
   }
 
@@ -1434,6 +1463,17 @@ int lg_save(lg_chain* c, void* buf, size_t* size) {
   std::memcpy(buf, blob.data(), blob.size());
   *size = blob.size();
   return LG_OK;
+}
+
+int lg_validate_sweeps(lg_chain* c, int64_t n) {
+  if (!c || n < 0) return lg_fail(LG_EINVAL, "bad argument");
+  if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_validate_sweeps on a batch member; use lg_batch_validate_sweeps");
+  return c->eng->validate(n);
+}
+
+int lg_batch_validate_sweeps(lg_batch* b, int64_t n) {
+  if (!b || n < 0) return lg_fail(LG_EINVAL, "bad argument");
+  return b->eng->validate(n);
 }
 
 int lg_set_iteration_cap(lg_chain* c, int cap) {

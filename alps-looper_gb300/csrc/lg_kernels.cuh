@@ -1728,6 +1728,81 @@ __global__ void __launch_bounds__(1024) k_end(Arena A) {
   if (threadIdx.x == 0) A.ctl->step = step + 1u;
 }
 
+// Structural invariants after a stage of a sweep (the test seam lg_validate_sweeps; never on the
+// hot path).  Every index the sweep kernels dereference comes from these structures: the bonds'
+// vertex ranges, the site segment offsets, the vertex <-> segment links, the union-find forest
+// and the off-diagonal lists.  Each index is range-checked here before it is used.  A failed
+// check counts in bad[0]; the first failure's code (stage * 10 + check) is kept in bad[1].
+__device__ __forceinline__ void val_fail(int* bad, int code) {
+  atomicAdd(bad, 1);
+  atomicCAS(bad + 1, 0, code);
+}
+
+__global__ void __launch_bounds__(256) k_validate(Arena A, int stage, int* bad) {
+  if (A.ctl->err) return;
+  const int nv_cap = A.ctl->nv_cap, ns_cap = A.ctl->ns_cap, ns = A.ctl->ns_total;
+  if (stage == 0) {  // after insertion: each bond's vertices inside its region, time ordered
+    LG_GRID_STRIDE(b, A.NB) {
+      const int n = A.bond_cnt[b];
+      if (n < 0) { val_fail(bad, 1); continue; }
+      if (n == 0) continue;
+      const int p = A.bond_ptr[b];
+      const int r = A.site_region[A.bond_s0[b]];
+      if (r < 0 || r >= A.R) { val_fail(bad, 2); continue; }
+      if (p < A.region_base[r] || p + n > A.region_base[r + 1] || A.region_base[r + 1] > nv_cap) {
+        val_fail(bad, 3);
+        continue;
+      }
+      uint64_t prev = 0;
+      for (int i = p; i < p + n; ++i) {
+        const uint64_t t = A.vtime[i];
+        if (t >= 0x3FF0000000000000ull || t < prev) { val_fail(bad, 4); break; }  // [0,1), ordered
+        if (A.vcode[i] > 7) { val_fail(bad, 5); break; }
+        prev = t;
+      }
+    }
+  } else if (stage == 2) {  // after the merge: segment ranges, vertex links, forest pointers
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (ns > ns_cap || ns < A.N)) val_fail(bad, 21);
+    LG_GRID_STRIDE(s, A.N) {
+      const int base = A.sbase[s], end = A.sbase[s + 1];
+      if (base < 0 || end <= base || end > ns) { val_fail(bad, 22); continue; }
+      int deg = 0;
+      for (int j = A.inc_off[s]; j < A.inc_off[s + 1]; ++j) deg += A.bond_cnt[A.inc[j]];
+      if (end - base != deg + 1) { val_fail(bad, 23); continue; }
+      if (A.stime[base] != 0ull) val_fail(bad, 24);
+      for (int x = base; x < end; ++x) {
+        if (x > base && A.stime[x] < A.stime[x - 1]) { val_fail(bad, 25); break; }
+        const int p = A.parent[x];
+        if (p < 0 || p > x) { val_fail(bad, 26); break; }  // hooks go to smaller indices
+        if (x == base) continue;
+        const int v = A.svert[x];
+        if (v < 0 || v >= nv_cap) { val_fail(bad, 27); break; }
+        const int side = (A.sinfo[x] & SI_SRC) ? 0 : 1;
+        if (A.vslot[2 * v + side] != x) { val_fail(bad, 28); break; }
+      }
+    }
+  } else if (stage == 4) {  // after the cluster sums: every parent is a root
+    LG_GRID_STRIDE(x, ns) {
+      const int r = A.parent[x];
+      if (r < 0 || r > x) { val_fail(bad, 41); continue; }
+      if (A.parent[r] != r) val_fail(bad, 42);
+    }
+  } else if (stage == 6) {  // after the sweep: the next sweep's off-diagonal lists
+    LG_GRID_STRIDE(s, A.N) {
+      const int b0 = A.off_base[s], n = A.off_cnt[s];
+      const int k = A.sbase[s + 1] - A.sbase[s] - 1;
+      if (b0 != A.sbase[s] || n < 0 || n > k) { val_fail(bad, 61); continue; }
+      const int z = A.inc_off[s + 1] - A.inc_off[s];
+      for (int i = 0; i < n; ++i) {
+        if (A.sdir[b0 + i] >= z) { val_fail(bad, 62); break; }
+        if (i > 0 && A.stime[b0 + i] < A.stime[b0 + i - 1]) { val_fail(bad, 63); break; }
+      }
+      // a spin-1/2 site's spin is periodic in imaginary time: an even number of flips
+      if ((n & 1) && A.ch[A.site_chain[s]].spin2 <= 1) val_fail(bad, 64);
+    }
+  }
+}
+
 // Moving chains into a new arena: site s of the new arena takes the state of site map[s] of
 // the old one (map[s] < 0: a new chain, left as initialised).  Pass 1 gathers list lengths.
 __global__ void k_repack_count(Arena A, const int* map, const int* old_off_cnt, int* cnt) {

@@ -116,6 +116,8 @@ def lib():
             "lg_fetch_records": (ctypes.c_int, [vp, vp, i64, vp]),
             "lg_keep_records": (ctypes.c_int, [vp, ctypes.c_int]),
             "lg_set_iteration_cap": (ctypes.c_int, [vp, ctypes.c_int]),
+            "lg_validate_sweeps": (ctypes.c_int, [vp, i64]),
+            "lg_batch_validate_sweeps": (ctypes.c_int, [vp, i64]),
             "lg_uf_label": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, i64, vp, vp, vp, i64, vp, vp]),
             "lg_uf_label_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, i64, vp, vp, vp, vp, vp, vp]),
             "lg_batch_create": (ctypes.c_int, [ctypes.c_int, vp, vp]),
@@ -320,6 +322,10 @@ class LoopWorker:
         check(lib().lg_correlation_sums(self._h, int(which), _p(out), ctypes.byref(ns)))
         return out, ns.value
 
+    def validate_sweeps(self, n: int):
+        """n sweeps with structural checks between the kernels (raises on a failed check)."""
+        check(lib().lg_validate_sweeps(self._h, int(n)))
+
     def set_iteration_cap(self, cap: int):
         """Test seam: union-find retries per union (0: default; < 0: none, forcing
         LG_EITERCAP)."""
@@ -451,6 +457,10 @@ class Batch:
         a, b = ctypes.c_int64(), ctypes.c_int64()
         check(lib().lg_batch_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def validate_sweeps(self, n: int):
+        """n sweeps of the arena with structural checks between the kernels."""
+        check(lib().lg_batch_validate_sweeps(self._h, int(n)))
 
     def time_sweeps(self, n, flush_bytes=0):
         return _time(lib().lg_batch_time_sweeps, self._h, n, flush_bytes)

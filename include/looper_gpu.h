@@ -193,6 +193,13 @@ int lg_keep_records(lg_chain* c, int on);
  * LG_EITERCAP.  After LG_EITERCAP the arena's state is lost and every lg_run reports the error
  * again, until lg_load / lg_set_state restores a single chain's state. */
 int lg_set_iteration_cap(lg_chain* c, int cap);
+/* Test seam (no counterpart in the reference): n sweeps run kernel by kernel, with structural
+ * checks after insertion, merge, cluster sums and the end of each sweep (vertex ranges inside
+ * their regions and time ordered, segment offsets and vertex <-> segment links consistent,
+ * union-find pointers decreasing and compressed, off-diagonal lists ordered and of even length
+ * per spin-1/2 site).  Every index is range-checked before use.  The sweeps count as done and
+ * give the same trajectory as lg_run.  LG_EDEVICE names the first failed check. */
+int lg_validate_sweeps(lg_chain* c, int64_t n);
 
 /* Cluster labels of a given cluster-construction configuration, computed on the GPU by the
  * segment union-find.  The configuration is a time-ordered vertex list (bond, graph 0..3) on a
@@ -231,6 +238,8 @@ int lg_batch_size(const lg_batch* b);
 int lg_batch_stats(const lg_batch* b, int64_t* total_sites, int64_t* site_sweeps);
 /* Access one chain of a batch through the single-chain test seams. */
 lg_chain* lg_batch_chain(lg_batch* b, int i);
+/* lg_validate_sweeps for a whole arena (test seam). */
+int lg_batch_validate_sweeps(lg_batch* b, int64_t n);
 
 /* ---- launch shapes and the autotuner (no counterpart in the reference) ---------------------
  * The shape of an arena's sweep launches.  No shape changes any result (trajectories, records
