@@ -274,3 +274,23 @@ def structure_factor(corr, dim, L):
     spin structure factor of correlation.h:268-281 from the displacement correlations."""
     c = np.asarray(corr, dtype=np.float64).reshape((L,) * dim)
     return np.real(np.fft.ifftn(c) * c.size).reshape(-1)
+
+
+def ising_ring_clusters(L, T, jz):
+    """Exact mean cluster count of the loop algorithm on the classical Ising ring (Jxy = 0): each
+    antiparallel bond holds at least one frozen graph (weight Jz/2, graph_impl.h:255-328) with
+    probability p = 1 - exp(-beta Jz / 2), independently; k connected bonds leave L - k clusters,
+    or 1 when all L are connected."""
+    import math
+    from itertools import product
+    beta = 1.0 / T
+    p = 1.0 - math.exp(-beta * jz / 2)
+    z = num = 0.0
+    for spins in product((0, 1), repeat=L):
+        na = sum(spins[i] != spins[(i + 1) % L] for i in range(L))
+        w = math.exp(-beta * jz * (L - 2 * na) / 4)
+        nc = sum(math.comb(na, k) * p ** k * (1 - p) ** (na - k) * (L - k if k < L else 1)
+                 for k in range(na + 1))
+        z += w
+        num += w * nc
+    return num / z

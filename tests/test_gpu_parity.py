@@ -258,3 +258,34 @@ def test_chain16_vs_exact_diagonalization(lg, golden):
         mean, err = obs[k]
         assert abs(mean - g["values"][k]) <= 3.5 * err, (k, mean, err, g["values"][k])
     w.close()
+
+
+def test_observables_vs_reference_path_integral_runs(lg, golden):
+    # every "loop; path integral" block of the reference's loop.op (S=1/2 and S=1 chains, L=4):
+    # the GPU's values within 3 combined standard errors of the reference's own binned results,
+    # including the mean number of clusters, which depends on the cluster algorithm itself.
+    # One printed value is itself an outlier: the Ising ring's cluster count (2.09204 +/- 0.0142)
+    # lies 3.7 sigma from the exact 2.1449, so that entry is checked against the exact value.
+    n = 0
+    for blk in golden("loop_op.json"):
+        if blk["algorithm"] != "loop; path integral":
+            continue
+        spin2 = blk.get("spin2", 1)
+        w = lg.LoopWorker(lg.make_params(LATTICE="chain", L=blk["L"], T=blk["T"], Jxy=blk["jxy"],
+                                         Jz=blk["jz"], local_S=spin2 / 2, SEED=2718 + n,
+                                         SWEEPS=1 << 16, THERMALIZATION=1 << 10,
+                                         INITIAL_SPINS="random"))
+        w.run((1 << 16) + (1 << 10))
+        obs = w.observables()
+        for k, (v, e) in blk["values"].items():
+            mean, err = obs[k]
+            if k == "Number of Clusters" and blk["jxy"] == 0.0 and spin2 == 1:
+                exact = orc.ising_ring_clusters(blk["L"], blk["T"], blk["jz"])
+                assert abs(v - exact) > 3 * float(e)            # the reference's outlier
+                assert abs(mean - exact) <= 3.0 * err, (k, mean, err, exact)
+            else:
+                tol = 3.0 * (float(e) ** 2 + err ** 2) ** 0.5
+                assert abs(mean - v) <= tol + 1e-9, (blk["T"], spin2, k, mean, err, v, e)
+            n += 1
+        w.close()
+    assert n >= 30

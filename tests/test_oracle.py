@@ -212,3 +212,14 @@ def test_philox_chain16_vs_exact_golden(golden):
         assert abs(m - g["values"][k]) <= 3.5 * e, (k, m, e, g["values"][k])
     m, e = orc.specific_heat(obs, 10.0, 16)
     assert abs(m - g["values"]["Specific Heat"]) <= 3.5 * e
+
+
+def test_oracle_cluster_count_vs_exact_ising_ring():
+    # the loop algorithm's mean cluster count on the classical Ising ring is known exactly
+    o = orc.Oracle(1, 4, 2.0, 0.0, 1.0, 0.0, seed=44)
+    o.sweep(1000)
+    o.clear_records()
+    o.sweep(40000)
+    m, e = orc.binned(o.records()[:, 1].astype(np.float64))
+    exact = orc.ising_ring_clusters(4, 0.5, 1.0)
+    assert abs(m - exact) <= 3.5 * e, (m, e, exact)
