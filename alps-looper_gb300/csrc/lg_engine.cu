@@ -149,6 +149,8 @@ struct Engine {
   int merge_cap = MERGE_CAP;      // k_merge staging capacity per warp (see set_merge_cap)
   cudaStream_t st2 = nullptr;     // the narrow kernels run beside the wide ones
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t st3 = nullptr;     // k_end runs beside the site pass
+  cudaEvent_t ev_fork3 = nullptr, ev_join3 = nullptr;
   cudaStream_t st = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -164,7 +166,10 @@ struct Engine {
     if (graph) cudaGraphDestroy(graph);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
+    if (ev_fork3) cudaEventDestroy(ev_fork3);
+    if (ev_join3) cudaEventDestroy(ev_join3);
     if (st2) cudaStreamDestroy(st2);
+    if (st3) cudaStreamDestroy(st3);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -207,6 +212,9 @@ struct Engine {
     LG_CUDA(cudaStreamCreateWithPriority(&st2, cudaStreamNonBlocking, stream_priority));
     LG_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     LG_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    LG_CUDA(cudaStreamCreateWithPriority(&st3, cudaStreamNonBlocking, stream_priority));
+    LG_CUDA(cudaEventCreateWithFlags(&ev_fork3, cudaEventDisableTiming));
+    LG_CUDA(cudaEventCreateWithFlags(&ev_join3, cudaEventDisableTiming));
     LG_CUDA(cudaFuncSetAttribute(k_corr, cudaFuncAttributeMaxDynamicSharedMemorySize, CORR_SMEM));
     // static tables
     long long nsite = 0, nbond = 0;
@@ -650,6 +658,15 @@ struct Engine {
     }
     mark(5);
     launches += 1;
+    // k_end (counters, the next record row, claim counters) needs nothing of the site pass, so
+    // it runs beside it on a third stream; k_corr reads the sweep counter before k_end advances
+    // it, so with correlations the order stays sequential
+    const bool end_beside = n_corr_tiles == 0;
+    if (end_beside) {
+      cudaEventRecord(ev_fork3, st);
+      cudaStreamWaitEvent(st3, ev_fork3, 0);
+      k_end<<<1, 1024, 0, st3>>>(A);
+    }
     fork(n_wide > 0 && n_narrow > 0);
     if (n_wide) {
       k_site_end<<<grid_for((long long)n_wide * 32, 256, 16), 256, 0, st>>>(A, wide_list, n_wide);
@@ -664,7 +681,12 @@ struct Engine {
       k_corr<<<n_corr_tiles, CORR_THREADS, corr_smem, st>>>(A);
       ++launches;
     }
-    k_end<<<1, 1024, 0, st>>>(A);
+    if (end_beside) {
+      cudaEventRecord(ev_join3, st3);
+      cudaStreamWaitEvent(st, ev_join3, 0);
+    } else {
+      k_end<<<1, 1024, 0, st>>>(A);
+    }
     mark(6);
     launches += 1;
     sweep_launches = launches;
