@@ -33,7 +33,7 @@ using namespace lg;
 // timed stages of one sweep, in launch order (an event is recorded after each stage)
 static const int kNumStages = 7;
 static const char* kStageNames[kNumStages] = {
-    "k_insert", "k_site_count+scan(sites)", "k_merge", "k_link+k_union", "k_accumulate", "k_cluster",
+    "k_insert", "k_site_count+scan(sites)", "k_merge", "k_union", "k_accumulate", "k_cluster",
     "k_site_end+k_end"};
 
 static std::atomic<uint64_t> g_launches{0};
@@ -485,7 +485,7 @@ struct Engine {
       s.narrow_k = 16.0;
     }
     const long long goal = 2ll * nsm;
-    s.acc_tile = ns_cap / 1024 >= goal ? 1024 : 512;
+    s.acc_tile = ns_cap / 2048 >= goal ? 2048 : (ns_cap / 1024 >= goal ? 1024 : 512);
     s.cl_tile = ns_cap / 4096 >= goal ? 4096 : 2048;
     s.un_warps = 8;
     return s;
@@ -629,14 +629,11 @@ struct Engine {
       ++launches;
     }
     join();
-    mark(2);
-    // k_link's plain stores come before every union (k_boundary's included)
-    k_link<<<grid_for(ns_cap, 256, 16), 256, 0, st>>>(A);
-    ++launches;
     if (any_spin_s) {
       k_boundary<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
       ++launches;
     }
+    mark(2);
     {
       const int w = shape.un_warps, per = w * UN_CHUNK;
       const int g = (ns_cap + per - 1) / per;  // one chunk per warp: no straggler tail
@@ -1137,10 +1134,9 @@ struct Engine {
     scan(d_site_cnt.p, d_sbase.p, N, &d_ctl.p->ns_total, ns_cap, 1, 0);
     k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32,
               MERGE_WARPS * merge_smem_per_warp(MERGE_CAP), st>>>(A, nullptr, N, MERGE_CAP);
-    k_link<<<grid_for(2 * nops + N, 256), 256, 0, st>>>(A);
     k_union<><<<grid_for(2 * nops + N, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
     k_compress<<<grid_for(2 * nops + N, 256), 256, 0, st>>>(A);
-    g_launches += 8;
+    g_launches += 7;
     LG_CUDA(cudaGetLastError());
     LG_CUDA(cudaStreamSynchronize(st));
     LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
@@ -1155,7 +1151,7 @@ struct Engine {
     froot.reserve(N + nops);
     for (int i = 0; i < N; ++i) froot.push_back(par[sb[i]]);
     for (long long i = 0; i < nops; ++i)
-      if (graphs[i] == 0) froot.push_back(par[vs[2 * (size_t)vidx[i]] & VS_SEG]);
+      if (graphs[i] == 0) froot.push_back(par[vs[2 * (size_t)vidx[i]]]);
     std::vector<int> minfrag(ns, -1);
     for (size_t f = 0; f < froot.size(); ++f)
       if (minfrag[froot[f]] < 0) minfrag[froot[f]] = (int)f;  // fragments visited in index order

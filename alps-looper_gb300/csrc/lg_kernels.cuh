@@ -8,8 +8,7 @@
 //   scan             site segment offsets
 //   k_merge          per site: time-ordered segment list, union-find init,
 //                    temporal closure                                          (:584-589)
-//   k_link           per vertex: the one link whose parent slot the vertex owns, as a plain store
-//   k_union          per vertex: lock-free unions of its other legs           (graph_impl.h:280-295)
+//   k_union          per vertex: lock-free unions of its four legs            (graph_impl.h:280-295)
 //   k_accumulate     per segment: parent := root, length into the root's class sums (:650-737)
 //   k_cluster        per root: flip coin, improved / field sums -> records     (:739-803)
 //   k_site_end       per site: spin flip; new vertex types from the flips of the clusters
@@ -26,8 +25,7 @@
 //            order of claims changes no result: cluster roots are segment indices and every sum
 //            is an exact integer.  Regions keep unused slots at their ends.)
 //            vtime u64 (FP64 bits), vcode u8 = g<<1|offdiag,
-//            vslot[2] i32 (segment of the leg on source / target site; the sign bit marks
-//            the top segment of a closing site)
+//            vslot[2] i32 (segment of the leg on source / target site)
 //   segments (site-major CSR by sbase, k_s+1 per site, bottom segment first) stime u64,
 //            sinfo u8, svert i32, sdir u8, parent i32, flip u8, cls[4] u64, cnt0[4] u32
 //   records  rec[step][chain][32] u64 — exact integer sums (see the R_* word map)
@@ -44,11 +42,6 @@ namespace lg {
 // SI_OFF: the vertex is off-diagonal
 enum : uint8_t { SI_SPIN = 1, SI_GNEG = 2, SI_FIRST = 4, SI_LAST = 8, SI_SRC = 16, SI_OFF = 128 };
 constexpr int SI_GSHIFT = 5;
-
-// vslot entries: the segment index, with the sign bit set on the top segment of a site whose
-// parent slot holds the temporal closure (k_link then leaves that segment's link to k_union)
-constexpr int VS_CLOSE = (int)0x80000000u;
-constexpr int VS_SEG = 0x7FFFFFFF;
 
 // What k_accumulate gathers for a cluster besides its class lengths, stored at its root's
 // segment index (32 bytes, read by k_cluster with the lengths as two requests): the tau = 0
@@ -719,7 +712,6 @@ __device__ void merge_site_serial(Arena& A, int s) {
     }
   }
   uint8_t spin = A.spin0[s];
-  const bool close = A.ch[A.site_chain[s]].spin2 <= 1;  // spin-S sites close in k_boundary
   A.stime[base] = 0ull;
   A.sinfo[base] = (uint8_t)(spin | gneg | SI_FIRST | (k == 0 ? SI_LAST : 0));
   A.svert[base] = -1;
@@ -753,10 +745,10 @@ __device__ void merge_site_serial(Arena& A, int s) {
     A.svert[x] = v;
     A.sdir[x] = (uint8_t)(best | (A.inc_dir ? A.inc_dir[j0 + best] << 3 : 0));
     A.parent[x] = x;
-    A.vslot[2 * v + sd] = x | (j == k && close ? VS_CLOSE : 0);
+    A.vslot[2 * v + sd] = x;
   }
   // closure (path_integral.C:584-589); spin-S sites close in k_boundary instead
-  if (k > 0 && close) A.parent[base + k] = base;
+  if (k > 0 && A.ch[A.site_chain[s]].spin2 <= 1) A.parent[base + k] = base;
 }
 
 // `cap` (a multiple of 32, at most MERGE_CAP) is the staging capacity per warp, sized by the
@@ -922,9 +914,8 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
                                ((cd >> 1) << SI_GSHIFT) | ((cd & 1u) ? SI_OFF : 0));
         A.svert[x] = v;
         A.sdir[x] = (uint8_t)(sv & 0x7F);
-        const bool closing = r == k - 1 && close;  // closure: top segment joins the bottom one
-        A.parent[x] = closing ? base : x;
-        A.vslot[2 * v + side] = x | (closing ? VS_CLOSE : 0);
+        A.parent[x] = (r == k - 1 && close) ? base : x;  // closure: top segment joins the bottom one
+        A.vslot[2 * v + side] = x;
       }
       carry ^= __popc(ball) & 1u;
     }
@@ -1050,35 +1041,6 @@ __global__ void __launch_bounds__(256) k_boundary(Arena A) {
 // upper legs; g = 1 joins lower-left with upper-right and lower-right with upper-left; frozen
 // graphs (g & 2) join all four legs.
 //
-// Segments are numbered site-major, so at a vertex on sites i < j the four legs' segments are
-// ordered a_i - 1 < a_i < a_j - 1 < a_j (a = the segment starting at the vertex).  a_j starts at
-// this vertex and nowhere else, and is the larger end of exactly one of the vertex's links: to
-// a_i (g != 1) or to a_i - 1 (g = 1).  Hooking a_j there is therefore a plain store into a slot
-// no other link writes (k_link, before any union runs), unless the slot already holds the
-// temporal closure (a_j the top segment of a closing site, VS_CLOSE): then the link is a union
-// like the others.  k_union makes the remaining links: one per vertex for g = 0 and g = 1, two
-// for frozen graphs.
-__device__ __forceinline__ int link_hi(int a, int b, int va, int vb, bool& closing) {
-  closing = (a > b ? va : vb) < 0;
-  return a > b ? a : b;
-}
-
-__global__ void __launch_bounds__(256) k_link(Arena A) {
-  if (A.ctl->err) return;
-  const int ns = A.ctl->ns_total;
-  LG_GRID_STRIDE(x, ns) {
-    const uint8_t in = A.sinfo[x];
-    if (!(in & SI_SRC)) continue;
-    const int2 vs = *reinterpret_cast<const int2*>(A.vslot + 2 * A.svert[x]);
-    const int b = vs.y & VS_SEG;
-    bool closing;
-    const int hi = link_hi(x, b, vs.x, vs.y, closing);
-    if (closing) continue;
-    const int lo = x ^ b ^ hi;
-    A.parent[hi] = ((in >> SI_GSHIFT) & 3) == 1 ? lo - 1 : lo;
-  }
-}
-
 // The warps run over chunks of 64 consecutive segments (site-major order); the source-side
 // segments of a chunk, about half of them, are compacted so that every lane makes the unions of
 // one vertex.  Neighbouring warps so work on neighbouring sites, whatever order the vertex
@@ -1091,7 +1053,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_union(Arena A) {
   if (A.ctl->err) return;
   __shared__ int pend[WARPS][UN_CHUNK];   // source-side segment a
   __shared__ int pb[WARPS][UN_CHUNK];     // target-side segment b of the same vertex
-  __shared__ uint8_t pg[WARPS][UN_CHUNK]; // graph | 4 when k_link left the vertex's own link
+  __shared__ uint8_t pg[WARPS][UN_CHUNK]; // graph
   const int ns = A.ctl->ns_total;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
@@ -1100,41 +1062,29 @@ __global__ void __launch_bounds__(WARPS * 32) k_union(Arena A) {
   bool ok = true;
   for (long long c0 = ((long long)blockIdx.x * WARPS + w) * UN_CHUNK; c0 < ns; c0 += stride) {
     const int x0 = (int)c0 + lane, x1 = x0 + 32;
-    // segment info and vertex of both halves of the chunk in one round trip, then both legs'
-    // vslot entries of the source-side ones
+    // segment info and vertex of both halves of the chunk in one round trip, then the target
+    // leg of the source-side ones
     const uint8_t i0 = x0 < ns ? A.sinfo[x0] : 0;
     const uint8_t i1 = x1 < ns ? A.sinfo[x1] : 0;
     const int v0 = x0 < ns ? A.svert[x0] : 0;
     const int v1 = x1 < ns ? A.svert[x1] : 0;
     const bool s0 = (i0 & SI_SRC) != 0, s1 = (i1 & SI_SRC) != 0;
-    const int2 w0 = s0 ? *reinterpret_cast<const int2*>(A.vslot + 2 * v0) : make_int2(0, 0);
-    const int2 w1 = s1 ? *reinterpret_cast<const int2*>(A.vslot + 2 * v1) : make_int2(0, 0);
+    const int b0 = s0 ? A.vslot[2 * v0 + 1] : 0;
+    const int b1 = s1 ? A.vslot[2 * v1 + 1] : 0;
     const unsigned m0 = __ballot_sync(0xFFFFFFFFu, s0), m1 = __ballot_sync(0xFFFFFFFFu, s1);
     const int n0 = __popc(m0), tot = n0 + __popc(m1);
-    if (s0) {
-      const int q = __popc(m0 & lt), b = w0.y & VS_SEG;
-      bool c;
-      link_hi(x0, b, w0.x, w0.y, c);
-      pend[w][q] = x0; pb[w][q] = b; pg[w][q] = (uint8_t)(((i0 >> SI_GSHIFT) & 3) | (c ? 4 : 0));
-    }
-    if (s1) {
-      const int q = n0 + __popc(m1 & lt), b = w1.y & VS_SEG;
-      bool c;
-      link_hi(x1, b, w1.x, w1.y, c);
-      pend[w][q] = x1; pb[w][q] = b; pg[w][q] = (uint8_t)(((i1 >> SI_GSHIFT) & 3) | (c ? 4 : 0));
-    }
+    if (s0) { const int q = __popc(m0 & lt); pend[w][q] = x0; pb[w][q] = b0; pg[w][q] = (i0 >> SI_GSHIFT) & 3; }
+    if (s1) { const int q = n0 + __popc(m1 & lt); pend[w][q] = x1; pb[w][q] = b1; pg[w][q] = (i1 >> SI_GSHIFT) & 3; }
     __syncwarp();
     for (int j = lane; j < tot; j += 32) {
-      const int a = pend[w][j], b = pb[w][j], g = pg[w][j] & 3;
-      const bool own = (pg[w][j] & 4) != 0;  // the link k_link left to the unions
-      const int hi = a > b ? a : b, lo = a ^ b ^ hi;
+      const int a = pend[w][j], b = pb[w][j], g = pg[w][j];
       int* P = A.parent;
       if (g == 1) {
-        ok &= uf_union(P, hi - 1, lo, cap);
-        if (own) ok &= uf_union(P, hi, lo - 1, cap);
+        ok &= uf_union(P, a - 1, b, cap);
+        ok &= uf_union(P, b - 1, a, cap);
       } else {
         ok &= uf_union(P, a - 1, b - 1, cap);
-        if (own) ok &= uf_union(P, a, b, cap);
+        ok &= uf_union(P, a, b, cap);
         if (g & 2) ok &= uf_union(P, a - 1, a, cap);
       }
     }
@@ -1828,7 +1778,7 @@ __global__ void __launch_bounds__(256) k_validate(Arena A, int stage, int* bad) 
         const int v = A.svert[x];
         if (v < 0 || v >= nv_cap) { val_fail(bad, 27); break; }
         const int side = (A.sinfo[x] & SI_SRC) ? 0 : 1;
-        if ((A.vslot[2 * v + side] & VS_SEG) != x) { val_fail(bad, 28); break; }
+        if (A.vslot[2 * v + side] != x) { val_fail(bad, 28); break; }
       }
     }
   } else if (stage == 4) {  // after the cluster sums: every parent is a root

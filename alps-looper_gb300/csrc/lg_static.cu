@@ -171,7 +171,7 @@ __global__ void ks_fragments_g0(Arena A, int ng0, const int* g0_input, const int
   if (A.ctl->err) return;
   LG_GRID_STRIDE(k, ng0) {
     const int v = v_of_input[g0_input[k]];
-    const int r = A.parent[A.vslot[2 * v] & VS_SEG];
+    const int r = A.parent[A.vslot[2 * v]];
     froot[A.N + k] = r;
     atomicMin(minfrag + r, (unsigned)(A.N + k));
   }
@@ -288,13 +288,10 @@ extern "C" int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_
   static_scan(A.site_cnt, A.sbase, n, &ctl->ns_total, partial, ctl, st);
   k_merge<<<grid_of((long long)n * 32, MERGE_WARPS * 32), MERGE_WARPS * 32,
             MERGE_WARPS * merge_smem_per_warp(MERGE_CAP), st>>>(A, nullptr, n, MERGE_CAP);
-  if (nv > 0) {
-    k_link<<<grid_of(ns, 256), 256, 0, st>>>(A);
-    k_union<><<<grid_of(ns, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
-  }
+  if (nv > 0) k_union<><<<grid_of(ns, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
   ks_compress<<<grid_of(ns, 256), 256, 0, st>>>(A);
   static_scan(g0flag, g0ord, nv, totals, partial, ctl, st);
-  g_launches += nv > 0 ? 9 : 5;  // the scans count their own
+  g_launches += nv > 0 ? 8 : 5;  // the scans count their own
   LG_CUDA(cudaGetLastError());
   int ng0 = 0, err = 0;
   LG_CUDA(cudaMemcpyAsync(&ng0, totals, sizeof(int), cudaMemcpyDeviceToHost, st));
