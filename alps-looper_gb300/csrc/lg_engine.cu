@@ -156,6 +156,7 @@ struct Engine {
   cudaGraphExec_t gexec = nullptr;
   bool use_graph = true;
   int nsm = 148;
+  int zmax = MAXZ;                // largest number of incident bonds of a site (merge instance)
   int stream_priority = 0;   // CUDA stream priority of the arena's streams (0: the default)
   bool keep_records = false;
   std::vector<uint64_t> kept;   // raw records of chain 0 (test seam)
@@ -244,9 +245,11 @@ struct Engine {
     // incident bonds per site, ascending bond id
     std::vector<int> deg(N, 0);
     for (int b = 0; b < NB; ++b) { deg[h_bond_s0[b]]++; deg[h_bond_s1[b]]++; }
+    zmax = 0;
     for (int s = 0; s < N; ++s) {
       if (deg[s] > MAXZ) return lg_fail(LG_EUNSUPPORTED, "site coordination %d > %d", deg[s], MAXZ);
       h_inc_off[s + 1] = h_inc_off[s] + deg[s];
+      zmax = std::max(zmax, deg[s]);
     }
     h_inc.assign(h_inc_off[N], 0);
     h_inc_side.assign(h_inc_off[N], 0);
@@ -620,12 +623,12 @@ struct Engine {
     mark(1);
     fork(n_wide > 0 && n_narrow > 0);
     if (n_wide) {
-      k_merge<<<grid_for((long long)n_wide * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32,
-                MERGE_WARPS * merge_smem_per_warp(merge_cap), st>>>(A, wide_list, n_wide, merge_cap);
+      launch_merge(zmax, grid_for((long long)n_wide * 32, MERGE_WARPS * 32, 16),
+                   MERGE_WARPS * merge_smem_per_warp(merge_cap), st, A, wide_list, n_wide, merge_cap);
       ++launches;
     }
     if (n_narrow) {
-      k_merge_narrow<<<grid_for(n_narrow, 256, 16), 256, 0, both ? st2 : st>>>(A, d_narrow_sites.p, n_narrow);
+      launch_merge_narrow(zmax, grid_for(n_narrow, 256, 16), both ? st2 : st, A, d_narrow_sites.p, n_narrow);
       ++launches;
     }
     join();
@@ -1132,8 +1135,8 @@ struct Engine {
     Arena A = arena();
     k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
     scan(d_site_cnt.p, d_sbase.p, N, &d_ctl.p->ns_total, ns_cap, 1, 0);
-    k_merge<<<grid_for((long long)N * 32, MERGE_WARPS * 32, 16), MERGE_WARPS * 32,
-              MERGE_WARPS * merge_smem_per_warp(MERGE_CAP), st>>>(A, nullptr, N, MERGE_CAP);
+    launch_merge(zmax, grid_for((long long)N * 32, MERGE_WARPS * 32, 16),
+                 MERGE_WARPS * merge_smem_per_warp(MERGE_CAP), st, A, nullptr, N, MERGE_CAP);
     k_union<><<<grid_for(2 * nops + N, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
     k_compress<<<grid_for(2 * nops + N, 256), 256, 0, st>>>(A);
     g_launches += 7;

@@ -689,17 +689,19 @@ __device__ __forceinline__ void warp_merge2(const uint64_t* XK, const uint16_t* 
   }
 }
 
+// Z: the largest site degree of the arena (2, 4 or MAXZ), the bound of every per-list loop.
+template <int Z>
 __device__ void merge_site_serial(Arena& A, int s) {
   const int j0 = A.inc_off[s];
   const int z = A.inc_off[s + 1] - j0;
   const int base = A.sbase[s];
   const int k = A.sbase[s + 1] - base - 1;
   const uint8_t gneg = A.gauge[s] < 0 ? SI_GNEG : 0;
-  int cur[MAXZ], end[MAXZ];
-  uint64_t ht[MAXZ];
-  uint8_t hc[MAXZ], side[MAXZ];
+  int cur[Z], end[Z];
+  uint64_t ht[Z];
+  uint8_t hc[Z], side[Z];
 #pragma unroll
-  for (int d = 0; d < MAXZ; ++d) {
+  for (int d = 0; d < Z; ++d) {
     if (d < z) {
       const int b = A.inc[j0 + d];
       cur[d] = A.bond_ptr[b];
@@ -722,7 +724,7 @@ __device__ void merge_site_serial(Arena& A, int s) {
     uint64_t bt = ht[0];
     uint8_t bdiag = (uint8_t)(~hc[0] & 1u);
 #pragma unroll
-    for (int d = 1; d < MAXZ; ++d) {
+    for (int d = 1; d < Z; ++d) {
       const uint8_t dg = (uint8_t)(~hc[d] & 1u);
       if (ht[d] < bt || (ht[d] == bt && dg < bdiag)) { best = d; bt = ht[d]; bdiag = dg; }
     }
@@ -730,7 +732,7 @@ __device__ void merge_site_serial(Arena& A, int s) {
     int v = 0;
     uint8_t sd = 0, code = 0;
 #pragma unroll
-    for (int d = 0; d < MAXZ; ++d) {
+    for (int d = 0; d < Z; ++d) {
       if (d == best) {
         v = cur[d]; sd = side[d]; code = hc[d];
         ++cur[d];
@@ -754,6 +756,7 @@ __device__ void merge_site_serial(Arena& A, int s) {
 // `cap` (a multiple of 32, at most MERGE_CAP) is the staging capacity per warp, sized by the
 // engine from the arena's largest expected endpoint count per site; the dynamic shared memory is
 // MERGE_WARPS * merge_smem_per_warp(cap) bytes.
+template <int Z>
 __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const int* sites, int nsites,
                                                               int cap) {
   if (A.ctl->err) return;
@@ -778,17 +781,17 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
       if (s == A.N - 1) A.ch_slot_off[A.C] = base + k + 1;
     }
     if (k > cap) {
-      if (lane == 0) merge_site_serial(A, s);
+      if (lane == 0) merge_site_serial<Z>(A, s);
       __syncwarp();
       continue;
     }
     // stage the incident lists: list d occupies [off[d], off[d+1])
-    int off[MAXZ + 1];
-    int ptr[MAXZ];
-    uint8_t sdv[MAXZ];  // per list: the segment's sdir value (incidence | direction << 3) | side << 7
+    int off[Z + 1];
+    int ptr[Z];
+    uint8_t sdv[Z];  // per list: the segment's sdir value (incidence | direction << 3) | side << 7
     off[0] = 0;
 #pragma unroll
-    for (int d = 0; d < MAXZ; ++d) {
+    for (int d = 0; d < Z; ++d) {
       if (d < z) {
         const int b = A.inc[j0 + d];
         ptr[d] = A.bond_ptr[b];
@@ -799,7 +802,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
       }
     }
 #pragma unroll
-    for (int d = 0; d < MAXZ; ++d) {
+    for (int d = 0; d < Z; ++d) {
       for (int i = lane; i < off[d + 1] - off[d]; i += 32) {
         const uint8_t c = A.vcode[ptr[d] + i];
         wsK[off[d] + i] = merge_key(A.vtime[ptr[d] + i], c);
@@ -818,10 +821,10 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
       if (lane < k) {
         int d = 0;
 #pragma unroll
-        for (int q = 1; q < MAXZ; ++q) if (lane >= off[q]) d = q;
+        for (int q = 1; q < Z; ++q) if (lane >= off[q]) d = q;
         key = wsK[lane];
 #pragma unroll
-        for (int q = 0; q < MAXZ; ++q) {  // lists q >= z are empty
+        for (int q = 0; q < Z; ++q) {  // lists q >= z are empty
           // keys are below 2^63, so "< key + 1" is "<= key"
           const int c = count_before<false>(wsK + off[q], off[q + 1] - off[q], key + (q < d ? 1u : 0u));
           r += q == d ? lane - off[q] : c;
@@ -831,22 +834,23 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
       if (lane < k) { wmK[r] = key; wmI[r] = (uint16_t)lane; }
       __syncwarp();
     }
-    int rs[MAXZ], rn[MAXZ];
+    int rs[Z], rn[Z];
 #pragma unroll
-    for (int q = 0; q < MAXZ; ++q) { rs[q] = off[q]; rn[q] = off[q + 1] - off[q]; }
+    for (int q = 0; q < Z; ++q) { rs[q] = off[q]; rn[q] = off[q + 1] - off[q]; }
     int nr = k <= 32 ? 1 : z;
     uint64_t* curK = k <= 32 ? wmK : wsK;
     const uint16_t* curI = k <= 32 ? wmI : nullptr;  // level 0: the index of a key is its position
     bool in_m = k <= 32;
+    constexpr int LEVELS = Z <= 2 ? 1 : (Z <= 4 ? 2 : 3);  // pairwise rounds for Z lists
 #pragma unroll
-    for (int level = 0; level < 3; ++level) {
+    for (int level = 0; level < LEVELS; ++level) {
       if (nr <= 1) break;
       uint64_t* nK = in_m ? wsK : wmK;
       uint16_t* nI = in_m ? wsI : wmI;
-      int ns2[MAXZ], nn2[MAXZ];
+      int ns2[Z], nn2[Z];
       int o = 0, nn = 0;
 #pragma unroll
-      for (int p = 0; p < MAXZ; p += 2) {
+      for (int p = 0; p < Z; p += 2) {
         if (p + 1 < nr) {
           warp_merge2(curK + rs[p], curI ? curI + rs[p] : nullptr, rs[p], rn[p],
                       curK + rs[p + 1], curI ? curI + rs[p + 1] : nullptr, rs[p + 1], rn[p + 1],
@@ -866,7 +870,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
       }
       __syncwarp();
 #pragma unroll
-      for (int q = 0; q < MAXZ / 2; ++q) { rs[q] = ns2[q]; rn[q] = nn2[q]; }
+      for (int q = 0; q < Z / 2; ++q) { rs[q] = ns2[q]; rn[q] = nn2[q]; }
       nr = nn;
       curK = nK;
       curI = nI;
@@ -901,11 +905,11 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
       if (ok) {
         int d = 0;
 #pragma unroll
-        for (int q = 1; q < MAXZ; ++q) if (e >= off[q]) d = q;
+        for (int q = 1; q < Z; ++q) if (e >= off[q]) d = q;
         int pd = 0, od = 0;
         uint8_t sv = 0;
 #pragma unroll
-        for (int q = 0; q < MAXZ; ++q) if (q == d) { pd = ptr[q]; od = off[q]; sv = sdv[q]; }
+        for (int q = 0; q < Z; ++q) if (q == d) { pd = ptr[q]; od = off[q]; sv = sdv[q]; }
         const int v = pd + (e - od);
         const int x = base + 1 + r;
         const uint8_t side = sv >> 7;
@@ -924,6 +928,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
 }
 
 // Thread-per-site form of the merge for sites with few endpoints.
+template <int Z>
 __global__ void __launch_bounds__(256) k_merge_narrow(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
   LG_GRID_STRIDE(i, nsites) {
@@ -931,8 +936,28 @@ __global__ void __launch_bounds__(256) k_merge_narrow(Arena A, const int* sites,
     const int c = A.site_chain[s];
     if (s == A.ch[c].site_off) A.ch_slot_off[c] = A.sbase[s];
     if (s == A.N - 1) A.ch_slot_off[A.C] = A.sbase[s + 1];
-    merge_site_serial(A, s);
+    merge_site_serial<Z>(A, s);
   }
+}
+
+// The merge kernels for an arena whose sites have at most zmax incident bonds: the instance
+// with the smallest list bound Z >= zmax (fewer registers and pairwise rounds).
+inline int merge_z(int zmax) { return zmax <= 2 ? 2 : (zmax <= 4 ? 4 : MAXZ); }
+
+inline void launch_merge(int zmax, int grid, size_t smem, cudaStream_t st, const Arena& A,
+                         const int* sites, int n, int cap) {
+  const int z = merge_z(zmax);
+  if (z == 2) k_merge<2><<<grid, MERGE_WARPS * 32, smem, st>>>(A, sites, n, cap);
+  else if (z == 4) k_merge<4><<<grid, MERGE_WARPS * 32, smem, st>>>(A, sites, n, cap);
+  else k_merge<MAXZ><<<grid, MERGE_WARPS * 32, smem, st>>>(A, sites, n, cap);
+}
+
+inline void launch_merge_narrow(int zmax, int grid, cudaStream_t st, const Arena& A,
+                                const int* sites, int n) {
+  const int z = merge_z(zmax);
+  if (z == 2) k_merge_narrow<2><<<grid, 256, 0, st>>>(A, sites, n);
+  else if (z == 4) k_merge_narrow<4><<<grid, 256, 0, st>>>(A, sites, n);
+  else k_merge_narrow<MAXZ><<<grid, 256, 0, st>>>(A, sites, n);
 }
 
 // Imaginary-time boundary of a spin-S site (spin2 > 1 virtual sites, path_integral.C:590-613 with

@@ -286,8 +286,8 @@ extern "C" int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_
   ks_sort_bonds<<<grid_of(nb, 128), 128, 0, st>>>(A, d_graphs, v_of_input);
   k_site_count<<<grid_of(n, 256), 256, 0, st>>>(A);
   static_scan(A.site_cnt, A.sbase, n, &ctl->ns_total, partial, ctl, st);
-  k_merge<<<grid_of((long long)n * 32, MERGE_WARPS * 32), MERGE_WARPS * 32,
-            MERGE_WARPS * merge_smem_per_warp(MERGE_CAP), st>>>(A, nullptr, n, MERGE_CAP);
+  launch_merge(2 * dim, grid_of((long long)n * 32, MERGE_WARPS * 32),
+               MERGE_WARPS * merge_smem_per_warp(MERGE_CAP), st, A, nullptr, n, MERGE_CAP);
   if (nv > 0) k_union<><<<grid_of(ns, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
   ks_compress<<<grid_of(ns, 256), 256, 0, st>>>(A);
   static_scan(g0flag, g0ord, nv, totals, partial, ctl, st);
