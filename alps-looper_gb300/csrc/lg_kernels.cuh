@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(INS_WARPS * 32, 7) k_insert(Arena A, const int
 // kept in thread-local memory by the counting walk; longer ones are walked again to write them.
 constexpr int INS_LOCAL = 16;
 
-__global__ void __launch_bounds__(256) k_insert_narrow(Arena A, const int* bonds, int nb) {
+__global__ void __launch_bounds__(256, 4) k_insert_narrow(Arena A, const int* bonds, int nb) {
   if (A.ctl->err) return;
   const int lane = threadIdx.x & 31;
   const int stride = gridDim.x * blockDim.x;        // a multiple of 32
