@@ -1473,6 +1473,46 @@ __device__ __forceinline__ void record_by_chain(const Arena& A, int c, const Roo
 // Each block handles one tile of TILE consecutive segments.  A tile inside one chain is reduced
 // in registers and shared memory (16-bit limbs, exact) and adds to the record once; a tile that
 // spans chains reduces each warp's roots per chain (record_by_chain).
+// A tile that spans chains.  A thread's roots come in segment order, so its chain never
+// decreases: it sums its roots of one chain in registers and hands them to the per-chain warp
+// reduction (record_by_chain) when its chain changes and at the end (every thread calls it on
+// every step, with chain -1 when it has nothing to hand over).  Kept out of line so that its
+// registers do not weigh on the single-chain path of k_cluster.
+__device__ __noinline__ void cluster_spanning_tile(const Arena& A, const int* roots, int nr) {
+  const int iters = (nr + (int)blockDim.x - 1) / (int)blockDim.x;
+  int i = threadIdx.x;
+  int x = i < nr ? roots[i] : 0;
+  RootClass cur = i < nr ? load_root_class(A, x) : RootClass{};
+  RootSums R;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) R.q[k] = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) R.w[k] = {0, 0};
+  int cc = -1;
+  for (int it = 0; it < iters; ++it) {
+    const int inext = i + blockDim.x;
+    const int xnext = inext < nr ? roots[inext] : 0;
+    RootClass nxt = inext < nr ? load_root_class(A, xnext) : RootClass{};
+    const int c = i < nr ? chain_of_segment(A, x) : -1;
+    const bool hand = cc >= 0 && c >= 0 && c != cc;
+    record_by_chain(A, hand ? cc : -1, R);
+    if (hand) {
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) R.q[k] = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) R.w[k] = {0, 0};
+    }
+    if (i < nr) {
+      root_sums(A, x, c, cur, R);
+      cc = c;
+    }
+    i = inext;
+    x = xnext;
+    cur = nxt;
+  }
+  record_by_chain(A, cc, R);
+}
+
 constexpr int CL_TILE = 4096;
 constexpr int CL_THREADS = 256;
 
@@ -1504,33 +1544,13 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
     __syncthreads();
     const int nr = nroots;
     const int cf = chain_of_segment(A, t0), cl = chain_of_segment(A, t1 - 1);
-    // software-pipelined: the next root's class sums are loaded while this one is processed
-    int i = threadIdx.x;
-    int x = i < nr ? roots[i] : 0;
-    RootClass cur = i < nr ? load_root_class(A, x) : RootClass{};
     if (cf != cl) {
-      // the tile spans chains: per-chain warp reductions (same trip count for every thread)
-      const int iters = (nr + (int)blockDim.x - 1) / (int)blockDim.x;
-      for (int it = 0; it < iters; ++it) {
-        const int inext = i + blockDim.x;
-        const int xnext = inext < nr ? roots[inext] : 0;
-        RootClass nxt = inext < nr ? load_root_class(A, xnext) : RootClass{};
-        RootSums R;
-#pragma unroll
-        for (int k = 0; k < NQ; ++k) R.q[k] = 0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) R.w[k] = {0, 0};
-        int c = -1;
-        if (i < nr) {
-          c = chain_of_segment(A, x);
-          root_sums(A, x, c, cur, R);
-        }
-        record_by_chain(A, c, R);
-        i = inext;
-        x = xnext;
-        cur = nxt;
-      }
+      cluster_spanning_tile(A, roots, nr);
     } else {
+      // software-pipelined: the next root's class sums are loaded while this one is processed
+      int i = threadIdx.x;
+      int x = i < nr ? roots[i] : 0;
+      RootClass cur = i < nr ? load_root_class(A, x) : RootClass{};
       RootSums acc;
 #pragma unroll
       for (int k = 0; k < NQ; ++k) acc.q[k] = 0;
