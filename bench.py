@@ -378,7 +378,10 @@ def run_ours(args, dist, ws, rank, local):
     prof, verts = w.profile_sweeps(16, FLUSH_BYTES)
     nv_mean = verts / 16.0
     sweep_ms = sum(prof.values()) / 16.0
-    bytes_alg = 64.0 * nv_mean + 16.0 * N_SITES  # per sweep (algorithmic)
+    # algorithmic bytes per sweep: 64 per vertex (record read and write 24, leg links 8, parent
+    # write and read 8, labels 12, estimator re-read 12) and 16 per site (spin read and write 8,
+    # boundary fragment 4, site label 4)
+    bytes_alg = 64.0 * nv_mean + 16.0 * N_SITES
     peak, peak_kind = _peaks()
     achieved = bytes_alg / (total_ms / args.steps / 1e3) / 1e9
     dom = max(prof, key=prof.get)
