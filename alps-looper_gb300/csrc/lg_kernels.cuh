@@ -1,20 +1,26 @@
 // Sweep kernels of the GB300 loop-cluster engine.
 //
-// One sweep of every chain in the arena (path_integral.C:355-864) is this kernel sequence:
+// One sweep of every chain in the arena (path_integral.C:355-864) is this kernel sequence, one
+// CUDA graph per arena.  Chains with few operators per site take the thread-per-element forms
+// (*_narrow) on a second stream beside the warp-per-site forms.
 //
-//   k_insert         per bond: new operator string (time, graph, type), written at a vertex
-//                    range claimed with one atomic add; capacity check          (:403-577)
-//   k_site_count     per site: number of segments = 1 + incident vertices
-//   scan             site segment offsets
-//   k_merge          per site: time-ordered segment list, union-find init,
-//                    temporal closure                                          (:584-589)
-//   k_union          per vertex: lock-free unions of its four legs            (graph_impl.h:280-295)
-//   k_accumulate     per segment: parent := root, length into the root's class sums (:650-737)
-//   k_cluster        per root: flip coin, improved / field sums -> records     (:739-803)
-//   k_site_end       per site: spin flip; new vertex types from the flips of the clusters
-//                    below and above each endpoint; compacted off-diagonal list (:805-823)
-//   k_end            per chain: operator count, sweep counter; clears the next sweep's record
-//                    row and claim counters                                    (:472-479 reset)
+//   k_insert(_narrow)  per bond: new operator string (time, graph, type), written at a vertex
+//                      range claimed with one atomic add; capacity check        (:403-577)
+//   k_site_blocks,     per site: number of segments = 1 + incident vertices, and the site
+//   k_site_offsets     segment offsets (k_site_count + a three-kernel scan above 2^20 sites)
+//   k_merge(_narrow)   per site: time-ordered segment list, union-find init, temporal closure
+//                      (:584-589); instanced by the arena's largest site degree
+//   k_boundary         spin S > 1/2 only, per real site: the tau = 0 boundary matching of its
+//                      virtual sites                                             (:590-613)
+//   k_union            per vertex: lock-free unions of its four legs          (graph_impl.h:280-295)
+//   k_accumulate       per segment: parent := root, length into the root's class sums (:650-737)
+//   k_cluster          per root: flip coin, improved / field sums -> records   (:739-803)
+//   k_site_end(_narrow) per site: spin flip; new vertex types from the flips of the clusters
+//                      below and above each endpoint; compacted off-diagonal list (:805-823)
+//   k_end              per chain, on a third stream beside k_site_end: operator count, sweep
+//                      counter; clears the next sweep's record row and claim counters
+//   k_corr             with MEASURE[Correlations] / [Structure Factor] only: exact spin
+//                      correlation sums per displacement (correlation.h)
 //
 // Memory layout (HBM, struct of arrays, 32-bit indices):
 //   sites    spin0[N] u8, off_base[N], off_cnt[N]     persistent between sweeps
@@ -27,7 +33,8 @@
 //            vtime u64 (FP64 bits), vcode u8 = g<<1|offdiag,
 //            vslot[2] i32 (segment of the leg on source / target site)
 //   segments (site-major CSR by sbase, k_s+1 per site, bottom segment first) stime u64,
-//            sinfo u8, svert i32, sdir u8, parent i32, flip u8, cls[4] u64, cnt0[4] u32
+//            sinfo u8, svert i32, sdir u8, parent i32, flip u8, cls[4] u64, rkw (tau = 0
+//            class counts u32[4], winding i32[4]; used at roots)
 //   records  rec[step][chain][32] u64 — exact integer sums (see the R_* word map)
 #pragma once
 #include <cstdint>
