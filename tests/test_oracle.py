@@ -4,7 +4,8 @@
 * union-find replay == test/union_find.op (parents, roots, tree sizes)
 * cluster labels == the reference union_find.h (both unify variants) on dumped configurations
 * ED restatement == loop.op's diagonalization blocks
-* philox mode: statistics within 3 sigma of exact diagonalization
+* philox mode: statistics within 3.5 sigma of exact diagonalization (chain, square and cubic
+  lattices; S = 1/2, 1, 3/2; antiferromagnetic, ferromagnetic, Ising, XY, field)
 """
 import math
 
@@ -188,6 +189,27 @@ def test_philox_spin1_chain_vs_ed():
 def test_philox_spin3half_xxz_field_chain_vs_ed():
     _check_vs_ed(1, 4, 1.0, 1.0, 0.5, 0.2, 1000, 30000, 13,
                  ["Energy", "Specific Heat", "Magnetization", "Susceptibility"], spin2=3)
+
+
+def test_philox_cubic_xxz_field_vs_ed():
+    # simple cubic L = 2 (8 sites; the periodic wrap doubles every bond, in ED as in the engine)
+    _check_vs_ed(3, 2, 0.5, 1.0, 0.5, 0.3, 1000, 30000, 14,
+                 ["Energy", "Specific Heat", "Magnetization", "Susceptibility",
+                  "Staggered Susceptibility"])
+
+
+def test_philox_ferro_xxz_field_chain_vs_ed():
+    # ferromagnetic couplings: the crossed graph (g = 1) and its frozen form
+    _check_vs_ed(1, 6, 0.5, -1.0, -0.5, 0.1, 1000, 40000, 15,
+                 ["Energy", "Specific Heat", "Magnetization", "Susceptibility",
+                  "Staggered Susceptibility"])
+
+
+def test_philox_xy_chain_vs_ed():
+    # Jz = 0: both graphs at equal weight
+    _check_vs_ed(1, 6, 0.4, 1.0, 0.0, 0.0, 1000, 40000, 16,
+                 ["Energy", "Specific Heat", "Susceptibility", "Staggered Magnetization^2",
+                  "Staggered Susceptibility"])
 
 
 def test_momentum_ed_matches_dense_ed():
