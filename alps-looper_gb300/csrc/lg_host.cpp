@@ -91,6 +91,15 @@ extern "C" int lg_params_parse(const char* text, lg_params* p) {
       *dst = x;
       return LG_OK;
     };
+    // integer keys: a finite value within [lo, hi], truncated toward zero as an int conversion
+    // of the parameter would (out-of-range and non-finite values are errors, never a cast)
+    auto integer = [&](double lo, double hi, double* dst) -> int {
+      if (!parse_num(val, &x) || !(x >= lo && x <= hi))
+        return lg_fail(LG_EINVAL, "bad value for %s: '%s'", key.c_str(), val.c_str());
+      *dst = std::trunc(x);
+      return LG_OK;
+    };
+    const double kInt = 2147483647.0, kExact = 9007199254740992.0;  // 2^31 - 1, 2^53
     int rc = LG_OK;
     if (key == "LATTICE") {
       if (val == "chain lattice" || val == "chain") p->lattice = LG_CHAIN;
@@ -98,7 +107,7 @@ extern "C" int lg_params_parse(const char* text, lg_params* p) {
       else if (val == "simple cubic lattice" || val == "cubic lattice" || val == "cubic") p->lattice = LG_CUBIC;
       else return lg_fail(LG_EUNSUPPORTED, "LATTICE '%s' not supported", val.c_str());
     } else if (key == "L") {
-      double d; rc = num(&d); p->L = (int)d;
+      double d = 0; if (!(rc = integer(-kInt, kInt, &d))) p->L = (int)d;
     } else if (key == "T") {
       rc = num(&p->T);
     } else if (key == "BETA" || key == "INVERSE_TEMPERATURE") {
@@ -116,11 +125,12 @@ extern "C" int lg_params_parse(const char* text, lg_params* p) {
     } else if (key == "FORCE_SCATTER") {
       rc = num(&p->force_scatter);
     } else if (key == "SWEEPS") {
-      double d; rc = num(&d); p->sweeps = (uint64_t)d;
+      double d = 0; if (!(rc = integer(0, kExact, &d))) p->sweeps = (uint64_t)d;
     } else if (key == "THERMALIZATION") {
-      double d; rc = num(&d); p->thermalization = (int64_t)d;
+      double d = 0; if (!(rc = integer(-kExact, kExact, &d))) p->thermalization = (int64_t)d;
     } else if (key == "SEED") {
-      double d; rc = num(&d); p->seed = (uint64_t)d;
+      double d = 0;  // below 2^64
+      if (!(rc = integer(0, 18446744073709549568.0, &d))) p->seed = (uint64_t)d;
     } else if (key == "INITIAL_SPINS") {
       if (val == "up") p->init_spins = 0;
       else if (val == "random") p->init_spins = 1;
@@ -134,12 +144,12 @@ extern "C" int lg_params_parse(const char* text, lg_params* p) {
       if (!parse_bool(val, &p->measure_structure_factor))
         return lg_fail(LG_EINVAL, "MEASURE[Structure Factor] must be true or false");
     } else if (key == "INITIAL_SITE") {
-      double d; rc = num(&d); p->initial_site = (int)d;
+      double d = 0; if (!(rc = integer(-kInt, kInt, &d))) p->initial_site = (int)d;
     } else if (key == "local_S") {
       double d; rc = num(&d);
       if (!rc) {
         const double t = 2 * d;
-        if (!(t >= 1) || std::fabs(t - std::round(t)) > 1e-9)
+        if (!(t >= 1 && t <= 64) || std::fabs(t - std::round(t)) > 1e-9)
           return lg_fail(LG_EINVAL, "local_S must be a positive multiple of 1/2");
         p->spin2 = (int)std::round(t);
       }

@@ -83,6 +83,53 @@ def test_params_parse_rejects_bad_values(lg):
     assert e.value.code == -4
 
 
+def test_params_parse_rejects_out_of_range_integers(lg):
+    # integer keys take finite values within their type's range, truncated toward zero
+    for text in ("L = 1e300", "L = nan", "L = inf", "L = -3e9", "SWEEPS = -5", "SWEEPS = 1e30",
+                 "SEED = nan", "SEED = -1", "SEED = 2e19", "THERMALIZATION = 1e300",
+                 "INITIAL_SITE = 3e9", "local_S = 1e300", "local_S = inf"):
+        with pytest.raises(lg.LoopError) as e:
+            lg.parse_params(text)
+        assert e.value.code == -1, text
+    p = lg.parse_params("L = 8.9; SWEEPS = 1e4; THERMALIZATION = -1; INITIAL_SITE = -1; "
+                        "SEED = 18446744073709549568")
+    assert (p.L, p.sweeps, p.thermalization, p.initial_site) == (8, 10000, -1, -1)
+    assert p.seed == 18446744073709549568
+
+
+def test_params_parse_survives_random_text(lg):
+    # random texts and random edits of a valid parameter file: the parser answers OK, LG_EINVAL
+    # or LG_EUNSUPPORTED (an unknown LATTICE) and nothing else; a memory fault would end the run
+    import numpy as np
+    rng = np.random.default_rng(11)
+    base = ('LATTICE = "square lattice"; L = 16\nT = 1/4 # comment\nJz = 0.5; Jxy = 1; h = 0.2\n'
+            'SWEEPS = 1024; THERMALIZATION = 128; SEED = 3; local_S = 1/2\n'
+            'MEASURE[Correlations] = true; INITIAL_SITE = 2; INITIAL_SPINS = random\n')
+    alphabet = list('=;#"[]/ \n\t.-+eE0123456789abcdfinLTJhSWEPNAMRCU_xyz') + ["nan", "inf"]
+    codes = set()
+    for i in range(4000):
+        if i % 4 == 0:
+            text = "".join(rng.choice(alphabet, size=int(rng.integers(0, 240))))
+        else:
+            t = list(base)
+            for _ in range(int(rng.integers(1, 8))):
+                k = int(rng.integers(0, len(t) + 1))
+                op = int(rng.integers(0, 3))
+                if op == 0 and k < len(t):
+                    del t[k]
+                elif op == 1:
+                    t.insert(k, str(rng.choice(alphabet)))
+                elif k < len(t):
+                    t[k] = str(rng.choice(alphabet))
+            text = "".join(t)
+        p = lg.Params()
+        lg.lib().lg_params_default(ctypes.byref(p))
+        rc = lg.lib().lg_params_parse(text.encode(), ctypes.byref(p))
+        assert rc in (0, -1, -4), (rc, text)
+        codes.add(rc)
+    assert {0, -1} <= codes
+
+
 def test_obs_names_match_reference_keys(lg):
     names = lg.obs_names()
     for key in ("Energy", "Energy Density", "Specific Heat", "Susceptibility",
