@@ -1054,13 +1054,6 @@ struct Engine {
 
   int set_state(int c, const int32_t* spins, const int32_t* bonds, const double* times, long long n,
                 uint64_t sweep) {
-    if (C == 1) {  // a complete state: a union-find failure (LG_EITERCAP) no longer applies
-      Ctl hc;
-      LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
-      hc.err = 0;
-      hc.step = 0;
-      LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
-    }
     const ChainSpec& s = spec[c];
     const int so = hch[c].site_off;
     SiteLists L;
@@ -1077,6 +1070,13 @@ struct Engine {
       tmp[s.s0[b]].push_back({tb, b + hch[c].bond_off});
       tmp[s.s1[b]].push_back({tb, b + hch[c].bond_off});
     }
+    // a spin-1/2 world line is periodic in imaginary time: an even number of flips per site
+    // (spin-S chains close through the boundary matching, which checks its own sectors)
+    if (s.spin2 <= 1)
+      for (int i = 0; i < s.N; ++i)
+        if (tmp[i].size() & 1)
+          return lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
+                                    "(not periodic in imaginary time)", i);
     for (int i = 0; i < s.N; ++i) {
       auto& T = tmp[i];
       std::stable_sort(T.begin(), T.end());  // (time, bond): the order the sweep produces
@@ -1087,6 +1087,13 @@ struct Engine {
           if (h_inc[j] == e.second) { dir = j - h_inc_off[gs]; break; }
         L[gs].push_back({e.first, (uint8_t)dir});
       }
+    }
+    if (C == 1) {  // a complete, valid state: a union-find failure (LG_EITERCAP) no longer applies
+      Ctl hc;
+      LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+      hc.err = 0;
+      hc.step = 0;
+      LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
     }
     if ((rc = upload_lists(L))) return rc;
     std::vector<uint8_t> sp(s.N);

@@ -557,7 +557,10 @@ int checkpoint_decode(const ChainSpec& s, const uint8_t* buf, size_t size,
   std::memcpy(&n, buf + 24, 8);
   if (ver != 1) return lg_fail(LG_ECORRUPT, "checkpoint version %u", ver);
   if ((int)dim != s.dim || (int)L != s.L) return lg_fail(LG_ECORRUPT, "checkpoint lattice mismatch");
-  if (size != head + (size_t)s.N + n * 12 + 8) return lg_fail(LG_ECORRUPT, "checkpoint size mismatch");
+  // n is checked against the size without multiplying it (a forged count must not wrap)
+  const size_t fixed = head + (size_t)s.N + 8;
+  if (size < fixed || (size - fixed) % 12 != 0 || n != (uint64_t)((size - fixed) / 12))
+    return lg_fail(LG_ECORRUPT, "checkpoint size mismatch");
   const uint8_t* p = buf + head;
   spins.resize(s.N);
   for (int i = 0; i < s.N; ++i) spins[i] = p[i];

@@ -143,7 +143,10 @@ double lg_progress(const lg_chain* c);
 /* ObservableSet contents after the runs so far (init_observables :307-321 + evaluators). */
 int lg_observables(lg_chain* c, lg_obs* out);
 /* loop_worker::save / load (path_integral.C:111-124): mcs, spins, operator string.
- * lg_save with buf == NULL stores the required size in *size. */
+ * lg_save with buf == NULL stores the required size in *size.  lg_load rejects a blob whose
+ * checksum, version, lattice, size or operators do not check (LG_ECORRUPT) and a configuration
+ * that is not periodic in imaginary time (LG_EINVAL, as lg_set_state); the chain then keeps its
+ * state. */
 int lg_save(lg_chain* c, void* buf, size_t* size);
 int lg_load(lg_chain* c, const void* buf, size_t size);
 /* Exchange Monte Carlo hooks (path_integral.C:97-109). */
@@ -177,7 +180,9 @@ int lg_last_error(char* buf, size_t n);
 
 /* ---- test seams --------------------------------------------------------------------------
  * Persistent configuration: spins at tau = 0 (0 up, 1 down) and the off-diagonal operators
- * (bond, FP64 time in [0,1)), time ordered.  *n receives the operator count. */
+ * (bond, FP64 time in [0,1)), time ordered.  *n receives the operator count.  lg_set_state
+ * returns LG_EINVAL for an operator out of range and, at S = 1/2, for a site with an odd number
+ * of operators (its world line would not be periodic in imaginary time). */
 int lg_get_state(lg_chain* c, int32_t* spins, int32_t* bonds, double* times, int64_t cap,
                  int64_t* n);
 int lg_set_state(lg_chain* c, const int32_t* spins, const int32_t* bonds, const double* times,

@@ -174,6 +174,23 @@ def test_set_state_then_sweep_matches_oracle(lg):
     _assert_same_state(g, o)
 
 
+def test_set_state_rejects_a_non_periodic_configuration(lg):
+    m = MODELS["cubic4_xxz_field"]
+    o = orc.Oracle(m["dim"], m["L"], m["beta"], m["jxy"], m["jz"], m["h"], seed=32)
+    o.sweep(15)
+    spins, bonds, times = o.state()
+    assert len(bonds) > 0
+    g = _gpu_chain(lg, m, 32)
+    g.set_state(spins, bonds, times, 15)
+    # one operator fewer: its two sites flip an odd number of times
+    with pytest.raises(lg.LoopError) as e:
+        g.set_state(spins, bonds[1:], times[1:], 15)
+    assert e.value.code == -1 and "periodic" in str(e.value)
+    g.run(6)  # the chain kept the valid state
+    o.sweep(6)
+    _assert_same_state(g, o)
+
+
 def test_checkpoint_roundtrip_and_corruption(lg):
     m = MODELS["square6_xxz_easy_plane"]
     g = _gpu_chain(lg, m, 3)
