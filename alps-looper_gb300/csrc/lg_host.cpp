@@ -222,6 +222,7 @@ int ChainSpec::init(const lg_params& p) {
   // only on bipartite lattices (model_parameter.h:615-662).  Signed models are not supported.
   if (jxy > 0 && !bipartite)
     return lg_fail(LG_EUNSUPPORTED, "Jxy > 0 on a non-bipartite lattice (odd L) has a sign problem");
+  if (!std::isfinite(p.force_scatter)) return lg_fail(LG_EINVAL, "FORCE_SCATTER must be finite");
   force_scatter = crop01(p.force_scatter);
   // graph weights: weight_impl.h:282-315 with Jx = Jy = Jxy (Jm = 0)
   const double jp = std::fabs(jxy), a = force_scatter;

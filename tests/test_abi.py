@@ -154,6 +154,11 @@ def test_invalid_models_are_rejected_before_device_work(lg):
     cases = [
         (dict(LATTICE="chain", L=1), -1),                                 # LG_EINVAL
         (dict(LATTICE="chain", L=8, T=-1.0), -1),
+        (dict(LATTICE="chain", L=8, T=float("nan")), -1),
+        (dict(LATTICE="chain", L=8, BETA=float("inf")), -1),
+        (dict(LATTICE="chain", L=8, T=1.0, Jz=float("inf")), -1),
+        (dict(LATTICE="chain", L=8, T=1.0, h=float("nan")), -1),
+        (dict(LATTICE="chain", L=8, T=1.0, FORCE_SCATTER=float("nan")), -1),
         (dict(LATTICE="cubic", L=162, T=1.0), -6),                        # > 2^22 sites: EBUDGET
         (dict(LATTICE="square", L=7, T=1.0), -4),                         # sign problem
         (dict(LATTICE="square", L=8, T=1.0, local_S=1), -4),              # 8 virtual neighbours
