@@ -1274,8 +1274,10 @@ struct lg_batch {
 extern "C" {
 
 int lg_last_error(char* buf, size_t n) {
-  if (buf && n) { std::snprintf(buf, n, "%s", g_err.c_str()); }
-  return (int)g_err.size();
+  return lg_guard([&]() -> int {
+    if (buf && n) { std::snprintf(buf, n, "%s", g_err.c_str()); }
+    return (int)g_err.size();
+  });
 }
 
 uint64_t lg_kernel_launches(void) { return g_launches.load(); }
@@ -1290,30 +1292,40 @@ const char* lg_version(void) {
 }
 
 int lg_create(const lg_params* p, lg_chain** out) {
-  if (!p || !out) return lg_fail(LG_EINVAL, "null argument");
-  ChainSpec s;
-  int rc = s.init(*p);
-  if (rc) return rc;
-  auto e = std::make_shared<Engine>();
-  rc = e->build({s});
-  if (rc) return rc;
-  lg_chain* c = new lg_chain();
-  c->eng = e;
-  *out = c;
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    if (!p || !out) return lg_fail(LG_EINVAL, "null argument");
+    ChainSpec s;
+    int rc = s.init(*p);
+    if (rc) return rc;
+    auto e = std::make_shared<Engine>();
+    rc = e->build({s});
+    if (rc) return rc;
+    lg_chain* c = new lg_chain();
+    c->eng = e;
+    *out = c;
+    return LG_OK;
+  });
 }
 
-int lg_destroy(lg_chain* c) { delete c; return LG_OK; }
+int lg_destroy(lg_chain* c) {
+  return lg_guard([&]() -> int {
+    delete c; return LG_OK;
+  });
+}
 
 int lg_run(lg_chain* c, int64_t n) {
-  if (!c || n < 0) return lg_fail(LG_EINVAL, "bad argument");
-  if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_run on a batch member; use lg_batch_run");
-  return c->eng->run(n);
+  return lg_guard([&]() -> int {
+    if (!c || n < 0) return lg_fail(LG_EINVAL, "bad argument");
+    if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_run on a batch member; use lg_batch_run");
+    return c->eng->run(n);
+  });
 }
 
 int lg_is_thermalized(const lg_chain* c) {
-  const ChainSpec& s = c->eng->spec[c->index];
-  return s.mcs >= (uint64_t)s.therm ? 1 : 0;
+  return lg_guard([&]() -> int {
+    const ChainSpec& s = c->eng->spec[c->index];
+    return s.mcs >= (uint64_t)s.therm ? 1 : 0;
+  });
 }
 
 double lg_progress(const lg_chain* c) {
@@ -1323,9 +1335,11 @@ double lg_progress(const lg_chain* c) {
 }
 
 int lg_observables(lg_chain* c, lg_obs* out) {
-  if (!c || !out) return lg_fail(LG_EINVAL, "null argument");
-  c->eng->acc[c->index].report(c->eng->spec[c->index], out);
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    if (!c || !out) return lg_fail(LG_EINVAL, "null argument");
+    c->eng->acc[c->index].report(c->eng->spec[c->index], out);
+    return LG_OK;
+  });
 }
 
 // Real part of the discrete Fourier transform sum_r e^{i k.r} f(r) over a periodic L^dim grid
@@ -1361,88 +1375,96 @@ static void grid_dft(int dim, int L, const std::vector<double>& f, std::vector<d
 }
 
 int lg_correlations(lg_chain* c, int kind, double* mean, double* err) {
-  if (!c || !mean) return lg_fail(LG_EINVAL, "null argument");
-  const Engine& e = *c->eng;
-  const ChainSpec& s = e.spec[c->index];
-  const ChainAcc& a = e.acc[c->index];
-  const int N = s.N;
-  std::vector<double> m, er;
-  if (kind == LG_CORR_SPIN || kind == LG_CORR_STAGGERED) {
-    if (!s.measure_corr) return lg_fail(LG_EINVAL, "the chain does not measure correlations");
-    if (kind == LG_CORR_STAGGERED && !s.bipartite)
-      return lg_fail(LG_EINVAL, "staggered correlations need a bipartite lattice");
-    const bool origin = s.corr_origin >= 0;
-    (origin ? a.corr_origin : a.corr_disp).mean_err(m, er);
-    if ((int)m.size() != N) { m.assign(N, NAN); er.assign(N, NAN); }
-    // correlation.h:243-264: 1/4 (1-2s)(1-2s'), times 1/N pairs per displacement without origin
-    const double f = origin ? 0.25 : 0.25 / N;
-    for (int i = 0; i < N; ++i) {
-      double g = 1.0;
-      if (kind == LG_CORR_STAGGERED)
-        g = origin ? (double)(s.gauge[s.corr_origin] * s.gauge[i]) : (double)s.gauge[i] * s.gauge[0];
-      mean[i] = f * g * m[i];
-      if (err) err[i] = f * er[i];
-    }
-    return LG_OK;
-  }
-  if (kind == LG_SFAC) {
-    if (!s.measure_sfac) return lg_fail(LG_EINVAL, "the chain does not measure the structure factor");
-    // S(k) = 1/N |sum_s (1/2 - s_s) e^{ik.r_s}|^2 (correlation.h:268-281) = sum_r e^{ik.r} C(r)
-    // with C(r) = 1/(4N) sum_i m_i m_{i+r}: the transform of the all-pairs sums, per sweep and so
-    // for the mean and for every bin mean
-    const VecAcc& v = a.corr_disp;
-    if ((int)v.sum.size() != N || v.count <= 0) {
-      for (int i = 0; i < N; ++i) { mean[i] = NAN; if (err) err[i] = NAN; }
+  return lg_guard([&]() -> int {
+    if (!c || !mean) return lg_fail(LG_EINVAL, "null argument");
+    const Engine& e = *c->eng;
+    const ChainSpec& s = e.spec[c->index];
+    const ChainAcc& a = e.acc[c->index];
+    const int N = s.N;
+    std::vector<double> m, er;
+    if (kind == LG_CORR_SPIN || kind == LG_CORR_STAGGERED) {
+      if (!s.measure_corr) return lg_fail(LG_EINVAL, "the chain does not measure correlations");
+      if (kind == LG_CORR_STAGGERED && !s.bipartite)
+        return lg_fail(LG_EINVAL, "staggered correlations need a bipartite lattice");
+      const bool origin = s.corr_origin >= 0;
+      (origin ? a.corr_origin : a.corr_disp).mean_err(m, er);
+      if ((int)m.size() != N) { m.assign(N, NAN); er.assign(N, NAN); }
+      // correlation.h:243-264: 1/4 (1-2s)(1-2s'), times 1/N pairs per displacement without origin
+      const double f = origin ? 0.25 : 0.25 / N;
+      for (int i = 0; i < N; ++i) {
+        double g = 1.0;
+        if (kind == LG_CORR_STAGGERED)
+          g = origin ? (double)(s.gauge[s.corr_origin] * s.gauge[i]) : (double)s.gauge[i] * s.gauge[0];
+        mean[i] = f * g * m[i];
+        if (err) err[i] = f * er[i];
+      }
       return LG_OK;
     }
-    std::vector<double> f(N), out;
-    for (int i = 0; i < N; ++i) f[i] = 0.25 * (double)v.sum[i] / (double)v.count / N;
-    grid_dft(s.dim, s.L, f, out);
-    for (int i = 0; i < N; ++i) mean[i] = out[i];
-    if (err) {
-      // bins merged into at most 32 groups for the error
-      const size_t B = v.bins.size();
-      const size_t G = std::min<size_t>(B, 32);
-      std::vector<double> var(N, 0.0);
-      int64_t tot = 0;
-      if (G >= 2) {
-        for (size_t g = 0; g < G; ++g) {
-          const size_t k0 = g * B / G, k1 = (g + 1) * B / G;
-          int64_t cnt = 0;
-          std::vector<double> fb(N, 0.0);
-          for (size_t k = k0; k < k1; ++k) {
-            cnt += v.bin_count[k];
-            for (int i = 0; i < N; ++i) fb[i] += (double)v.bins[k][i];
-          }
-          for (int i = 0; i < N; ++i) fb[i] = 0.25 * fb[i] / (double)cnt / N;
-          grid_dft(s.dim, s.L, fb, out);
-          for (int i = 0; i < N; ++i) var[i] += (double)cnt * (out[i] - mean[i]) * (out[i] - mean[i]);
-          tot += cnt;
-        }
-        for (int i = 0; i < N; ++i) err[i] = std::sqrt(var[i] / (double)tot / (double)(G - 1));
-      } else {
-        for (int i = 0; i < N; ++i) err[i] = NAN;
+    if (kind == LG_SFAC) {
+      if (!s.measure_sfac) return lg_fail(LG_EINVAL, "the chain does not measure the structure factor");
+      // S(k) = 1/N |sum_s (1/2 - s_s) e^{ik.r_s}|^2 (correlation.h:268-281) = sum_r e^{ik.r} C(r)
+      // with C(r) = 1/(4N) sum_i m_i m_{i+r}: the transform of the all-pairs sums, per sweep and so
+      // for the mean and for every bin mean
+      const VecAcc& v = a.corr_disp;
+      if ((int)v.sum.size() != N || v.count <= 0) {
+        for (int i = 0; i < N; ++i) { mean[i] = NAN; if (err) err[i] = NAN; }
+        return LG_OK;
       }
+      std::vector<double> f(N), out;
+      for (int i = 0; i < N; ++i) f[i] = 0.25 * (double)v.sum[i] / (double)v.count / N;
+      grid_dft(s.dim, s.L, f, out);
+      for (int i = 0; i < N; ++i) mean[i] = out[i];
+      if (err) {
+        // bins merged into at most 32 groups for the error
+        const size_t B = v.bins.size();
+        const size_t G = std::min<size_t>(B, 32);
+        std::vector<double> var(N, 0.0);
+        int64_t tot = 0;
+        if (G >= 2) {
+          for (size_t g = 0; g < G; ++g) {
+            const size_t k0 = g * B / G, k1 = (g + 1) * B / G;
+            int64_t cnt = 0;
+            std::vector<double> fb(N, 0.0);
+            for (size_t k = k0; k < k1; ++k) {
+              cnt += v.bin_count[k];
+              for (int i = 0; i < N; ++i) fb[i] += (double)v.bins[k][i];
+            }
+            for (int i = 0; i < N; ++i) fb[i] = 0.25 * fb[i] / (double)cnt / N;
+            grid_dft(s.dim, s.L, fb, out);
+            for (int i = 0; i < N; ++i) var[i] += (double)cnt * (out[i] - mean[i]) * (out[i] - mean[i]);
+            tot += cnt;
+          }
+          for (int i = 0; i < N; ++i) err[i] = std::sqrt(var[i] / (double)tot / (double)(G - 1));
+        } else {
+          for (int i = 0; i < N; ++i) err[i] = NAN;
+        }
+      }
+      return LG_OK;
     }
-    return LG_OK;
-  }
-  return lg_fail(LG_EINVAL, "unknown correlation kind %d", kind);
+    return lg_fail(LG_EINVAL, "unknown correlation kind %d", kind);
+  });
 }
 
 int lg_correlation_sums(lg_chain* c, int which, int64_t* sums, int64_t* nsweeps) {
-  if (!c || !sums) return lg_fail(LG_EINVAL, "null argument");
-  const Engine& e = *c->eng;
-  const ChainSpec& s = e.spec[c->index];
-  const ChainAcc& a = e.acc[c->index];
-  const bool on = which == 0 ? e.hch[c->index].corr_disp != 0 : e.hch[c->index].corr_origin >= 0;
-  if (which < 0 || which > 1 || !on) return lg_fail(LG_EINVAL, "the chain does not keep these sums");
-  const VecAcc& v = which ? a.corr_origin : a.corr_disp;
-  for (int i = 0; i < s.N; ++i) sums[i] = (int)v.sum.size() == s.N ? v.sum[i] : 0;
-  if (nsweeps) *nsweeps = v.count;
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    if (!c || !sums) return lg_fail(LG_EINVAL, "null argument");
+    const Engine& e = *c->eng;
+    const ChainSpec& s = e.spec[c->index];
+    const ChainAcc& a = e.acc[c->index];
+    const bool on = which == 0 ? e.hch[c->index].corr_disp != 0 : e.hch[c->index].corr_origin >= 0;
+    if (which < 0 || which > 1 || !on) return lg_fail(LG_EINVAL, "the chain does not keep these sums");
+    const VecAcc& v = which ? a.corr_origin : a.corr_disp;
+    for (int i = 0; i < s.N; ++i) sums[i] = (int)v.sum.size() == s.N ? v.sum[i] : 0;
+    if (nsweeps) *nsweeps = v.count;
+    return LG_OK;
+  });
 }
 
-int lg_set_beta(lg_chain* c, double beta) { return c->eng->set_beta(c->index, beta); }
+int lg_set_beta(lg_chain* c, double beta) {
+  return lg_guard([&]() -> int {
+    return c->eng->set_beta(c->index, beta);
+  });
+}
 
 double lg_weight_parameter(lg_chain* c) { return (double)c->eng->spec[c->index].last_nop; }
 
@@ -1450,134 +1472,172 @@ double lg_log_weight(double gw, double beta) { return std::log(beta) * gw; }
 
 int lg_get_state(lg_chain* c, int32_t* spins, int32_t* bonds, double* times, int64_t cap,
                  int64_t* n) {
-  std::vector<int32_t> sp, bd;
-  std::vector<double> tm;
-  int rc = c->eng->get_state(c->index, sp, bd, tm);
-  if (rc) return rc;
-  if (spins) std::memcpy(spins, sp.data(), sp.size() * sizeof(int32_t));
-  int64_t m = std::min<int64_t>(cap, (int64_t)bd.size());
-  if (bonds && m > 0) std::memcpy(bonds, bd.data(), m * sizeof(int32_t));
-  if (times && m > 0) std::memcpy(times, tm.data(), m * sizeof(double));
-  if (n) *n = (int64_t)bd.size();
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    std::vector<int32_t> sp, bd;
+    std::vector<double> tm;
+    int rc = c->eng->get_state(c->index, sp, bd, tm);
+    if (rc) return rc;
+    if (spins) std::memcpy(spins, sp.data(), sp.size() * sizeof(int32_t));
+    int64_t m = std::min<int64_t>(cap, (int64_t)bd.size());
+    if (bonds && m > 0) std::memcpy(bonds, bd.data(), m * sizeof(int32_t));
+    if (times && m > 0) std::memcpy(times, tm.data(), m * sizeof(double));
+    if (n) *n = (int64_t)bd.size();
+    return LG_OK;
+  });
 }
 
 int lg_set_state(lg_chain* c, const int32_t* spins, const int32_t* bonds, const double* times,
                  int64_t n, uint64_t sweep) {
-  return c->eng->set_state(c->index, spins, bonds, times, n, sweep);
+  return lg_guard([&]() -> int {
+    return c->eng->set_state(c->index, spins, bonds, times, n, sweep);
+  });
 }
 
 int lg_keep_records(lg_chain* c, int on) {
-  if (c->index != 0) return lg_fail(LG_EINVAL, "records are kept for chain 0 only");
-  c->eng->keep_records = on != 0;
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    if (c->index != 0) return lg_fail(LG_EINVAL, "records are kept for chain 0 only");
+    c->eng->keep_records = on != 0;
+    return LG_OK;
+  });
 }
 
 int lg_fetch_records(lg_chain* c, uint64_t* out, int64_t cap, int64_t* n) {
-  auto& k = c->eng->kept;
-  int64_t rows = (int64_t)(k.size() / LG_RECORD_WORDS);
-  int64_t m = std::min(rows, cap);
-  if (out && m > 0) std::memcpy(out, k.data(), m * LG_RECORD_WORDS * sizeof(uint64_t));
-  k.erase(k.begin(), k.begin() + m * LG_RECORD_WORDS);
-  if (n) *n = m;
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    auto& k = c->eng->kept;
+    int64_t rows = (int64_t)(k.size() / LG_RECORD_WORDS);
+    int64_t m = std::min(rows, cap);
+    if (out && m > 0) std::memcpy(out, k.data(), m * LG_RECORD_WORDS * sizeof(uint64_t));
+    k.erase(k.begin(), k.begin() + m * LG_RECORD_WORDS);
+    if (n) *n = m;
+    return LG_OK;
+  });
 }
 
 int lg_save(lg_chain* c, void* buf, size_t* size) {
-  std::vector<int32_t> sp, bd;
-  std::vector<double> tm;
-  int rc = c->eng->get_state(c->index, sp, bd, tm);
-  if (rc) return rc;
-  std::vector<uint8_t> blob;
-  checkpoint_encode(c->eng->spec[c->index], sp, bd, tm, blob);
-  if (!buf) { *size = blob.size(); return LG_OK; }
-  if (*size < blob.size()) { *size = blob.size(); return lg_fail(LG_EINVAL, "buffer too small"); }
-  std::memcpy(buf, blob.data(), blob.size());
-  *size = blob.size();
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    std::vector<int32_t> sp, bd;
+    std::vector<double> tm;
+    int rc = c->eng->get_state(c->index, sp, bd, tm);
+    if (rc) return rc;
+    std::vector<uint8_t> blob;
+    checkpoint_encode(c->eng->spec[c->index], sp, bd, tm, blob);
+    if (!buf) { *size = blob.size(); return LG_OK; }
+    if (*size < blob.size()) { *size = blob.size(); return lg_fail(LG_EINVAL, "buffer too small"); }
+    std::memcpy(buf, blob.data(), blob.size());
+    *size = blob.size();
+    return LG_OK;
+  });
 }
 
 int lg_validate_sweeps(lg_chain* c, int64_t n) {
-  if (!c || n < 0) return lg_fail(LG_EINVAL, "bad argument");
-  if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_validate_sweeps on a batch member; use lg_batch_validate_sweeps");
-  return c->eng->validate(n);
+  return lg_guard([&]() -> int {
+    if (!c || n < 0) return lg_fail(LG_EINVAL, "bad argument");
+    if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_validate_sweeps on a batch member; use lg_batch_validate_sweeps");
+    return c->eng->validate(n);
+  });
 }
 
 int lg_batch_validate_sweeps(lg_batch* b, int64_t n) {
-  if (!b || n < 0) return lg_fail(LG_EINVAL, "bad argument");
-  return b->eng->validate(n);
+  return lg_guard([&]() -> int {
+    if (!b || n < 0) return lg_fail(LG_EINVAL, "bad argument");
+    return b->eng->validate(n);
+  });
 }
 
 int lg_set_iteration_cap(lg_chain* c, int cap) {
-  if (!c) return lg_fail(LG_EINVAL, "null argument");
-  return c->eng->set_iter_cap(cap);
+  return lg_guard([&]() -> int {
+    if (!c) return lg_fail(LG_EINVAL, "null argument");
+    return c->eng->set_iter_cap(cap);
+  });
 }
 
 int lg_load(lg_chain* c, const void* buf, size_t size) {
-  std::vector<int32_t> sp, bd;
-  std::vector<double> tm;
-  uint64_t mcs = 0;
-  int rc = checkpoint_decode(c->eng->spec[c->index], (const uint8_t*)buf, size, sp, bd, tm, &mcs);
-  if (rc) return rc;
-  return c->eng->set_state(c->index, sp.data(), bd.data(), tm.data(), (int64_t)bd.size(), mcs);
+  return lg_guard([&]() -> int {
+    std::vector<int32_t> sp, bd;
+    std::vector<double> tm;
+    uint64_t mcs = 0;
+    int rc = checkpoint_decode(c->eng->spec[c->index], (const uint8_t*)buf, size, sp, bd, tm, &mcs);
+    if (rc) return rc;
+    return c->eng->set_state(c->index, sp.data(), bd.data(), tm.data(), (int64_t)bd.size(), mcs);
+  });
 }
 
 int lg_uf_label(int lattice, int L, int64_t nops, const int32_t* bonds, const int32_t* graphs,
                 int32_t* labels, int64_t cap, int64_t* nfrag, int64_t* nc) {
-  lg_params p;
-  lg_params_default(&p);
-  p.lattice = lattice; p.L = L; p.T = 1.0; p.Jxy = 0.0; p.Jz = 1.0;  // no sign check needed
-  ChainSpec s;
-  int rc = s.init(p);
-  if (rc) return rc;
-  Engine e;
-  rc = e.build({s});
-  if (rc) return rc;
-  std::vector<int32_t> lab;
-  long long n_c = 0;
-  rc = e.uf_label(nops, bonds, graphs, lab, &n_c);
-  if (rc) return rc;
-  if (nfrag) *nfrag = (int64_t)lab.size();
-  if (nc) *nc = n_c;
-  if (labels) std::memcpy(labels, lab.data(), std::min<int64_t>(cap, (int64_t)lab.size()) * sizeof(int32_t));
-  return (int64_t)lab.size() > cap ? lg_fail(LG_EINVAL, "labels buffer too small") : LG_OK;
+  return lg_guard([&]() -> int {
+    lg_params p;
+    lg_params_default(&p);
+    p.lattice = lattice; p.L = L; p.T = 1.0; p.Jxy = 0.0; p.Jz = 1.0;  // no sign check needed
+    ChainSpec s;
+    int rc = s.init(p);
+    if (rc) return rc;
+    Engine e;
+    rc = e.build({s});
+    if (rc) return rc;
+    std::vector<int32_t> lab;
+    long long n_c = 0;
+    rc = e.uf_label(nops, bonds, graphs, lab, &n_c);
+    if (rc) return rc;
+    if (nfrag) *nfrag = (int64_t)lab.size();
+    if (nc) *nc = n_c;
+    if (labels) std::memcpy(labels, lab.data(), std::min<int64_t>(cap, (int64_t)lab.size()) * sizeof(int32_t));
+    return (int64_t)lab.size() > cap ? lg_fail(LG_EINVAL, "labels buffer too small") : LG_OK;
+  });
 }
 
 int lg_batch_create(int n, const lg_params* p, lg_batch** out) {
-  if (n <= 0 || !p || !out) return lg_fail(LG_EINVAL, "bad argument");
-  std::vector<ChainSpec> specs(n);
-  for (int i = 0; i < n; ++i) {
-    int rc = specs[i].init(p[i]);
+  return lg_guard([&]() -> int {
+    if (n <= 0 || !p || !out) return lg_fail(LG_EINVAL, "bad argument");
+    std::vector<ChainSpec> specs(n);
+    for (int i = 0; i < n; ++i) {
+      int rc = specs[i].init(p[i]);
+      if (rc) return rc;
+    }
+    auto e = std::make_shared<Engine>();
+    int rc = e->build(specs);
     if (rc) return rc;
-  }
-  auto e = std::make_shared<Engine>();
-  int rc = e->build(specs);
-  if (rc) return rc;
-  lg_batch* b = new lg_batch();
-  b->eng = e;
-  b->views.resize(n);
-  for (int i = 0; i < n; ++i) { b->views[i].eng = e; b->views[i].index = i; }
-  *out = b;
-  return LG_OK;
+    lg_batch* b = new lg_batch();
+    b->eng = e;
+    b->views.resize(n);
+    for (int i = 0; i < n; ++i) { b->views[i].eng = e; b->views[i].index = i; }
+    *out = b;
+    return LG_OK;
+  });
 }
 
-int lg_batch_destroy(lg_batch* b) { delete b; return LG_OK; }
-int lg_batch_run(lg_batch* b, int64_t n) { return b->eng->run(n); }
-int lg_batch_size(const lg_batch* b) { return b->eng->C; }
+int lg_batch_destroy(lg_batch* b) {
+  return lg_guard([&]() -> int {
+    delete b; return LG_OK;
+  });
+}
+int lg_batch_run(lg_batch* b, int64_t n) {
+  return lg_guard([&]() -> int {
+    return b->eng->run(n);
+  });
+}
+int lg_batch_size(const lg_batch* b) {
+  return lg_guard([&]() -> int {
+    return b->eng->C;
+  });
+}
 lg_chain* lg_batch_chain(lg_batch* b, int i) {
   return (i >= 0 && i < (int)b->views.size()) ? &b->views[i] : nullptr;
 }
 int lg_batch_observables(lg_batch* b, int chain, lg_obs* out) {
-  if (chain < 0 || chain >= b->eng->C) return lg_fail(LG_EINVAL, "chain index");
-  b->eng->acc[chain].report(b->eng->spec[chain], out);
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    if (chain < 0 || chain >= b->eng->C) return lg_fail(LG_EINVAL, "chain index");
+    b->eng->acc[chain].report(b->eng->spec[chain], out);
+    return LG_OK;
+  });
 }
 int lg_batch_stats(const lg_batch* b, int64_t* total_sites, int64_t* site_sweeps) {
-  long long ts = 0, ss = 0;
-  for (auto& s : b->eng->spec) { ts += s.volume; ss += (long long)s.volume * (long long)s.mcs; }
-  if (total_sites) *total_sites = ts;
-  if (site_sweeps) *site_sweeps = ss;
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    long long ts = 0, ss = 0;
+    for (auto& s : b->eng->spec) { ts += s.volume; ss += (long long)s.volume * (long long)s.mcs; }
+    if (total_sites) *total_sites = ts;
+    if (site_sweeps) *site_sweeps = ss;
+    return LG_OK;
+  });
 }
 
 
@@ -1603,15 +1663,19 @@ static int autotune_engine(Engine& e, int trial, size_t flush_bytes, lg_shape* c
 
 int lg_autotune(lg_chain* c, int trial_sweeps, size_t flush_bytes, lg_shape* chosen, char* report,
                 size_t report_len) {
-  if (!c || trial_sweeps < 1) return lg_fail(LG_EINVAL, "bad argument");
-  if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_autotune on a batch member; use lg_batch_autotune");
-  return autotune_engine(*c->eng, trial_sweeps, flush_bytes, chosen, report, report_len);
+  return lg_guard([&]() -> int {
+    if (!c || trial_sweeps < 1) return lg_fail(LG_EINVAL, "bad argument");
+    if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_autotune on a batch member; use lg_batch_autotune");
+    return autotune_engine(*c->eng, trial_sweeps, flush_bytes, chosen, report, report_len);
+  });
 }
 
 int lg_batch_autotune(lg_batch* b, int trial_sweeps, size_t flush_bytes, lg_shape* chosen,
                       char* report, size_t report_len) {
-  if (!b || trial_sweeps < 1) return lg_fail(LG_EINVAL, "bad argument");
-  return autotune_engine(*b->eng, trial_sweeps, flush_bytes, chosen, report, report_len);
+  return lg_guard([&]() -> int {
+    if (!b || trial_sweeps < 1) return lg_fail(LG_EINVAL, "bad argument");
+    return autotune_engine(*b->eng, trial_sweeps, flush_bytes, chosen, report, report_len);
+  });
 }
 
 static int set_shape_engine(Engine& e, const lg_shape* in) {
@@ -1625,55 +1689,75 @@ static int set_shape_engine(Engine& e, const lg_shape* in) {
 }
 
 int lg_get_shape(const lg_chain* c, lg_shape* out) {
-  if (!c || !out) return lg_fail(LG_EINVAL, "null argument");
-  shape_out(c->eng->shape, out);
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    if (!c || !out) return lg_fail(LG_EINVAL, "null argument");
+    shape_out(c->eng->shape, out);
+    return LG_OK;
+  });
 }
 
 int lg_set_shape(lg_chain* c, const lg_shape* in) {
-  if (!c || !in) return lg_fail(LG_EINVAL, "null argument");
-  if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_set_shape on a batch member; use lg_batch_set_shape");
-  return set_shape_engine(*c->eng, in);
+  return lg_guard([&]() -> int {
+    if (!c || !in) return lg_fail(LG_EINVAL, "null argument");
+    if (c->eng->C != 1) return lg_fail(LG_EINVAL, "lg_set_shape on a batch member; use lg_batch_set_shape");
+    return set_shape_engine(*c->eng, in);
+  });
 }
 
 int lg_batch_get_shape(const lg_batch* b, lg_shape* out) {
-  if (!b || !out) return lg_fail(LG_EINVAL, "null argument");
-  shape_out(b->eng->shape, out);
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    if (!b || !out) return lg_fail(LG_EINVAL, "null argument");
+    shape_out(b->eng->shape, out);
+    return LG_OK;
+  });
 }
 
 int lg_batch_set_shape(lg_batch* b, const lg_shape* in) {
-  if (!b || !in) return lg_fail(LG_EINVAL, "null argument");
-  return set_shape_engine(*b->eng, in);
+  return lg_guard([&]() -> int {
+    if (!b || !in) return lg_fail(LG_EINVAL, "null argument");
+    return set_shape_engine(*b->eng, in);
+  });
 }
 
 int lg_time_sweeps(lg_chain* c, int64_t n, size_t flush_bytes, float* ms) {
-  if (!c || n < 0 || !ms) return lg_fail(LG_EINVAL, "bad argument");
-  return c->eng->run(n, ms, flush_bytes);
+  return lg_guard([&]() -> int {
+    if (!c || n < 0 || !ms) return lg_fail(LG_EINVAL, "bad argument");
+    return c->eng->run(n, ms, flush_bytes);
+  });
 }
 
 int lg_batch_time_sweeps(lg_batch* b, int64_t n, size_t flush_bytes, float* ms) {
-  if (!b || n < 0 || !ms) return lg_fail(LG_EINVAL, "bad argument");
-  return b->eng->run(n, ms, flush_bytes);
+  return lg_guard([&]() -> int {
+    if (!b || n < 0 || !ms) return lg_fail(LG_EINVAL, "bad argument");
+    return b->eng->run(n, ms, flush_bytes);
+  });
 }
 
 int lg_profile_sweeps(lg_chain* c, int64_t n, size_t flush_bytes, double* kernel_ms,
                       int64_t* vertices) {
-  long long v = 0;
-  int rc = c->eng->profile(n, flush_bytes, kernel_ms, &v);
-  if (vertices) *vertices = v;
-  return rc;
+  return lg_guard([&]() -> int {
+    long long v = 0;
+    int rc = c->eng->profile(n, flush_bytes, kernel_ms, &v);
+    if (vertices) *vertices = v;
+    return rc;
+  });
 }
 
 int lg_batch_profile_sweeps(lg_batch* b, int64_t n, size_t flush_bytes, double* kernel_ms,
                             int64_t* vertices) {
-  long long v = 0;
-  int rc = b->eng->profile(n, flush_bytes, kernel_ms, &v);
-  if (vertices) *vertices = v;
-  return rc;
+  return lg_guard([&]() -> int {
+    long long v = 0;
+    int rc = b->eng->profile(n, flush_bytes, kernel_ms, &v);
+    if (vertices) *vertices = v;
+    return rc;
+  });
 }
 
-int lg_num_kernels(void) { return kNumStages; }
+int lg_num_kernels(void) {
+  return lg_guard([&]() -> int {
+    return kNumStages;
+  });
+}
 const char* lg_kernel_name(int k) { return (k >= 0 && k < kNumStages) ? kStageNames[k] : ""; }
 
 }  // extern "C"

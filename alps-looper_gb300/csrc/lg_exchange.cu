@@ -61,72 +61,84 @@ uint64_t lg_exchange_chain_seed(uint64_t seed, int i) {
 }
 
 int lg_exchange_create(const lg_params* p, int n, const double* betas, lg_exchange** out) {
-  if (!p || !betas || !out || n < 1) return lg_fail(LG_EINVAL, "bad argument");
-  std::vector<ChainSpec> specs(n);
-  for (int i = 0; i < n; ++i) {
-    if (!(betas[i] > 0) || !std::isfinite(betas[i])) return lg_fail(LG_EINVAL, "beta %d must be positive", i);
-    lg_params q = *p;
-    q.beta = betas[i];
-    q.seed = lg_exchange_chain_seed(p->seed, i);
-    int rc = specs[i].init(q);
+  return lg_guard([&]() -> int {
+    if (!p || !betas || !out || n < 1) return lg_fail(LG_EINVAL, "bad argument");
+    std::vector<ChainSpec> specs(n);
+    for (int i = 0; i < n; ++i) {
+      if (!(betas[i] > 0) || !std::isfinite(betas[i])) return lg_fail(LG_EINVAL, "beta %d must be positive", i);
+      lg_params q = *p;
+      q.beta = betas[i];
+      q.seed = lg_exchange_chain_seed(p->seed, i);
+      int rc = specs[i].init(q);
+      if (rc) return rc;
+    }
+    auto e = std::make_shared<Engine>();
+    int rc = e->build(specs);
     if (rc) return rc;
-  }
-  auto e = std::make_shared<Engine>();
-  int rc = e->build(specs);
-  if (rc) return rc;
-  lg_exchange* x = new lg_exchange();
-  x->eng = e;
-  x->betas.assign(betas, betas + n);
-  x->chain_of_temp.resize(n);
-  x->temp_of_chain.resize(n);
-  for (int i = 0; i < n; ++i) x->chain_of_temp[i] = x->temp_of_chain[i] = i;
-  x->attempts.assign(n > 1 ? n - 1 : 0, 0);
-  x->accepts.assign(n > 1 ? n - 1 : 0, 0);
-  x->views.resize(n);
-  for (int i = 0; i < n; ++i) { x->views[i].eng = e; x->views[i].index = i; }
-  x->seed = p->seed ^ 0x5851F42D4C957F2Dull;
-  *out = x;
-  return LG_OK;
+    lg_exchange* x = new lg_exchange();
+    x->eng = e;
+    x->betas.assign(betas, betas + n);
+    x->chain_of_temp.resize(n);
+    x->temp_of_chain.resize(n);
+    for (int i = 0; i < n; ++i) x->chain_of_temp[i] = x->temp_of_chain[i] = i;
+    x->attempts.assign(n > 1 ? n - 1 : 0, 0);
+    x->accepts.assign(n > 1 ? n - 1 : 0, 0);
+    x->views.resize(n);
+    for (int i = 0; i < n; ++i) { x->views[i].eng = e; x->views[i].index = i; }
+    x->seed = p->seed ^ 0x5851F42D4C957F2Dull;
+    *out = x;
+    return LG_OK;
+  });
 }
 
-int lg_exchange_destroy(lg_exchange* x) { delete x; return LG_OK; }
+int lg_exchange_destroy(lg_exchange* x) {
+  return lg_guard([&]() -> int {
+    delete x; return LG_OK;
+  });
+}
 
 int lg_exchange_run(lg_exchange* x, int64_t nsweeps, int interval) {
-  if (!x || nsweeps < 0 || interval < 1) return lg_fail(LG_EINVAL, "bad argument");
-  while (nsweeps > 0) {
-    const int m = (int)std::min<int64_t>(nsweeps, interval - x->since);
-    int rc = x->eng->run(m);
-    if (rc) return rc;
-    nsweeps -= m;
-    x->since += m;
-    if (x->since >= interval) {
-      x->since = 0;
-      if ((rc = x->exchange())) return rc;
+  return lg_guard([&]() -> int {
+    if (!x || nsweeps < 0 || interval < 1) return lg_fail(LG_EINVAL, "bad argument");
+    while (nsweeps > 0) {
+      const int m = (int)std::min<int64_t>(nsweeps, interval - x->since);
+      int rc = x->eng->run(m);
+      if (rc) return rc;
+      nsweeps -= m;
+      x->since += m;
+      if (x->since >= interval) {
+        x->since = 0;
+        if ((rc = x->exchange())) return rc;
+      }
     }
-  }
-  return LG_OK;
+    return LG_OK;
+  });
 }
 
 int lg_exchange_observables(lg_exchange* x, int t, lg_obs* out) {
-  if (!x || !out || t < 0 || t >= (int)x->betas.size()) return lg_fail(LG_EINVAL, "bad argument");
-  // the chain now at temperature t carries beta_t, which the evaluators need
-  const int c = x->chain_of_temp[t];
-  x->eng->acc[t].report(x->eng->spec[c], out);
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    if (!x || !out || t < 0 || t >= (int)x->betas.size()) return lg_fail(LG_EINVAL, "bad argument");
+    // the chain now at temperature t carries beta_t, which the evaluators need
+    const int c = x->chain_of_temp[t];
+    x->eng->acc[t].report(x->eng->spec[c], out);
+    return LG_OK;
+  });
 }
 
 int lg_exchange_state(const lg_exchange* x, int32_t* chain_of_temp, uint64_t* attempts,
                       uint64_t* accepts) {
-  if (!x) return lg_fail(LG_EINVAL, "null argument");
-  const int n = (int)x->betas.size();
-  for (int t = 0; t < n; ++t) {
-    if (chain_of_temp) chain_of_temp[t] = x->chain_of_temp[t];
-    if (t + 1 < n) {
-      if (attempts) attempts[t] = x->attempts[t];
-      if (accepts) accepts[t] = x->accepts[t];
+  return lg_guard([&]() -> int {
+    if (!x) return lg_fail(LG_EINVAL, "null argument");
+    const int n = (int)x->betas.size();
+    for (int t = 0; t < n; ++t) {
+      if (chain_of_temp) chain_of_temp[t] = x->chain_of_temp[t];
+      if (t + 1 < n) {
+        if (attempts) attempts[t] = x->attempts[t];
+        if (accepts) accepts[t] = x->accepts[t];
+      }
     }
-  }
-  return LG_OK;
+    return LG_OK;
+  });
 }
 
 lg_chain* lg_exchange_chain(lg_exchange* x, int c) {

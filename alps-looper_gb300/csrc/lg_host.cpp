@@ -72,91 +72,93 @@ static bool parse_num(const std::string& v, double* out) {
 }
 
 extern "C" int lg_params_parse(const char* text, lg_params* p) {
-  if (!text || !p) return lg_fail(LG_EINVAL, "null argument");
-  std::string all(text);
-  size_t i = 0;
-  while (i < all.size()) {
-    size_t j = all.find_first_of(";\n", i);
-    if (j == std::string::npos) j = all.size();
-    std::string line = all.substr(i, j - i);
-    i = j + 1;
-    size_t hash = line.find('#');
-    if (hash != std::string::npos) line = line.substr(0, hash);
-    size_t eq = line.find('=');
-    if (eq == std::string::npos) continue;
-    std::string key = trim(line.substr(0, eq)), val = trim(line.substr(eq + 1));
-    double x = 0;
-    auto num = [&](double* dst) -> int {
-      if (!parse_num(val, &x)) return lg_fail(LG_EINVAL, "bad value for %s: '%s'", key.c_str(), val.c_str());
-      *dst = x;
-      return LG_OK;
-    };
-    // integer keys: a finite value within [lo, hi], truncated toward zero as an int conversion
-    // of the parameter would (out-of-range and non-finite values are errors, never a cast)
-    auto integer = [&](double lo, double hi, double* dst) -> int {
-      if (!parse_num(val, &x) || !(x >= lo && x <= hi))
-        return lg_fail(LG_EINVAL, "bad value for %s: '%s'", key.c_str(), val.c_str());
-      *dst = std::trunc(x);
-      return LG_OK;
-    };
-    const double kInt = 2147483647.0, kExact = 9007199254740992.0;  // 2^31 - 1, 2^53
-    int rc = LG_OK;
-    if (key == "LATTICE") {
-      if (val == "chain lattice" || val == "chain") p->lattice = LG_CHAIN;
-      else if (val == "square lattice" || val == "square") p->lattice = LG_SQUARE;
-      else if (val == "simple cubic lattice" || val == "cubic lattice" || val == "cubic") p->lattice = LG_CUBIC;
-      else return lg_fail(LG_EUNSUPPORTED, "LATTICE '%s' not supported", val.c_str());
-    } else if (key == "L") {
-      double d = 0; if (!(rc = integer(-kInt, kInt, &d))) p->L = (int)d;
-    } else if (key == "T") {
-      rc = num(&p->T);
-    } else if (key == "BETA" || key == "INVERSE_TEMPERATURE") {
-      rc = num(&p->beta);
-    } else if (key == "TEMPERATURE") {
-      rc = num(&p->T);
-    } else if (key == "J") {
-      rc = num(&p->J);
-    } else if (key == "Jz") {
-      rc = num(&p->Jz);
-    } else if (key == "Jxy") {
-      rc = num(&p->Jxy);
-    } else if (key == "h") {
-      rc = num(&p->h);
-    } else if (key == "FORCE_SCATTER") {
-      rc = num(&p->force_scatter);
-    } else if (key == "SWEEPS") {
-      double d = 0; if (!(rc = integer(0, kExact, &d))) p->sweeps = (uint64_t)d;
-    } else if (key == "THERMALIZATION") {
-      double d = 0; if (!(rc = integer(-kExact, kExact, &d))) p->thermalization = (int64_t)d;
-    } else if (key == "SEED") {
-      double d = 0;  // below 2^64
-      if (!(rc = integer(0, 18446744073709549568.0, &d))) p->seed = (uint64_t)d;
-    } else if (key == "INITIAL_SPINS") {
-      if (val == "up") p->init_spins = 0;
-      else if (val == "random") p->init_spins = 1;
-      else return lg_fail(LG_EINVAL, "INITIAL_SPINS must be up or random");
-    } else if (key == "DISABLE_IMPROVED_ESTIMATOR") {
-      p->disable_improved_estimator = (val == "0" || val == "false") ? 0 : 1;
-    } else if (key == "MEASURE[Correlations]") {
-      if (!parse_bool(val, &p->measure_correlations))
-        return lg_fail(LG_EINVAL, "MEASURE[Correlations] must be true or false");
-    } else if (key == "MEASURE[Structure Factor]") {
-      if (!parse_bool(val, &p->measure_structure_factor))
-        return lg_fail(LG_EINVAL, "MEASURE[Structure Factor] must be true or false");
-    } else if (key == "INITIAL_SITE") {
-      double d = 0; if (!(rc = integer(-kInt, kInt, &d))) p->initial_site = (int)d;
-    } else if (key == "local_S") {
-      double d; rc = num(&d);
-      if (!rc) {
-        const double t = 2 * d;
-        if (!(t >= 1 && t <= 64) || std::fabs(t - std::round(t)) > 1e-9)
-          return lg_fail(LG_EINVAL, "local_S must be a positive multiple of 1/2");
-        p->spin2 = (int)std::round(t);
+  return lg_guard([&]() -> int {
+    if (!text || !p) return lg_fail(LG_EINVAL, "null argument");
+    std::string all(text);
+    size_t i = 0;
+    while (i < all.size()) {
+      size_t j = all.find_first_of(";\n", i);
+      if (j == std::string::npos) j = all.size();
+      std::string line = all.substr(i, j - i);
+      i = j + 1;
+      size_t hash = line.find('#');
+      if (hash != std::string::npos) line = line.substr(0, hash);
+      size_t eq = line.find('=');
+      if (eq == std::string::npos) continue;
+      std::string key = trim(line.substr(0, eq)), val = trim(line.substr(eq + 1));
+      double x = 0;
+      auto num = [&](double* dst) -> int {
+        if (!parse_num(val, &x)) return lg_fail(LG_EINVAL, "bad value for %s: '%s'", key.c_str(), val.c_str());
+        *dst = x;
+        return LG_OK;
+      };
+      // integer keys: a finite value within [lo, hi], truncated toward zero as an int conversion
+      // of the parameter would (out-of-range and non-finite values are errors, never a cast)
+      auto integer = [&](double lo, double hi, double* dst) -> int {
+        if (!parse_num(val, &x) || !(x >= lo && x <= hi))
+          return lg_fail(LG_EINVAL, "bad value for %s: '%s'", key.c_str(), val.c_str());
+        *dst = std::trunc(x);
+        return LG_OK;
+      };
+      const double kInt = 2147483647.0, kExact = 9007199254740992.0;  // 2^31 - 1, 2^53
+      int rc = LG_OK;
+      if (key == "LATTICE") {
+        if (val == "chain lattice" || val == "chain") p->lattice = LG_CHAIN;
+        else if (val == "square lattice" || val == "square") p->lattice = LG_SQUARE;
+        else if (val == "simple cubic lattice" || val == "cubic lattice" || val == "cubic") p->lattice = LG_CUBIC;
+        else return lg_fail(LG_EUNSUPPORTED, "LATTICE '%s' not supported", val.c_str());
+      } else if (key == "L") {
+        double d = 0; if (!(rc = integer(-kInt, kInt, &d))) p->L = (int)d;
+      } else if (key == "T") {
+        rc = num(&p->T);
+      } else if (key == "BETA" || key == "INVERSE_TEMPERATURE") {
+        rc = num(&p->beta);
+      } else if (key == "TEMPERATURE") {
+        rc = num(&p->T);
+      } else if (key == "J") {
+        rc = num(&p->J);
+      } else if (key == "Jz") {
+        rc = num(&p->Jz);
+      } else if (key == "Jxy") {
+        rc = num(&p->Jxy);
+      } else if (key == "h") {
+        rc = num(&p->h);
+      } else if (key == "FORCE_SCATTER") {
+        rc = num(&p->force_scatter);
+      } else if (key == "SWEEPS") {
+        double d = 0; if (!(rc = integer(0, kExact, &d))) p->sweeps = (uint64_t)d;
+      } else if (key == "THERMALIZATION") {
+        double d = 0; if (!(rc = integer(-kExact, kExact, &d))) p->thermalization = (int64_t)d;
+      } else if (key == "SEED") {
+        double d = 0;  // below 2^64
+        if (!(rc = integer(0, 18446744073709549568.0, &d))) p->seed = (uint64_t)d;
+      } else if (key == "INITIAL_SPINS") {
+        if (val == "up") p->init_spins = 0;
+        else if (val == "random") p->init_spins = 1;
+        else return lg_fail(LG_EINVAL, "INITIAL_SPINS must be up or random");
+      } else if (key == "DISABLE_IMPROVED_ESTIMATOR") {
+        p->disable_improved_estimator = (val == "0" || val == "false") ? 0 : 1;
+      } else if (key == "MEASURE[Correlations]") {
+        if (!parse_bool(val, &p->measure_correlations))
+          return lg_fail(LG_EINVAL, "MEASURE[Correlations] must be true or false");
+      } else if (key == "MEASURE[Structure Factor]") {
+        if (!parse_bool(val, &p->measure_structure_factor))
+          return lg_fail(LG_EINVAL, "MEASURE[Structure Factor] must be true or false");
+      } else if (key == "INITIAL_SITE") {
+        double d = 0; if (!(rc = integer(-kInt, kInt, &d))) p->initial_site = (int)d;
+      } else if (key == "local_S") {
+        double d; rc = num(&d);
+        if (!rc) {
+          const double t = 2 * d;
+          if (!(t >= 1 && t <= 64) || std::fabs(t - std::round(t)) > 1e-9)
+            return lg_fail(LG_EINVAL, "local_S must be a positive multiple of 1/2");
+          p->spin2 = (int)std::round(t);
+        }
       }
+      if (rc) return rc;
     }
-    if (rc) return rc;
-  }
-  return LG_OK;
+    return LG_OK;
+  });
 }
 
 // ---------------------------------------------------------------------------------------------

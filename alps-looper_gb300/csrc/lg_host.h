@@ -1,6 +1,8 @@
 // Host-side model setup, observables and checkpoints of the GB300 loop-cluster engine.
 #pragma once
 #include <cstdint>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -8,6 +10,24 @@
 #include "lg_types.h"
 
 int lg_fail(int code, const char* fmt, ...);
+
+// Every int entry point of the C ABI runs its body through lg_guard, so that no C++ exception
+// crosses the ABI: a failed host allocation becomes LG_ENOMEM, anything else LG_EDEVICE, each
+// with its message in lg_last_error.
+template <class F>
+inline int lg_guard(F&& body) {
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+    return lg_fail(LG_ENOMEM, "host memory allocation failed");
+  } catch (const std::length_error& e) {
+    return lg_fail(LG_ENOMEM, "host allocation too large (%s)", e.what());
+  } catch (const std::exception& e) {
+    return lg_fail(LG_EDEVICE, "unexpected exception: %s", e.what());
+  } catch (...) {
+    return lg_fail(LG_EDEVICE, "unexpected exception");
+  }
+}
 
 // One chain's model, lattice and Monte Carlo schedule, validated from lg_params.
 struct ChainSpec {

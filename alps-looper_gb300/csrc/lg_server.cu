@@ -230,88 +230,106 @@ void lg_server_config_default(lg_server_config* c) {
 }
 
 double lg_request_bytes(const lg_params* p) {
-  ChainSpec s;
-  if (s.init(*p)) return -1.0;
-  return chain_bytes(s);
+  if (!p) return -1.0;
+  try {  // no exception crosses the ABI (an invalid or unsupported request: -1)
+    ChainSpec s;
+    if (s.init(*p)) return -1.0;
+    return chain_bytes(s);
+  } catch (...) {
+    lg_fail(LG_ENOMEM, "host memory allocation failed");
+    return -1.0;
+  }
 }
 
 int lg_server_create(const lg_server_config* cfg, lg_server** out) {
-  if (!cfg || !out || cfg->sweeps_per_tick < 1 || !(cfg->budget_bytes > 0) || cfg->lanes < 1 ||
-      cfg->lanes > lg_server::MAX_LANES)
-    return lg_fail(LG_EINVAL, "bad server configuration");
-  lg_server* s = new lg_server();
-  s->cfg = *cfg;
-  s->nlanes = cfg->lanes;
-  s->t0 = std::chrono::steady_clock::now();
-  cudaGetDevice(&s->device);
-  // lane 0 (the smallest requests) gets the greatest stream priority, so that its short sweeps
-  // are scheduled ahead of the long ones of the larger lanes
-  int least = 0, greatest = 0;
-  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess)
-    for (int k = 0; k < s->nlanes; ++k) s->lanes[k].priority = std::min(least, greatest + k);
-  for (int k = 0; k < s->nlanes; ++k) s->lanes[k].th = std::thread([s, k] { s->loop(k); });
-  *out = s;
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    if (!cfg || !out || cfg->sweeps_per_tick < 1 || !(cfg->budget_bytes > 0) || cfg->lanes < 1 ||
+        cfg->lanes > lg_server::MAX_LANES)
+      return lg_fail(LG_EINVAL, "bad server configuration");
+    lg_server* s = new lg_server();
+    s->cfg = *cfg;
+    s->nlanes = cfg->lanes;
+    s->t0 = std::chrono::steady_clock::now();
+    cudaGetDevice(&s->device);
+    // lane 0 (the smallest requests) gets the greatest stream priority, so that its short sweeps
+    // are scheduled ahead of the long ones of the larger lanes
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess)
+      for (int k = 0; k < s->nlanes; ++k) s->lanes[k].priority = std::min(least, greatest + k);
+    for (int k = 0; k < s->nlanes; ++k) s->lanes[k].th = std::thread([s, k] { s->loop(k); });
+    *out = s;
+    return LG_OK;
+  });
 }
 
 int lg_server_submit(lg_server* s, const lg_params* p, uint64_t* id) {
-  if (!s || !p) return lg_fail(LG_EINVAL, "null argument");
-  lg_server::Req r;
-  int rc = r.spec.init(*p);
-  if (rc) return rc;
-  r.bytes = chain_bytes(r.spec);
-  std::lock_guard<std::mutex> lk(s->mu);
-  if (s->fatal) return lg_fail(s->fatal, "server stopped: %s", s->fatal_msg.c_str());
-  r.id = s->next_id++;
-  r.t_submit = server_now(s->t0);
-  r.t_start = -1;
-  s->pending[s->lane_of(r.spec)].push_back(r);
-  s->stats.submitted++;
-  if (id) *id = r.id;
-  s->cv.notify_all();
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    if (!s || !p) return lg_fail(LG_EINVAL, "null argument");
+    lg_server::Req r;
+    int rc = r.spec.init(*p);
+    if (rc) return rc;
+    r.bytes = chain_bytes(r.spec);
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->fatal) return lg_fail(s->fatal, "server stopped: %s", s->fatal_msg.c_str());
+    r.id = s->next_id++;
+    r.t_submit = server_now(s->t0);
+    r.t_start = -1;
+    s->pending[s->lane_of(r.spec)].push_back(r);
+    s->stats.submitted++;
+    if (id) *id = r.id;
+    s->cv.notify_all();
+    return LG_OK;
+  });
 }
 
 int lg_server_poll(lg_server* s, lg_result* out, int cap, int* n) {
-  std::lock_guard<std::mutex> lk(s->mu);
-  int m = std::min<int>(cap, (int)s->done.size());
-  for (int i = 0; i < m; ++i) out[i] = s->done[i];
-  s->done.erase(s->done.begin(), s->done.begin() + m);
-  if (n) *n = m;
-  if (s->fatal) return lg_fail(s->fatal, "server stopped: %s", s->fatal_msg.c_str());
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    std::lock_guard<std::mutex> lk(s->mu);
+    int m = std::min<int>(cap, (int)s->done.size());
+    for (int i = 0; i < m; ++i) out[i] = s->done[i];
+    s->done.erase(s->done.begin(), s->done.begin() + m);
+    if (n) *n = m;
+    if (s->fatal) return lg_fail(s->fatal, "server stopped: %s", s->fatal_msg.c_str());
+    return LG_OK;
+  });
 }
 
 int lg_server_wait(lg_server* s, double timeout_s) {
-  std::unique_lock<std::mutex> lk(s->mu);
-  const bool ok = s->cv.wait_for(lk, std::chrono::duration<double>(timeout_s), [&] {
-    return s->fatal || s->stats.completed + s->stats.rejected >= s->stats.submitted;
+  return lg_guard([&]() -> int {
+    std::unique_lock<std::mutex> lk(s->mu);
+    const bool ok = s->cv.wait_for(lk, std::chrono::duration<double>(timeout_s), [&] {
+      return s->fatal || s->stats.completed + s->stats.rejected >= s->stats.submitted;
+    });
+    if (s->fatal) return lg_fail(s->fatal, "server stopped: %s", s->fatal_msg.c_str());
+    return ok ? LG_OK : lg_fail(LG_ENOTREADY, "requests still running");
   });
-  if (s->fatal) return lg_fail(s->fatal, "server stopped: %s", s->fatal_msg.c_str());
-  return ok ? LG_OK : lg_fail(LG_ENOTREADY, "requests still running");
 }
 
 int lg_server_get_stats(lg_server* s, lg_server_stats* out) {
-  std::lock_guard<std::mutex> lk(s->mu);
-  *out = s->stats;
-  out->active_bytes = s->active_bytes;
-  out->queued = 0;
-  for (int k = 0; k < s->nlanes; ++k) out->queued += (int64_t)s->pending[k].size();
-  out->elapsed_s = server_now(s->t0);
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->stats;
+    out->active_bytes = s->active_bytes;
+    out->queued = 0;
+    for (int k = 0; k < s->nlanes; ++k) out->queued += (int64_t)s->pending[k].size();
+    out->elapsed_s = server_now(s->t0);
+    return LG_OK;
+  });
 }
 
 int lg_server_destroy(lg_server* s) {
-  if (!s) return LG_OK;
-  {
-    std::lock_guard<std::mutex> lk(s->mu);
-    s->stop = true;
-    s->cv.notify_all();
-  }
-  for (int k = 0; k < s->nlanes; ++k)
-    if (s->lanes[k].th.joinable()) s->lanes[k].th.join();
-  delete s;
-  return LG_OK;
+  return lg_guard([&]() -> int {
+    if (!s) return LG_OK;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->stop = true;
+      s->cv.notify_all();
+    }
+    for (int k = 0; k < s->nlanes; ++k)
+      if (s->lanes[k].th.joinable()) s->lanes[k].th.join();
+    delete s;
+    return LG_OK;
+  });
 }
 
 }  // extern "C"

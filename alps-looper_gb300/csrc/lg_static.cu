@@ -209,110 +209,112 @@ int grid_of(long long n, int threads) {
 extern "C" int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_t* d_bonds,
                                   const int32_t* d_graphs, int32_t* d_labels, int64_t* nfrag,
                                   int64_t* nc, void* stream) {
-  if (lattice < LG_CHAIN || lattice > LG_CUBIC || L < 2)
-    return lg_fail(LG_EINVAL, "lg_uf_label_static: bad lattice");
-  const int dim = lattice;
-  long long N = 1;
-  for (int i = 0; i < dim; ++i) { N *= L; if (N > LG_STATIC_MAX_SITES) break; }
-  if (N > LG_STATIC_MAX_SITES)
-    return lg_fail(LG_EBUDGET, "lg_uf_label_static: %lld sites exceed the static limit of %d",
-                   N, LG_STATIC_MAX_SITES);
-  if (nops < 0 || nops > LG_STATIC_MAX_OPS)
-    return lg_fail(LG_EBUDGET, "lg_uf_label_static: %lld vertices exceed the static limit of %d",
-                   (long long)nops, LG_STATIC_MAX_OPS);
-  if (nops > 0 && (!d_bonds || !d_graphs)) return lg_fail(LG_EINVAL, "null input");
-  if (!d_labels) return lg_fail(LG_EINVAL, "null output");
-  void* base = nullptr;
-  int rc = scratch_address(&base);
-  if (rc) return rc;
-  cudaStream_t st = (cudaStream_t)stream;
-  const int n = (int)N, nb = n * dim, nv = (int)nops, ns = 2 * nv + n, nf = n + nv;
+  return lg_guard([&]() -> int {
+    if (lattice < LG_CHAIN || lattice > LG_CUBIC || L < 2)
+      return lg_fail(LG_EINVAL, "lg_uf_label_static: bad lattice");
+    const int dim = lattice;
+    long long N = 1;
+    for (int i = 0; i < dim; ++i) { N *= L; if (N > LG_STATIC_MAX_SITES) break; }
+    if (N > LG_STATIC_MAX_SITES)
+      return lg_fail(LG_EBUDGET, "lg_uf_label_static: %lld sites exceed the static limit of %d",
+                     N, LG_STATIC_MAX_SITES);
+    if (nops < 0 || nops > LG_STATIC_MAX_OPS)
+      return lg_fail(LG_EBUDGET, "lg_uf_label_static: %lld vertices exceed the static limit of %d",
+                     (long long)nops, LG_STATIC_MAX_OPS);
+    if (nops > 0 && (!d_bonds || !d_graphs)) return lg_fail(LG_EINVAL, "null input");
+    if (!d_labels) return lg_fail(LG_EINVAL, "null output");
+    void* base = nullptr;
+    int rc = scratch_address(&base);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int n = (int)N, nb = n * dim, nv = (int)nops, ns = 2 * nv + n, nf = n + nv;
 
-  Carve cv{static_cast<unsigned char*>(base)};
-  Arena A{};
-  A.C = 1; A.N = n; A.NB = nb;
-  DChain* ch = cv.take<DChain>(1);
-  A.ch = ch;
-  A.inc_off = cv.take<int>(n + 1);
-  A.inc = cv.take<int>((size_t)2 * dim * n);
-  A.inc_side = cv.take<uint8_t>((size_t)2 * dim * n);
-  A.gauge = cv.take<int8_t>(n);
-  A.site_chain = cv.take<int>(n);
-  A.ch_slot_off = cv.take<int>(2);
-  A.spin0 = cv.take<uint8_t>(n);
-  A.bond_cnt = cv.take<int>(nb);
-  A.bond_ptr = cv.take<int>(nb + 1);
-  A.site_cnt = cv.take<int>(n);
-  A.sbase = cv.take<int>(n + 1);
-  A.vtime = cv.take<uint64_t>(nv + 1);
-  A.vcode = cv.take<uint8_t>(nv + 1);
-  A.vslot = cv.take<int>(2 * (size_t)nv + 2);
-  A.stime = cv.take<uint64_t>(ns);
-  A.sinfo = cv.take<uint8_t>(ns);
-  A.svert = cv.take<int>(ns);
-  A.sdir = cv.take<uint8_t>(ns);
-  A.parent = cv.take<int>(ns);
-  Ctl* ctl = cv.take<Ctl>(1);
-  A.ctl = ctl;
-  int* fill = cv.take<int>(nb);
-  int* g0flag = cv.take<int>(nv + 1);
-  int* g0ord = cv.take<int>(nv + 1);
-  int* g0_input = cv.take<int>(nv + 1);
-  int* v_of_input = cv.take<int>(nv + 1);
-  int* froot = cv.take<int>(nf);
-  unsigned* minfrag = cv.take<unsigned>(ns);
-  int* flag = cv.take<int>(nf);
-  int* id = cv.take<int>(nf + 1);
-  int* totals = cv.take<int>(4);
-  const int maxn = std::max(std::max(nb, ns), nf) + 1;
-  int* partial = cv.take<int>(maxn / SCAN_TILE + 2);
-  if (cv.used > LG_STATIC_SCRATCH_BYTES)
-    return lg_fail(LG_EBUDGET, "lg_uf_label_static: %zu bytes of scratch needed, %zu available",
-                   cv.used, LG_STATIC_SCRATCH_BYTES);
+    Carve cv{static_cast<unsigned char*>(base)};
+    Arena A{};
+    A.C = 1; A.N = n; A.NB = nb;
+    DChain* ch = cv.take<DChain>(1);
+    A.ch = ch;
+    A.inc_off = cv.take<int>(n + 1);
+    A.inc = cv.take<int>((size_t)2 * dim * n);
+    A.inc_side = cv.take<uint8_t>((size_t)2 * dim * n);
+    A.gauge = cv.take<int8_t>(n);
+    A.site_chain = cv.take<int>(n);
+    A.ch_slot_off = cv.take<int>(2);
+    A.spin0 = cv.take<uint8_t>(n);
+    A.bond_cnt = cv.take<int>(nb);
+    A.bond_ptr = cv.take<int>(nb + 1);
+    A.site_cnt = cv.take<int>(n);
+    A.sbase = cv.take<int>(n + 1);
+    A.vtime = cv.take<uint64_t>(nv + 1);
+    A.vcode = cv.take<uint8_t>(nv + 1);
+    A.vslot = cv.take<int>(2 * (size_t)nv + 2);
+    A.stime = cv.take<uint64_t>(ns);
+    A.sinfo = cv.take<uint8_t>(ns);
+    A.svert = cv.take<int>(ns);
+    A.sdir = cv.take<uint8_t>(ns);
+    A.parent = cv.take<int>(ns);
+    Ctl* ctl = cv.take<Ctl>(1);
+    A.ctl = ctl;
+    int* fill = cv.take<int>(nb);
+    int* g0flag = cv.take<int>(nv + 1);
+    int* g0ord = cv.take<int>(nv + 1);
+    int* g0_input = cv.take<int>(nv + 1);
+    int* v_of_input = cv.take<int>(nv + 1);
+    int* froot = cv.take<int>(nf);
+    unsigned* minfrag = cv.take<unsigned>(ns);
+    int* flag = cv.take<int>(nf);
+    int* id = cv.take<int>(nf + 1);
+    int* totals = cv.take<int>(4);
+    const int maxn = std::max(std::max(nb, ns), nf) + 1;
+    int* partial = cv.take<int>(maxn / SCAN_TILE + 2);
+    if (cv.used > LG_STATIC_SCRATCH_BYTES)
+      return lg_fail(LG_EBUDGET, "lg_uf_label_static: %zu bytes of scratch needed, %zu available",
+                     cv.used, LG_STATIC_SCRATCH_BYTES);
 
-  // everything that must start at zero (or at the atomicMin identity)
-  DChain hch{};
-  LG_CUDA(cudaMemcpyAsync(ch, &hch, sizeof(DChain), cudaMemcpyHostToDevice, st));
-  LG_CUDA(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
-  LG_CUDA(cudaMemsetAsync(A.bond_cnt, 0, nb * sizeof(int), st));
-  LG_CUDA(cudaMemsetAsync(fill, 0, nb * sizeof(int), st));
-  LG_CUDA(cudaMemsetAsync(minfrag, 0xFF, (size_t)ns * sizeof(unsigned), st));
-  LG_CUDA(cudaMemsetAsync(totals, 0, 4 * sizeof(int), st));
+    // everything that must start at zero (or at the atomicMin identity)
+    DChain hch{};
+    LG_CUDA(cudaMemcpyAsync(ch, &hch, sizeof(DChain), cudaMemcpyHostToDevice, st));
+    LG_CUDA(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
+    LG_CUDA(cudaMemsetAsync(A.bond_cnt, 0, nb * sizeof(int), st));
+    LG_CUDA(cudaMemsetAsync(fill, 0, nb * sizeof(int), st));
+    LG_CUDA(cudaMemsetAsync(minfrag, 0xFF, (size_t)ns * sizeof(unsigned), st));
+    LG_CUDA(cudaMemsetAsync(totals, 0, 4 * sizeof(int), st));
 
-  ks_lattice<<<grid_of(n, 128), 128, 0, st>>>(A, dim, L);
-  if (nv > 0) ks_count<<<grid_of(nv, 256), 256, 0, st>>>(A, d_bonds, d_graphs, nv, g0flag);
-  static_scan(A.bond_cnt, A.bond_ptr, nb, &ctl->nv_total, partial, ctl, st);
-  if (nv > 0) ks_scatter<<<grid_of(nv, 256), 256, 0, st>>>(A, d_bonds, nv, fill);
-  ks_sort_bonds<<<grid_of(nb, 128), 128, 0, st>>>(A, d_graphs, v_of_input);
-  k_site_count<<<grid_of(n, 256), 256, 0, st>>>(A);
-  static_scan(A.site_cnt, A.sbase, n, &ctl->ns_total, partial, ctl, st);
-  launch_merge(2 * dim, grid_of((long long)n * 32, MERGE_WARPS * 32),
-               MERGE_WARPS * merge_smem_per_warp(MERGE_CAP), st, A, nullptr, n, MERGE_CAP);
-  if (nv > 0) k_union<><<<grid_of(ns, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
-  ks_compress<<<grid_of(ns, 256), 256, 0, st>>>(A);
-  static_scan(g0flag, g0ord, nv, totals, partial, ctl, st);
-  g_launches += nv > 0 ? 8 : 5;  // the scans count their own
-  LG_CUDA(cudaGetLastError());
-  int ng0 = 0, err = 0;
-  LG_CUDA(cudaMemcpyAsync(&ng0, totals, sizeof(int), cudaMemcpyDeviceToHost, st));
-  LG_CUDA(cudaMemcpyAsync(&err, &ctl->err, sizeof(int), cudaMemcpyDeviceToHost, st));
-  LG_CUDA(cudaStreamSynchronize(st));
-  if (err == 3) return lg_fail(LG_EINVAL, "lg_uf_label_static: bond or graph out of range");
-  if (err) return lg_fail(LG_EITERCAP, "lg_uf_label_static: union-find failed (%d)", err);
-  const int nfrag_ = n + ng0;
-  ks_fragments<<<grid_of(std::max(n, nv), 256), 256, 0, st>>>(A, nv, g0flag, g0ord, v_of_input,
-                                                            g0_input, froot, minfrag);
-  if (ng0 > 0)
-    ks_fragments_g0<<<grid_of(ng0, 256), 256, 0, st>>>(A, ng0, g0_input, v_of_input, froot, minfrag);
-  ks_repflag<<<grid_of(nfrag_, 256), 256, 0, st>>>(A, nfrag_, froot, minfrag, flag);
-  static_scan(flag, id, nfrag_, totals + 1, partial, ctl, st);
-  ks_label<<<grid_of(nfrag_, 256), 256, 0, st>>>(A, nfrag_, froot, minfrag, id, d_labels);
-  g_launches += ng0 > 0 ? 4 : 3;
-  LG_CUDA(cudaGetLastError());
-  int ncl = 0;
-  LG_CUDA(cudaMemcpyAsync(&ncl, totals + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-  LG_CUDA(cudaStreamSynchronize(st));
-  if (nfrag) *nfrag = nfrag_;
-  if (nc) *nc = ncl;
-  return LG_OK;
+    ks_lattice<<<grid_of(n, 128), 128, 0, st>>>(A, dim, L);
+    if (nv > 0) ks_count<<<grid_of(nv, 256), 256, 0, st>>>(A, d_bonds, d_graphs, nv, g0flag);
+    static_scan(A.bond_cnt, A.bond_ptr, nb, &ctl->nv_total, partial, ctl, st);
+    if (nv > 0) ks_scatter<<<grid_of(nv, 256), 256, 0, st>>>(A, d_bonds, nv, fill);
+    ks_sort_bonds<<<grid_of(nb, 128), 128, 0, st>>>(A, d_graphs, v_of_input);
+    k_site_count<<<grid_of(n, 256), 256, 0, st>>>(A);
+    static_scan(A.site_cnt, A.sbase, n, &ctl->ns_total, partial, ctl, st);
+    launch_merge(2 * dim, grid_of((long long)n * 32, MERGE_WARPS * 32),
+                 MERGE_WARPS * merge_smem_per_warp(MERGE_CAP), st, A, nullptr, n, MERGE_CAP);
+    if (nv > 0) k_union<><<<grid_of(ns, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
+    ks_compress<<<grid_of(ns, 256), 256, 0, st>>>(A);
+    static_scan(g0flag, g0ord, nv, totals, partial, ctl, st);
+    g_launches += nv > 0 ? 8 : 5;  // the scans count their own
+    LG_CUDA(cudaGetLastError());
+    int ng0 = 0, err = 0;
+    LG_CUDA(cudaMemcpyAsync(&ng0, totals, sizeof(int), cudaMemcpyDeviceToHost, st));
+    LG_CUDA(cudaMemcpyAsync(&err, &ctl->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    LG_CUDA(cudaStreamSynchronize(st));
+    if (err == 3) return lg_fail(LG_EINVAL, "lg_uf_label_static: bond or graph out of range");
+    if (err) return lg_fail(LG_EITERCAP, "lg_uf_label_static: union-find failed (%d)", err);
+    const int nfrag_ = n + ng0;
+    ks_fragments<<<grid_of(std::max(n, nv), 256), 256, 0, st>>>(A, nv, g0flag, g0ord, v_of_input,
+                                                              g0_input, froot, minfrag);
+    if (ng0 > 0)
+      ks_fragments_g0<<<grid_of(ng0, 256), 256, 0, st>>>(A, ng0, g0_input, v_of_input, froot, minfrag);
+    ks_repflag<<<grid_of(nfrag_, 256), 256, 0, st>>>(A, nfrag_, froot, minfrag, flag);
+    static_scan(flag, id, nfrag_, totals + 1, partial, ctl, st);
+    ks_label<<<grid_of(nfrag_, 256), 256, 0, st>>>(A, nfrag_, froot, minfrag, id, d_labels);
+    g_launches += ng0 > 0 ? 4 : 3;
+    LG_CUDA(cudaGetLastError());
+    int ncl = 0;
+    LG_CUDA(cudaMemcpyAsync(&ncl, totals + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    LG_CUDA(cudaStreamSynchronize(st));
+    if (nfrag) *nfrag = nfrag_;
+    if (nc) *nc = ncl;
+    return LG_OK;
+  });
 }

@@ -148,6 +148,30 @@ def test_request_bytes_estimate(lg):
     assert lg.request_bytes(lg.make_params(LATTICE="square", L=7, T=1.0)) < 0  # sign problem
 
 
+def test_host_allocation_failure_is_a_status_not_an_exception(lg):
+    # lg_batch_create sizes its host-side chain table before reading any parameters: a count of
+    # 2^31 - 1 chains (over 150 GB of table) fails to allocate, which the ABI must report as
+    # LG_ENOMEM instead of letting std::bad_alloc through (that would end this process).  Only
+    # where the kernel refuses an allocation larger than the machine's memory.
+    try:
+        mode = open("/proc/sys/vm/overcommit_memory").read().strip()
+        mem = {}
+        for ln in open("/proc/meminfo"):
+            k, v = ln.split(":")
+            mem[k] = int(v.split()[0]) * 1024
+    except OSError:
+        pytest.skip("no /proc to check the overcommit policy")
+    n = 2 ** 31 - 1
+    if mode == "1" or mem.get("MemTotal", 0) + mem.get("SwapTotal", 0) >= n * 72:
+        pytest.skip("the kernel might grant the allocation")
+    p = lg.Params()
+    lg.lib().lg_params_default(ctypes.byref(p))
+    out = ctypes.c_void_p()
+    rc = lg.lib().lg_batch_create(n, ctypes.byref(p), ctypes.byref(out))
+    assert rc == -2, (rc, lg.last_error())
+    assert "allocation" in lg.last_error()
+
+
 def test_invalid_models_are_rejected_before_device_work(lg):
     # lg_create validates the parameters (ChainSpec::init) before touching the GPU, so each of
     # these returns its status code on a machine without one
