@@ -256,7 +256,20 @@ int lg_server_create(const lg_server_config* cfg, lg_server** out) {
     int least = 0, greatest = 0;
     if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess)
       for (int k = 0; k < s->nlanes; ++k) s->lanes[k].priority = std::min(least, greatest + k);
-    for (int k = 0; k < s->nlanes; ++k) s->lanes[k].th = std::thread([s, k] { s->loop(k); });
+    // a lane that throws stops the server like a failed sweep does (fail: every later call
+    // reports it); nothing escapes the thread, which would end the process
+    for (int k = 0; k < s->nlanes; ++k)
+      s->lanes[k].th = std::thread([s, k] {
+        try {
+          s->loop(k);
+        } catch (const std::bad_alloc&) {
+          s->fail(lg_fail(LG_ENOMEM, "server lane %d: host memory allocation failed", k));
+        } catch (const std::exception& e) {
+          s->fail(lg_fail(LG_EDEVICE, "server lane %d: unexpected exception: %s", k, e.what()));
+        } catch (...) {
+          s->fail(lg_fail(LG_EDEVICE, "server lane %d: unexpected exception", k));
+        }
+      });
     *out = s;
     return LG_OK;
   });
