@@ -147,7 +147,7 @@ extern "C" int lg_params_parse(const char* text, lg_params* p) {
       } else if (key == "INITIAL_SITE") {
         double d = 0; if (!(rc = integer(-kInt, kInt, &d))) p->initial_site = (int)d;
       } else if (key == "local_S") {
-        double d; rc = num(&d);
+        double d = 0; rc = num(&d);
         if (!rc) {
           const double t = 2 * d;
           if (!(t >= 1 && t <= 64) || std::fabs(t - std::round(t)) > 1e-9)
