@@ -160,6 +160,10 @@ struct Engine {
   int stream_priority = 0;   // CUDA stream priority of the arena's streams (0: the default)
   bool keep_records = false;
   std::vector<uint64_t> kept;   // raw records of chain 0 (test seam)
+  // per-sweep observable values of the measurement sweeps (lg_keep_values / lg_fetch_values),
+  // LG_NUM_VALUES doubles per sweep, per chain
+  std::vector<uint8_t> keep_vals;
+  std::vector<std::vector<double>> vals;
   std::vector<uint64_t> hrec;
 
   ~Engine() {
@@ -202,6 +206,8 @@ struct Engine {
     spec = specs;
     C = (int)spec.size();
     acc.assign(C, ChainAcc());
+    keep_vals.assign(C, 0);
+    vals.assign(C, {});
     acc_of_chain.resize(C);
     for (int c = 0; c < C; ++c) acc_of_chain[c] = c;
     int dev = 0;
@@ -921,6 +927,11 @@ struct Engine {
         s.last_nop = rec[R_NOP];
         if (s.mcs >= (uint64_t)s.therm && s.mcs < (uint64_t)(s.therm + s.sweeps)) {
           acc[acc_of_chain[c]].push(s, rec);
+          if (keep_vals[c]) {
+            const size_t o = vals[c].size();
+            vals[c].resize(o + LG_NUM_VALUES);
+            record_scalars(s, rec, vals[c].data() + o);
+          }
           if (n_corr_tiles) ++measured[c];
         }
         ++s.mcs;
@@ -1508,6 +1519,36 @@ int lg_fetch_records(lg_chain* c, uint64_t* out, int64_t cap, int64_t* n) {
     int64_t m = std::min(rows, cap);
     if (out && m > 0) std::memcpy(out, k.data(), m * LG_RECORD_WORDS * sizeof(uint64_t));
     k.erase(k.begin(), k.begin() + m * LG_RECORD_WORDS);
+    if (n) *n = m;
+    return LG_OK;
+  });
+}
+
+int lg_value_mask(const lg_chain* c, uint64_t* mask) {
+  return lg_guard([&]() -> int {
+    if (!c || !mask) return lg_fail(LG_EINVAL, "null argument");
+    *mask = value_mask(c->eng->spec[c->index]);
+    return LG_OK;
+  });
+}
+
+int lg_keep_values(lg_chain* c, int on) {
+  return lg_guard([&]() -> int {
+    if (!c) return lg_fail(LG_EINVAL, "null argument");
+    c->eng->keep_vals[c->index] = on ? 1 : 0;
+    if (!on) c->eng->vals[c->index].clear();
+    return LG_OK;
+  });
+}
+
+int lg_fetch_values(lg_chain* c, double* out, int64_t cap, int64_t* n) {
+  return lg_guard([&]() -> int {
+    if (!c || cap < 0 || (cap > 0 && !out)) return lg_fail(LG_EINVAL, "bad argument");
+    auto& k = c->eng->vals[c->index];
+    const int64_t rows = (int64_t)(k.size() / LG_NUM_VALUES);
+    const int64_t m = std::min(rows, cap);
+    if (m > 0) std::memcpy(out, k.data(), (size_t)m * LG_NUM_VALUES * sizeof(double));
+    k.erase(k.begin(), k.begin() + (size_t)m * LG_NUM_VALUES);
     if (n) *n = m;
     return LG_OK;
   });

@@ -392,6 +392,124 @@ void record_values(const ChainSpec& s, const uint64_t* r, double* v) {
   }
 }
 
+uint64_t value_mask(const ChainSpec& s) {
+  uint64_t m = 0;
+  for (int i = 0; i < LG_NUM_VALUES; ++i) {
+    const bool gen = (i >= LG_VAL_GEN_MAGNETIZATION2 && i <= LG_VAL_GEN_SUSCEPTIBILITY) ||
+                     (i >= LG_VAL_GEN_STAG_MAGNETIZATION2 && i <= LG_VAL_GEN_STAG_SUSCEPTIBILITY);
+    const bool stag = i >= LG_VAL_STAG_MAGNETIZATION && i <= LG_VAL_GEN_STAG_SUSCEPTIBILITY;
+    if (gen && !s.improved) continue;      // susceptibility.h:69-75, 86-92
+    if (stag && !s.bipartite) continue;    // susceptibility.h:76
+    m |= 1ull << i;
+  }
+  return m;
+}
+
+// The pushes of loop_worker::run for one sweep record: path_integral.C:832-836 and 849-860,
+// energy.h:76-84, susceptibility.h:200-254 (improved) or :303-335 (normal), stiffness.h:124-127
+// (improved) or :160-165 (normal).  The record's integer sums map onto the collector fields:
+// umag0 = M0/2, umag2 = M0SQ/4, umag4 = M0Q/16, usize2 = N0SQ/4, usize4 = N0Q/16 (tau = 0
+// cluster sums), umag = MSQ 2^-80/4, usize = LSQ 2^-80/4 (time-integrated, 2^-40 units), and the
+// staggered ones likewise; the normal estimator's umag = M0/2 and umag_a = MA 2^-40/2.
+void record_scalars(const ChainSpec& s, const uint64_t* r, double* v) {
+  const double beta = s.beta, vol = (double)s.volume;
+  double raw[NUM_RAW];
+  record_values(s, r, raw);
+  for (int i = 0; i < LG_NUM_VALUES; ++i) v[i] = std::nan("");
+  const uint64_t mask = value_mask(s);
+  auto p2 = [](double x) { return x * x; };
+  auto p4 = [](double x) { return x * x * x * x; };
+  v[LG_VAL_TEMPERATURE] = 1 / beta;
+  v[LG_VAL_INVERSE_TEMPERATURE] = beta;
+  v[LG_VAL_VOLUME] = vol;
+  v[LG_VAL_NUMBER_OF_SITES] = vol;
+  v[LG_VAL_NUMBER_OF_CLUSTERS] = raw[RAW_NC];
+  v[LG_VAL_ENERGY] = raw[RAW_E];
+  v[LG_VAL_ENERGY_DENSITY] = raw[RAW_E] / vol;
+  v[LG_VAL_ENERGY2] = raw[RAW_E2];
+  const double t80 = std::ldexp(1.0, -80), t40 = std::ldexp(1.0, -40);
+  if (s.improved) {
+    const double umag0 = i64(r[R_M0]) / 2, umag2 = (double)r[R_M0SQ] / 4, umag4 = u128d(r, R_M0Q) / 16;
+    const double usize2 = (double)r[R_N0SQ] / 4, usize4 = u128d(r, R_N0Q) / 16;
+    const double umag = u128d(r, R_MSQ) * t80 / 4, usize = u128d(r, R_LSQ) * t80 / 4;
+    const double smag0 = i64(r[R_SM0]) / 2, smag2 = (double)r[R_SM0SQ] / 4, smag4 = u128d(r, R_SM0Q) / 16;
+    const double ssize2 = (double)r[R_SN0SQ] / 4, ssize4 = u128d(r, R_SN0Q) / 16;
+    const double smag = u128d(r, R_SMSQ) * t80 / 4, ssize = u128d(r, R_SLSQ) * t80 / 4;
+    v[LG_VAL_MAGNETIZATION] = 0.0;
+    v[LG_VAL_MAGNETIZATION_DENSITY] = 0.0;
+    v[LG_VAL_ABS_MAGNETIZATION] = std::fabs(umag0);
+    v[LG_VAL_ABS_MAGNETIZATION_DENSITY] = std::fabs(umag0) / vol;
+    v[LG_VAL_MAGNETIZATION2] = umag2;
+    v[LG_VAL_MAGNETIZATION_DENSITY2] = umag2 / p2(vol);
+    v[LG_VAL_MAGNETIZATION4] = 3 * p2(umag2) - 2 * umag4;
+    v[LG_VAL_MAGNETIZATION_DENSITY4] = (3 * p2(umag2) - 2 * umag4) / p4(vol);
+    v[LG_VAL_SUSCEPTIBILITY] = beta * umag / vol;
+    v[LG_VAL_GEN_MAGNETIZATION2] = usize2;
+    v[LG_VAL_GEN_MAGNETIZATION_DENSITY2] = usize2 / p2(vol);
+    v[LG_VAL_GEN_MAGNETIZATION4] = 3 * p2(usize2) - 2 * usize4;
+    v[LG_VAL_GEN_MAGNETIZATION_DENSITY4] = (3 * p2(usize2) - 2 * usize4) / p4(vol);
+    v[LG_VAL_GEN_SUSCEPTIBILITY] = beta * usize / vol;
+    v[LG_VAL_STAG_MAGNETIZATION] = 0.0;
+    v[LG_VAL_STAG_MAGNETIZATION_DENSITY] = 0.0;
+    v[LG_VAL_ABS_STAG_MAGNETIZATION] = std::fabs(smag0);
+    v[LG_VAL_ABS_STAG_MAGNETIZATION_DENSITY] = std::fabs(smag0) / vol;
+    v[LG_VAL_STAG_MAGNETIZATION2] = smag2;
+    v[LG_VAL_STAG_MAGNETIZATION_DENSITY2] = smag2 / p2(vol);
+    v[LG_VAL_STAG_MAGNETIZATION4] = 3 * p2(smag2) - 2 * smag4;
+    v[LG_VAL_STAG_MAGNETIZATION_DENSITY4] = (3 * p2(smag2) - 2 * smag4) / p4(vol);
+    v[LG_VAL_STAG_SUSCEPTIBILITY] = beta * smag / vol;
+    v[LG_VAL_GEN_STAG_MAGNETIZATION2] = ssize2;
+    v[LG_VAL_GEN_STAG_MAGNETIZATION_DENSITY2] = ssize2 / p2(vol);
+    v[LG_VAL_GEN_STAG_MAGNETIZATION4] = 3 * p2(ssize2) - 2 * ssize4;
+    v[LG_VAL_GEN_STAG_MAGNETIZATION_DENSITY4] = (3 * p2(ssize2) - 2 * ssize4) / p4(vol);
+    v[LG_VAL_GEN_STAG_SUSCEPTIBILITY] = beta * ssize / vol;
+  } else {
+    const double umag = i64(r[R_M0]) / 2, smag = i64(r[R_SM0]) / 2;
+    const double umag_a = i64(r[R_MA]) * t40 / 2, smag_a = i64(r[R_SMA]) * t40 / 2;
+    v[LG_VAL_MAGNETIZATION] = umag;
+    v[LG_VAL_MAGNETIZATION_DENSITY] = umag / vol;
+    v[LG_VAL_ABS_MAGNETIZATION] = std::fabs(umag);
+    v[LG_VAL_ABS_MAGNETIZATION_DENSITY] = std::fabs(umag) / vol;
+    v[LG_VAL_MAGNETIZATION2] = p2(umag);
+    v[LG_VAL_MAGNETIZATION_DENSITY2] = p2(umag / vol);
+    v[LG_VAL_MAGNETIZATION4] = p4(umag);
+    v[LG_VAL_MAGNETIZATION_DENSITY4] = p4(umag / vol);
+    v[LG_VAL_SUSCEPTIBILITY] = beta * p2(umag_a) / vol;
+    v[LG_VAL_STAG_MAGNETIZATION] = smag;
+    v[LG_VAL_STAG_MAGNETIZATION_DENSITY] = smag / vol;
+    v[LG_VAL_ABS_STAG_MAGNETIZATION] = std::fabs(smag);
+    v[LG_VAL_ABS_STAG_MAGNETIZATION_DENSITY] = std::fabs(smag) / vol;
+    v[LG_VAL_STAG_MAGNETIZATION2] = p2(smag);
+    v[LG_VAL_STAG_MAGNETIZATION_DENSITY2] = p2(smag / vol);
+    v[LG_VAL_STAG_MAGNETIZATION4] = p4(smag);
+    v[LG_VAL_STAG_MAGNETIZATION_DENSITY4] = p4(smag / vol);
+    v[LG_VAL_STAG_SUSCEPTIBILITY] = beta * p2(smag_a) / vol;
+  }
+  v[LG_VAL_STIFFNESS] = raw[RAW_STIFF];
+  for (int i = 0; i < LG_NUM_VALUES; ++i)
+    if (!(mask >> i & 1)) v[i] = std::nan("");
+}
+
+extern "C" const char* lg_value_name(int i) {
+  static const char* names[LG_NUM_VALUES] = {
+      "Temperature", "Inverse Temperature", "Volume", "Number of Sites", "Number of Clusters",
+      "Energy", "Energy Density", "Energy^2",
+      "Magnetization", "Magnetization Density", "|Magnetization|", "|Magnetization Density|",
+      "Magnetization^2", "Magnetization Density^2", "Magnetization^4", "Magnetization Density^4",
+      "Susceptibility",
+      "Generalized Magnetization^2", "Generalized Magnetization Density^2",
+      "Generalized Magnetization^4", "Generalized Magnetization Density^4",
+      "Generalized Susceptibility",
+      "Staggered Magnetization", "Staggered Magnetization Density", "|Staggered Magnetization|",
+      "|Staggered Magnetization Density|", "Staggered Magnetization^2",
+      "Staggered Magnetization Density^2", "Staggered Magnetization^4",
+      "Staggered Magnetization Density^4", "Staggered Susceptibility",
+      "Generalized Staggered Magnetization^2", "Generalized Staggered Magnetization Density^2",
+      "Generalized Staggered Magnetization^4", "Generalized Staggered Magnetization Density^4",
+      "Generalized Staggered Susceptibility", "Stiffness"};
+  return (i >= 0 && i < LG_NUM_VALUES) ? names[i] : "";
+}
+
 void BinAcc::push(double x) {
   ++count;
   sum += x;

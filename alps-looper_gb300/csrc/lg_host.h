@@ -91,6 +91,11 @@ struct ChainAcc {
 // Observable values of one sweep record (path_integral.C:827-862).
 void record_values(const ChainSpec& s, const uint64_t* rec, double* v);
 
+// The LG_NUM_VALUES per-sweep values loop_worker::run pushes (LG_VAL_*), NaN where the chain's
+// estimator / lattice pushes no such entry; value_mask has bit i set for the pushed ones.
+void record_scalars(const ChainSpec& s, const uint64_t* rec, double* v);
+uint64_t value_mask(const ChainSpec& s);
+
 void checkpoint_encode(const ChainSpec& s, const std::vector<int32_t>& spins,
                        const std::vector<int32_t>& bonds, const std::vector<double>& times,
                        std::vector<uint8_t>& blob);

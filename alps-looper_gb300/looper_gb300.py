@@ -97,6 +97,10 @@ def lib():
             "lg_params_default": (None, [vp]),
             "lg_params_parse": (ctypes.c_int, [ctypes.c_char_p, vp]),
             "lg_obs_name": (ctypes.c_char_p, [ctypes.c_int]),
+            "lg_value_name": (ctypes.c_char_p, [ctypes.c_int]),
+            "lg_value_mask": (ctypes.c_int, [vp, vp]),
+            "lg_keep_values": (ctypes.c_int, [vp, ctypes.c_int]),
+            "lg_fetch_values": (ctypes.c_int, [vp, vp, i64, vp]),
             "lg_create": (ctypes.c_int, [vp, vp]),
             "lg_destroy": (ctypes.c_int, [vp]),
             "lg_run": (ctypes.c_int, [vp, i64]),
@@ -234,6 +238,13 @@ def parse_params(text: str) -> Params:
     lib().lg_params_default(ctypes.byref(p))
     check(lib().lg_params_parse(text.encode(), ctypes.byref(p)))
     return p
+
+
+NUM_VALUES = 37  # LG_NUM_VALUES
+
+
+def value_name(i):
+    return lib().lg_value_name(i).decode()
 
 
 def obs_names():
@@ -419,6 +430,25 @@ class LoopWorker:
         n = ctypes.c_int64()
         check(lib().lg_fetch_records(self._h, _p(out), cap, ctypes.byref(n)))
         return out[:n.value * RECORD_WORDS].reshape(n.value, RECORD_WORDS).copy()
+
+    def value_names(self):
+        """The ObservableSet keys this chain's sweeps push (lg_value_mask), in LG_VAL order."""
+        m = ctypes.c_uint64()
+        check(lib().lg_value_mask(self._h, ctypes.byref(m)))
+        return [value_name(i) for i in range(NUM_VALUES) if m.value >> i & 1]
+
+    def keep_values(self, on=True):
+        check(lib().lg_keep_values(self._h, 1 if on else 0))
+
+    def fetch_values(self, cap=1 << 16):
+        """Per-sweep values of the measurement sweeps since the last fetch: {name: array}."""
+        out = np.zeros(cap * NUM_VALUES, dtype=np.float64)
+        n = ctypes.c_int64()
+        check(lib().lg_fetch_values(self._h, _p(out), cap, ctypes.byref(n)))
+        rows = out[:n.value * NUM_VALUES].reshape(n.value, NUM_VALUES)
+        m = ctypes.c_uint64()
+        check(lib().lg_value_mask(self._h, ctypes.byref(m)))
+        return {value_name(i): rows[:, i].copy() for i in range(NUM_VALUES) if m.value >> i & 1}
 
 
 class Batch:

@@ -127,6 +127,59 @@ typedef struct lg_obs {
 /* Observable name (the reference's ObservableSet key) for an LG_OBS_* index. */
 const char* lg_obs_name(int index);
 
+/* ---- per-sweep measurement values -----------------------------------------------------------
+ * The scalar values loop_worker::run pushes into the ObservableSet after every sweep
+ * (path_integral.C:832-861): its own entries (:832-836), energy::commit (energy.h:76-84),
+ * susceptibility's improved or normal commit (susceptibility.h:200-254, :303-335) and
+ * stiffness's (stiffness.h:124-127, :160-165), registered by init_observables
+ * (path_integral.C:307-321, susceptibility.h:59-93).  A worker plug-in pushes each fetched row
+ * into its ObservableSet under lg_value_name(i), so that ALPS's own binning and evaluators
+ * (Specific Heat, Binder ratios) run unchanged.  Which entries a chain pushes depends on its
+ * estimator and lattice (lg_value_mask); the others are NaN in a fetched row. */
+enum {
+  LG_VAL_TEMPERATURE = 0,               /* "Temperature"                                      */
+  LG_VAL_INVERSE_TEMPERATURE,           /* "Inverse Temperature"                              */
+  LG_VAL_VOLUME,                        /* "Volume"                                           */
+  LG_VAL_NUMBER_OF_SITES,               /* "Number of Sites"                                  */
+  LG_VAL_NUMBER_OF_CLUSTERS,            /* "Number of Clusters"                               */
+  LG_VAL_ENERGY,                        /* "Energy"                                           */
+  LG_VAL_ENERGY_DENSITY,                /* "Energy Density"                                   */
+  LG_VAL_ENERGY2,                       /* "Energy^2"                                         */
+  LG_VAL_MAGNETIZATION,                 /* "Magnetization"                                    */
+  LG_VAL_MAGNETIZATION_DENSITY,         /* "Magnetization Density"                            */
+  LG_VAL_ABS_MAGNETIZATION,             /* "|Magnetization|"                                  */
+  LG_VAL_ABS_MAGNETIZATION_DENSITY,     /* "|Magnetization Density|"                          */
+  LG_VAL_MAGNETIZATION2,                /* "Magnetization^2"                                  */
+  LG_VAL_MAGNETIZATION_DENSITY2,        /* "Magnetization Density^2"                          */
+  LG_VAL_MAGNETIZATION4,                /* "Magnetization^4"                                  */
+  LG_VAL_MAGNETIZATION_DENSITY4,        /* "Magnetization Density^4"                          */
+  LG_VAL_SUSCEPTIBILITY,                /* "Susceptibility"                                   */
+  LG_VAL_GEN_MAGNETIZATION2,            /* "Generalized Magnetization^2"          (improved)  */
+  LG_VAL_GEN_MAGNETIZATION_DENSITY2,    /* "Generalized Magnetization Density^2"  (improved)  */
+  LG_VAL_GEN_MAGNETIZATION4,            /* "Generalized Magnetization^4"          (improved)  */
+  LG_VAL_GEN_MAGNETIZATION_DENSITY4,    /* "Generalized Magnetization Density^4"  (improved)  */
+  LG_VAL_GEN_SUSCEPTIBILITY,            /* "Generalized Susceptibility"           (improved)  */
+  LG_VAL_STAG_MAGNETIZATION,            /* "Staggered Magnetization"              (bipartite) */
+  LG_VAL_STAG_MAGNETIZATION_DENSITY,    /* "Staggered Magnetization Density"                  */
+  LG_VAL_ABS_STAG_MAGNETIZATION,        /* "|Staggered Magnetization|"                        */
+  LG_VAL_ABS_STAG_MAGNETIZATION_DENSITY,/* "|Staggered Magnetization Density|"                */
+  LG_VAL_STAG_MAGNETIZATION2,           /* "Staggered Magnetization^2"                        */
+  LG_VAL_STAG_MAGNETIZATION_DENSITY2,   /* "Staggered Magnetization Density^2"                */
+  LG_VAL_STAG_MAGNETIZATION4,           /* "Staggered Magnetization^4"                        */
+  LG_VAL_STAG_MAGNETIZATION_DENSITY4,   /* "Staggered Magnetization Density^4"                */
+  LG_VAL_STAG_SUSCEPTIBILITY,           /* "Staggered Susceptibility"                         */
+  LG_VAL_GEN_STAG_MAGNETIZATION2,       /* "Generalized Staggered Magnetization^2"            */
+  LG_VAL_GEN_STAG_MAGNETIZATION_DENSITY2,/* "... Density^2"           (bipartite, improved)   */
+  LG_VAL_GEN_STAG_MAGNETIZATION4,       /* "Generalized Staggered Magnetization^4"            */
+  LG_VAL_GEN_STAG_MAGNETIZATION_DENSITY4,/* "... Density^4"                                   */
+  LG_VAL_GEN_STAG_SUSCEPTIBILITY,       /* "Generalized Staggered Susceptibility"             */
+  LG_VAL_STIFFNESS,                     /* "Stiffness"                                        */
+  LG_NUM_VALUES
+};
+
+/* ObservableSet key of value i (LG_VAL_*). */
+const char* lg_value_name(int index);
+
 /* ---- one chain: the loop_worker interface ------------------------------------------------- */
 typedef struct lg_chain lg_chain;
 
@@ -151,6 +204,18 @@ int lg_save(lg_chain* c, void* buf, size_t* size);
 int lg_load(lg_chain* c, const void* buf, size_t size);
 /* Exchange Monte Carlo hooks (path_integral.C:97-109). */
 int lg_set_beta(lg_chain* c, double beta);
+
+/* Per-sweep values (LG_VAL_*): the ObservableSet pushes of loop_worker::run, one row of
+ * LG_NUM_VALUES doubles per measurement sweep (sweeps after THERMALIZATION, the ones
+ * lg_observables accumulates).  lg_keep_values(c, 1) starts keeping the rows of the sweeps that
+ * follow (off by default); lg_fetch_values moves up to cap rows, oldest first, into out
+ * (cap * LG_NUM_VALUES doubles) and stores the number of rows in *n.  *mask receives bit i set
+ * for every value the chain pushes: the Generalized entries only with the improved estimator
+ * (no field, path_integral.C:217), the Staggered ones only on a bipartite lattice
+ * (susceptibility.h:75-93).  Works for members of a batch too (lg_batch_chain). */
+int lg_value_mask(const lg_chain* c, uint64_t* mask);
+int lg_keep_values(lg_chain* c, int on);
+int lg_fetch_values(lg_chain* c, double* out, int64_t cap, int64_t* n);
 
 /* ---- spin correlations and structure factor (correlation.h:38-300) ------------------------
  * The reference's normal estimator of looper::correlation, measured from the tau = 0 spins at

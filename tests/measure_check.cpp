@@ -5,7 +5,9 @@
 // DISABLE_IMPROVED_ESTIMATOR, is checked without a GPU.
 //
 //   measure_check dim L beta jxy jz h spin2 disable_improved therm sweeps seed
-// prints one line per observable: "<name>\t<mean>\t<error>".
+// prints one line per observable: "<name>\t<mean>\t<error>", then one line per value a
+// worker plug-in pushes per sweep (record_scalars, what lg_fetch_values returns):
+// "V\t<name>\t<plain mean over the measurement sweeps>".
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -75,10 +77,18 @@ int main(int argc, char** argv) {
   orc_destroy(h);
 
   ChainAcc acc;
-  for (int i = therm; i < n; ++i) acc.push(s, rec.data() + (size_t)i * w);
+  std::vector<double> vsum(LG_NUM_VALUES, 0.0), row(LG_NUM_VALUES);
+  for (int i = therm; i < n; ++i) {
+    acc.push(s, rec.data() + (size_t)i * w);
+    record_scalars(s, rec.data() + (size_t)i * w, row.data());
+    for (int k = 0; k < LG_NUM_VALUES; ++k) vsum[k] += row[k];
+  }
   lg_obs o;
   acc.report(s, &o);
   for (int k = 0; k < LG_NUM_OBS; ++k)
     std::printf("%s\t%.17g\t%.17g\n", lg_obs_name(k), o.mean[k], o.error[k]);
+  const uint64_t mask = value_mask(s);
+  for (int k = 0; k < LG_NUM_VALUES; ++k)
+    if (mask >> k & 1) std::printf("V\t%s\t%.17g\n", lg_value_name(k), vsum[k] / (double)(n - therm));
   return 0;
 }

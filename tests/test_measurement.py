@@ -44,8 +44,11 @@ def _observables(exe, dim, L, beta, jxy, jz, h, spin2, disable, therm, sweeps, s
     assert r.returncode == 0, r.stderr
     out = {}
     for ln in r.stdout.splitlines():
-        name, m, e = ln.split("\t")
-        out[name] = (float(m), float(e))
+        f = ln.split("\t")
+        if f[0] == "V":
+            out["V:" + f[1]] = float(f[2])
+        else:
+            out[f[0]] = (float(f[1]), float(f[2]))
     return out
 
 
@@ -71,3 +74,39 @@ def test_host_measurement_of_oracle_records_vs_ed(exe, name):
         m, e = got[k]
         assert e > 0, k
         assert abs(m - ref[k]) <= 3.5 * e + 1e-12, (name, k, m, e, ref[k])
+
+
+# Values a worker plug-in pushes per sweep (lg_fetch_values) whose plain mean is, by the
+# reference's own definitions, the mean lg_observables reports under the same name.
+SAME = ["Energy", "Energy Density", "Energy^2", "Magnetization", "|Magnetization|",
+        "Magnetization^2", "Magnetization^4", "Susceptibility", "Staggered Magnetization^2",
+        "Staggered Magnetization^4", "Staggered Susceptibility", "Generalized Magnetization^2",
+        "Generalized Susceptibility", "Number of Clusters", "Stiffness"]
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_per_sweep_values_reproduce_observables(exe, name):
+    """The per-sweep values a parapack plug-in pushes into its ObservableSet average to the
+    means lg_observables reports (path_integral.C:827-862 pushes; the engine's binned view)."""
+    dim, L, beta, jxy, jz, h, spin2, disable = CASES[name]
+    got = _observables(exe, dim, L, beta, jxy, jz, h, spin2, disable, 50, 3000, 7 + len(name))
+    improved = not disable and h == 0.0
+    checked = 0
+    for k in SAME:
+        if ("V:" + k) not in got:
+            assert k.startswith("Generalized") and not improved, k
+            continue
+        m = got[k][0]
+        assert got["V:" + k] == pytest.approx(m, rel=1e-12, abs=1e-300), (name, k)
+        checked += 1
+    assert checked >= 12
+    # constant entries and the reference's fixed zeros of the improved estimator
+    assert got["V:Inverse Temperature"] == beta
+    assert got["V:Temperature"] == pytest.approx(1.0 / beta, rel=1e-15)
+    assert got["V:Volume"] == L ** dim and got["V:Number of Sites"] == L ** dim
+    if improved:
+        assert got["V:Magnetization"] == 0.0 and got["V:Staggered Magnetization"] == 0.0
+        assert "V:Generalized Staggered Susceptibility" in got
+    else:
+        assert "V:Generalized Magnetization^2" not in got
+    assert got["V:Energy Density"] == pytest.approx(got["V:Energy"] / L ** dim, rel=1e-12)
