@@ -16,7 +16,8 @@ namespace lg {
 
 // Stream tags (third Philox counter word).
 enum : uint32_t {
-  TAG_PROPOSAL = 1, TAG_OFFDIAG = 2, TAG_FLIP = 3, TAG_SPIN = 4, TAG_EXCHANGE = 5, TAG_PERM = 6
+  TAG_PROPOSAL = 1, TAG_OFFDIAG = 2, TAG_FLIP = 3, TAG_SPIN = 4, TAG_EXCHANGE = 5, TAG_PERM = 6,
+  TAG_TAIL = 7
 };
 
 // Philox4x32-10 (Salmon et al., SC'11): 10 rounds of two 32x32->64 multiplies with the paper's
@@ -67,6 +68,15 @@ __device__ __forceinline__ float log_open(float u) {
   float ef = (float)e;
   float t = fmaf(ef, 1.42860677e-06f, lnm);
   return fmaf(ef, 0.693145752f, t);
+}
+
+// The uniform of an exponential gap, -ln U of which is the gap in mean gaps.  U = (2x+1) 2^-24
+// from the top 23 bits x of w; in the lowest bin (x = 0: U < 2^-23, probability 2^-23) U is
+// refined by the top 23 bits t of a second word, U = (2t+1) 2^-47 (exact: a power-of-two scale).
+// The largest gap is so -ln 2^-47 = 32.6 mean gaps, and a draw reaches the end of the table with
+// probability 2^-47 (7e-15).  `tail` is read only in the lowest bin.
+__device__ __forceinline__ float gap_uniform(uint32_t w, uint32_t tail) {
+  return (w >> 9) ? uniform_open(w) : __fmul_rn(uniform_open(tail), 1.1920928955078125e-7f);
 }
 
 // exp(x), |x| <= 80 (clamped): x = k ln2 + r, degree-7 Taylor polynomial, times 2^k.

@@ -1,24 +1,27 @@
 // lg_uf_label_static: the cluster labelling of lg_uf_label without any allocation.
 //
 // Some callers of this library cannot call cudaMalloc.
-// - Code that runs while a CUDA stream capture is open: allocating would break the capture.
 // - A plug-in whose host framework owns every device allocation through its own pool, where a
 //   library allocation outside that pool is forbidden or would defeat its memory budgeting.
-// - Code on a latency-critical path where a cudaMalloc/cudaFree pair (an implicit device
-//   synchronisation) is not acceptable.
+// - Code on a latency-critical path that cannot take the device-wide synchronisation of
+//   cudaFree.  (This call synchronises only its own stream, once, to return the counts.)
 //
 // For them this entry point takes device pointers for its inputs and outputs.  It keeps every
 // intermediate array (bond lists, segments, the union-find forest, fragment ids) in one
 // file-scope static device array of LG_STATIC_SCRATCH_BYTES, which every GPU that loads this
 // library holds until the process exits.  The work is the one lg_uf_label does with allocated
 // buffers: the same segment merge and lock-free union-find kernels, with the reference-numbered
-// labels assigned on the device.
+// labels assigned on the device.  Vertices are placed into their bonds' lists by a stable
+// two-pass radix sort on the bond index (linear work, so a lattice of two sites with 2^18
+// vertices is as cheap as any other input of that size).
 //
 // Limits: at most LG_STATIC_MAX_SITES sites and LG_STATIC_MAX_OPS vertices per call; larger
 // inputs are rejected with LG_EBUDGET before any device work.
 //
 // Set-up: the first call on each device, with that device current, looks up the array's device
-// address with cudaGetSymbolAddress.  Make that first call before opening any stream capture.
+// address with cudaGetSymbolAddress and keeps it for the life of the process.  Make that first
+// call before opening any stream capture.  cudaDeviceReset unloads the array, so the kept address
+// is stale after a reset: do not call this entry point on a device that was reset.
 //
 // Sharing: every call uses the same array, and the array keeps what the last call left.  The
 // call clears everything that must start at zero.  Calls whose device work overlaps (for
@@ -113,31 +116,75 @@ __global__ void ks_count(Arena A, const int32_t* bonds, const int32_t* graphs, i
   }
 }
 
-// Place vertices into their bond's slice (in arbitrary order, keyed by input index).
-__global__ void ks_scatter(Arena A, const int32_t* bonds, int nops, int* fill) {
-  if (A.ctl->err) return;
-  LG_GRID_STRIDE(i, nops) {
-    const int b = bonds[i];
-    const int v = A.bond_ptr[b] + atomicAdd(fill + b, 1);
-    A.vtime[v] = (uint64_t)i;
+// Stable LSD radix sort of the vertices by bond index (two 8-bit digits: bonds < 2^16), so that
+// each bond's vertices come out in input (time) order.  Tiles of RS_TILE entries; the digit
+// counts of every tile are stored digit-major, hist[d * ntiles + t], so that their exclusive
+// scan gives each (digit, tile) its first output position in stable order.
+constexpr int RS_THREADS = 256;
+constexpr int RS_PER = 8;
+constexpr int RS_TILE = RS_THREADS * RS_PER;
+
+__global__ void __launch_bounds__(RS_THREADS) ks_radix_hist(const int32_t* key, int n, int shift,
+                                                            int* hist, int ntiles, const Ctl* ctl) {
+  if (ctl->err) return;
+  __shared__ int h[256];
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    for (int i = threadIdx.x; i < 256; i += RS_THREADS) h[i] = 0;
+    __syncthreads();
+    for (int j = 0; j < RS_PER; ++j) {
+      const int e = t * RS_TILE + j * RS_THREADS + threadIdx.x;
+      if (e < n) atomicAdd(&h[(key[e] >> shift) & 255], 1);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += RS_THREADS) hist[i * ntiles + t] = h[i];
+    __syncthreads();
   }
 }
 
-// Sort each bond slice by input index (the given time order); keys become i + 1.
-__global__ void ks_sort_bonds(Arena A, const int32_t* graphs, int* v_of_input) {
-  if (A.ctl->err) return;
-  LG_GRID_STRIDE(b, A.NB) {
-    const int lo = A.bond_ptr[b], hi = A.bond_ptr[b + 1];
-    for (int i = lo + 1; i < hi; ++i)
-      for (int j = i; j > lo && A.vtime[j - 1] > A.vtime[j]; --j) {
-        const uint64_t t = A.vtime[j]; A.vtime[j] = A.vtime[j - 1]; A.vtime[j - 1] = t;
+// Scatter of one digit pass.  A tile's entries are placed in order: chunk by chunk, and within a
+// chunk warp by warp, each lane after the lanes of its warp with the same digit (match_any) and
+// after everything placed before with that digit (base[d]).  val == nullptr: the value of entry e
+// is e (the input index).
+__global__ void __launch_bounds__(RS_THREADS) ks_radix_scatter(const int32_t* key, const int* val,
+                                                               int n, int shift, const int* hoff,
+                                                               int ntiles, int32_t* kout, int* vout,
+                                                               const Ctl* ctl) {
+  if (ctl->err) return;
+  __shared__ int base[256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    for (int i = threadIdx.x; i < 256; i += RS_THREADS) base[i] = hoff[i * ntiles + t];
+    __syncthreads();
+    for (int c = 0; c < RS_PER; ++c) {
+      const int e = t * RS_TILE + c * RS_THREADS + threadIdx.x;
+      const bool ok = e < n;
+      const int k = ok ? key[e] : 0;
+      const int d = ok ? (k >> shift) & 255 : 256 + lane;  // lanes past the end: no group
+      const unsigned grp = __match_any_sync(0xFFFFFFFFu, d);
+      const int r = __popc(grp & ((1u << lane) - 1u));
+      const bool last = (grp >> lane) == 1u;                // highest lane of its group
+      for (int ww = 0; ww < RS_THREADS / 32; ++ww) {
+        if (w == ww) {
+          const int pos = ok ? base[d] + r : 0;
+          __syncwarp();
+          if (ok && last) base[d] += __popc(grp);
+          if (ok) { kout[pos] = k; vout[pos] = val ? val[e] : e; }
+        }
+        __syncthreads();
       }
-    for (int v = lo; v < hi; ++v) {
-      const int i = (int)A.vtime[v];
-      v_of_input[i] = v;
-      A.vcode[v] = (uint8_t)(graphs[i] << 1);
-      A.vtime[v] = (uint64_t)i + 1;
     }
+  }
+}
+
+// Vertex slots from the sorted order: position p holds input idx[p]; its key is idx + 1 (the
+// given time order) and its code the input graph.
+__global__ void ks_place(Arena A, const int* idx, const int32_t* graphs, int nops, int* v_of_input) {
+  if (A.ctl->err) return;
+  LG_GRID_STRIDE(p, nops) {
+    const int i = idx[p];
+    v_of_input[i] = p;
+    A.vtime[p] = (uint64_t)i + 1;
+    A.vcode[p] = (uint8_t)(graphs[i] << 1);
   }
 }
 
@@ -255,7 +302,6 @@ extern "C" int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_
     A.parent = cv.take<int>(ns);
     Ctl* ctl = cv.take<Ctl>(1);
     A.ctl = ctl;
-    int* fill = cv.take<int>(nb);
     int* g0flag = cv.take<int>(nv + 1);
     int* g0ord = cv.take<int>(nv + 1);
     int* g0_input = cv.take<int>(nv + 1);
@@ -265,7 +311,15 @@ extern "C" int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_
     int* flag = cv.take<int>(nf);
     int* id = cv.take<int>(nf + 1);
     int* totals = cv.take<int>(4);
-    const int maxn = std::max(std::max(nb, ns), nf) + 1;
+    const int ntiles = nv > 0 ? (nv + RS_TILE - 1) / RS_TILE : 1;
+    int* hist = cv.take<int>((size_t)256 * ntiles);
+    int* hoff = cv.take<int>((size_t)256 * ntiles + 1);
+    // the radix sort's key / value buffers reuse arrays that are filled only after it
+    int32_t* keyA = froot;
+    int* valA = flag;
+    int32_t* keyB = id;
+    int* valB = g0_input;
+    const int maxn = std::max(std::max(std::max(nb, ns), nf), 256 * ntiles) + 1;
     int* partial = cv.take<int>(maxn / SCAN_TILE + 2);
     if (cv.used > LG_STATIC_SCRATCH_BYTES)
       return lg_fail(LG_EBUDGET, "lg_uf_label_static: %zu bytes of scratch needed, %zu available",
@@ -276,15 +330,23 @@ extern "C" int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_
     LG_CUDA(cudaMemcpyAsync(ch, &hch, sizeof(DChain), cudaMemcpyHostToDevice, st));
     LG_CUDA(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
     LG_CUDA(cudaMemsetAsync(A.bond_cnt, 0, nb * sizeof(int), st));
-    LG_CUDA(cudaMemsetAsync(fill, 0, nb * sizeof(int), st));
     LG_CUDA(cudaMemsetAsync(minfrag, 0xFF, (size_t)ns * sizeof(unsigned), st));
     LG_CUDA(cudaMemsetAsync(totals, 0, 4 * sizeof(int), st));
 
     ks_lattice<<<grid_of(n, 128), 128, 0, st>>>(A, dim, L);
     if (nv > 0) ks_count<<<grid_of(nv, 256), 256, 0, st>>>(A, d_bonds, d_graphs, nv, g0flag);
     static_scan(A.bond_cnt, A.bond_ptr, nb, &ctl->nv_total, partial, ctl, st);
-    if (nv > 0) ks_scatter<<<grid_of(nv, 256), 256, 0, st>>>(A, d_bonds, nv, fill);
-    ks_sort_bonds<<<grid_of(nb, 128), 128, 0, st>>>(A, d_graphs, v_of_input);
+    if (nv > 0) {
+      const int g = std::min(ntiles, 4096);
+      ks_radix_hist<<<g, RS_THREADS, 0, st>>>(d_bonds, nv, 0, hist, ntiles, ctl);
+      static_scan(hist, hoff, 256 * ntiles, totals + 2, partial, ctl, st);
+      ks_radix_scatter<<<g, RS_THREADS, 0, st>>>(d_bonds, nullptr, nv, 0, hoff, ntiles, keyA, valA, ctl);
+      ks_radix_hist<<<g, RS_THREADS, 0, st>>>(keyA, nv, 8, hist, ntiles, ctl);
+      static_scan(hist, hoff, 256 * ntiles, totals + 3, partial, ctl, st);
+      ks_radix_scatter<<<g, RS_THREADS, 0, st>>>(keyA, valA, nv, 8, hoff, ntiles, keyB, valB, ctl);
+      ks_place<<<grid_of(nv, 256), 256, 0, st>>>(A, valB, d_graphs, nv, v_of_input);
+      g_launches += 5;
+    }
     k_site_count<<<grid_of(n, 256), 256, 0, st>>>(A);
     static_scan(A.site_cnt, A.sbase, n, &ctl->ns_total, partial, ctl, st);
     launch_merge(2 * dim, grid_of((long long)n * 32, MERGE_WARPS * 32),
@@ -292,7 +354,7 @@ extern "C" int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_
     if (nv > 0) k_union<><<<grid_of(ns, UN_WARPS * UN_CHUNK), UN_WARPS * 32, 0, st>>>(A);
     ks_compress<<<grid_of(ns, 256), 256, 0, st>>>(A);
     static_scan(g0flag, g0ord, nv, totals, partial, ctl, st);
-    g_launches += nv > 0 ? 8 : 5;  // the scans count their own
+    g_launches += nv > 0 ? 6 : 4;  // the scans and the sort count their own
     LG_CUDA(cudaGetLastError());
     int ng0 = 0, err = 0;
     LG_CUDA(cudaMemcpyAsync(&ng0, totals, sizeof(int), cudaMemcpyDeviceToHost, st));

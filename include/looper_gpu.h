@@ -281,17 +281,19 @@ int lg_validate_sweeps(lg_chain* c, int64_t n);
 int lg_uf_label(int lattice, int L, int64_t nops, const int32_t* bonds, const int32_t* graphs,
                 int32_t* labels, int64_t cap, int64_t* nfrag, int64_t* nc);
 
-/* Allocation-free variant of lg_uf_label, for callers that cannot call cudaMalloc: code running
- * inside an open stream capture, a plug-in whose host framework owns all device memory, or a
- * latency-critical path that cannot afford the implicit synchronisation of cudaMalloc/cudaFree.
+/* Allocation-free variant of lg_uf_label, for callers that cannot call cudaMalloc: a plug-in
+ * whose host framework owns every device allocation through its own pool, or a latency-critical
+ * path that cannot take the device-wide synchronisation of cudaFree.
  * This entry point has no counterpart in the reference.
  * d_bonds, d_graphs (nops entries) and d_labels (N + number of graph-0 vertices entries) are
  * device pointers owned by the caller; stream is a cudaStream_t (NULL: the default stream).
  * All intermediate data live in a fixed 32 MiB static device array that each GPU loading this
  * library holds until the process exits.  Limits: 16384 sites and 262144 vertices; larger inputs
  * return LG_EBUDGET.  The first call on a device looks up that array's address (make it before
- * any stream capture).  Calls share the array: calls whose device work overlaps race and must
- * be serialised.  The call synchronises its stream to return *nfrag and *nc. */
+ * any stream capture); the address is kept for the life of the process, so do not call this
+ * entry point on a device after cudaDeviceReset.  Calls share the array: calls whose device work
+ * overlaps race and must be serialised.  The call synchronises its stream once, to return
+ * *nfrag and *nc. */
 int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_t* d_bonds,
                        const int32_t* d_graphs, int32_t* d_labels, int64_t* nfrag, int64_t* nc,
                        void* stream);

@@ -71,7 +71,7 @@ static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
 }
 
 // Stream tags (third counter word).
-enum { TAG_PROPOSAL = 1, TAG_OFFDIAG = 2, TAG_FLIP = 3, TAG_SPIN = 4, TAG_PERM = 6 };
+enum { TAG_PROPOSAL = 1, TAG_OFFDIAG = 2, TAG_FLIP = 3, TAG_SPIN = 4, TAG_PERM = 6, TAG_TAIL = 7 };
 
 static void rng4(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t out[4]) {
   uint32_t c[4] = {c0, c1, c2, c3};
@@ -87,6 +87,13 @@ static inline uint64_t d_bits(double d) { uint64_t b; std::memcpy(&b, &d, 8); re
 // Open-interval uniform float: (2x+1) * 2^-24 with x the top 23 bits of w.  Exact.
 static inline float uniform_open(uint32_t w) {
   return (float)(((w >> 9) << 1) | 1u) * 5.9604644775390625e-8f;
+}
+
+// The uniform of an exponential gap (-ln U mean gaps): (2x+1) 2^-24 from the top 23 bits x of w,
+// refined in the lowest bin (x = 0, U < 2^-23) by the top 23 bits t of a second word `tail`:
+// U = (2t+1) 2^-47, so that the gap's tail reaches -ln 2^-47 = 32.6 mean gaps.
+static inline float gap_uniform(uint32_t w, uint32_t tail) {
+  return (w >> 9) ? uniform_open(w) : uniform_open(tail) * 1.1920928955078125e-7f;
 }
 
 // Natural log for u in (0,1): u = m 2^e with m in [sqrt(1/2), sqrt(2)), s = (m-1)/(m+1),
@@ -405,7 +412,13 @@ struct chain_t {
         for (int k = 0;; ++k) {
           if ((k & 1) == 0) rng4(seed, sweep, (uint32_t)b, TAG_PROPOSAL, (uint32_t)(k >> 1), w);
           uint32_t wu = w[(k & 1) * 2], wg = w[(k & 1) * 2 + 1];
-          float gap = -log_spec(uniform_open(wu)) * inv_rate;
+          uint32_t tail = 0;
+          if ((wu >> 9) == 0) {
+            uint32_t t4[4];
+            rng4(seed, sweep, (uint32_t)b, TAG_TAIL, (uint32_t)k, t4);
+            tail = t4[0];
+          }
+          float gap = -log_spec(gap_uniform(wu, tail)) * inv_rate;
           bool ge1;
           uint64_t dither = ((uint64_t)(wu & 0x1FFu) << 16) | (wg & 0xFFFFu);
           uint64_t q = float_to_fix52(gap, dither, &ge1);
@@ -898,6 +911,7 @@ void orc_philox_raw(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
   for (int i = 0; i < 4; ++i) out[i] = c[i];
 }
 float orc_log_spec(float u) { return orc::log_spec(u); }
+float orc_gap_uniform(uint32_t w, uint32_t tail) { return orc::gap_uniform(w, tail); }
 float orc_exp_spec(float x) { return orc::exp_spec(x); }
 double orc_weights(double jxy, double jz, double fs, double* v) {
   orc::bond_weight w = orc::make_weight(jxy, jz, fs);

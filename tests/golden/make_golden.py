@@ -10,7 +10,8 @@ Sources:
     labelled by the reference's own looper/union_find.h, compiled in place by oracle/Makefile
     (oracle/_ref/uf_deterministic, oracle/_ref/uf_weighted).
 
-Usage:  make -C oracle all ref && python tests/golden/make_golden.py [/root/reference]
+Usage:  make -C oracle all ref REFERENCE=<ref> && python tests/golden/make_golden.py <ref>
+        (<ref>: a checkout of the reference; required)
 """
 from __future__ import annotations
 
@@ -196,7 +197,9 @@ def ed_chain16():
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference checkout>")
+    ref = sys.argv[1]
     data = {
         "standalone_loop_op.json": standalone(ref),
         "union_find_op.json": union_find(ref),

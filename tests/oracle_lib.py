@@ -36,6 +36,8 @@ def lib():
             getattr(L, f).argtypes = None
         L.orc_log_spec.restype = ctypes.c_float
         L.orc_log_spec.argtypes = [ctypes.c_float]
+        L.orc_gap_uniform.restype = ctypes.c_float
+        L.orc_gap_uniform.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
         L.orc_exp_spec.restype = ctypes.c_float
         L.orc_exp_spec.argtypes = [ctypes.c_float]
         L.orc_weights.restype = ctypes.c_double

@@ -40,6 +40,32 @@ def test_float_log_exp_accuracy():
         assert abs(L.orc_exp_spec(float(x)) - ref) <= 4e-7 * ref
 
 
+def test_exponential_gap_tail():
+    """The exponential gaps (path_integral.C:71,412-420 draws them as double exponentials) come
+    from -ln U with U a float uniform.  The lowest of its 2^23 bins (U < 2^-23) is refined by 23
+    more random bits, so the largest gap is 32.6 mean gaps instead of -ln 2^-24 = 16.6: a draw
+    reaches the end of the table with probability 2^-47.  The refinement keeps the bin's mean,
+    and -ln U stays accurate down there."""
+    import math
+    L = orc.lib()
+    u_last = L.orc_gap_uniform(0, 0)                       # x = 0, t = 0: U = 2^-47
+    assert u_last == 2.0 ** -47
+    g_max = -L.orc_log_spec(u_last)
+    assert abs(g_max - 47 * math.log(2)) <= 1e-5 * g_max and g_max > 32.5
+    # outside the lowest bin nothing changes: U = (2x+1) 2^-24
+    for w in (1 << 9, 12345 << 9, 0xFFFFFFFF, 0x80000000):
+        assert L.orc_gap_uniform(w, 0xDEADBEEF) == ((w >> 9) * 2 + 1) * 2.0 ** -24
+    # inside it, U = (2t+1) 2^-47 for the top 23 bits t of the tail word: exact, and the bin's
+    # mean over t is its old centre 2^-24
+    ts = list(range(0, 1 << 23, 4099)) + [(1 << 23) - 1]
+    for t in ts:
+        u = L.orc_gap_uniform(0x1FF, t << 9)
+        assert u == (2 * t + 1) * 2.0 ** -47
+        assert abs(-L.orc_log_spec(u) + math.log(u)) <= 3e-7 * -math.log(u)
+    n = 1 << 23                                            # sum_t (2t+1) = n^2
+    assert n * n * 2.0 ** -47 / n == 2.0 ** -24
+
+
 def test_standalone_matches_golden(golden):
     g = golden("standalone_loop_op.json")
     out, _ = orc.standalone(g["L"], g["T"], g["sweeps"], g["therm"])
