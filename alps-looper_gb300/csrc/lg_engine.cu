@@ -27,6 +27,7 @@
 #include "../../include/looper_gpu.h"
 #include "lg_kernels.cuh"
 #include "lg_host.h"
+#include "lg_resident.cuh"
 
 using namespace lg;
 
@@ -37,6 +38,22 @@ static const char* kStageNames[kNumStages] = {
     "k_site_end+k_end"};
 
 static std::atomic<uint64_t> g_launches{0};
+// bytes moved between host and device by this library (lg_copy_bytes, a measurement seam)
+static std::atomic<uint64_t> g_h2d_bytes{0}, g_d2h_bytes{0};
+
+static void count_copy(size_t n, cudaMemcpyKind k) {
+  if (k == cudaMemcpyHostToDevice) g_h2d_bytes += n;
+  else if (k == cudaMemcpyDeviceToHost) g_d2h_bytes += n;
+}
+static cudaError_t lg_copy(void* dst, const void* src, size_t n, cudaMemcpyKind k) {
+  count_copy(n, k);
+  return cudaMemcpy(dst, src, n, k);
+}
+static cudaError_t lg_copy_async(void* dst, const void* src, size_t n, cudaMemcpyKind k,
+                                 cudaStream_t st) {
+  count_copy(n, k);
+  return cudaMemcpyAsync(dst, src, n, k, st);
+}
 static thread_local std::string g_err;
 
 int lg_fail(int code, const char* fmt, ...) {
@@ -61,6 +78,8 @@ struct DBuf {
   T* p = nullptr;
   size_t n = 0;
   ~DBuf() { if (p) cudaFree(p); }
+  void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+  void swap(DBuf& o) { std::swap(p, o.p); std::swap(n, o.n); }
   int alloc(size_t count) {
     if (p) { cudaFree(p); p = nullptr; }
     n = count;
@@ -79,13 +98,22 @@ struct DBuf {
 //   acc_tile  segments per block in k_accumulate (512, 1024, 2048)
 //   cl_tile   segments per block in k_cluster (2048, 4096, 8192)
 //   un_warps  warps per block in k_union (4, 8, 16)
+//   resident  run the arena's sweeps as chain-resident launches (k_resident: one CTA per chain,
+//             a chunk of sweeps per launch) where every chain fits in shared memory; the fields
+//             above then wait for the arena to return to the grid path
 struct Shape {
   double insert_k = 32.0;
   double narrow_k = 32.0;
   int acc_tile = 1024;
   int cl_tile = 4096;
   int un_warps = 8;
+  int resident = 0;
 };
+
+// Shared memory a chain-resident CTA may use by default: at most this much keeps two CTAs per SM.
+constexpr size_t RES_SMEM_DEFAULT = 100 * 1024;
+// The most any CTA can have (sm_103a: 227 KB of dynamic shared memory per block).
+constexpr size_t RES_SMEM_MAX = 227 * 1024;
 
 // ----------------------------------------------------------------------------------------------
 struct Engine {
@@ -122,6 +150,7 @@ struct Engine {
   // spin correlations: k_corr work tiles and the per-chunk exact sums (arena site indexed)
   int n_corr_tiles = 0, corr_smem = 0;
   bool any_spin_s = false;   // some chain has S > 1/2: k_boundary closes its sites
+  bool all_nofield = false;  // no chain has a field: flips are coins (the site pass draws them)
   // structural checks between stages (lg_validate_sweeps): the failure counter and first code;
   // never part of a captured graph
   int* val_bad = nullptr;
@@ -165,6 +194,16 @@ struct Engine {
   std::vector<uint8_t> keep_vals;
   std::vector<std::vector<double>> vals;
   std::vector<uint64_t> hrec;
+  // ---- chain-resident sweeps (k_resident): the persistent state is double-buffered; d_spin0,
+  // d_off_base, d_off_cnt, d_stime, d_sdir hold the current state (lists at off_base in the list
+  // arrays, res_lcap entries per chain) and the rb_* set receives the next one
+  bool resident = false;
+  bool allow_resident = false;
+  int res_vcap = 0, res_nmax = 0, res_nbmax = 0, res_lcap = 0, res_scap = 0, res_grid = 0;
+  size_t res_smem = 0;
+  DBuf<uint8_t> rb_spin0, rb_sdir;
+  DBuf<int> rb_off_base, rb_off_cnt;
+  DBuf<uint64_t> rb_stime;
 
   ~Engine() {
     if (gexec) cudaGraphExecDestroy(gexec);
@@ -202,8 +241,9 @@ struct Engine {
   }
 
   // ---- construction ----
-  int build(const std::vector<ChainSpec>& specs) {
+  int build(const std::vector<ChainSpec>& specs, bool may_reside = false) {
     spec = specs;
+    allow_resident = may_reside;
     C = (int)spec.size();
     acc.assign(C, ChainAcc());
     keep_vals.assign(C, 0);
@@ -294,32 +334,39 @@ struct Engine {
     int maxparts = std::max((NB + SCAN_TILE - 1) / SCAN_TILE, (N + SCAN_TILE - 1) / SCAN_TILE);
     maxparts = std::max(maxparts, (N + SITE_SCAN_BLOCK - 1) / SITE_SCAN_BLOCK);  // k_site_blocks
     if ((rc = d_partial.alloc(maxparts + 1))) return rc;
-    LG_CUDA(cudaMemcpy(d_ch.p, hch.data(), C * sizeof(DChain), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_bond_s0.p, h_bond_s0.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_bond_s1.p, h_bond_s1.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_bond_chain.p, h_bond_chain.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_bond_dir0.p, h_bond_dir0.data(), NB, cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_inc_off.p, h_inc_off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_inc.p, h_inc.data(), h_inc.size() * sizeof(int), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_inc_side.p, h_inc_side.data(), h_inc_side.size(), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_inc_nbr.p, h_inc_nbr.data(), h_inc_nbr.size() * sizeof(int), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_inc_dir.p, h_inc_dir.data(), h_inc_dir.size(), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_gauge.p, h_gauge.data(), N, cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_site_chain.p, h_site_chain.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_ch.p, hch.data(), C * sizeof(DChain), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_bond_s0.p, h_bond_s0.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_bond_s1.p, h_bond_s1.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_bond_chain.p, h_bond_chain.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_bond_dir0.p, h_bond_dir0.data(), NB, cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_inc_off.p, h_inc_off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_inc.p, h_inc.data(), h_inc.size() * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_inc_side.p, h_inc_side.data(), h_inc_side.size(), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_inc_nbr.p, h_inc_nbr.data(), h_inc_nbr.size() * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_inc_dir.p, h_inc_dir.data(), h_inc_dir.size(), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_gauge.p, h_gauge.data(), N, cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_site_chain.p, h_site_chain.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     h_active.assign(C, 1);
-    LG_CUDA(cudaMemcpy(d_active.p, h_active.data(), C, cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_active.p, h_active.data(), C, cudaMemcpyHostToDevice));
     std::vector<uint32_t> sw(C);
     for (int c = 0; c < C; ++c) sw[c] = (uint32_t)spec[c].mcs;
-    LG_CUDA(cudaMemcpy(d_sweep.p, sw.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_sweep.p, sw.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice));
     // vertex regions and per-sweep buffers from the expected operator count
     LG_CUDA(cudaMemset(d_ctl.p, 0, sizeof(Ctl)));
     if ((rc = build_corr())) return rc;
     any_spin_s = false;
-    for (int c = 0; c < C; ++c) any_spin_s |= spec[c].spin2 > 1;
-    if ((rc = build_regions())) return rc;
-    if ((rc = alloc_dynamic(region_total, false))) return rc;
-    set_merge_cap();
-    if ((rc = set_shape(default_shape()))) return rc;
+    all_nofield = true;
+    for (int c = 0; c < C; ++c) {
+      any_spin_s |= spec[c].spin2 > 1;
+      all_nofield &= hch[c].field == 0;
+    }
+    if (allow_resident && res_fits(res_vcap_for(1.0), RES_SMEM_DEFAULT)) {
+      if ((rc = setup_resident(res_vcap_for(1.0)))) return rc;
+      shape = default_shape();
+      shape.resident = 1;
+    } else {
+      if ((rc = setup_grid())) return rc;
+    }
     // initial spins (one launch per distinct init mode)
     Arena A = arena();
     int random = spec.empty() ? 0 : spec[0].init_spins;
@@ -331,9 +378,179 @@ struct Engine {
         std::vector<uint8_t> sp(spec[c].N);
         for (int i = 0; i < spec[c].N; ++i)
           sp[i] = spec[c].init_spins ? (uint8_t)(philox(spec[c].dchain.seed, 0xFFFFFFFFu, (uint32_t)i, TAG_SPIN, 0).x & 1u) : 0;
-        LG_CUDA(cudaMemcpyAsync(d_spin0.p + hch[c].site_off, sp.data(), sp.size(), cudaMemcpyHostToDevice, st));
+        LG_CUDA(lg_copy_async(d_spin0.p + hch[c].site_off, sp.data(), sp.size(), cudaMemcpyHostToDevice, st));
       }
     LG_CUDA(cudaStreamSynchronize(st));
+    return LG_OK;
+  }
+
+  // ---- grid path buffers: vertex regions, per-sweep arrays, merge staging, launch shape
+  int setup_grid() {
+    int rc;
+    if ((rc = build_regions())) return rc;
+    if ((rc = alloc_dynamic(region_total, false))) return rc;
+    set_merge_cap();
+    return set_shape(default_shape());
+  }
+
+  // ---- chain-resident sweeps ----
+  // Vertex capacity per chain for a margin factor f: the largest expected operator count of the
+  // arena's chains (ChainSpec::expected_vertices: 1.6 beta W N_b + 8 sqrt + 64) times f.
+  int res_vcap_for(double f) const {
+    double v = 0;
+    for (auto& s : spec) v = std::max(v, s.expected_vertices());
+    return (int)std::min(1e9, std::ceil(f * v / 32.0) * 32.0);
+  }
+  // Every chain qualifies (spin 1/2, no correlation measurement) and a chain of vcap vertices
+  // fits in `limit` bytes of shared memory.
+  bool res_fits(int vcap, size_t limit) const {
+    if (n_corr_tiles || any_spin_s || C == 0 || zmax > 6) return false;
+    int nmax = 0, nbmax = 0;
+    for (auto& s : spec) { nmax = std::max(nmax, s.N); nbmax = std::max(nbmax, s.NB); }
+    if ((long long)nmax + 2ll * vcap > (1ll << 24)) return false;
+    return res_layout(nmax, nbmax, vcap).bytes + 256 <= limit;
+  }
+  // Buffers of the resident path for vertex capacity vcap per chain (the state arrays keep their
+  // contents only through download_lists / upload_lists, which the callers do).
+  int setup_resident(int vcap) {
+    res_nmax = res_nbmax = 0;
+    for (auto& s : spec) { res_nmax = std::max(res_nmax, s.N); res_nbmax = std::max(res_nbmax, s.NB); }
+    res_vcap = vcap;
+    res_lcap = 2 * vcap;
+    res_scap = res_nmax + 2 * vcap;
+    const ResLayout Ly = res_layout(res_nmax, res_nbmax, vcap);
+    res_smem = Ly.bytes;
+    const int z = merge_z(zmax);
+    const void* fn = z == 2 ? (const void*)k_resident<2> : z == 4 ? (const void*)k_resident<4>
+                                                                   : (const void*)k_resident<6>;
+    LG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)res_smem));
+    int per_sm = 0;
+    LG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, RES_THREADS, res_smem));
+    if (per_sm < 1) return lg_fail(LG_EBUDGET, "chain-resident sweep does not fit an SM");
+    res_grid = (int)std::min<long long>(C, (long long)nsm * per_sm);
+    const size_t lt = (size_t)C * res_lcap, sc = (size_t)C * res_scap;
+    int rc;
+    if ((rc = d_stime.alloc(lt)) || (rc = d_sdir.alloc(lt)) || (rc = rb_stime.alloc(lt)) ||
+        (rc = rb_sdir.alloc(lt)) || (rc = rb_spin0.alloc(N)) || (rc = rb_off_base.alloc(N)) ||
+        (rc = rb_off_cnt.alloc(N)) || (rc = d_cls.alloc(4 * sc)) || (rc = d_rkw.alloc(sc)) ||
+        (rc = d_rec.alloc((size_t)rec_rows * C * REC_WORDS)))
+      return rc;
+    LG_CUDA(cudaMemset(d_cls.p, 0, 4 * sc * sizeof(unsigned long long)));
+    LG_CUDA(cudaMemset(d_rkw.p, 0, sc * sizeof(RootKW)));
+    // the grid path's per-sweep arrays are not used here
+    d_vtime.release(); d_vcode.release(); d_vslot.release(); d_sinfo.release(); d_svert.release();
+    d_parent.release(); d_flip.release();
+    drop_graph();
+    resident = true;
+    return LG_OK;
+  }
+
+  // Move the arena between the two paths, keeping its state (spins, off-diagonal lists, sweep
+  // counters, accumulators): every result is the same on both.
+  int to_grid() {
+    if (!resident) return LG_OK;
+    SiteLists L;
+    int rc = download_lists(L);
+    if (rc) return rc;
+    rb_stime.release(); rb_sdir.release(); rb_spin0.release(); rb_off_base.release(); rb_off_cnt.release();
+    resident = false;
+    if ((rc = setup_grid())) return rc;
+    return upload_lists(L);
+  }
+  int to_resident(size_t limit = RES_SMEM_MAX - 1024) {
+    if (resident) return LG_OK;
+    if (!res_fits(res_vcap_for(1.0), limit)) return lg_fail(LG_EUNSUPPORTED, "the arena's chains do not fit the chain-resident path");
+    SiteLists L;
+    int rc = download_lists(L);
+    if (rc) return rc;
+    if ((rc = setup_resident(res_vcap_for(1.0)))) return rc;
+    return upload_lists(L);
+  }
+
+  // run() on the resident path: chunks of up to rec_rows sweeps, one k_resident launch each.
+  // A chunk that fails leaves the state it started from in place: on an overflow the capacity
+  // grows (or the arena moves to the grid path) and the chunk runs again with the same random
+  // numbers, so capacity never changes a trajectory.
+  int run_resident(long long n, float* ms, size_t flush_bytes) {
+    DBuf<uint8_t> flushbuf;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ms) {
+      if (flush_bytes) { int rc = flushbuf.alloc(flush_bytes); if (rc) return rc; }
+      LG_CUDA(cudaEventCreate(&e0));
+      LG_CUDA(cudaEventCreate(&e1));
+    }
+    struct EvG { cudaEvent_t a, b; ~EvG() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); } } eg{e0, e1};
+    long long done_total = 0;
+    while (n > 0) {
+      if (!resident) {  // moved to the grid path by an overflow: the rest runs there
+        return run(n, ms ? ms + done_total : nullptr, flush_bytes);
+      }
+      const int m = (int)std::min<long long>(n, rec_rows);
+      ResArgs R;
+      R.m = m; R.nmax = res_nmax; R.nbmax = res_nbmax; R.vcap = res_vcap; R.lcap = res_lcap;
+      R.scap = res_scap;
+      R.spin_in = d_spin0.p; R.obase_in = d_off_base.p; R.ocnt_in = d_off_cnt.p;
+      R.st_in = d_stime.p; R.sd_in = d_sdir.p;
+      R.spin_out = rb_spin0.p; R.obase_out = rb_off_base.p; R.ocnt_out = rb_off_cnt.p;
+      R.st_out = rb_stime.p; R.sd_out = rb_sdir.p;
+      Arena A = arena();
+      if (ms) {
+        if (flush_bytes) LG_CUDA(cudaMemsetAsync(flushbuf.p, (int)(done_total & 0xFF), flush_bytes, st));
+        LG_CUDA(cudaEventRecord(e0, st));
+      }
+      const int z = merge_z(zmax);
+      if (z == 2) k_resident<2><<<res_grid, RES_THREADS, res_smem, st>>>(A, R);
+      else if (z == 4) k_resident<4><<<res_grid, RES_THREADS, res_smem, st>>>(A, R);
+      else k_resident<6><<<res_grid, RES_THREADS, res_smem, st>>>(A, R);
+      ++g_launches;
+      if (ms) LG_CUDA(cudaEventRecord(e1, st));
+      LG_CUDA(cudaGetLastError());
+      Ctl hc;
+      LG_CUDA(lg_copy_async(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+      LG_CUDA(cudaStreamSynchronize(st));
+      if (hc.err) {
+        // the chunk is dropped: sweep counters back to the host's count
+        std::vector<uint32_t> sw(C);
+        for (int c = 0; c < C; ++c) sw[c] = (uint32_t)spec[c].mcs;
+        LG_CUDA(lg_copy(d_sweep.p, sw.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        if (hc.err == ERR_ITERCAP) {
+          return lg_fail(LG_EITERCAP, "union-find iteration cap hit; the chain state is lost "
+                                      "(load a checkpoint to continue)");
+        }
+        Ctl z0 = hc;
+        z0.err = 0;
+        LG_CUDA(lg_copy(d_ctl.p, &z0, sizeof(Ctl), cudaMemcpyHostToDevice));
+        // overflow: more capacity, or the grid path when a CTA cannot hold it
+        const int v2 = (int)std::min<long long>(1ll << 24, ((long long)res_vcap * 3 / 2 + 63) & ~31ll);
+        SiteLists L;
+        int rc = download_lists(L);
+        if (rc) return rc;
+        if (res_fits(v2, RES_SMEM_MAX - 1024)) {
+          if ((rc = setup_resident(v2))) return rc;
+        } else {
+          rb_stime.release(); rb_sdir.release(); rb_spin0.release(); rb_off_base.release();
+          rb_off_cnt.release();
+          resident = false;
+          shape.resident = 0;
+          if ((rc = setup_grid())) return rc;
+        }
+        if ((rc = upload_lists(L))) return rc;
+        continue;
+      }
+      d_spin0.swap(rb_spin0); d_off_base.swap(rb_off_base); d_off_cnt.swap(rb_off_cnt);
+      d_stime.swap(rb_stime); d_sdir.swap(rb_sdir);
+      hrec.resize((size_t)m * C * REC_WORDS);
+      LG_CUDA(lg_copy(hrec.data(), d_rec.p, hrec.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+      int rc = consume(m);
+      if (rc) return rc;
+      if (ms) {
+        float t = 0;
+        LG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        for (int i = 0; i < m; ++i) ms[done_total + i] = t / m;
+      }
+      done_total += m;
+      n -= m;
+    }
     return LG_OK;
   }
 
@@ -358,7 +575,7 @@ struct Engine {
     if ((rc = d_corr_tiles.alloc(tiles.size())) || (rc = d_corr_disp.alloc(disp ? N : 0)) ||
         (rc = d_corr_origin.alloc(orig ? N : 0)))
       return rc;
-    LG_CUDA(cudaMemcpy(d_corr_tiles.p, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_corr_tiles.p, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
     if (disp) LG_CUDA(cudaMemset(d_corr_disp.p, 0, (size_t)N * sizeof(long long)));
     if (orig) LG_CUDA(cudaMemset(d_corr_origin.p, 0, (size_t)N * sizeof(long long)));
     if (!disp) d_corr_disp.n = 0;
@@ -388,7 +605,7 @@ struct Engine {
     R = (int)h_region_cap.size();
     int rc;
     if ((rc = d_site_region.alloc(N)) || (rc = d_region_fill.alloc(R))) return rc;
-    LG_CUDA(cudaMemcpy(d_site_region.p, h_site_region.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_site_region.p, h_site_region.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     return layout_regions();
   }
 
@@ -405,7 +622,7 @@ struct Engine {
     region_total = tot;
     int rc = d_region_base.alloc(R + 1);
     if (rc) return rc;
-    LG_CUDA(cudaMemcpy(d_region_base.p, base.data(), (R + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_region_base.p, base.data(), (R + 1) * sizeof(int), cudaMemcpyHostToDevice));
     drop_graph();
     return LG_OK;
   }
@@ -422,7 +639,7 @@ struct Engine {
   // After an overflowing sweep: grow every region whose demand passed its capacity.
   int grow_regions() {
     std::vector<unsigned long long> fill(R);
-    LG_CUDA(cudaMemcpy(fill.data(), d_region_fill.p, R * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(fill.data(), d_region_fill.p, R * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
     bool grew = false;
     for (int r = 0; r < R; ++r) {
       if ((long long)fill[r] <= h_region_cap[r]) continue;
@@ -465,16 +682,16 @@ struct Engine {
     LG_CUDA(cudaMemset(d_cls.p, 0, 4 * (size_t)new_ns * sizeof(unsigned long long)));
     LG_CUDA(cudaMemset(d_rkw.p, 0, (size_t)new_ns * sizeof(RootKW)));
     if (keep) {
-      LG_CUDA(cudaMemcpy(d_stime.p, old_t.p, keep_n * sizeof(uint64_t), cudaMemcpyDeviceToDevice));
-      LG_CUDA(cudaMemcpy(d_sdir.p, old_d.p, keep_n, cudaMemcpyDeviceToDevice));
+      LG_CUDA(lg_copy(d_stime.p, old_t.p, keep_n * sizeof(uint64_t), cudaMemcpyDeviceToDevice));
+      LG_CUDA(lg_copy(d_sdir.p, old_d.p, keep_n, cudaMemcpyDeviceToDevice));
     }
     nv_cap = new_nv;
     ns_cap = new_ns;
     if ((rc = clear_sweep_state())) return rc;
     Ctl hc;
-    LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
     hc.nv_cap = nv_cap; hc.ns_cap = ns_cap;
-    LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
     drop_graph();
     return LG_OK;
   }
@@ -524,8 +741,19 @@ struct Engine {
     if (!(sh.acc_tile == 512 || sh.acc_tile == 1024 || sh.acc_tile == 2048) ||
         !(sh.cl_tile == 2048 || sh.cl_tile == 4096 || sh.cl_tile == 8192) ||
         !(sh.un_warps == 4 || sh.un_warps == 8 || sh.un_warps == 16) || !(sh.narrow_k >= 0) ||
-        !(sh.insert_k >= 0))
+        !(sh.insert_k >= 0) || !(sh.resident == 0 || sh.resident == 1))
       return lg_fail(LG_EINVAL, "bad launch shape");
+    if (sh.resident && !resident) {
+      int rc = to_resident();
+      if (rc) return rc;
+    } else if (!sh.resident && resident) {
+      int rc = to_grid();
+      if (rc) return rc;
+    }
+    if (resident) {  // the grid fields are kept for when the arena returns to the grid path
+      shape = sh;
+      return LG_OK;
+    }
     std::vector<int> ws, nsl, is, nbl;
     for (int c = 0; c < C; ++c) {
       const double mu = endpoints_per_site(c);
@@ -542,7 +770,7 @@ struct Engine {
       int r = d.alloc(std::max<size_t>(h.size(), 1));
       if (r) return r;
       if (!h.empty())
-        LG_CUDA(cudaMemcpy(d.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+        LG_CUDA(lg_copy(d.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
       return LG_OK;
     };
     n_wide = (int)ws.size();
@@ -659,6 +887,22 @@ struct Engine {
     }
     mark(4);
     launches += 2;
+    // Without a field every cluster's flip is a coin keyed by its root, which the site pass can
+    // draw itself: it then runs on the second stream beside k_cluster (whose flip array it no
+    // longer reads), and k_end follows both.
+    const bool coin = all_nofield;
+    if (coin) {
+      cudaEventRecord(ev_fork, st);
+      cudaStreamWaitEvent(st2, ev_fork, 0);
+      if (n_wide) {
+        k_site_end<true><<<grid_for((long long)n_wide * 32, 256, 16), 256, 0, st2>>>(A, wide_list, n_wide);
+        ++launches;
+      }
+      if (n_narrow) {
+        k_site_end_narrow<true><<<grid_for(n_narrow, 256, 16), 256, 0, st2>>>(A, d_narrow_sites.p, n_narrow);
+        ++launches;
+      }
+    }
     {
       const int t = shape.cl_tile, g = (ns_cap + t - 1) / t;  // one tile per block
       if (t == 2048) k_cluster<2048><<<g, CL_THREADS, 0, st>>>(A);
@@ -667,6 +911,20 @@ struct Engine {
     }
     mark(5);
     launches += 1;
+    if (coin) {
+      cudaEventRecord(ev_join, st2);
+      cudaStreamWaitEvent(st, ev_join, 0);
+      if (n_corr_tiles) {
+        k_corr<<<n_corr_tiles, CORR_THREADS, corr_smem, st>>>(A);
+        ++launches;
+      }
+      k_end<<<1, 1024, 0, st>>>(A);
+      mark(6);
+      launches += 1;
+      sweep_launches = launches;
+      g_launches += launches;
+      return;
+    }
     // k_end (counters, the next record row, claim counters) needs nothing of the site pass, so
     // it runs beside it on a third stream; k_corr reads the sweep counter before k_end advances
     // it, so with correlations the order stays sequential
@@ -718,6 +976,7 @@ struct Engine {
   // Run n sweeps of every chain.  With ms != nullptr every sweep is bracketed by events and
   // preceded by an L2 flush of flush_bytes (outside the brackets).
   int run(long long n, float* ms = nullptr, size_t flush_bytes = 0) {
+    if (resident) return run_resident(n, ms, flush_bytes);
     DBuf<uint8_t> flushbuf;
     std::vector<cudaEvent_t> ev;
     if (ms) {
@@ -746,12 +1005,12 @@ struct Engine {
       }
       LG_CUDA(cudaGetLastError());
       Ctl hc;
-      LG_CUDA(cudaMemcpyAsync(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+      LG_CUDA(lg_copy_async(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
       LG_CUDA(cudaStreamSynchronize(st));
       int done = (int)hc.step;
       if (done > 0) {
         hrec.resize((size_t)done * C * REC_WORDS);
-        LG_CUDA(cudaMemcpy(hrec.data(), d_rec.p, hrec.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        LG_CUDA(lg_copy(hrec.data(), d_rec.p, hrec.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
         if ((rc = consume(done))) return rc;
         if (ms)
           for (int i = 0; i < done; ++i)
@@ -767,22 +1026,22 @@ struct Engine {
         // checkpoint is loaded (set_state on a single-chain engine)
         Ctl zk = hc;
         zk.step = 0;
-        LG_CUDA(cudaMemcpy(d_ctl.p, &zk, sizeof(Ctl), cudaMemcpyHostToDevice));
+        LG_CUDA(lg_copy(d_ctl.p, &zk, sizeof(Ctl), cudaMemcpyHostToDevice));
         clear_sweep_state();
         return lg_fail(LG_EITERCAP, "union-find iteration cap hit; the chain state is lost "
                                     "(load a checkpoint to continue)");
       }
       if (hc.err == ERR_BOUNDARY) {
-        LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
+        LG_CUDA(lg_copy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
         clear_sweep_state();
         return lg_fail(LG_EINVAL, "spin-S configuration not periodic in imaginary time");
       }
       if (hc.err == ERR_OVERFLOW) {
-        LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
+        LG_CUDA(lg_copy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
         rc = grow_regions();
         if (rc) return rc;
       } else {
-        LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
+        LG_CUDA(lg_copy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
       }
       if ((rc = clear_sweep_state())) return rc;
       n -= done;
@@ -792,6 +1051,11 @@ struct Engine {
 
   // n sweeps launched kernel by kernel with events between stages (no graph).
   int profile(long long n, size_t flush_bytes, double* kernel_ms, long long* vertices) {
+    if (resident) {  // the per-kernel profile is a grid-path measurement
+      int rc = to_grid();
+      if (rc) return rc;
+      shape.resident = 0;
+    }
     DBuf<uint8_t> flushbuf;
     if (flush_bytes) { int rc = flushbuf.alloc(flush_bytes); if (rc) return rc; }
     cudaEvent_t ev[kNumStages + 1];
@@ -805,7 +1069,7 @@ struct Engine {
       enqueue_sweep(ev);
       LG_CUDA(cudaGetLastError());
       Ctl hc;
-      LG_CUDA(cudaMemcpyAsync(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+      LG_CUDA(lg_copy_async(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
       LG_CUDA(cudaStreamSynchronize(st));
       if (hc.err) {
         long long left = n;
@@ -823,11 +1087,11 @@ struct Engine {
       }
       verts += (hc.ns_total - N) / 2;  // every vertex adds a segment at each of its two sites
       hrec.resize((size_t)C * REC_WORDS);
-      LG_CUDA(cudaMemcpy(hrec.data(), d_rec.p, hrec.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+      LG_CUDA(lg_copy(hrec.data(), d_rec.p, hrec.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
       if (int rc = consume(1)) return rc;
       Ctl z = hc;
       z.step = 0;
-      LG_CUDA(cudaMemcpy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
+      LG_CUDA(lg_copy(d_ctl.p, &z, sizeof(Ctl), cudaMemcpyHostToDevice));
       if (int rc = clear_sweep_state()) return rc;
       --n;
     }
@@ -843,6 +1107,30 @@ struct Engine {
     if (trial < 1) trial = 1;
     char line[160];
     report.clear();
+    // the chain-resident path, where the arena qualifies: timed first, over whole chunks
+    const int trial2 = std::max(trial, 8);
+    double res_ms = -1;
+    const bool can_res = allow_resident && res_fits(res_vcap_for(1.0), RES_SMEM_DEFAULT);
+    if (can_res) {
+      Shape r = shape;
+      r.resident = 1;
+      int rc = set_shape(r);
+      if (rc) return rc;
+      std::vector<float> t(trial2);
+      if ((rc = run(1))) return rc;
+      if ((rc = run(trial2, t.data(), flush_bytes))) return rc;
+      if (resident) {
+        res_ms = 0;
+        for (float x : t) res_ms += x;
+        res_ms /= trial2;
+        std::snprintf(line, sizeof(line), "resident (one CTA per chain, %d sweeps per launch): %.4f ms\n",
+                      trial2, res_ms);
+        report += line;
+      }
+      Shape g = shape;
+      g.resident = 0;
+      if ((rc = set_shape(g))) return rc;
+    }
     auto time_shape = [&](const Shape& sh, double* ms) -> int {
       int rc = set_shape(sh);
       if (rc) return rc;
@@ -909,8 +1197,24 @@ struct Engine {
       Shape c = best; c.un_warps = w;
       if ((rc = consider(c))) return rc;
     }
-    std::snprintf(line, sizeof(line), "chosen: insert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d (%.4f ms)\n",
-                  best.insert_k, best.narrow_k, best.acc_tile, best.cl_tile, best.un_warps, best_ms);
+    if ((rc = set_shape(best))) return rc;
+    if (res_ms > 0) {
+      // the best grid shape timed as it runs (CUDA graph), against the resident time
+      std::vector<float> t(trial2);
+      if ((rc = run(trial2, t.data(), flush_bytes))) return rc;
+      double g = 0;
+      for (float x : t) g += x;
+      g /= trial2;
+      std::snprintf(line, sizeof(line), "grid (CUDA graph, best shape): %.4f ms\n", g);
+      report += line;
+      if (res_ms < 0.98 * g) {
+        best.resident = 1;
+        best_ms = res_ms;
+      }
+    }
+    std::snprintf(line, sizeof(line), "chosen: %sinsert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d (%.4f ms)\n",
+                  best.resident ? "resident; " : "", best.insert_k, best.narrow_k, best.acc_tile,
+                  best.cl_tile, best.un_warps, best_ms);
     report += line;
     return set_shape(best);
   }
@@ -945,7 +1249,7 @@ struct Engine {
       DBuf<long long>& d = which ? d_corr_origin : d_corr_disp;
       if (!d.n) continue;
       h_corr.resize(N);
-      LG_CUDA(cudaMemcpy(h_corr.data(), d.p, (size_t)N * sizeof(long long), cudaMemcpyDeviceToHost));
+      LG_CUDA(lg_copy(h_corr.data(), d.p, (size_t)N * sizeof(long long), cudaMemcpyDeviceToHost));
       LG_CUDA(cudaMemsetAsync(d.p, 0, (size_t)N * sizeof(long long), st));
       for (int c = 0; c < C; ++c) {
         const bool on = which ? hch[c].corr_origin >= 0 : hch[c].corr_disp != 0;
@@ -966,17 +1270,17 @@ struct Engine {
     int so = hch[c].site_off;
     std::vector<uint8_t> sp(s.N);
     std::vector<int> ob(s.N), oc(s.N);
-    LG_CUDA(cudaMemcpy(sp.data(), d_spin0.p + so, s.N, cudaMemcpyDeviceToHost));
-    LG_CUDA(cudaMemcpy(ob.data(), d_off_base.p + so, s.N * sizeof(int), cudaMemcpyDeviceToHost));
-    LG_CUDA(cudaMemcpy(oc.data(), d_off_cnt.p + so, s.N * sizeof(int), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(sp.data(), d_spin0.p + so, s.N, cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(ob.data(), d_off_base.p + so, s.N * sizeof(int), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(oc.data(), d_off_cnt.p + so, s.N * sizeof(int), cudaMemcpyDeviceToHost));
     spins.assign(sp.begin(), sp.end());
     std::vector<std::pair<uint64_t, int>> ops;
     for (int i = 0; i < s.N; ++i) {
       if (!oc[i]) continue;
       std::vector<uint64_t> t(oc[i]);
       std::vector<uint8_t> d(oc[i]);
-      LG_CUDA(cudaMemcpy(t.data(), d_stime.p + ob[i], oc[i] * sizeof(uint64_t), cudaMemcpyDeviceToHost));
-      LG_CUDA(cudaMemcpy(d.data(), d_sdir.p + ob[i], oc[i], cudaMemcpyDeviceToHost));
+      LG_CUDA(lg_copy(t.data(), d_stime.p + ob[i], oc[i] * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+      LG_CUDA(lg_copy(d.data(), d_sdir.p + ob[i], oc[i], cudaMemcpyDeviceToHost));
       int gs = so + i;
       for (int j = 0; j < oc[i]; ++j) {
         int idx = h_inc_off[gs] + d[j];
@@ -998,15 +1302,15 @@ struct Engine {
 
   int download_lists(SiteLists& L) {
     std::vector<int> ob(N), oc(N);
-    LG_CUDA(cudaMemcpy(ob.data(), d_off_base.p, N * sizeof(int), cudaMemcpyDeviceToHost));
-    LG_CUDA(cudaMemcpy(oc.data(), d_off_cnt.p, N * sizeof(int), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(ob.data(), d_off_base.p, N * sizeof(int), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(oc.data(), d_off_cnt.p, N * sizeof(int), cudaMemcpyDeviceToHost));
     L.assign(N, {});
     for (int i = 0; i < N; ++i) {
       if (!oc[i]) continue;
       std::vector<uint64_t> t(oc[i]);
       std::vector<uint8_t> d(oc[i]);
-      LG_CUDA(cudaMemcpy(t.data(), d_stime.p + ob[i], oc[i] * sizeof(uint64_t), cudaMemcpyDeviceToHost));
-      LG_CUDA(cudaMemcpy(d.data(), d_sdir.p + ob[i], oc[i], cudaMemcpyDeviceToHost));
+      LG_CUDA(lg_copy(t.data(), d_stime.p + ob[i], oc[i] * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+      LG_CUDA(lg_copy(d.data(), d_sdir.p + ob[i], oc[i], cudaMemcpyDeviceToHost));
       L[i].resize(oc[i]);
       for (int j = 0; j < oc[i]; ++j) L[i][j] = {t[j], d[j]};
     }
@@ -1018,7 +1322,29 @@ struct Engine {
     std::vector<int> ob(N), oc(N);
     long long total = 0;
     for (int i = 0; i < N; ++i) { ob[i] = (int)total; oc[i] = (int)L[i].size(); total += oc[i]; }
-    if (total > ns_cap) {
+    if (resident) {
+      // the list arrays hold res_lcap entries per chain; a chain with more grows the capacity
+      long long need = 0;
+      for (int c = 0; c < C; ++c) {
+        long long t = 0;
+        for (int i = 0; i < spec[c].N; ++i) t += (long long)L[hch[c].site_off + i].size();
+        need = std::max(need, t);
+      }
+      if (need > res_lcap || total > (long long)d_stime.n) {
+        const int v2 = (int)std::min<long long>(1ll << 24, ((std::max<long long>(need, res_lcap) * 3 / 4) + 63) & ~31ll);
+        if (!res_fits(v2, RES_SMEM_MAX - 1024)) {
+          resident = false;
+          shape.resident = 0;
+          rb_stime.release(); rb_sdir.release(); rb_spin0.release(); rb_off_base.release();
+          rb_off_cnt.release();
+          int rc = setup_grid();
+          if (rc) return rc;
+          return upload_lists(L);
+        }
+        int rc = setup_resident(v2);
+        if (rc) return rc;
+      }
+    } else if (total > ns_cap) {
       int rc = alloc_dynamic(total + 4096, false);
       if (rc) return rc;
     }
@@ -1026,11 +1352,11 @@ struct Engine {
     std::vector<uint8_t> d(total);
     for (int i = 0; i < N; ++i)
       for (int j = 0; j < oc[i]; ++j) { t[ob[i] + j] = L[i][j].first; d[ob[i] + j] = L[i][j].second; }
-    LG_CUDA(cudaMemcpy(d_off_base.p, ob.data(), N * sizeof(int), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_off_cnt.p, oc.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_off_base.p, ob.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_off_cnt.p, oc.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     if (total) {
-      LG_CUDA(cudaMemcpy(d_stime.p, t.data(), total * sizeof(uint64_t), cudaMemcpyHostToDevice));
-      LG_CUDA(cudaMemcpy(d_sdir.p, d.data(), total, cudaMemcpyHostToDevice));
+      LG_CUDA(lg_copy(d_stime.p, t.data(), total * sizeof(uint64_t), cudaMemcpyHostToDevice));
+      LG_CUDA(lg_copy(d_sdir.p, d.data(), total, cudaMemcpyHostToDevice));
     }
     return LG_OK;
   }
@@ -1038,6 +1364,11 @@ struct Engine {
   // n sweeps kernel by kernel with the structural checks of k_validate after insertion, merge,
   // cluster sums and the end of the sweep.  LG_EDEVICE names the first failed check.
   int validate(long long n) {
+    if (resident) {  // the structural checks are of the grid path's arrays
+      int rc = to_grid();
+      if (rc) return rc;
+      shape.resident = 0;
+    }
     DBuf<int> bad;
     int rc = bad.alloc(2);
     if (rc) return rc;
@@ -1049,7 +1380,7 @@ struct Engine {
     val_bad = nullptr;
     if (rc) return rc;
     int hb[2];
-    LG_CUDA(cudaMemcpy(hb, bad.p, sizeof(hb), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(hb, bad.p, sizeof(hb), cudaMemcpyDeviceToHost));
     if (hb[0]) return lg_fail(LG_EDEVICE, "structural check %d failed (%d failures)", hb[1], hb[0]);
     return LG_OK;
   }
@@ -1057,9 +1388,9 @@ struct Engine {
   // Union-find retries per union (Ctl::iter_cap): a test seam for the LG_EITERCAP path.
   int set_iter_cap(int cap) {
     Ctl hc;
-    LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
     hc.iter_cap = cap;
-    LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
     return LG_OK;
   }
 
@@ -1101,17 +1432,17 @@ struct Engine {
     }
     if (C == 1) {  // a complete, valid state: a union-find failure (LG_EITERCAP) no longer applies
       Ctl hc;
-      LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+      LG_CUDA(lg_copy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
       hc.err = 0;
       hc.step = 0;
-      LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
+      LG_CUDA(lg_copy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
     }
     if ((rc = upload_lists(L))) return rc;
     std::vector<uint8_t> sp(s.N);
     for (int i = 0; i < s.N; ++i) sp[i] = (uint8_t)(spins[i] & 1);
-    LG_CUDA(cudaMemcpy(d_spin0.p + so, sp.data(), s.N, cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_spin0.p + so, sp.data(), s.N, cudaMemcpyHostToDevice));
     uint32_t sw = (uint32_t)sweep;
-    LG_CUDA(cudaMemcpy(d_sweep.p + c, &sw, sizeof(uint32_t), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_sweep.p + c, &sw, sizeof(uint32_t), cudaMemcpyHostToDevice));
     spec[c].mcs = sweep;
     return LG_OK;
   }
@@ -1141,15 +1472,15 @@ struct Engine {
       vc[v] = (uint8_t)(graphs[i] << 1);
       vidx[i] = v;
     }
-    LG_CUDA(cudaMemcpy(d_bond_cnt.p, cnt.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
-    LG_CUDA(cudaMemcpy(d_bond_ptr.p, ptr.data(), (NB + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_bond_cnt.p, cnt.data(), NB * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_bond_ptr.p, ptr.data(), (NB + 1) * sizeof(int), cudaMemcpyHostToDevice));
     if (nops) {
-      LG_CUDA(cudaMemcpy(d_vtime.p, vt.data(), nops * sizeof(uint64_t), cudaMemcpyHostToDevice));
-      LG_CUDA(cudaMemcpy(d_vcode.p, vc.data(), nops, cudaMemcpyHostToDevice));
+      LG_CUDA(lg_copy(d_vtime.p, vt.data(), nops * sizeof(uint64_t), cudaMemcpyHostToDevice));
+      LG_CUDA(lg_copy(d_vcode.p, vc.data(), nops, cudaMemcpyHostToDevice));
     }
     Ctl hc{};
     hc.nv_total = (int)nops; hc.nv_cap = nv_cap; hc.ns_cap = ns_cap;
-    LG_CUDA(cudaMemcpy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
     Arena A = arena();
     k_site_count<<<grid_for(N, 256, 16), 256, 0, st>>>(A);
     scan(d_site_cnt.p, d_sbase.p, N, &d_ctl.p->ns_total, ns_cap, 1, 0);
@@ -1160,13 +1491,13 @@ struct Engine {
     g_launches += 7;
     LG_CUDA(cudaGetLastError());
     LG_CUDA(cudaStreamSynchronize(st));
-    LG_CUDA(cudaMemcpy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
     if (hc.err) return lg_fail(LG_EITERCAP, "union-find failed (%d)", hc.err);
     long long ns = 2 * nops + N;
     std::vector<int> par(ns), sb(N + 1), vs(2 * std::max<long long>(nops, 1));
-    LG_CUDA(cudaMemcpy(par.data(), d_parent.p, ns * sizeof(int), cudaMemcpyDeviceToHost));
-    LG_CUDA(cudaMemcpy(sb.data(), d_sbase.p, (N + 1) * sizeof(int), cudaMemcpyDeviceToHost));
-    if (nops) LG_CUDA(cudaMemcpy(vs.data(), d_vslot.p, 2 * nops * sizeof(int), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(par.data(), d_parent.p, ns * sizeof(int), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(sb.data(), d_sbase.p, (N + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    if (nops) LG_CUDA(lg_copy(vs.data(), d_vslot.p, 2 * nops * sizeof(int), cudaMemcpyDeviceToHost));
     // fragments: site bottoms, then graph-0 vertices in the given order
     std::vector<int> froot;
     froot.reserve(N + nops);
@@ -1193,7 +1524,7 @@ struct Engine {
     h_active[c] = on ? 1 : 0;
     const bool all = std::all_of(h_active.begin(), h_active.end(), [](uint8_t a) { return a != 0; });
     if (all != was_all) drop_graph();  // the arena's all_active flag is a launch parameter
-    LG_CUDA(cudaMemcpyAsync(d_active.p + c, &h_active[c], 1, cudaMemcpyHostToDevice, st));
+    LG_CUDA(lg_copy_async(d_active.p + c, &h_active[c], 1, cudaMemcpyHostToDevice, st));
     LG_CUDA(cudaStreamSynchronize(st));
     return LG_OK;
   }
@@ -1204,7 +1535,7 @@ struct Engine {
   int adopt(Engine& old, const std::vector<int>& from) {
     std::vector<int> map(N, -1);
     std::vector<uint32_t> sw(C);
-    LG_CUDA(cudaMemcpy(sw.data(), d_sweep.p, C * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(sw.data(), d_sweep.p, C * sizeof(uint32_t), cudaMemcpyDeviceToHost));
     for (int c = 0; c < C; ++c) {
       const int o = from[c];
       if (o < 0) continue;
@@ -1215,21 +1546,28 @@ struct Engine {
       acc[c] = old.acc[o];
       sw[c] = (uint32_t)old.spec[o].mcs;
     }
-    LG_CUDA(cudaMemcpy(d_sweep.p, sw.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_sweep.p, sw.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice));
     DBuf<int> dmap, dcnt, dbase;
     int rc;
     if ((rc = dmap.alloc(N)) || (rc = dcnt.alloc(N)) || (rc = dbase.alloc(N + 1))) return rc;
-    LG_CUDA(cudaMemcpy(dmap.p, map.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(dmap.p, map.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     Arena A = arena();
     k_repack_count<<<grid_for(N, 256), 256, 0, st>>>(A, dmap.p, old.d_off_cnt.p, dcnt.p);
     LG_CUDA(cudaMemsetAsync(d_ctl.p, 0, sizeof(int), st));
     scan(dcnt.p, dbase.p, N, &d_ctl.p->ns_total, 0x7FFFFFFF, 0, 0);
     g_launches += 3;
-    LG_CUDA(cudaMemcpyAsync(d_off_cnt.p, dcnt.p, N * sizeof(int), cudaMemcpyDeviceToDevice, st));
+    LG_CUDA(lg_copy_async(d_off_cnt.p, dcnt.p, N * sizeof(int), cudaMemcpyDeviceToDevice, st));
     int total = 0;
-    LG_CUDA(cudaMemcpyAsync(&total, dbase.p + N, sizeof(int), cudaMemcpyDeviceToHost, st));
+    LG_CUDA(lg_copy_async(&total, dbase.p + N, sizeof(int), cudaMemcpyDeviceToHost, st));
     LG_CUDA(cudaStreamSynchronize(st));
-    if (total > ns_cap) {
+    if (resident) {
+      // the lists land packed in the list array; a chain longer than its slots grows them on
+      // its first sweep (overflow), as any other
+      if (total > (long long)d_stime.n) {
+        if ((rc = d_stime.alloc(total)) || (rc = d_sdir.alloc(total))) return rc;
+        A = arena();
+      }
+    } else if (total > ns_cap) {
       if ((rc = alloc_dynamic(total + 4096, false))) return rc;
       A = arena();
     }
@@ -1252,7 +1590,7 @@ struct Engine {
     for (int c : {c1, c2}) {
       hch[c].inv_rate = spec[c].dchain.inv_rate;
       hch[c].flip_coef = spec[c].dchain.flip_coef;
-      LG_CUDA(cudaMemcpyAsync(d_ch.p + c, &hch[c], sizeof(DChain), cudaMemcpyHostToDevice, st));
+      LG_CUDA(lg_copy_async(d_ch.p + c, &hch[c], sizeof(DChain), cudaMemcpyHostToDevice, st));
     }
     LG_CUDA(cudaStreamSynchronize(st));
     return LG_OK;
@@ -1263,8 +1601,9 @@ struct Engine {
     if (rc) return rc;
     hch[c].inv_rate = spec[c].dchain.inv_rate;
     hch[c].flip_coef = spec[c].dchain.flip_coef;
-    LG_CUDA(cudaMemcpy(d_ch.p + c, &hch[c], sizeof(DChain), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_ch.p + c, &hch[c], sizeof(DChain), cudaMemcpyHostToDevice));
     acc[c] = ChainAcc();
+    if (resident) return LG_OK;  // a grown operator count grows the capacity on overflow
     set_merge_cap();
     return set_shape(shape);  // the chain's narrow / wide class depends on beta
   }
@@ -1293,6 +1632,11 @@ int lg_last_error(char* buf, size_t n) {
 
 uint64_t lg_kernel_launches(void) { return g_launches.load(); }
 
+void lg_copy_bytes(uint64_t* h2d, uint64_t* d2h) {
+  if (h2d) *h2d = g_h2d_bytes.load();
+  if (d2h) *d2h = g_d2h_bytes.load();
+}
+
 const char* lg_version(void) {
   static std::string v;
   if (v.empty()) {
@@ -1309,7 +1653,7 @@ int lg_create(const lg_params* p, lg_chain** out) {
     int rc = s.init(*p);
     if (rc) return rc;
     auto e = std::make_shared<Engine>();
-    rc = e->build({s});
+    rc = e->build({s}, true);
     if (rc) return rc;
     lg_chain* c = new lg_chain();
     c->eng = e;
@@ -1635,7 +1979,7 @@ int lg_batch_create(int n, const lg_params* p, lg_batch** out) {
       if (rc) return rc;
     }
     auto e = std::make_shared<Engine>();
-    int rc = e->build(specs);
+    int rc = e->build(specs, true);
     if (rc) return rc;
     lg_batch* b = new lg_batch();
     b->eng = e;
@@ -1689,6 +2033,7 @@ static void shape_out(const Shape& s, lg_shape* out) {
   out->acc_tile = s.acc_tile;
   out->cl_tile = s.cl_tile;
   out->union_warps = s.un_warps;
+  out->resident = s.resident;
   out->reserved = 0;
 }
 
@@ -1726,6 +2071,7 @@ static int set_shape_engine(Engine& e, const lg_shape* in) {
   s.acc_tile = in->acc_tile;
   s.cl_tile = in->cl_tile;
   s.un_warps = in->union_warps;
+  s.resident = in->resident;
   return e.set_shape(s);
 }
 

@@ -698,7 +698,7 @@ __device__ __forceinline__ void warp_merge2(const uint64_t* XK, const uint16_t* 
   }
 }
 
-// Z: the largest site degree of the arena (2, 4 or MAXZ), the bound of every per-list loop.
+// Z: the largest site degree of the arena (2, 4, 6, 12 or MAXZ), the bound of every per-list loop.
 template <int Z>
 __device__ void merge_site_serial(Arena& A, int s) {
   const int j0 = A.inc_off[s];
@@ -754,7 +754,7 @@ __device__ void merge_site_serial(Arena& A, int s) {
     A.sinfo[x] = (uint8_t)(spin | gneg | (j == k ? SI_LAST : 0) | (sd == 0 ? SI_SRC : 0) |
                            ((code >> 1) << SI_GSHIFT) | ((code & 1u) ? SI_OFF : 0));
     A.svert[x] = v;
-    A.sdir[x] = (uint8_t)(best | (A.inc_dir ? A.inc_dir[j0 + best] << 3 : 0));
+    A.sdir[x] = (uint8_t)(best | (A.inc_dir ? A.inc_dir[j0 + best] << SD_DSHIFT : 0));
     A.parent[x] = x;
     A.vslot[2 * v + sd] = x;
   }
@@ -797,7 +797,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
     // stage the incident lists: list d occupies [off[d], off[d+1])
     int off[Z + 1];
     int ptr[Z];
-    uint8_t sdv[Z];  // per list: the segment's sdir value (incidence | direction << 3) | side << 7
+    uint8_t sdv[Z];  // per list: the segment's sdir value (incidence | direction << 5) | side << 7
     off[0] = 0;
 #pragma unroll
     for (int d = 0; d < Z; ++d) {
@@ -805,7 +805,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
         const int b = A.inc[j0 + d];
         ptr[d] = A.bond_ptr[b];
         off[d + 1] = off[d] + A.bond_cnt[b];
-        sdv[d] = (uint8_t)(d | (A.inc_dir ? A.inc_dir[j0 + d] << 3 : 0) | (A.inc_side[j0 + d] << 7));
+        sdv[d] = (uint8_t)(d | (A.inc_dir ? A.inc_dir[j0 + d] << SD_DSHIFT : 0) | (A.inc_side[j0 + d] << 7));
       } else {
         ptr[d] = 0; off[d + 1] = off[d]; sdv[d] = 0;
       }
@@ -850,7 +850,7 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
     uint64_t* curK = k <= 32 ? wmK : wsK;
     const uint16_t* curI = k <= 32 ? wmI : nullptr;  // level 0: the index of a key is its position
     bool in_m = k <= 32;
-    constexpr int LEVELS = Z <= 2 ? 1 : (Z <= 4 ? 2 : 3);  // pairwise rounds for Z lists
+    constexpr int LEVELS = Z <= 2 ? 1 : Z <= 4 ? 2 : Z <= 8 ? 3 : Z <= 16 ? 4 : 5;  // pairwise rounds
 #pragma unroll
     for (int level = 0; level < LEVELS; ++level) {
       if (nr <= 1) break;
@@ -951,13 +951,17 @@ __global__ void __launch_bounds__(256) k_merge_narrow(Arena A, const int* sites,
 
 // The merge kernels for an arena whose sites have at most zmax incident bonds: the instance
 // with the smallest list bound Z >= zmax (fewer registers and pairwise rounds).
-inline int merge_z(int zmax) { return zmax <= 2 ? 2 : (zmax <= 4 ? 4 : MAXZ); }
+inline int merge_z(int zmax) {
+  return zmax <= 2 ? 2 : zmax <= 4 ? 4 : zmax <= 6 ? 6 : zmax <= 12 ? 12 : MAXZ;
+}
 
 inline void launch_merge(int zmax, int grid, size_t smem, cudaStream_t st, const Arena& A,
                          const int* sites, int n, int cap) {
   const int z = merge_z(zmax);
   if (z == 2) k_merge<2><<<grid, MERGE_WARPS * 32, smem, st>>>(A, sites, n, cap);
   else if (z == 4) k_merge<4><<<grid, MERGE_WARPS * 32, smem, st>>>(A, sites, n, cap);
+  else if (z == 6) k_merge<6><<<grid, MERGE_WARPS * 32, smem, st>>>(A, sites, n, cap);
+  else if (z == 12) k_merge<12><<<grid, MERGE_WARPS * 32, smem, st>>>(A, sites, n, cap);
   else k_merge<MAXZ><<<grid, MERGE_WARPS * 32, smem, st>>>(A, sites, n, cap);
 }
 
@@ -966,6 +970,8 @@ inline void launch_merge_narrow(int zmax, int grid, cudaStream_t st, const Arena
   const int z = merge_z(zmax);
   if (z == 2) k_merge_narrow<2><<<grid, 256, 0, st>>>(A, sites, n);
   else if (z == 4) k_merge_narrow<4><<<grid, 256, 0, st>>>(A, sites, n);
+  else if (z == 6) k_merge_narrow<6><<<grid, 256, 0, st>>>(A, sites, n);
+  else if (z == 12) k_merge_narrow<12><<<grid, 256, 0, st>>>(A, sites, n);
   else k_merge_narrow<MAXZ><<<grid, 256, 0, st>>>(A, sites, n);
 }
 
@@ -1178,8 +1184,9 @@ __device__ __forceinline__ SegContrib seg_contrib(uint8_t info, uint8_t info1, u
   c.q = (info & SI_SPIN) * 2 + ((info & SI_GNEG) ? 1 : 0);
   c.w[0] = c.w[1] = c.w[2] = 0;
   const int sg = (info & SI_SPIN) ? -1 : 1;
-  if ((info & SI_SRC) && !((info >> SI_GSHIFT) & 2)) c.w[dir >> 3] -= sg;
-  if (!(info & SI_LAST) && (info1 & SI_SRC) && !((info1 >> SI_GSHIFT) & 2)) c.w[dir1 >> 3] += sg;
+  if ((info & SI_SRC) && !((info >> SI_GSHIFT) & 2)) c.w[(dir >> SD_DSHIFT) & 3] -= sg;
+  if (!(info & SI_LAST) && (info1 & SI_SRC) && !((info1 >> SI_GSHIFT) & 2))
+    c.w[(dir1 >> SD_DSHIFT) & 3] += sg;
   return c;
 }
 
@@ -1364,22 +1371,15 @@ __device__ __forceinline__ RootClass load_root_class(const Arena& A, int x) {
   return rc;
 }
 
-// Flip decision of root x of chain c and its record contribution, added into R; clears the
-// root's class sums.
-__device__ __forceinline__ void root_sums(const Arena& A, int x, int c, const RootClass& rcl,
-                                          RootSums& R) {
-  const DChain ch = A.ch[c];
-  ulonglong2* S = reinterpret_cast<ulonglong2*>(A.cls + 4 * (size_t)x);
-  S[0] = make_ulonglong2(0ull, 0ull);
-  S[1] = make_ulonglong2(0ull, 0ull);
-  *reinterpret_cast<uint4*>(A.rkw[x].K) = make_uint4(0u, 0u, 0u, 0u);
-  *reinterpret_cast<int4*>(A.rkw[x].W) = make_int4(0, 0, 0, 0);
+// Flip decision of a cluster whose root has the chain-local segment index `key`, and its record
+// contribution (from its class integers rcl), added into R.  Returns the flip.
+__device__ __forceinline__ uint8_t root_record(const DChain& ch, uint32_t sweep, uint32_t key,
+                                               const RootClass& rcl, RootSums& R) {
   const long long s0 = (long long)rcl.S[0], s1 = (long long)rcl.S[1], s2 = (long long)rcl.S[2],
                   s3 = (long long)rcl.S[3];
   const long long k0 = rcl.K[0], k1 = rcl.K[1], k2 = rcl.K[2], k3 = rcl.K[3];
   const long long Ms = s0 + s1 - s2 - s3, SMs = s0 - s1 - s2 + s3;
-  const uint32_t key = (uint32_t)(x - A.ch_slot_off[c]);
-  const rnd4 r = philox(ch.seed, A.ch_sweep[c], key, TAG_FLIP, 0);
+  const rnd4 r = philox(ch.seed, sweep, key, TAG_FLIP, 0);
   uint8_t f;
   if (!ch.field) {
     f = r.x < 0x80000000u ? 1 : 0;
@@ -1388,7 +1388,6 @@ __device__ __forceinline__ void root_sums(const Arena& A, int x, int c, const Ro
     const float e = exp_clamped(xf);
     f = __fmul_rn(uniform_open(r.x), __fadd_rn(1.0f, e)) < 1.0f ? 1 : 0;
   }
-  A.flip[x] = f;
   auto ab = [](long long v) { return (unsigned long long)(v < 0 ? -v : v); };
   {
     const long long n0 = k0 + k1 + k2 + k3, m0 = k0 + k1 - k2 - k3;
@@ -1421,6 +1420,19 @@ __device__ __forceinline__ void root_sums(const Arena& A, int x, int c, const Ro
   add_u128(R.w[5], mul64(ab(Ms), ab(Ms)));
   add_u128(R.w[6], mul64(SL, SL));
   add_u128(R.w[7], mul64(ab(SMs), ab(SMs)));
+  return f;
+}
+
+// Flip decision of root x of chain c and its record contribution, added into R; clears the
+// root's class sums.
+__device__ __forceinline__ void root_sums(const Arena& A, int x, int c, const RootClass& rcl,
+                                          RootSums& R) {
+  ulonglong2* S = reinterpret_cast<ulonglong2*>(A.cls + 4 * (size_t)x);
+  S[0] = make_ulonglong2(0ull, 0ull);
+  S[1] = make_ulonglong2(0ull, 0ull);
+  *reinterpret_cast<uint4*>(A.rkw[x].K) = make_uint4(0u, 0u, 0u, 0u);
+  *reinterpret_cast<int4*>(A.rkw[x].W) = make_int4(0, 0, 0, 0);
+  A.flip[x] = root_record(A.ch[c], A.ch_sweep[c], (uint32_t)(x - A.ch_slot_off[c]), rcl, R);
 }
 
 __device__ __forceinline__ void record_atomics(const Arena& A, int c, const RootSums& R) {
@@ -1625,6 +1637,21 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
 // Root of segment x (after k_accumulate every parent is a root).
 __device__ __forceinline__ int seg_root(const int* P, int x) { return P[x]; }
 
+// The flip of a cluster of a chain without a field: the coin of root_record, keyed by the
+// chain-local index of the cluster's root, so it can be drawn wherever the root is known.  With
+// COIN the site pass draws it itself instead of reading k_cluster's flip array, and so runs
+// beside k_cluster instead of after it.
+struct CoinKey { uint64_t seed; uint32_t sweep; int slot_off; };
+__device__ __forceinline__ CoinKey coin_key(const Arena& A, int s) {
+  const int c = A.site_chain[s];
+  return CoinKey{A.ch[c].seed, A.ch_sweep[c], A.ch_slot_off[c]};
+}
+template <bool COIN>
+__device__ __forceinline__ uint8_t cluster_flip(const Arena& A, const CoinKey& k, int root) {
+  if (COIN) return philox(k.seed, k.sweep, (uint32_t)(root - k.slot_off), TAG_FLIP, 0).x < 0x80000000u ? 1 : 0;
+  return A.flip[root];
+}
+
 // Per site (one warp each): flip the tau = 0 spin with its bottom segment's cluster
 // (path_integral.C:822-823) and keep, in time order and in place at the start of the site's
 // segment range, the endpoints whose vertex is off-diagonal after the flips: the next sweep's
@@ -1635,6 +1662,7 @@ __device__ __forceinline__ int seg_root(const int* P, int x) { return P[x]; }
 // the new type at endpoint x is its old type ^ flip(cluster of x-1) ^ flip(cluster of x), the
 // same at both of its sites.  Every lane reads its step's segments before any lane writes, and a kept
 // endpoint never moves forward, so the in-place compaction reads no overwritten slot.
+template <bool COIN = false>
 __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
   const int lane = threadIdx.x & 31;
@@ -1643,7 +1671,8 @@ __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int
     const int s = sites ? sites[si] : si;
     const int base = A.sbase[s];
     const int k = A.sbase[s + 1] - base - 1;
-    const uint8_t fb = A.flip[seg_root(A.parent, base)];
+    const CoinKey ck = COIN ? coin_key(A, s) : CoinKey{0, 0, 0};
+    const uint8_t fb = cluster_flip<COIN>(A, ck, seg_root(A.parent, base));
     if (lane == 0 && fb) A.spin0[s] ^= 1u;
     uint8_t below = fb;   // flip of the cluster under the step's first segment
     int n = 0;
@@ -1654,8 +1683,8 @@ __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int
       int pa = 0, pb = 0;
       if (ja <= k) { ia = A.sinfo[base + ja]; pa = A.parent[base + ja]; }
       if (jb <= k) { ib = A.sinfo[base + jb]; pb = A.parent[base + jb]; }
-      if (ja <= k) fa = A.flip[pa];
-      if (jb <= k) fbb = A.flip[pb];
+      if (ja <= k) fa = cluster_flip<COIN>(A, ck, pa);
+      if (jb <= k) fbb = cluster_flip<COIN>(A, ck, pb);
       uint8_t prev_a = (uint8_t)__shfl_up_sync(0xFFFFFFFFu, (unsigned)fa, 1);
       uint8_t prev_b = (uint8_t)__shfl_up_sync(0xFFFFFFFFu, (unsigned)fbb, 1);
       const uint8_t top_a = (uint8_t)__shfl_sync(0xFFFFFFFFu, (unsigned)fa, 31);
@@ -1665,8 +1694,8 @@ __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int
       const bool kb = jb <= k && ((((ib & SI_OFF) ? 1u : 0u) ^ prev_b ^ fbb) != 0);
       uint64_t ta = 0, tb = 0;
       uint8_t da = 0, db = 0;
-      if (ka) { ta = A.stime[base + ja]; da = A.sdir[base + ja] & 7; }  // the list keeps the
-      if (kb) { tb = A.stime[base + jb]; db = A.sdir[base + jb] & 7; }  // incidence index
+      if (ka) { ta = A.stime[base + ja]; da = A.sdir[base + ja] & SD_IMASK; }  // the list keeps
+      if (kb) { tb = A.stime[base + jb]; db = A.sdir[base + jb] & SD_IMASK; }  // the incidence
       const unsigned balla = __ballot_sync(0xFFFFFFFFu, ka);
       const unsigned ballb = __ballot_sync(0xFFFFFFFFu, kb);
       __syncwarp();
@@ -1691,21 +1720,23 @@ __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int
 
 // Thread-per-site form of k_site_end for sites with few endpoints (kept entries never move
 // forward, so the in-place compaction reads no overwritten slot).
+template <bool COIN = false>
 __global__ void __launch_bounds__(256) k_site_end_narrow(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
   LG_GRID_STRIDE(i, nsites) {
     const int s = sites[i];
     const int base = A.sbase[s];
     const int k = A.sbase[s + 1] - base - 1;
-    uint8_t fprev = A.flip[seg_root(A.parent, base)];
+    const CoinKey ck = COIN ? coin_key(A, s) : CoinKey{0, 0, 0};
+    uint8_t fprev = cluster_flip<COIN>(A, ck, seg_root(A.parent, base));
     if (fprev) A.spin0[s] ^= 1u;
     int n = 0;
     for (int j = 1; j <= k; ++j) {
       const int x = base + j;
-      const uint8_t fx = A.flip[seg_root(A.parent, x)];
+      const uint8_t fx = cluster_flip<COIN>(A, ck, seg_root(A.parent, x));
       if ((((A.sinfo[x] & SI_OFF) ? 1u : 0u) ^ fprev ^ fx) != 0) {
         A.stime[base + n] = A.stime[x];
-        A.sdir[base + n] = A.sdir[x] & 7;  // the list keeps the incidence index
+        A.sdir[base + n] = A.sdir[x] & SD_IMASK;  // the list keeps the incidence index
         ++n;
       }
       fprev = fx;

@@ -128,7 +128,8 @@ struct lg_server {
     if (!specs.empty()) {
       ne.reset(new Engine());
       ne->stream_priority = ln.priority;
-      int rc = ne->build(specs);
+      // the smallest size class runs chain-resident where its chains fit a CTA
+      int rc = ne->build(specs, &ln == &lanes[0]);
       if (rc) return rc;
       if (ln.eng) {
         rc = ne->adopt(*ln.eng, from);

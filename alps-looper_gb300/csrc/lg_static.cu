@@ -327,7 +327,7 @@ extern "C" int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_
 
     // everything that must start at zero (or at the atomicMin identity)
     DChain hch{};
-    LG_CUDA(cudaMemcpyAsync(ch, &hch, sizeof(DChain), cudaMemcpyHostToDevice, st));
+    LG_CUDA(lg_copy_async(ch, &hch, sizeof(DChain), cudaMemcpyHostToDevice, st));
     LG_CUDA(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
     LG_CUDA(cudaMemsetAsync(A.bond_cnt, 0, nb * sizeof(int), st));
     LG_CUDA(cudaMemsetAsync(minfrag, 0xFF, (size_t)ns * sizeof(unsigned), st));
@@ -357,8 +357,8 @@ extern "C" int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_
     g_launches += nv > 0 ? 6 : 4;  // the scans and the sort count their own
     LG_CUDA(cudaGetLastError());
     int ng0 = 0, err = 0;
-    LG_CUDA(cudaMemcpyAsync(&ng0, totals, sizeof(int), cudaMemcpyDeviceToHost, st));
-    LG_CUDA(cudaMemcpyAsync(&err, &ctl->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    LG_CUDA(lg_copy_async(&ng0, totals, sizeof(int), cudaMemcpyDeviceToHost, st));
+    LG_CUDA(lg_copy_async(&err, &ctl->err, sizeof(int), cudaMemcpyDeviceToHost, st));
     LG_CUDA(cudaStreamSynchronize(st));
     if (err == 3) return lg_fail(LG_EINVAL, "lg_uf_label_static: bond or graph out of range");
     if (err) return lg_fail(LG_EITERCAP, "lg_uf_label_static: union-find failed (%d)", err);
@@ -373,7 +373,7 @@ extern "C" int lg_uf_label_static(int lattice, int L, int64_t nops, const int32_
     g_launches += ng0 > 0 ? 4 : 3;
     LG_CUDA(cudaGetLastError());
     int ncl = 0;
-    LG_CUDA(cudaMemcpyAsync(&ncl, totals + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    LG_CUDA(lg_copy_async(&ncl, totals + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     LG_CUDA(cudaStreamSynchronize(st));
     if (nfrag) *nfrag = nfrag_;
     if (nc) *nc = ncl;

@@ -4,7 +4,12 @@
 
 namespace lg {
 
-constexpr int MAXZ = 6;                 // largest coordination number (simple cubic)
+constexpr int MAXZ = 24;                // largest number of (virtual) bonds at a (virtual) site:
+                                        // 2 dim 2S, e.g. S = 2 on the simple-cubic lattice
+// segment direction byte (sdir): the incidence index of the segment's vertex at its site in
+// bits 0-4, the bond's lattice direction in bits 5-6
+constexpr int SD_DSHIFT = 5;
+constexpr int SD_IMASK = 31;
 constexpr int REC_WORDS = 32;           // uint64 words per sweep record
 constexpr int ITER_CAP = 1 << 22;       // union-find retry cap per union
 

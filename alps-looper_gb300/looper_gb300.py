@@ -68,11 +68,13 @@ class Shape(ctypes.Structure):
     """Launch shape of an arena (lg_shape): changes speed only, never a result."""
     _fields_ = [("insert_k", ctypes.c_double), ("narrow_k", ctypes.c_double),
                 ("acc_tile", ctypes.c_int), ("cl_tile", ctypes.c_int),
-                ("union_warps", ctypes.c_int), ("reserved", ctypes.c_int)]
+                ("union_warps", ctypes.c_int), ("resident", ctypes.c_int),
+                ("reserved", ctypes.c_int)]
 
     def as_dict(self):
         return {"insert_k": self.insert_k, "narrow_k": self.narrow_k, "acc_tile": self.acc_tile,
-                "cl_tile": self.cl_tile, "union_warps": self.union_warps}
+                "cl_tile": self.cl_tile, "union_warps": self.union_warps,
+                "resident": self.resident}
 
 
 class ServerStats(ctypes.Structure):
@@ -159,6 +161,7 @@ def lib():
             "lg_server_get_stats": (ctypes.c_int, [vp, vp]),
             "lg_server_destroy": (ctypes.c_int, [vp]),
             "lg_kernel_launches": (u64, []),
+            "lg_copy_bytes": (None, [vp, vp]),
             "lg_version": (ctypes.c_char_p, []),
         }
         for name, (res, args) in sig.items():
@@ -661,6 +664,13 @@ def uf_label_static(lattice, L, nops, d_bonds, d_graphs, d_labels, stream=0):
 
 def kernel_launches() -> int:
     return lib().lg_kernel_launches()
+
+
+def copy_bytes():
+    """(host -> device, device -> host) bytes copied by the library so far."""
+    a, b = ctypes.c_uint64(), ctypes.c_uint64()
+    lib().lg_copy_bytes(ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
 
 
 def version() -> str:

@@ -322,13 +322,21 @@ int lg_batch_validate_sweeps(lg_batch* b, int64_t n);
  *   narrow_k     the same split for the per-site merge and list compaction
  *   acc_tile     segments per CTA of the cluster-sum accumulation: 512, 1024 or 2048
  *   cl_tile      segments per CTA of the cluster flip / estimator kernel: 2048, 4096 or 8192
- *   union_warps  warps per CTA of the union-find kernel: 4, 8 or 16 */
+ *   union_warps  warps per CTA of the union-find kernel: 4, 8 or 16
+ *   resident     1: the chain-resident path, where every chain of the arena qualifies (S = 1/2,
+ *                no correlation measurement, a sweep's operators within one CTA's shared memory):
+ *                one CTA per chain runs a whole chunk of up to 64 sweeps in one launch, with the
+ *                sweep's vertices, segments and union-find forest in shared memory; 0: the grid
+ *                path (one CUDA graph of grid-wide kernels per sweep).  lg_create and
+ *                lg_batch_create start small arenas on the resident path; a chain that outgrows a
+ *                CTA moves to the grid path by itself. */
 typedef struct lg_shape {
   double insert_k;
   double narrow_k;
   int acc_tile;
   int cl_tile;
   int union_warps;
+  int resident;
   int reserved;
 } lg_shape;
 
@@ -436,6 +444,9 @@ const char* lg_kernel_name(int k);
 /* ---- build / device info ------------------------------------------------------------------ */
 /* Number of device kernel launches issued by this process so far (all handles). */
 uint64_t lg_kernel_launches(void);
+/* Bytes this library has copied host -> device and device -> host so far (all handles); either
+ * pointer may be NULL.  A measurement seam: the end-to-end benchmark counts its transfers. */
+void lg_copy_bytes(uint64_t* h2d, uint64_t* d2h);
 /* Version string (engine and CUDA). */
 const char* lg_version(void);
 

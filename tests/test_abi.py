@@ -185,8 +185,8 @@ def test_invalid_models_are_rejected_before_device_work(lg):
         (dict(LATTICE="chain", L=8, T=1.0, FORCE_SCATTER=float("nan")), -1),
         (dict(LATTICE="cubic", L=162, T=1.0), -6),                        # > 2^22 sites: EBUDGET
         (dict(LATTICE="square", L=7, T=1.0), -4),                         # sign problem
-        (dict(LATTICE="square", L=8, T=1.0, local_S=1), -4),              # 8 virtual neighbours
-        (dict(LATTICE="chain", L=8, T=1.0, local_S=2.5), -4),             # S > 3/2 on a chain
+        (dict(LATTICE="cubic", L=4, T=1.0, local_S=2.5), -4),             # 30 virtual neighbours
+        (dict(LATTICE="chain", L=8, T=1.0, local_S=4.5), -4),             # 2S > 8 virtual sites
         (dict(LATTICE="chain", L=8, T=1.0, local_S=1, MEASURE_CORRELATIONS=True), -4),
         (dict(LATTICE="chain", L=8, T=1.0, MEASURE_CORRELATIONS=True, INITIAL_SITE=8), -1),
     ]

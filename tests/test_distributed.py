@@ -57,7 +57,7 @@ def test_reference_arm_under_torchrun_two_ranks():
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py",
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3"]
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3", "--ref-warmup", "1"]
     env = dict(os.environ, OMP_NUM_THREADS="1")
     r = subprocess.run(cmd, cwd=REPO, capture_output=True, text=True, timeout=600, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
@@ -67,3 +67,4 @@ def test_reference_arm_under_torchrun_two_ranks():
     assert out["impl"] == "reference" and out["n_gpus"] == 2
     assert out["value"] > 0 and out["cpu_baseline"]["kind"] == "port"
     assert out["e2e"]["h2d_bytes_per_step"] == 0
+    assert out["steps"] == 1 and out["operators_per_s"] > 0

@@ -1,7 +1,7 @@
 """GPU parity: the CUDA sweep against the CPU oracle and the reference's golden data.
 
 * cluster labels of dumped configurations == the reference union_find.h (deterministic unify),
-  partitions == the default weighted unify                                  (bit exact)
+  partitions == the default weighted unify, up to 1.2e6 vertices            (bit exact)
 * whole trajectories (spins, operator strings, per-sweep integer records) == the oracle
   running the same random streams, for Heisenberg / XXZ / Ising / ferromagnet / field models
   on chain, square and cubic lattices                                      (bit exact)
@@ -39,6 +39,31 @@ def test_uf_labels_bit_exact_vs_reference_union_find(lg, golden, idx):
     assert nc == c["nc"]
     assert lab.tolist() == c["labels_deterministic"]
     assert _canon(lab) == _canon(c["labels_weighted"])
+
+
+@pytest.mark.parametrize("name", ["square32_b16", "square128_b64"])
+def test_uf_labels_at_scale_bit_exact_vs_reference_union_find(lg, golden, name):
+    """Configurations of 2e4 and 1.2e6 vertices (the latter the bench workload's size, where the
+    lock-free unions really race), made again by the oracle from their seeds: the GPU labels equal
+    those of the reference's own looper/union_find.h (deterministic unify), compiled in place in
+    the build container (tests/golden/make_uf_scale.py)."""
+    import hashlib
+    import os
+    meta = golden("uf_scale.json")[name]
+    o = orc.Oracle(meta["dim"], meta["L"], meta["beta"], 1.0, 1.0, 0.0, seed=meta["seed"])
+    o.sweep(meta["sweeps"])
+    cfg = o.last_config()
+    o.close()
+    bonds = np.asarray(cfg["bonds"], dtype=np.int32)
+    graphs = np.asarray(cfg["graphs"], dtype=np.int32)
+    sha = hashlib.sha256(bonds.astype("<i4").tobytes() + graphs.astype("<i4").tobytes()).hexdigest()
+    assert sha == meta["config_sha256"]          # the same configuration as in the build container
+    lab, nc = lg.uf_label(meta["dim"], meta["L"], bonds, graphs)
+    assert nc == meta["nc"] and len(lab) == meta["nfrag"]
+    assert hashlib.sha256(np.asarray(lab, dtype="<i4").tobytes()).hexdigest() == meta["labels_sha256"]
+    if name == "square32_b16":
+        z = np.load(os.path.join(os.path.dirname(__file__), "golden", "uf_scale_32.npz"))
+        assert np.array_equal(z["labels"], lab)
 
 
 def test_uf_labels_random_configs_vs_oracle(lg):
@@ -90,11 +115,16 @@ def _assert_same_state(g, o):
     assert gt.view(np.uint64).tolist() == ot.view(np.uint64).tolist()
 
 
+@pytest.mark.parametrize("path", ["grid", "resident"])
 @pytest.mark.parametrize("name", sorted(MODELS))
-def test_trajectory_bit_exact_vs_oracle(lg, name):
+def test_trajectory_bit_exact_vs_oracle(lg, name, path):
+    """Both sweep paths: the grid path (one CUDA graph of grid-wide kernels per sweep) and the
+    chain-resident path (one CTA per chain, whole chunks of sweeps in shared memory)."""
     m = MODELS[name]
     seed = 1234 + len(name)
     g = _gpu_chain(lg, m, seed)
+    g.shape = dict(resident=1 if path == "resident" else 0)
+    assert g.shape["resident"] == (path == "resident")
     g.keep_records(True)
     o = orc.Oracle(m["dim"], m["L"], m["beta"], m["jxy"], m["jz"], m["h"], seed=seed)
     for _ in range(4):
@@ -109,6 +139,27 @@ def test_trajectory_bit_exact_vs_oracle(lg, name):
     g.close()
 
 
+def test_resident_equals_grid_over_a_long_run(lg):
+    """The two sweep paths agree bit for bit over thousands of sweeps (chunks of 64 sweeps per
+    resident launch), on the CPU-runnable chain workload's model."""
+    def mk(res):
+        w = lg.LoopWorker(lg.make_params(LATTICE="chain", L=16, T=0.1, J=1.0, SEED=1234,
+                                         SWEEPS=1 << 14, THERMALIZATION=1 << 12,
+                                         INITIAL_SPINS="random"))
+        w.shape = dict(resident=res)
+        w.keep_records(True)
+        return w
+    a, b = mk(1), mk(0)
+    for _ in range(5):
+        a.run(1000)
+        b.run(1000)
+        assert (a.fetch_records() == b.fetch_records()).all()
+    for x, y in zip(a.state(), b.state()):
+        assert np.array_equal(x, y)
+    a.close()
+    b.close()
+
+
 def test_all_up_start_matches_oracle(lg):
     m = MODELS["square8_heisenberg"]
     g = _gpu_chain(lg, m, 5, random_spins=False)
@@ -119,7 +170,8 @@ def test_all_up_start_matches_oracle(lg):
     _assert_same_state(g, o)
 
 
-def test_batch_member_equals_alone(lg):
+@pytest.mark.parametrize("path", ["grid", "resident"])
+def test_batch_member_equals_alone(lg, path):
     names = ["square8_heisenberg", "chain16_heisenberg", "cubic4_xxz_field", "chain10_ising"]
     params = []
     for i, n in enumerate(names):
@@ -128,6 +180,7 @@ def test_batch_member_equals_alone(lg):
                                      Jz=m["jz"], h=m["h"], SEED=77 + i, SWEEPS=1000,
                                      THERMALIZATION=0, INITIAL_SPINS="random"))
     b = lg.Batch(params)
+    b.shape = dict(resident=1 if path == "resident" else 0)
     b.chain(0).keep_records(True)
     b.run(30)
     for i, p in enumerate(params):

@@ -1,8 +1,9 @@
 """Launch shapes and the autotuner change speed only, never a result.
 
-A shape picks, per arena, which chains run insertion / merge / list compaction with a thread per
-bond or site ("narrow") instead of a warp per site, and the CTA sizes of the union-find, cluster
-sum and cluster flip kernels.  Every shape must give the same trajectories and the same exact
+A shape picks, per arena, the path (chain-resident: one CTA per chain, whole chunks of sweeps in
+shared memory; or the grid path of grid-wide kernels) and, on the grid path, which chains run
+insertion / merge / list compaction with a thread per bond or site ("narrow") instead of a warp
+per site, and the CTA sizes of the union-find, cluster sum and cluster flip kernels.  Every shape must give the same trajectories and the same exact
 per-sweep sums, so the arena below (chains of mixed lattices, temperatures, anisotropy and field,
 all smaller than one k_cluster tile so that the per-chain reductions of tiles spanning chains are
 exercised) is run under several shapes and compared bit for bit.
@@ -31,10 +32,11 @@ MODELS = [
 ]
 
 SHAPES = [
-    dict(insert_k=0.0, narrow_k=0.0),                             # every chain warp-per-site
-    dict(insert_k=1e300, narrow_k=1e300),                         # every chain thread-per-site
-    dict(insert_k=1e300, narrow_k=10.0, acc_tile=512, cl_tile=2048, union_warps=4),
-    dict(insert_k=10.0, narrow_k=32.0, acc_tile=2048, cl_tile=8192, union_warps=16),
+    dict(insert_k=0.0, narrow_k=0.0, resident=0),                 # every chain warp-per-site
+    dict(insert_k=1e300, narrow_k=1e300, resident=0),             # every chain thread-per-site
+    dict(insert_k=1e300, narrow_k=10.0, acc_tile=512, cl_tile=2048, union_warps=4, resident=0),
+    dict(insert_k=10.0, narrow_k=32.0, acc_tile=2048, cl_tile=8192, union_warps=16, resident=0),
+    dict(resident=1),                                             # one CTA per chain
 ]
 
 
@@ -118,7 +120,8 @@ def test_single_chain_autotune(lg):
 def test_single_chain_shape_roundtrip(lg):
     w = lg.LoopWorker(lg.make_params(LATTICE="cubic", L=4, BETA=2.0, SEED=9, SWEEPS=4096,
                                      THERMALIZATION=0))
-    w.shape = dict(insert_k=1e300, narrow_k=1e300, acc_tile=512, cl_tile=2048, union_warps=16)
+    w.shape = dict(insert_k=1e300, narrow_k=1e300, acc_tile=512, cl_tile=2048, union_warps=16,
+                   resident=0)
     sh = w.shape
     assert sh["acc_tile"] == 512 and sh["cl_tile"] == 2048 and sh["union_warps"] == 16
     w.run(5)
@@ -132,3 +135,21 @@ def test_single_chain_shape_roundtrip(lg):
     np.testing.assert_array_equal(spins_a, spins_b)
     np.testing.assert_array_equal(bonds_a, bonds_b)
     np.testing.assert_array_equal(times_a.view(np.uint64), times_b.view(np.uint64))
+
+
+def test_paths_switch_mid_run_without_changing_the_trajectory(lg):
+    """A batch moved between the chain-resident and the grid path every few sweeps (the state
+    moves with it: spins, off-diagonal lists, sweep counters, accumulators) ends where the same
+    batch run on one path ends."""
+    ref = lg.Batch(_params(lg))
+    ref.shape = dict(resident=0)
+    ref.run(45)
+    want = _snapshot(ref)
+    ref.close()
+    b = lg.Batch(_params(lg))
+    for k, res in ((7, 1), (10, 0), (3, 1), (25, 0)):
+        b.shape = dict(resident=res)
+        assert b.shape["resident"] == res
+        b.run(k)
+    _assert_same(want, _snapshot(b))
+    b.close()

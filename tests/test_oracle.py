@@ -217,6 +217,18 @@ def test_philox_spin3half_xxz_field_chain_vs_ed():
                  ["Energy", "Specific Heat", "Magnetization", "Susceptibility"], spin2=3)
 
 
+def test_philox_square_spin1_vs_ed():
+    # S = 1 on the 2x2 square lattice: 8 virtual spin-1/2 bonds meet at every virtual site
+    _check_vs_ed(2, 2, 0.5, 1.0, 1.0, 0.0, 1000, 20000, 15,
+                 ["Energy", "Specific Heat", "Susceptibility", "Staggered Magnetization^2"], spin2=2)
+
+
+def test_philox_cubic_spin1_xxz_field_vs_ed():
+    # S = 1 XXZ in a field on the 2x2x2 cube: 12 virtual bonds per virtual site
+    _check_vs_ed(3, 2, 1.0, 1.0, 0.5, 0.2, 1000, 10000, 16,
+                 ["Energy", "Magnetization", "Susceptibility"], spin2=2)
+
+
 def test_philox_cubic_xxz_field_vs_ed():
     # simple cubic L = 2 (8 sites; the periodic wrap doubles every bond, in ED as in the engine)
     _check_vs_ed(3, 2, 0.5, 1.0, 0.5, 0.3, 1000, 30000, 14,
@@ -271,3 +283,35 @@ def test_oracle_cluster_count_vs_exact_ising_ring():
     m, e = orc.binned(o.records()[:, 1].astype(np.float64))
     exact = orc.ising_ring_clusters(4, 0.5, 1.0)
     assert abs(m - exact) <= 3.5 * e, (m, e, exact)
+
+
+def _scale_case(golden, name):
+    import hashlib
+    import os
+    meta = golden("uf_scale.json")[name]
+    o = orc.Oracle(meta["dim"], meta["L"], meta["beta"], 1.0, 1.0, 0.0, seed=meta["seed"])
+    o.sweep(meta["sweeps"])
+    cfg = o.last_config()
+    o.close()
+    bonds = np.asarray(cfg["bonds"], dtype=np.int32)
+    graphs = np.asarray(cfg["graphs"], dtype=np.int32)
+    sha = hashlib.sha256(bonds.astype("<i4").tobytes() + graphs.astype("<i4").tobytes()).hexdigest()
+    return meta, bonds, graphs, sha
+
+
+@pytest.mark.parametrize("name", ["square32_b16", "square128_b64"])
+def test_uf_labels_at_scale_match_reference_union_find(golden, name):
+    """Configurations of 2e4 and 1.2e6 vertices (the bench workload's size), made again by the
+    oracle from their seeds, labelled by the oracle's union-find: the same labels as the
+    reference's own looper/union_find.h (deterministic unify) gave in the build container."""
+    import hashlib
+    import os
+    meta, bonds, graphs, sha = _scale_case(golden, name)
+    assert len(bonds) == meta["nops"] and sha == meta["config_sha256"]
+    lab, nc = orc.uf_label(meta["dim"], meta["L"], bonds, graphs, deterministic=True)
+    assert nc == meta["nc"] and len(lab) == meta["nfrag"]
+    assert hashlib.sha256(np.asarray(lab, dtype="<i4").tobytes()).hexdigest() == meta["labels_sha256"]
+    if name == "square32_b16":
+        z = np.load(os.path.join(os.path.dirname(__file__), "golden", "uf_scale_32.npz"))
+        assert np.array_equal(z["bonds"], bonds) and np.array_equal(z["graphs"], graphs)
+        assert np.array_equal(z["labels"], lab)
