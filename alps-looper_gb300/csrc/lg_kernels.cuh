@@ -170,7 +170,7 @@ __device__ int insert_bond_serial(const Arena& A, int b, int out0, uint64_t* lt 
       const uint32_t wu = (k & 1u) ? r.z : r.x;
       const uint32_t wg = (k & 1u) ? r.w : r.y;
       ++k;
-      const uint32_t tail = (wu >> 9) ? 0u : philox(ch.seed, sweep, bl, TAG_TAIL, k - 1).x;
+      const uint32_t tail = (wu >> 9) ? 0u : gap_tail_word(ch.seed, sweep, bl, k - 1);
       const float gap = __fmul_rn(-log_open(gap_uniform(wu, tail)), ch.inv_rate);
       const uint64_t q = gap_fix52(gap, ((uint64_t)(wu & 0x1FFu) << 16) | (wg & 0xFFFFu));
       if (q >= FIX52_ONE) { more = false; return; }
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(INS_WARPS * 32, 7) k_insert(Arena A, const int
         const uint32_t rw = __shfl_xor_sync(0xFFFFFFFFu, r.w, 1);
         const uint32_t wu = (k & 1u) ? rz : r.x;
         const uint32_t wg = (k & 1u) ? rw : r.y;
-        const uint32_t tail = (wu >> 9) ? 0u : philox(ch.seed, sweep, bl, TAG_TAIL, k).x;
+        const uint32_t tail = (wu >> 9) ? 0u : gap_tail_word(ch.seed, sweep, bl, k);
         const float gap = __fmul_rn(-log_open(gap_uniform(wu, tail)), ch.inv_rate);
         uint64_t q = gap_fix52(gap, ((uint64_t)(wu & 0x1FFu) << 16) | (wg & 0xFFFFu));
         const bool stop = q >= FIX52_ONE;

@@ -79,6 +79,13 @@ __device__ __forceinline__ float gap_uniform(uint32_t w, uint32_t tail) {
   return (w >> 9) ? uniform_open(w) : __fmul_rn(uniform_open(tail), 1.1920928955078125e-7f);
 }
 
+// The refining word of proposal k of a bond (needed in the lowest bin only, once per 2^23
+// draws), kept out of line so that the common path carries no second Philox.
+__device__ __noinline__ uint32_t gap_tail_word(uint64_t seed, uint32_t sweep, uint32_t bond,
+                                               uint32_t k) {
+  return philox(seed, sweep, bond, TAG_TAIL, k).x;
+}
+
 // exp(x), |x| <= 80 (clamped): x = k ln2 + r, degree-7 Taylor polynomial, times 2^k.
 __device__ __forceinline__ float exp_clamped(float x) {
   x = fminf(fmaxf(x, -80.0f), 80.0f);

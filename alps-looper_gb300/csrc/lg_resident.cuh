@@ -158,7 +158,7 @@ __device__ int res_insert_bond(const Arena& A, const ResSmem& M, const DChain& c
     const uint32_t wu = (k & 1u) ? r.z : r.x;
     const uint32_t wg = (k & 1u) ? r.w : r.y;
     ++k;
-    const uint32_t tail = (wu >> 9) ? 0u : philox(ch.seed, sweep, (uint32_t)bl, TAG_TAIL, k - 1).x;
+    const uint32_t tail = (wu >> 9) ? 0u : gap_tail_word(ch.seed, sweep, (uint32_t)bl, k - 1);
     const float gap = __fmul_rn(-log_open(gap_uniform(wu, tail)), ch.inv_rate);
     const uint64_t q = gap_fix52(gap, ((uint64_t)(wu & 0x1FFu) << 16) | (wg & 0xFFFFu));
     if (q >= FIX52_ONE) { more = false; return; }
