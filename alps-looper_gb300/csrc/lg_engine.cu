@@ -28,6 +28,7 @@
 #include "lg_kernels.cuh"
 #include "lg_host.h"
 #include "lg_resident.cuh"
+#include "lg_sse.cuh"
 
 using namespace lg;
 
@@ -150,7 +151,6 @@ struct Engine {
   // spin correlations: k_corr work tiles and the per-chunk exact sums (arena site indexed)
   int n_corr_tiles = 0, corr_smem = 0;
   bool any_spin_s = false;   // some chain has S > 1/2: k_boundary closes its sites
-  bool all_nofield = false;  // no chain has a field: flips are coins (the site pass draws them)
   // structural checks between stages (lg_validate_sweeps): the failure counter and first code;
   // never part of a captured graph
   int* val_bad = nullptr;
@@ -204,6 +204,14 @@ struct Engine {
   DBuf<uint8_t> rb_spin0, rb_sdir;
   DBuf<int> rb_off_base, rb_off_cnt;
   DBuf<uint64_t> rb_stime;
+  // ---- the SSE form (k_sse: one thread per chain): operator strings of sse_ocap entries per
+  // chain, double-buffered with the spins (rb_spin0) like the resident path's state
+  bool sse = false;
+  int sse_ocap = 0, sse_fcap = 0, sse_grid = 0;
+  DBuf<uint32_t> sse_ops, sse_ops_b, sse_ops_t;
+  DBuf<int> sse_nop, sse_nop_b, sse_loops, sse_frag, sse_wnd, sse_cur;
+  DBuf<long long> sse_est;
+  DBuf<uint8_t> sse_spc, sse_flip;
 
   ~Engine() {
     if (gexec) cudaGraphExecDestroy(gexec);
@@ -355,12 +363,17 @@ struct Engine {
     LG_CUDA(cudaMemset(d_ctl.p, 0, sizeof(Ctl)));
     if ((rc = build_corr())) return rc;
     any_spin_s = false;
-    all_nofield = true;
     for (int c = 0; c < C; ++c) {
       any_spin_s |= spec[c].spin2 > 1;
-      all_nofield &= hch[c].field == 0;
     }
-    if (allow_resident && res_fits(res_vcap_for(1.0), RES_SMEM_DEFAULT)) {
+    bool any_sse = false, all_sse = true;
+    for (auto& s : spec) { any_sse |= s.sse; all_sse &= s.sse; }
+    if (any_sse && !all_sse)
+      return lg_fail(LG_EINVAL, "an arena holds either path-integral or SSE chains, not both");
+    sse = any_sse;
+    if (sse) {
+      if ((rc = setup_sse(res_vcap_for(1.0), false))) return rc;
+    } else if (allow_resident && res_fits(res_vcap_for(1.0), RES_SMEM_DEFAULT)) {
       if ((rc = setup_resident(res_vcap_for(1.0)))) return rc;
       shape = default_shape();
       shape.resident = 1;
@@ -381,6 +394,152 @@ struct Engine {
         LG_CUDA(lg_copy_async(d_spin0.p + hch[c].site_off, sp.data(), sp.size(), cudaMemcpyHostToDevice, st));
       }
     LG_CUDA(cudaStreamSynchronize(st));
+    return LG_OK;
+  }
+
+  // ---- the SSE form ----
+  // Buffers for ocap operators per chain.  With keep, the current strings, counts and spins
+  // survive (an overflow grows the capacity and replays the chunk).
+  int setup_sse(int ocap, bool keep) {
+    std::vector<uint32_t> ops;
+    std::vector<int> nops;
+    if (keep) {
+      ops.resize((size_t)C * sse_ocap);
+      nops.resize(C);
+      LG_CUDA(lg_copy(ops.data(), sse_ops.p, ops.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+      LG_CUDA(lg_copy(nops.data(), sse_nop.p, C * sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    int nmax = 0;
+    for (auto& s : spec) nmax = std::max(nmax, s.N);
+    const long long fc = (long long)nmax + ocap;
+    if ((long long)C * fc * 8 > (1ll << 34))
+      return lg_fail(LG_EBUDGET, "SSE arena too large (%d chains of %lld fragments)", C, fc);
+    const int old_ocap = sse_ocap;
+    sse_ocap = ocap;
+    sse_fcap = (int)fc;
+    const size_t oc = (size_t)C * ocap, fcn = (size_t)C * fc;
+    int rc;
+    if ((rc = sse_ops.alloc(oc)) || (rc = sse_ops_b.alloc(oc)) || (rc = sse_ops_t.alloc(oc)) ||
+        (rc = sse_nop.alloc(C)) || (rc = sse_nop_b.alloc(C)) || (rc = sse_loops.alloc(2 * oc)) ||
+        (rc = sse_frag.alloc(fcn)) || (rc = sse_est.alloc(8 * fcn)) || (rc = sse_wnd.alloc(3 * fcn)) ||
+        (rc = sse_cur.alloc(N)) || (rc = sse_spc.alloc(N)) || (rc = sse_flip.alloc(fcn)) ||
+        (rc = rb_spin0.alloc(N)) || (rc = d_rec.alloc((size_t)rec_rows * C * REC_WORDS)))
+      return rc;
+    if (keep) {
+      std::vector<uint32_t> nw(oc, 0u);
+      for (int c = 0; c < C; ++c)
+        for (int i = 0; i < nops[c] && i < ocap; ++i) nw[(size_t)c * ocap + i] = ops[(size_t)c * old_ocap + i];
+      LG_CUDA(lg_copy(sse_ops.p, nw.data(), oc * sizeof(uint32_t), cudaMemcpyHostToDevice));
+      LG_CUDA(lg_copy(sse_nop.p, nops.data(), C * sizeof(int), cudaMemcpyHostToDevice));
+    } else {
+      LG_CUDA(cudaMemset(sse_nop.p, 0, C * sizeof(int)));
+    }
+    sse_grid = std::max(1, std::min((C + SSE_THREADS - 1) / SSE_THREADS, nsm * 16));
+    return LG_OK;
+  }
+
+  // run() on the SSE form: chunks of up to rec_rows sweeps, one k_sse launch each; a chunk in
+  // which a string outgrows its capacity is dropped and replayed after the capacity grows.
+  int run_sse(long long n, float* ms, size_t flush_bytes) {
+    DBuf<uint8_t> flushbuf;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ms) {
+      if (flush_bytes) { int rc = flushbuf.alloc(flush_bytes); if (rc) return rc; }
+      LG_CUDA(cudaEventCreate(&e0));
+      LG_CUDA(cudaEventCreate(&e1));
+    }
+    struct EvG { cudaEvent_t a, b; ~EvG() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); } } eg{e0, e1};
+    long long done_total = 0;
+    while (n > 0) {
+      const int m = (int)std::min<long long>(n, rec_rows);
+      SseArgs S;
+      S.m = m; S.ocap = sse_ocap; S.fcap = sse_fcap;
+      S.spin_in = d_spin0.p; S.spin_out = rb_spin0.p;
+      S.ops_in = sse_ops.p; S.ops_out = sse_ops_b.p; S.ops_tmp = sse_ops_t.p;
+      S.nop_in = sse_nop.p; S.nop_out = sse_nop_b.p;
+      S.loops = sse_loops.p; S.frag = sse_frag.p; S.est = sse_est.p; S.wnd = sse_wnd.p;
+      S.cur = sse_cur.p; S.spc = sse_spc.p; S.flipf = sse_flip.p;
+      if (ms) {
+        if (flush_bytes) LG_CUDA(cudaMemsetAsync(flushbuf.p, (int)(done_total & 0xFF), flush_bytes, st));
+        LG_CUDA(cudaEventRecord(e0, st));
+      }
+      k_sse<<<sse_grid, SSE_THREADS, 0, st>>>(arena(), S);
+      ++g_launches;
+      if (ms) LG_CUDA(cudaEventRecord(e1, st));
+      LG_CUDA(cudaGetLastError());
+      Ctl hc;
+      LG_CUDA(lg_copy_async(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+      LG_CUDA(cudaStreamSynchronize(st));
+      if (hc.err) {
+        std::vector<uint32_t> sw(C);
+        for (int c = 0; c < C; ++c) sw[c] = (uint32_t)spec[c].mcs;
+        LG_CUDA(lg_copy(d_sweep.p, sw.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        Ctl z0 = hc;
+        z0.err = 0;
+        LG_CUDA(lg_copy(d_ctl.p, &z0, sizeof(Ctl), cudaMemcpyHostToDevice));
+        if (hc.err != ERR_OVERFLOW) return lg_fail(LG_EDEVICE, "SSE sweep failed (%d)", hc.err);
+        const long long o2 = std::min<long long>(1ll << 28, ((long long)sse_ocap * 3 / 2 + 63) & ~31ll);
+        if (o2 <= sse_ocap) return lg_fail(LG_EBUDGET, "SSE operator string too long");
+        int rc = setup_sse((int)o2, true);
+        if (rc) return rc;
+        continue;
+      }
+      d_spin0.swap(rb_spin0);
+      sse_ops.swap(sse_ops_b);
+      sse_nop.swap(sse_nop_b);
+      hrec.resize((size_t)m * C * REC_WORDS);
+      LG_CUDA(lg_copy(hrec.data(), d_rec.p, hrec.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+      int rc = consume(m);
+      if (rc) return rc;
+      if (ms) {
+        float t = 0;
+        LG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        for (int i = 0; i < m; ++i) ms[done_total + i] = t / m;
+      }
+      done_total += m;
+      n -= m;
+    }
+    return LG_OK;
+  }
+
+  // The SSE state of chain c: spins and the whole operator string (bond << 1 | off-diagonal).
+  int sse_get(int c, std::vector<int32_t>& spins, std::vector<uint32_t>& ops) {
+    const ChainSpec& s = spec[c];
+    std::vector<uint8_t> sp(s.N);
+    LG_CUDA(lg_copy(sp.data(), d_spin0.p + hch[c].site_off, s.N, cudaMemcpyDeviceToHost));
+    spins.assign(sp.begin(), sp.end());
+    int n = 0;
+    LG_CUDA(lg_copy(&n, sse_nop.p + c, sizeof(int), cudaMemcpyDeviceToHost));
+    ops.resize(n);
+    if (n) LG_CUDA(lg_copy(ops.data(), sse_ops.p + (size_t)c * sse_ocap, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return LG_OK;
+  }
+
+  // Replace chain c's SSE state (checked first: bonds in range, and every site's spin periodic
+  // through the string).
+  int sse_set(int c, const int32_t* spins, const std::vector<uint32_t>& ops, uint64_t sweep) {
+    const ChainSpec& s = spec[c];
+    std::vector<uint8_t> sp(s.N), cur(s.N);
+    for (int i = 0; i < s.N; ++i) cur[i] = sp[i] = (uint8_t)(spins[i] & 1);
+    for (size_t i = 0; i < ops.size(); ++i) {
+      const uint32_t b = ops[i] >> 1;
+      if ((int)b >= s.NB) return lg_fail(LG_EINVAL, "operator %zu out of range", i);
+      if (ops[i] & 1u) { cur[s.s0[b]] ^= 1u; cur[s.s1[b]] ^= 1u; }
+    }
+    for (int i = 0; i < s.N; ++i)
+      if (cur[i] != sp[i])
+        return lg_fail(LG_EINVAL, "site %d: the string is not periodic in imaginary time", i);
+    if ((long long)ops.size() > sse_ocap) {
+      int rc = setup_sse((int)std::min<long long>(1ll << 28, ((long long)ops.size() * 3 / 2 + 63) & ~31ll), true);
+      if (rc) return rc;
+    }
+    const int n = (int)ops.size();
+    LG_CUDA(lg_copy(sse_nop.p + c, &n, sizeof(int), cudaMemcpyHostToDevice));
+    if (n) LG_CUDA(lg_copy(sse_ops.p + (size_t)c * sse_ocap, ops.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    LG_CUDA(lg_copy(d_spin0.p + hch[c].site_off, sp.data(), s.N, cudaMemcpyHostToDevice));
+    const uint32_t sw = (uint32_t)sweep;
+    LG_CUDA(lg_copy(d_sweep.p + c, &sw, sizeof(uint32_t), cudaMemcpyHostToDevice));
+    spec[c].mcs = sweep;
     return LG_OK;
   }
 
@@ -738,6 +897,7 @@ struct Engine {
 
   // Adopt a launch shape: classify chains as narrow or wide and upload the class lists.
   int set_shape(const Shape& sh) {
+    if (sse) { shape = sh; return LG_OK; }  // the SSE form has no launch shape
     if (!(sh.acc_tile == 512 || sh.acc_tile == 1024 || sh.acc_tile == 2048) ||
         !(sh.cl_tile == 2048 || sh.cl_tile == 4096 || sh.cl_tile == 8192) ||
         !(sh.un_warps == 4 || sh.un_warps == 8 || sh.un_warps == 16) || !(sh.narrow_k >= 0) ||
@@ -887,22 +1047,6 @@ struct Engine {
     }
     mark(4);
     launches += 2;
-    // Without a field every cluster's flip is a coin keyed by its root, which the site pass can
-    // draw itself: it then runs on the second stream beside k_cluster (whose flip array it no
-    // longer reads), and k_end follows both.
-    const bool coin = all_nofield;
-    if (coin) {
-      cudaEventRecord(ev_fork, st);
-      cudaStreamWaitEvent(st2, ev_fork, 0);
-      if (n_wide) {
-        k_site_end<true><<<grid_for((long long)n_wide * 32, 256, 16), 256, 0, st2>>>(A, wide_list, n_wide);
-        ++launches;
-      }
-      if (n_narrow) {
-        k_site_end_narrow<true><<<grid_for(n_narrow, 256, 16), 256, 0, st2>>>(A, d_narrow_sites.p, n_narrow);
-        ++launches;
-      }
-    }
     {
       const int t = shape.cl_tile, g = (ns_cap + t - 1) / t;  // one tile per block
       if (t == 2048) k_cluster<2048><<<g, CL_THREADS, 0, st>>>(A);
@@ -911,20 +1055,6 @@ struct Engine {
     }
     mark(5);
     launches += 1;
-    if (coin) {
-      cudaEventRecord(ev_join, st2);
-      cudaStreamWaitEvent(st, ev_join, 0);
-      if (n_corr_tiles) {
-        k_corr<<<n_corr_tiles, CORR_THREADS, corr_smem, st>>>(A);
-        ++launches;
-      }
-      k_end<<<1, 1024, 0, st>>>(A);
-      mark(6);
-      launches += 1;
-      sweep_launches = launches;
-      g_launches += launches;
-      return;
-    }
     // k_end (counters, the next record row, claim counters) needs nothing of the site pass, so
     // it runs beside it on a third stream; k_corr reads the sweep counter before k_end advances
     // it, so with correlations the order stays sequential
@@ -976,6 +1106,7 @@ struct Engine {
   // Run n sweeps of every chain.  With ms != nullptr every sweep is bracketed by events and
   // preceded by an L2 flush of flush_bytes (outside the brackets).
   int run(long long n, float* ms = nullptr, size_t flush_bytes = 0) {
+    if (sse) return run_sse(n, ms, flush_bytes);
     if (resident) return run_resident(n, ms, flush_bytes);
     DBuf<uint8_t> flushbuf;
     std::vector<cudaEvent_t> ev;
@@ -1051,6 +1182,7 @@ struct Engine {
 
   // n sweeps launched kernel by kernel with events between stages (no graph).
   int profile(long long n, size_t flush_bytes, double* kernel_ms, long long* vertices) {
+    if (sse) return lg_fail(LG_EUNSUPPORTED, "the per-kernel profile is a path-integral measurement");
     if (resident) {  // the per-kernel profile is a grid-path measurement
       int rc = to_grid();
       if (rc) return rc;
@@ -1104,6 +1236,10 @@ struct Engine {
   // with the narrow / wide split, and the fastest shape is kept.  The timed sweeps are the
   // chains' own sweeps: no shape changes a result, so tuning costs no extra sweeps.
   int autotune(int trial, size_t flush_bytes, std::string& report) {
+    if (sse) {  // one thread per chain: nothing to choose
+      report = "chosen: SSE form (one thread per chain)\n";
+      return run(trial);
+    }
     if (trial < 1) trial = 1;
     char line[160];
     report.clear();
@@ -1266,6 +1402,15 @@ struct Engine {
   // ---- state access (test seams, checkpoints) ----
   int get_state(int c, std::vector<int32_t>& spins, std::vector<int32_t>& bonds,
                 std::vector<double>& times) {
+    if (sse) {  // the off-diagonal operators, with (index + 1/2) / n as their time (the order)
+      std::vector<uint32_t> ops;
+      int rc = sse_get(c, spins, ops);
+      if (rc) return rc;
+      bonds.clear(); times.clear();
+      for (size_t i = 0; i < ops.size(); ++i)
+        if (ops[i] & 1u) { bonds.push_back((int32_t)(ops[i] >> 1)); times.push_back((i + 0.5) / ops.size()); }
+      return LG_OK;
+    }
     const ChainSpec& s = spec[c];
     int so = hch[c].site_off;
     std::vector<uint8_t> sp(s.N);
@@ -1305,14 +1450,18 @@ struct Engine {
     LG_CUDA(lg_copy(ob.data(), d_off_base.p, N * sizeof(int), cudaMemcpyDeviceToHost));
     LG_CUDA(lg_copy(oc.data(), d_off_cnt.p, N * sizeof(int), cudaMemcpyDeviceToHost));
     L.assign(N, {});
+    // one copy of each list array over the span the lists occupy
+    long long lo = -1, hi = 0;
+    for (int i = 0; i < N; ++i)
+      if (oc[i]) { lo = lo < 0 ? ob[i] : std::min<long long>(lo, ob[i]); hi = std::max<long long>(hi, (long long)ob[i] + oc[i]); }
+    if (lo < 0) return LG_OK;
+    std::vector<uint64_t> t(hi - lo);
+    std::vector<uint8_t> d(hi - lo);
+    LG_CUDA(lg_copy(t.data(), d_stime.p + lo, t.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    LG_CUDA(lg_copy(d.data(), d_sdir.p + lo, d.size(), cudaMemcpyDeviceToHost));
     for (int i = 0; i < N; ++i) {
-      if (!oc[i]) continue;
-      std::vector<uint64_t> t(oc[i]);
-      std::vector<uint8_t> d(oc[i]);
-      LG_CUDA(lg_copy(t.data(), d_stime.p + ob[i], oc[i] * sizeof(uint64_t), cudaMemcpyDeviceToHost));
-      LG_CUDA(lg_copy(d.data(), d_sdir.p + ob[i], oc[i], cudaMemcpyDeviceToHost));
       L[i].resize(oc[i]);
-      for (int j = 0; j < oc[i]; ++j) L[i][j] = {t[j], d[j]};
+      for (int j = 0; j < oc[i]; ++j) L[i][j] = {t[ob[i] - lo + j], d[ob[i] - lo + j]};
     }
     return LG_OK;
   }
@@ -1364,6 +1513,7 @@ struct Engine {
   // n sweeps kernel by kernel with the structural checks of k_validate after insertion, merge,
   // cluster sums and the end of the sweep.  LG_EDEVICE names the first failed check.
   int validate(long long n) {
+    if (sse) return lg_fail(LG_EUNSUPPORTED, "the structural checks are of the path-integral form");
     if (resident) {  // the structural checks are of the grid path's arrays
       int rc = to_grid();
       if (rc) return rc;
@@ -1396,38 +1546,55 @@ struct Engine {
 
   int set_state(int c, const int32_t* spins, const int32_t* bonds, const double* times, long long n,
                 uint64_t sweep) {
+    if (sse) return lg_fail(LG_EUNSUPPORTED, "an SSE chain takes its state from lg_load (diagonal operators included)");
     const ChainSpec& s = spec[c];
     const int so = hch[c].site_off;
-    SiteLists L;
-    int rc = download_lists(L);
-    if (rc) return rc;
-    for (int i = 0; i < s.N; ++i) L[so + i].clear();
-    std::vector<std::vector<std::pair<uint64_t, int>>> tmp(s.N);  // (time bits, global bond)
+    // the chain's endpoints by counting sort: per site, then (time, bond) within each site
+    std::vector<long long> start(s.N + 1, 0);
     for (long long i = 0; i < n; ++i) {
       const int b = bonds[i];
       if (b < 0 || b >= s.NB || !(times[i] >= 0.0 && times[i] < 1.0))
         return lg_fail(LG_EINVAL, "operator %lld out of range", i);
-      uint64_t tb;
-      std::memcpy(&tb, &times[i], 8);
-      tmp[s.s0[b]].push_back({tb, b + hch[c].bond_off});
-      tmp[s.s1[b]].push_back({tb, b + hch[c].bond_off});
+      ++start[s.s0[b] + 1];
+      ++start[s.s1[b] + 1];
     }
     // a spin-1/2 world line is periodic in imaginary time: an even number of flips per site
     // (spin-S chains close through the boundary matching, which checks its own sectors)
     if (s.spin2 <= 1)
       for (int i = 0; i < s.N; ++i)
-        if (tmp[i].size() & 1)
+        if (start[i + 1] & 1)
           return lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
                                     "(not periodic in imaginary time)", i);
+    for (int i = 0; i < s.N; ++i) start[i + 1] += start[i];
+    std::vector<std::pair<uint64_t, int>> ep(2 * n);  // (time bits, global bond)
+    {
+      std::vector<long long> fill(start.begin(), start.end() - 1);
+      for (long long i = 0; i < n; ++i) {
+        const int b = bonds[i];
+        uint64_t tb;
+        std::memcpy(&tb, &times[i], 8);
+        ep[fill[s.s0[b]]++] = {tb, b + hch[c].bond_off};
+        ep[fill[s.s1[b]]++] = {tb, b + hch[c].bond_off};
+      }
+    }
+    SiteLists L;
+    int rc;
+    if (C > 1) {  // the other chains' lists stay as they are
+      if ((rc = download_lists(L))) return rc;
+    } else {
+      L.assign(N, {});
+    }
     for (int i = 0; i < s.N; ++i) {
-      auto& T = tmp[i];
-      std::stable_sort(T.begin(), T.end());  // (time, bond): the order the sweep produces
+      std::sort(ep.begin() + start[i], ep.begin() + start[i + 1]);  // the order the sweep produces
       const int gs = so + i;
-      for (auto& e : T) {
+      auto& Li = L[gs];
+      Li.clear();
+      Li.reserve(start[i + 1] - start[i]);
+      for (long long k = start[i]; k < start[i + 1]; ++k) {
         int dir = -1;
         for (int j = h_inc_off[gs]; j < h_inc_off[gs + 1]; ++j)
-          if (h_inc[j] == e.second) { dir = j - h_inc_off[gs]; break; }
-        L[gs].push_back({e.first, (uint8_t)dir});
+          if (h_inc[j] == ep[k].second) { dir = j - h_inc_off[gs]; break; }
+        Li.push_back({ep[k].first, (uint8_t)dir});
       }
     }
     if (C == 1) {  // a complete, valid state: a union-find failure (LG_EITERCAP) no longer applies
@@ -1590,6 +1757,7 @@ struct Engine {
     for (int c : {c1, c2}) {
       hch[c].inv_rate = spec[c].dchain.inv_rate;
       hch[c].flip_coef = spec[c].dchain.flip_coef;
+      hch[c].sse_bw = spec[c].dchain.sse_bw;
       LG_CUDA(lg_copy_async(d_ch.p + c, &hch[c], sizeof(DChain), cudaMemcpyHostToDevice, st));
     }
     LG_CUDA(cudaStreamSynchronize(st));
@@ -1601,9 +1769,10 @@ struct Engine {
     if (rc) return rc;
     hch[c].inv_rate = spec[c].dchain.inv_rate;
     hch[c].flip_coef = spec[c].dchain.flip_coef;
+    hch[c].sse_bw = spec[c].dchain.sse_bw;
     LG_CUDA(lg_copy(d_ch.p + c, &hch[c], sizeof(DChain), cudaMemcpyHostToDevice));
     acc[c] = ChainAcc();
-    if (resident) return LG_OK;  // a grown operator count grows the capacity on overflow
+    if (resident || sse) return LG_OK;  // a grown operator count grows the capacity on overflow
     set_merge_cap();
     return set_shape(shape);  // the chain's narrow / wide class depends on beta
   }
@@ -1902,8 +2071,14 @@ int lg_save(lg_chain* c, void* buf, size_t* size) {
   return lg_guard([&]() -> int {
     std::vector<int32_t> sp, bd;
     std::vector<double> tm;
-    int rc = c->eng->get_state(c->index, sp, bd, tm);
-    if (rc) return rc;
+    int rc;
+    if (c->eng->sse) {  // the whole string: bond << 1 | type, in order
+      std::vector<uint32_t> ops;
+      if ((rc = c->eng->sse_get(c->index, sp, ops))) return rc;
+      for (size_t i = 0; i < ops.size(); ++i) { bd.push_back((int32_t)ops[i]); tm.push_back((i + 0.5) / ops.size()); }
+    } else if ((rc = c->eng->get_state(c->index, sp, bd, tm))) {
+      return rc;
+    }
     std::vector<uint8_t> blob;
     checkpoint_encode(c->eng->spec[c->index], sp, bd, tm, blob);
     if (!buf) { *size = blob.size(); return LG_OK; }
@@ -1943,6 +2118,12 @@ int lg_load(lg_chain* c, const void* buf, size_t size) {
     uint64_t mcs = 0;
     int rc = checkpoint_decode(c->eng->spec[c->index], (const uint8_t*)buf, size, sp, bd, tm, &mcs);
     if (rc) return rc;
+    if (c->eng->sse) {
+      for (size_t i = 1; i < tm.size(); ++i)
+        if (!(tm[i] > tm[i - 1])) return lg_fail(LG_ECORRUPT, "checkpoint operators out of order");
+      std::vector<uint32_t> ops(bd.begin(), bd.end());
+      return c->eng->sse_set(c->index, sp.data(), ops, mcs);
+    }
     return c->eng->set_state(c->index, sp.data(), bd.data(), tm.data(), (int64_t)bd.size(), mcs);
   });
 }

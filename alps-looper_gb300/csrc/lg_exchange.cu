@@ -1,8 +1,10 @@
 // Exchange Monte Carlo (parallel tempering) over a ladder of inverse temperatures, in one arena.
 //
 // The reference runs this with ALPS parapack's exchange worker around loop_worker
-// (path_integral.C:874-875).  The worker supplies two hooks (path_integral.C:98-109):
-// - weight_parameter() = the operator count n of the current configuration;
+// (path_integral.C:874-875, sse.C:388).  The worker supplies two hooks (path_integral.C:98-109,
+// sse.C:69-71):
+// - weight_parameter() = the operator count n of the current configuration (the SSE form: the
+//   length of the whole operator string);
 // - log_weight(n, beta) = n log beta, since a configuration's weight is proportional to beta^n
 //   in normalised imaginary time.
 // Here every temperature of the ladder is one chain of a single arena.  Every `interval` sweeps,

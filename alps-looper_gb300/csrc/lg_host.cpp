@@ -34,6 +34,7 @@ extern "C" void lg_params_default(lg_params* p) {
   p->measure_structure_factor = 0;
   p->initial_site = -1;
   p->spin2 = 1;
+  p->algorithm = LG_PATH_INTEGRAL;
 }
 
 static bool parse_bool(const std::string& v, int* out) {
@@ -146,6 +147,13 @@ extern "C" int lg_params_parse(const char* text, lg_params* p) {
           return lg_fail(LG_EINVAL, "MEASURE[Structure Factor] must be true or false");
       } else if (key == "INITIAL_SITE") {
         double d = 0; if (!(rc = integer(-kInt, kInt, &d))) p->initial_site = (int)d;
+      } else if (key == "ALGORITHM") {
+        if (val == "loop; path integral" || val == "loop; path integral; exchange")
+          p->algorithm = LG_PATH_INTEGRAL;
+        else if (val == "loop; sse" || val == "loop; sse; exchange")
+          p->algorithm = LG_SSE;
+        else
+          return lg_fail(LG_EUNSUPPORTED, "ALGORITHM \"%s\" is not a loop worker of this library", val.c_str());
       } else if (key == "local_S") {
         double d = 0; rc = num(&d);
         if (!rc) {
@@ -259,6 +267,20 @@ int ChainSpec::init(const lg_params& p) {
   }
   const double s01 = v[0] + v[1];
   dchain.Poff = prob32(s01 > 0 ? v[0] / s01 : 1.0);
+  // the SSE worker's diagonal graph choice (graph_impl.h:297-312)
+  dchain.Pd0 = prob32(v[0] + v[2] > 0 ? v[0] / (v[0] + v[2]) : 1.0);
+  dchain.Pd1 = prob32(v[1] + v[3] > 0 ? v[1] / (v[1] + v[3]) : 1.0);
+  sse = p.algorithm == LG_SSE;
+  if (p.algorithm != LG_PATH_INTEGRAL && p.algorithm != LG_SSE)
+    return lg_fail(LG_EINVAL, "unknown ALGORITHM %d", p.algorithm);
+  if (sse) {
+    // sse.C:139 checks the model without longitudinal field support; S > 1/2 and correlations
+    // are not built for the SSE form here
+    if (field) return lg_fail(LG_EUNSUPPORTED, "the SSE worker supports no longitudinal field");
+    if (spin2 > 1) return lg_fail(LG_EUNSUPPORTED, "the SSE form runs S = 1/2 only");
+    if (p.measure_correlations || p.measure_structure_factor)
+      return lg_fail(LG_EUNSUPPORTED, "correlations are measured by the path-integral form only");
+  }
   dchain.field = field ? 1 : 0;
   // correlations (correlation.h:62-110): the structure factor needs the all-pairs sums; the
   // correlations use them too unless INITIAL_SITE picks one origin
@@ -329,6 +351,7 @@ int ChainSpec::set_beta(double b) {
   beta = b;
   dchain.inv_rate = W > 0 ? (float)(1.0 / (beta * W)) : 0.0f;
   dchain.flip_coef = (float)(beta * h * std::ldexp(1.0, -40));
+  dchain.sse_bw = beta * W * NB;
   return LG_OK;
 }
 
@@ -342,6 +365,15 @@ double ChainSpec::expected_vertices() const {
 // ---------------------------------------------------------------------------------------------
 static double i64(uint64_t x) { return (double)(int64_t)x; }
 static double u128d(const uint64_t* r, int i) { return (double)r[i] + std::ldexp((double)r[i + 1], 64); }
+
+// A susceptibility from its two collector sums: path integral (susceptibility.h:225-226 etc.)
+// beta * integral / V, the integral in beta units; SSE (susceptibility.h:224-225, with
+// divide_if_positive) beta * (integral / n + tau0) / (n + 1) / V, the integral in operator units.
+static double chi(const ChainSpec& s, double nop, double integral, double tau0) {
+  const double V = (double)s.volume;
+  if (!s.sse) return s.beta * integral / V;
+  return s.beta * ((nop > 0 ? integral / nop : 0.0) + tau0) / (nop + 1) / V;
+}
 
 void record_values(const ChainSpec& s, const uint64_t* r, double* v) {
   const double beta = s.beta, V = (double)s.volume;
@@ -362,7 +394,9 @@ void record_values(const ChainSpec& s, const uint64_t* r, double* v) {
     for (int d = 0; d < 3; ++d) w2 += i64(r[R_W0 + d]) * i64(r[R_W0 + d]) / 4;
     v[RAW_STIFF] = w2 / (beta * dim);
   }
-  const double t80 = std::ldexp(1.0, -80), t40 = std::ldexp(1.0, -40);
+  // world-line lengths: 2^-40 of beta on the path-integral form, operator indices on the SSE form
+  const double u2 = s.sse ? 1.0 : std::ldexp(1.0, -80), u1 = s.sse ? 1.0 : std::ldexp(1.0, -40);
+  (void)V;
   if (s.improved) {                                                // susceptibility.h:200-254
     const double m2 = (double)r[R_M0SQ] / 4, m4 = u128d(r, R_M0Q) / 16;
     const double sm2 = (double)r[R_SM0SQ] / 4, sm4 = u128d(r, R_SM0Q) / 16;
@@ -370,23 +404,23 @@ void record_values(const ChainSpec& s, const uint64_t* r, double* v) {
     v[RAW_ABSM] = std::fabs(i64(r[R_M0])) / 2;
     v[RAW_M2] = m2;
     v[RAW_M4] = 3 * m2 * m2 - 2 * m4;
-    v[RAW_CHI] = beta * u128d(r, R_MSQ) * t80 / 4 / V;
+    v[RAW_CHI] = chi(s, nop, u128d(r, R_MSQ) * u2 / 4, m2);
     v[RAW_SM2] = sm2;
     v[RAW_SM4] = 3 * sm2 * sm2 - 2 * sm4;
-    v[RAW_SCHI] = beta * u128d(r, R_SMSQ) * t80 / 4 / V;
+    v[RAW_SCHI] = chi(s, nop, u128d(r, R_SMSQ) * u2 / 4, sm2);
     v[RAW_GM2] = (double)r[R_N0SQ] / 4;
-    v[RAW_GCHI] = beta * u128d(r, R_LSQ) * t80 / 4 / V;
+    v[RAW_GCHI] = chi(s, nop, u128d(r, R_LSQ) * u2 / 4, (double)r[R_N0SQ] / 4);
   } else {                                                         // susceptibility.h:303-335
     const double m = i64(r[R_M0]) / 2, sm = i64(r[R_SM0]) / 2;
-    const double ma = i64(r[R_MA]) * t40 / 2, sma = i64(r[R_SMA]) * t40 / 2;
+    const double ma = i64(r[R_MA]) * u1 / 2, sma = i64(r[R_SMA]) * u1 / 2;
     v[RAW_M] = m;
     v[RAW_ABSM] = std::fabs(m);
     v[RAW_M2] = m * m;
     v[RAW_M4] = m * m * m * m;
-    v[RAW_CHI] = beta * ma * ma / V;
+    v[RAW_CHI] = chi(s, nop, ma * ma, m * m);
     v[RAW_SM2] = sm * sm;
     v[RAW_SM4] = sm * sm * sm * sm;
-    v[RAW_SCHI] = beta * sma * sma / V;
+    v[RAW_SCHI] = chi(s, nop, sma * sma, sm * sm);
     v[RAW_GM2] = 0;
     v[RAW_GCHI] = 0;
   }
@@ -427,14 +461,15 @@ void record_scalars(const ChainSpec& s, const uint64_t* r, double* v) {
   v[LG_VAL_ENERGY] = raw[RAW_E];
   v[LG_VAL_ENERGY_DENSITY] = raw[RAW_E] / vol;
   v[LG_VAL_ENERGY2] = raw[RAW_E2];
-  const double t80 = std::ldexp(1.0, -80), t40 = std::ldexp(1.0, -40);
+  const double u2 = s.sse ? 1.0 : std::ldexp(1.0, -80), u1 = s.sse ? 1.0 : std::ldexp(1.0, -40);
+  const double nop = (double)r[R_NOP];
   if (s.improved) {
     const double umag0 = i64(r[R_M0]) / 2, umag2 = (double)r[R_M0SQ] / 4, umag4 = u128d(r, R_M0Q) / 16;
     const double usize2 = (double)r[R_N0SQ] / 4, usize4 = u128d(r, R_N0Q) / 16;
-    const double umag = u128d(r, R_MSQ) * t80 / 4, usize = u128d(r, R_LSQ) * t80 / 4;
+    const double umag = u128d(r, R_MSQ) * u2 / 4, usize = u128d(r, R_LSQ) * u2 / 4;
     const double smag0 = i64(r[R_SM0]) / 2, smag2 = (double)r[R_SM0SQ] / 4, smag4 = u128d(r, R_SM0Q) / 16;
     const double ssize2 = (double)r[R_SN0SQ] / 4, ssize4 = u128d(r, R_SN0Q) / 16;
-    const double smag = u128d(r, R_SMSQ) * t80 / 4, ssize = u128d(r, R_SLSQ) * t80 / 4;
+    const double smag = u128d(r, R_SMSQ) * u2 / 4, ssize = u128d(r, R_SLSQ) * u2 / 4;
     v[LG_VAL_MAGNETIZATION] = 0.0;
     v[LG_VAL_MAGNETIZATION_DENSITY] = 0.0;
     v[LG_VAL_ABS_MAGNETIZATION] = std::fabs(umag0);
@@ -443,12 +478,12 @@ void record_scalars(const ChainSpec& s, const uint64_t* r, double* v) {
     v[LG_VAL_MAGNETIZATION_DENSITY2] = umag2 / p2(vol);
     v[LG_VAL_MAGNETIZATION4] = 3 * p2(umag2) - 2 * umag4;
     v[LG_VAL_MAGNETIZATION_DENSITY4] = (3 * p2(umag2) - 2 * umag4) / p4(vol);
-    v[LG_VAL_SUSCEPTIBILITY] = beta * umag / vol;
+    v[LG_VAL_SUSCEPTIBILITY] = chi(s, nop, umag, umag2);
     v[LG_VAL_GEN_MAGNETIZATION2] = usize2;
     v[LG_VAL_GEN_MAGNETIZATION_DENSITY2] = usize2 / p2(vol);
     v[LG_VAL_GEN_MAGNETIZATION4] = 3 * p2(usize2) - 2 * usize4;
     v[LG_VAL_GEN_MAGNETIZATION_DENSITY4] = (3 * p2(usize2) - 2 * usize4) / p4(vol);
-    v[LG_VAL_GEN_SUSCEPTIBILITY] = beta * usize / vol;
+    v[LG_VAL_GEN_SUSCEPTIBILITY] = chi(s, nop, usize, usize2);
     v[LG_VAL_STAG_MAGNETIZATION] = 0.0;
     v[LG_VAL_STAG_MAGNETIZATION_DENSITY] = 0.0;
     v[LG_VAL_ABS_STAG_MAGNETIZATION] = std::fabs(smag0);
@@ -457,15 +492,15 @@ void record_scalars(const ChainSpec& s, const uint64_t* r, double* v) {
     v[LG_VAL_STAG_MAGNETIZATION_DENSITY2] = smag2 / p2(vol);
     v[LG_VAL_STAG_MAGNETIZATION4] = 3 * p2(smag2) - 2 * smag4;
     v[LG_VAL_STAG_MAGNETIZATION_DENSITY4] = (3 * p2(smag2) - 2 * smag4) / p4(vol);
-    v[LG_VAL_STAG_SUSCEPTIBILITY] = beta * smag / vol;
+    v[LG_VAL_STAG_SUSCEPTIBILITY] = chi(s, nop, smag, smag2);
     v[LG_VAL_GEN_STAG_MAGNETIZATION2] = ssize2;
     v[LG_VAL_GEN_STAG_MAGNETIZATION_DENSITY2] = ssize2 / p2(vol);
     v[LG_VAL_GEN_STAG_MAGNETIZATION4] = 3 * p2(ssize2) - 2 * ssize4;
     v[LG_VAL_GEN_STAG_MAGNETIZATION_DENSITY4] = (3 * p2(ssize2) - 2 * ssize4) / p4(vol);
-    v[LG_VAL_GEN_STAG_SUSCEPTIBILITY] = beta * ssize / vol;
+    v[LG_VAL_GEN_STAG_SUSCEPTIBILITY] = chi(s, nop, ssize, ssize2);
   } else {
     const double umag = i64(r[R_M0]) / 2, smag = i64(r[R_SM0]) / 2;
-    const double umag_a = i64(r[R_MA]) * t40 / 2, smag_a = i64(r[R_SMA]) * t40 / 2;
+    const double umag_a = i64(r[R_MA]) * u1 / 2, smag_a = i64(r[R_SMA]) * u1 / 2;
     v[LG_VAL_MAGNETIZATION] = umag;
     v[LG_VAL_MAGNETIZATION_DENSITY] = umag / vol;
     v[LG_VAL_ABS_MAGNETIZATION] = std::fabs(umag);
@@ -474,7 +509,7 @@ void record_scalars(const ChainSpec& s, const uint64_t* r, double* v) {
     v[LG_VAL_MAGNETIZATION_DENSITY2] = p2(umag / vol);
     v[LG_VAL_MAGNETIZATION4] = p4(umag);
     v[LG_VAL_MAGNETIZATION_DENSITY4] = p4(umag / vol);
-    v[LG_VAL_SUSCEPTIBILITY] = beta * p2(umag_a) / vol;
+    v[LG_VAL_SUSCEPTIBILITY] = chi(s, nop, p2(umag_a), p2(umag));
     v[LG_VAL_STAG_MAGNETIZATION] = smag;
     v[LG_VAL_STAG_MAGNETIZATION_DENSITY] = smag / vol;
     v[LG_VAL_ABS_STAG_MAGNETIZATION] = std::fabs(smag);
@@ -483,7 +518,7 @@ void record_scalars(const ChainSpec& s, const uint64_t* r, double* v) {
     v[LG_VAL_STAG_MAGNETIZATION_DENSITY2] = p2(smag / vol);
     v[LG_VAL_STAG_MAGNETIZATION4] = p4(smag);
     v[LG_VAL_STAG_MAGNETIZATION_DENSITY4] = p4(smag / vol);
-    v[LG_VAL_STAG_SUSCEPTIBILITY] = beta * p2(smag_a) / vol;
+    v[LG_VAL_STAG_SUSCEPTIBILITY] = chi(s, nop, p2(smag_a), p2(smag));
   }
   v[LG_VAL_STIFFNESS] = raw[RAW_STIFF];
   for (int i = 0; i < LG_NUM_VALUES; ++i)
@@ -630,8 +665,11 @@ extern "C" const char* lg_obs_name(int i) {
 
 // ---------------------------------------------------------------------------------------------
 // Checkpoint: the worker's save/load content (path_integral.C:111-124: mcs, spins, operators).
-// Layout (little endian): "LGCK" u32 version=1, u32 dim, u32 L, u64 mcs, u64 n_ops,
-// N x u8 spins, n_ops x (i32 bond, f64 time), u64 FNV-1a of everything before it.
+// Layout (little endian): "LGCK" u32 version, u32 dim, u32 L, u64 mcs, u64 n_ops,
+// N x u8 spins, n_ops x (i32 bond, f64 time), u64 FNV-1a of everything before it.  Version 1:
+// the path-integral form, its off-diagonal operators with their times.  Version 2: the SSE form
+// (sse.C save: mcs, spins, operators), every operator of the string as bond << 1 | off-diagonal,
+// with (index + 1/2) / n_ops as its time (the order).
 // ---------------------------------------------------------------------------------------------
 static uint64_t fnv1a(const uint8_t* p, size_t n) {
   uint64_t h = 1469598103934665603ull;
@@ -650,7 +688,7 @@ void checkpoint_encode(const ChainSpec& s, const std::vector<int32_t>& spins,
                        std::vector<uint8_t>& blob) {
   blob.clear();
   blob.insert(blob.end(), {'L', 'G', 'C', 'K'});
-  put_raw(blob, (uint32_t)1);
+  put_raw(blob, (uint32_t)(s.sse ? 2 : 1));  // 2: the SSE form, operators as bond << 1 | type
   put_raw(blob, (uint32_t)s.dim);
   put_raw(blob, (uint32_t)s.L);
   put_raw(blob, (uint64_t)s.mcs);
@@ -676,7 +714,7 @@ int checkpoint_decode(const ChainSpec& s, const uint8_t* buf, size_t size,
   std::memcpy(&L, buf + 12, 4);
   std::memcpy(&m, buf + 16, 8);
   std::memcpy(&n, buf + 24, 8);
-  if (ver != 1) return lg_fail(LG_ECORRUPT, "checkpoint version %u", ver);
+  if (ver != (s.sse ? 2u : 1u)) return lg_fail(LG_ECORRUPT, "checkpoint version %u", ver);
   if ((int)dim != s.dim || (int)L != s.L) return lg_fail(LG_ECORRUPT, "checkpoint lattice mismatch");
   // n is checked against the size without multiplying it (a forged count must not wrap)
   const size_t fixed = head + (size_t)s.N + 8;
@@ -692,7 +730,7 @@ int checkpoint_decode(const ChainSpec& s, const uint8_t* buf, size_t size,
     std::memcpy(&bonds[i], p, 4);
     std::memcpy(&times[i], p + 4, 8);
     p += 12;
-    if (bonds[i] < 0 || bonds[i] >= s.NB || !(times[i] >= 0.0 && times[i] < 1.0))
+    if (bonds[i] < 0 || bonds[i] >= (s.sse ? 2 : 1) * s.NB || !(times[i] >= 0.0 && times[i] < 1.0))
       return lg_fail(LG_ECORRUPT, "checkpoint operator %llu out of range", (unsigned long long)i);
   }
   *mcs = m;

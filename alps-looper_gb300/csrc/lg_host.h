@@ -45,6 +45,7 @@ struct ChainSpec {
   int init_spins = 0;
   bool field = false, improved = true;
   bool measure_corr = false, measure_sfac = false;
+  bool sse = false;              // ALGORITHM "loop; sse" (the SSE worker, k_sse)
   int corr_origin = -1;
   lg::DChain dchain{};
 

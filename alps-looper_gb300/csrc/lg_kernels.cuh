@@ -1637,21 +1637,6 @@ __global__ void __launch_bounds__(CL_THREADS) k_cluster(Arena A) {
 // Root of segment x (after k_accumulate every parent is a root).
 __device__ __forceinline__ int seg_root(const int* P, int x) { return P[x]; }
 
-// The flip of a cluster of a chain without a field: the coin of root_record, keyed by the
-// chain-local index of the cluster's root, so it can be drawn wherever the root is known.  With
-// COIN the site pass draws it itself instead of reading k_cluster's flip array, and so runs
-// beside k_cluster instead of after it.
-struct CoinKey { uint64_t seed; uint32_t sweep; int slot_off; };
-__device__ __forceinline__ CoinKey coin_key(const Arena& A, int s) {
-  const int c = A.site_chain[s];
-  return CoinKey{A.ch[c].seed, A.ch_sweep[c], A.ch_slot_off[c]};
-}
-template <bool COIN>
-__device__ __forceinline__ uint8_t cluster_flip(const Arena& A, const CoinKey& k, int root) {
-  if (COIN) return philox(k.seed, k.sweep, (uint32_t)(root - k.slot_off), TAG_FLIP, 0).x < 0x80000000u ? 1 : 0;
-  return A.flip[root];
-}
-
 // Per site (one warp each): flip the tau = 0 spin with its bottom segment's cluster
 // (path_integral.C:822-823) and keep, in time order and in place at the start of the site's
 // segment range, the endpoints whose vertex is off-diagonal after the flips: the next sweep's
@@ -1662,7 +1647,6 @@ __device__ __forceinline__ uint8_t cluster_flip(const Arena& A, const CoinKey& k
 // the new type at endpoint x is its old type ^ flip(cluster of x-1) ^ flip(cluster of x), the
 // same at both of its sites.  Every lane reads its step's segments before any lane writes, and a kept
 // endpoint never moves forward, so the in-place compaction reads no overwritten slot.
-template <bool COIN = false>
 __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
   const int lane = threadIdx.x & 31;
@@ -1671,8 +1655,7 @@ __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int
     const int s = sites ? sites[si] : si;
     const int base = A.sbase[s];
     const int k = A.sbase[s + 1] - base - 1;
-    const CoinKey ck = COIN ? coin_key(A, s) : CoinKey{0, 0, 0};
-    const uint8_t fb = cluster_flip<COIN>(A, ck, seg_root(A.parent, base));
+    const uint8_t fb = A.flip[seg_root(A.parent, base)];
     if (lane == 0 && fb) A.spin0[s] ^= 1u;
     uint8_t below = fb;   // flip of the cluster under the step's first segment
     int n = 0;
@@ -1683,8 +1666,8 @@ __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int
       int pa = 0, pb = 0;
       if (ja <= k) { ia = A.sinfo[base + ja]; pa = A.parent[base + ja]; }
       if (jb <= k) { ib = A.sinfo[base + jb]; pb = A.parent[base + jb]; }
-      if (ja <= k) fa = cluster_flip<COIN>(A, ck, pa);
-      if (jb <= k) fbb = cluster_flip<COIN>(A, ck, pb);
+      if (ja <= k) fa = A.flip[pa];
+      if (jb <= k) fbb = A.flip[pb];
       uint8_t prev_a = (uint8_t)__shfl_up_sync(0xFFFFFFFFu, (unsigned)fa, 1);
       uint8_t prev_b = (uint8_t)__shfl_up_sync(0xFFFFFFFFu, (unsigned)fbb, 1);
       const uint8_t top_a = (uint8_t)__shfl_sync(0xFFFFFFFFu, (unsigned)fa, 31);
@@ -1720,20 +1703,18 @@ __global__ void __launch_bounds__(256) k_site_end(Arena A, const int* sites, int
 
 // Thread-per-site form of k_site_end for sites with few endpoints (kept entries never move
 // forward, so the in-place compaction reads no overwritten slot).
-template <bool COIN = false>
 __global__ void __launch_bounds__(256) k_site_end_narrow(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
   LG_GRID_STRIDE(i, nsites) {
     const int s = sites[i];
     const int base = A.sbase[s];
     const int k = A.sbase[s + 1] - base - 1;
-    const CoinKey ck = COIN ? coin_key(A, s) : CoinKey{0, 0, 0};
-    uint8_t fprev = cluster_flip<COIN>(A, ck, seg_root(A.parent, base));
+    uint8_t fprev = A.flip[seg_root(A.parent, base)];
     if (fprev) A.spin0[s] ^= 1u;
     int n = 0;
     for (int j = 1; j <= k; ++j) {
       const int x = base + j;
-      const uint8_t fx = cluster_flip<COIN>(A, ck, seg_root(A.parent, x));
+      const uint8_t fx = A.flip[seg_root(A.parent, x)];
       if ((((A.sinfo[x] & SI_OFF) ? 1u : 0u) ^ fprev ^ fx) != 0) {
         A.stime[base + n] = A.stime[x];
         A.sdir[base + n] = A.sdir[x] & SD_IMASK;  // the list keeps the incidence index

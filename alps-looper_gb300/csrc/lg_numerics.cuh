@@ -17,7 +17,7 @@ namespace lg {
 // Stream tags (third Philox counter word).
 enum : uint32_t {
   TAG_PROPOSAL = 1, TAG_OFFDIAG = 2, TAG_FLIP = 3, TAG_SPIN = 4, TAG_EXCHANGE = 5, TAG_PERM = 6,
-  TAG_TAIL = 7
+  TAG_TAIL = 7, TAG_SSE = 8
 };
 
 // Philox4x32-10 (Salmon et al., SC'11): 10 rounds of two 32x32->64 multiplies with the paper's

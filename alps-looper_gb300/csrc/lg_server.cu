@@ -282,6 +282,7 @@ int lg_server_submit(lg_server* s, const lg_params* p, uint64_t* id) {
     lg_server::Req r;
     int rc = r.spec.init(*p);
     if (rc) return rc;
+    if (r.spec.sse) return lg_fail(LG_EUNSUPPORTED, "the server runs path-integral chains");
     r.bytes = chain_bytes(r.spec);
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->fatal) return lg_fail(s->fatal, "server stopped: %s", s->fatal_msg.c_str());

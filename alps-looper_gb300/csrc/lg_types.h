@@ -43,6 +43,11 @@ struct DChain {
   int corr_disp, corr_origin;
   uint32_t corr_from, corr_to;
   int spin2;                   // 2S: virtual sites per real site (their boundary: k_boundary)
+  // the SSE worker (k_sse): beta times the total bond weight, and the diagonal graph choice of
+  // graph_impl.h:297-312 on the 2^32 scale (antiparallel: graph 0 below Pd0, else 2; parallel:
+  // graph 1 below Pd1, else 3)
+  double sse_bw;
+  uint64_t Pd0, Pd1;
 };
 
 struct Ctl {

@@ -43,7 +43,8 @@ class Params(ctypes.Structure):
                 ("thermalization", ctypes.c_int64), ("seed", ctypes.c_uint64),
                 ("init_spins", ctypes.c_int), ("disable_improved_estimator", ctypes.c_int),
                 ("measure_correlations", ctypes.c_int), ("measure_structure_factor", ctypes.c_int),
-                ("initial_site", ctypes.c_int), ("spin2", ctypes.c_int)]
+                ("initial_site", ctypes.c_int), ("spin2", ctypes.c_int),
+                ("algorithm", ctypes.c_int)]
 
 
 class Obs(ctypes.Structure):
@@ -197,7 +198,7 @@ def make_params(**kw) -> Params:
     p = Params()
     lib().lg_params_default(ctypes.byref(p))
     for k, v in kw.items():
-        key = k.upper() if k.upper() in ("LATTICE", "BETA", "SWEEPS", "THERMALIZATION", "SEED",
+        key = k.upper() if k.upper() in ("LATTICE", "BETA", "SWEEPS", "THERMALIZATION", "SEED", "ALGORITHM",
                                          "FORCE_SCATTER", "INITIAL_SPINS",
                                          "DISABLE_IMPROVED_ESTIMATOR", "MEASURE_CORRELATIONS",
                                          "MEASURE_STRUCTURE_FACTOR", "INITIAL_SITE") else k
@@ -229,6 +230,8 @@ def make_params(**kw) -> Params:
             p.measure_structure_factor = 1 if v else 0
         elif key == "INITIAL_SITE":
             p.initial_site = int(v)
+        elif key == "ALGORITHM":
+            p.algorithm = 1 if str(v).lower() in ("sse", "loop; sse", "1") else 0
         elif key in ("local_S", "LOCAL_S"):
             p.spin2 = int(round(2 * float(v)))
         else:

@@ -403,6 +403,15 @@ def served_requests(lg, n=4096, seed=2024):
     return out
 
 
+def _leg(fn, *a):
+    """A supplementary measurement (config-0 chain, batched, replicas, served): its failure is
+    reported in its own entry of the line instead of ending the run."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
 def run_served(lg, n_requests, plain_sample=32, lanes=3):
     """The served request stream (Poisson arrivals at 200/s) through lg_server_*, against the
     plain path on a sample of the same requests run alone from an equilibrated start."""
@@ -544,16 +553,16 @@ def run_ours(args, dist, ws, rank, local):
                          "equilibrated state, %.1f s, 1 thread (CPU restatement of "
                          "path_integral.C in oracle/)" % (r["sweeps"], r["seconds"])}
     w.close()
-    config0 = run_config0(lg) if rank == 0 and args.config0 else None
+    config0 = _leg(run_config0, lg) if rank == 0 and args.config0 else None
     batched = None
     if rank == 0 and args.batched_steps > 0:
-        batched = run_batched(lg, args.batched_steps, args.batched_therm)
+        batched = _leg(run_batched, lg, args.batched_steps, args.batched_therm)
     replicas = None
     if rank == 0 and args.replica_steps > 0:
-        replicas = run_replicas(lg, args.replica_steps, args.replica_therm)
+        replicas = _leg(run_replicas, lg, args.replica_steps, args.replica_therm)
     served = None
     if rank == 0 and args.served_requests > 0:
-        served = run_served(lg, args.served_requests)
+        served = _leg(run_served, lg, args.served_requests)
     if rank != 0:
         return None
     out = {

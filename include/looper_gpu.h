@@ -71,7 +71,13 @@ typedef struct lg_params {
                                      runs on 2S virtual spin-1/2 sites per site (lattice.h
                                      virtual graph) with the random boundary matching of
                                      path_integral.C:590-613                                    */
+  int algorithm;                  /* ALGORITHM: LG_PATH_INTEGRAL ("loop; path integral", default)
+                                     or LG_SSE ("loop; sse": the stochastic series expansion
+                                     worker of sse.C, S = 1/2 without field, run one GPU thread
+                                     per chain)                                                 */
 } lg_params;
+
+enum { LG_PATH_INTEGRAL = 0, LG_SSE = 1 };
 
 /* Fill defaults: chain, L=8, T=0.2, J=1, Jz=Jxy=NaN, h=0, SWEEPS=65536 (montecarlo.h:41),
  * THERMALIZATION=-1, SEED=29833, all spins up. */
@@ -81,7 +87,7 @@ void lg_params_default(lg_params* p);
  * Keys: LATTICE ("chain lattice" | "square lattice" | "simple cubic lattice"), L, T, BETA, J,
  * Jz, Jxy, h, FORCE_SCATTER, SWEEPS, THERMALIZATION, SEED, INITIAL_SPINS ("up" | "random"),
  * DISABLE_IMPROVED_ESTIMATOR, MEASURE[Correlations], MEASURE[Structure Factor], INITIAL_SITE,
- * local_S (1/2, 1, 3/2).
+ * local_S (1/2, 1, 3/2 ...), ALGORITHM ("loop; path integral" | "loop; sse").
  * Unknown keys are ignored, as ALPS does for keys a worker does not
  * read.  Returns LG_EINVAL with a message on a malformed value. */
 int lg_params_parse(const char* text, lg_params* p);

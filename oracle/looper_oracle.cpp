@@ -638,6 +638,220 @@ struct chain_t {
 };
 
 // ----------------------------------------------------------------------------------------------
+// SSE chain: restates the stochastic-series-expansion loop worker (sse.C:180-371) for S=1/2 XXZ
+// models without field, in philox mode.  The configuration is an ordered operator string with no
+// times; operator code = bond << 1 | off-diagonal.  One sweep:
+//   * diagonal update & labelling (sse.C:201-276): a walk over the old string; before every
+//     operator (and once more at the end) an insertion is tried with probability
+//     beta W_tot / (n + 1), n the running operator count, and tried again while accepted and
+//     compatible; a diagonal operator is removed with probability n / (beta W_tot), otherwise its
+//     graph is re-chosen (choose_diagonal, graph_impl.h:297-312); an off-diagonal one re-chooses
+//     (choose_offdiagonal, :314-327).  Spins propagate and fragments reconnect (:280-295).
+//   * closure of every site's top onto its bottom (sse.C:275-277)
+//   * cluster ids (sse.C:305-306) and the improved estimators in a second pass over the new string
+//     with the loop_l / loop_u fragments of each operator (sse.C:314-354; graph_impl.h:489-494);
+//     the operator index is the time.  The normal estimator's time-integrated magnetization is
+//     accumulated in the first pass at the off-diagonal operators (sse.C:255-259).
+//   * a coin per cluster, then operator types and spins flipped (sse.C:359-371)
+// Random numbers: the words of Philox(seed; sweep, 0, TAG_SSE, k), k = 0, 1, ..., four per counter,
+// consumed in the walk's order: per insertion trial one uniform ((w + 1/2) 2^-32) and, when
+// accepted, one word for the bond (floor(w NB / 2^32): the weights of all bonds are equal) and one
+// for the graph; per removal trial one uniform and, when kept, one word for the graph choice.  The
+// coin of a cluster is keyed by its smallest fragment index (sites first, then one fragment per
+// graph-0 operator in string order).
+// ----------------------------------------------------------------------------------------------
+enum { TAG_SSE = 8 };
+
+struct sse_chain_t {
+  lattice lat;
+  bond_weight bw;
+  double beta = 1, bwt = 0;  // bwt = beta * W * NB (sse.C:203, graph_weight of all bonds)
+  uint64_t seed = 0;
+  uint64_t T0 = 0, T1 = 0, T2 = 0, Poff = 0, Pd0 = 0, Pd1 = 0;
+  std::vector<int> spins;
+  std::vector<uint32_t> ops;
+  uint32_t sweep = 0;
+  std::vector<uint64_t> records;
+
+  void init_derived() {
+    const double W = bw.W;
+    if (W > 0) {
+      T0 = prob_u32(bw.v[0] / W);
+      T1 = prob_u32((bw.v[0] + bw.v[1]) / W);
+      T2 = prob_u32((bw.v[0] + bw.v[1] + bw.v[2]) / W);
+    }
+    const double s01 = bw.v[0] + bw.v[1], s02 = bw.v[0] + bw.v[2], s13 = bw.v[1] + bw.v[3];
+    Poff = prob_u32(s01 > 0 ? bw.v[0] / s01 : 1.0);
+    Pd0 = prob_u32(s02 > 0 ? bw.v[0] / s02 : 1.0);   // antiparallel: graph 0 or 2
+    Pd1 = prob_u32(s13 > 0 ? bw.v[1] / s13 : 1.0);   // parallel: graph 1 or 3
+    bwt = beta * W * lat.NB;
+  }
+
+  struct stream {
+    uint64_t seed;
+    uint32_t sweep, ctr = 0;
+    int k = 4;
+    uint32_t w[4] = {0, 0, 0, 0};
+    uint32_t word() {
+      if (k == 4) { rng4(seed, sweep, 0u, TAG_SSE, ctr++, w); k = 0; }
+      return w[k++];
+    }
+    double uniform() { return ((double)word() + 0.5) * 2.3283064365386963e-10; }
+  };
+
+  struct sop { uint32_t b; int off, g, loop0, loop1; };
+
+  void sweep_once() {
+    const int N = lat.N, NB = lat.NB;
+    stream r{seed, sweep};
+    std::vector<int> sc(spins), current(N);
+    uf frag;
+    frag.deterministic = true;
+    frag.reset(N);
+    for (int s = 0; s < N; ++s) current[s] = s;
+    std::vector<sop> nops;
+    // normal estimator (susceptibility.h:270-300): (1-2c) t at every piece end minus at its begin
+    int64_t MA = 0, SMA = 0;
+    int nop = (int)ops.size();
+    size_t i = 0;
+    bool try_gap = true;
+    while (try_gap || i < ops.size()) {
+      sop o{};
+      if (try_gap) {
+        if (!((double)(nop + 1) * r.uniform() < bwt)) { try_gap = false; continue; }
+        o.b = (uint32_t)(((uint64_t)r.word() * (uint64_t)NB) >> 32);
+        const uint32_t wg = r.word();
+        o.g = (int)(wg >= T0) + (int)(wg >= T1) + (int)(wg >= T2);
+        const int c0 = sc[lat.s0[o.b]], c1 = sc[lat.s1[o.b]];
+        if (!((o.g & 1) ^ c0 ^ c1)) { try_gap = false; continue; }   // is_compatible
+        o.off = 0;
+        ++nop;
+      } else {
+        o.b = ops[i] >> 1;
+        o.off = (int)(ops[i] & 1u);
+        const int c0 = sc[lat.s0[o.b]], c1 = sc[lat.s1[o.b]];
+        if (!o.off) {
+          if (bwt * r.uniform() < (double)nop) { --nop; ++i; continue; }
+          const int c = 1 ^ c0 ^ c1;
+          o.g = (((uint64_t)r.word() < (c ? Pd1 : Pd0)) ? 0 : 2) ^ c;
+        } else {
+          o.g = ((uint64_t)r.word() < Poff) ? 0 : 1;
+        }
+        ++i;
+        try_gap = true;
+      }
+      const int t = (int)nops.size();
+      const int s0 = lat.s0[o.b], s1 = lat.s1[o.b];
+      if (o.off) {
+        for (int s : {s0, s1}) {
+          const int sg = 1 - 2 * sc[s];
+          MA += 2 * (int64_t)sg * t;                 // end at t with c, begin at t with 1 - c
+          SMA += 2 * (int64_t)lat.gauge[s] * sg * t;
+          sc[s] ^= 1;
+        }
+      }
+      if (o.g & 2) {
+        o.loop0 = o.loop1 = current[s0] = current[s1] = frag.unify(current[s0], current[s1]);
+      } else if (o.g == 0) {
+        const int f = frag.add();
+        o.loop0 = frag.unify(current[s0], current[s1]);
+        o.loop1 = current[s0] = current[s1] = f;
+      } else {
+        o.loop0 = current[s0];
+        o.loop1 = current[s1];
+        std::swap(current[s0], current[s1]);
+      }
+      nops.push_back(o);
+    }
+    const int64_t T = (int64_t)nops.size();
+    for (int s = 0; s < N; ++s) {                    // stop_top of the normal estimator
+      MA += (int64_t)(1 - 2 * sc[s]) * T;
+      SMA += (int64_t)lat.gauge[s] * (1 - 2 * sc[s]) * T;
+    }
+    for (int s = 0; s < N; ++s) frag.unify(s, current[s]);
+    const int nf = (int)frag.parent.size();
+    const int nc = frag.set_ids();
+
+    // ---- improved estimators, second pass (sse.C:314-354) ----
+    std::vector<int64_t> n0(nc, 0), m0(nc, 0), sn0(nc, 0), sm0(nc, 0);
+    std::vector<int64_t> Lc(nc, 0), Mc(nc, 0), SLc(nc, 0), SMc(nc, 0), wind((size_t)nc * 3, 0);
+    std::vector<int> key(nc, nf);
+    for (int f = 0; f < nf; ++f) key[frag.id[f]] = std::min(key[frag.id[f]], f);
+    auto piece = [&](int fr, int sgn, int64_t t, int s, int c) {
+      const int cl = frag.id[fr], sg = 1 - 2 * c, g = lat.gauge[s];
+      Lc[cl] += sgn * t; Mc[cl] += sgn * sg * t; SLc[cl] += sgn * g * t; SMc[cl] += sgn * g * sg * t;
+    };
+    std::vector<int> c2(spins);
+    int64_t M0tot = 0, SM0tot = 0;
+    for (int s = 0; s < N; ++s) {                    // start_bottom
+      const int cl = frag.id[s], sg = 1 - 2 * c2[s], g = lat.gauge[s];
+      n0[cl] += 1; m0[cl] += sg; sn0[cl] += g; sm0[cl] += g * sg;
+      M0tot += sg; SM0tot += g * sg;
+    }
+    for (int64_t t = 0; t < T; ++t) {
+      const sop& o = nops[t];
+      if (o.g & 2) continue;                          // frozen graphs contribute nothing
+      const int s0 = lat.s0[o.b], s1 = lat.s1[o.b], d = lat.bdir[o.b];
+      const int l0 = o.loop0, l1 = (o.g == 0) ? o.loop0 : o.loop1;   // loop_l0, loop_l1
+      const int u0 = o.loop1, u1 = (o.g == 0) ? o.loop1 : o.loop0;   // loop_u0, loop_u1
+      piece(l0, +1, t, s0, c2[s0]);
+      piece(l1, +1, t, s1, c2[s1]);
+      wind[(size_t)frag.id[l0] * 3 + d] += 1 - 2 * c2[s0];             // end_bs
+      if (o.off) { c2[s0] ^= 1; c2[s1] ^= 1; }
+      piece(u0, -1, t, s0, c2[s0]);
+      piece(u1, -1, t, s1, c2[s1]);
+      wind[(size_t)frag.id[u0] * 3 + d] -= 1 - 2 * c2[s0];             // begin_bs
+    }
+    for (int s = 0; s < N; ++s) piece(current[s], +1, T, s, c2[s]);    // stop_top
+
+    // ---- coins, record, flips ----
+    std::vector<uint8_t> flip(nc);
+    for (int cl = 0; cl < nc; ++cl) {
+      uint32_t w[4];
+      rng4(seed, sweep, (uint32_t)key[cl], TAG_FLIP, 0, w);
+      flip[cl] = (w[0] < 0x80000000u) ? 1 : 0;
+    }
+    std::vector<uint64_t> rec(R_WORDS, 0);
+    rec[R_NOP] = (uint64_t)T;
+    rec[R_NC] = (uint64_t)nc;
+    rec[R_M0] = (uint64_t)M0tot;
+    rec[R_SM0] = (uint64_t)SM0tot;
+    for (int cl = 0; cl < nc; ++cl) {
+      rec[R_M0SQ] += (uint64_t)(m0[cl] * m0[cl]);
+      rec[R_N0SQ] += (uint64_t)(n0[cl] * n0[cl]);
+      rec[R_SM0SQ] += (uint64_t)(sm0[cl] * sm0[cl]);
+      rec[R_SN0SQ] += (uint64_t)(sn0[cl] * sn0[cl]);
+      auto q4 = [](int64_t x) { u128 a = (u128)(uint64_t)(x * x); return a * a; };
+      add128(rec.data(), R_M0Q_LO, q4(m0[cl]));
+      add128(rec.data(), R_N0Q_LO, q4(n0[cl]));
+      add128(rec.data(), R_SM0Q_LO, q4(sm0[cl]));
+      add128(rec.data(), R_SN0Q_LO, q4(sn0[cl]));
+      auto sq = [](int64_t x) { uint64_t a = (uint64_t)(x < 0 ? -x : x); return (u128)a * a; };
+      add128(rec.data(), R_LSQ_LO, sq(Lc[cl]));
+      add128(rec.data(), R_MSQ_LO, sq(Mc[cl]));
+      add128(rec.data(), R_SLSQ_LO, sq(SLc[cl]));
+      add128(rec.data(), R_SMSQ_LO, sq(SMc[cl]));
+      for (int d = 0; d < 3; ++d) {
+        const int64_t w = wind[(size_t)cl * 3 + d];
+        rec[R_WSQ] += (uint64_t)(w * w);
+        rec[R_W0 + d] += (uint64_t)w;
+      }
+    }
+    rec[R_FLD] = 0;                                   // no field on the SSE form
+    rec[R_MA] = (uint64_t)MA;
+    rec[R_SMA] = (uint64_t)SMA;
+    records.insert(records.end(), rec.begin(), rec.end());
+    ops.assign(nops.size(), 0u);
+    for (size_t k = 0; k < nops.size(); ++k) {
+      const int off = nops[k].off ^ (flip[frag.id[nops[k].loop0]] ^ flip[frag.id[nops[k].loop1]]);
+      ops[k] = (nops[k].b << 1) | (uint32_t)off;
+    }
+    for (int s = 0; s < N; ++s) if (flip[frag.id[s]]) spins[s] ^= 1;
+    ++sweep;
+  }
+};
+
+// ----------------------------------------------------------------------------------------------
 // Standalone mode: restates standalone/loop.C:39-195 (Heisenberg AF chain, mt19937(29833)),
 // with the weighted union-find of standalone/union_find.h:113-126 (full compression).
 // ----------------------------------------------------------------------------------------------
@@ -852,6 +1066,53 @@ int orc_last_labels(void* h, int* labels, int cap) {
   return c->last_nfrag;
 }
 int orc_last_nc(void* h) { return static_cast<orc::chain_t*>(h)->last_nc; }
+
+// SSE chains (sse_chain_t): create from the same parameters (h must be 0, spin2 1), sweep, the
+// per-sweep records, and the state (spins at the bottom and the operator codes in order).
+void* orc_sse_create(const orc_params* p) {
+  if (std::fabs(p->h) > 0 || p->spin2 > 1) return nullptr;
+  orc::sse_chain_t* c = new orc::sse_chain_t();
+  c->lat.build(p->dim, p->L, 1);
+  c->bw = orc::make_weight(p->jxy, p->jz, p->force_scatter);
+  c->beta = p->beta;
+  c->seed = p->seed;
+  c->init_derived();
+  c->spins.assign(c->lat.N, 0);
+  if (p->random_spins) {
+    for (int s = 0; s < c->lat.N; ++s) {
+      uint32_t w[4];
+      orc::rng4(c->seed, 0xFFFFFFFFu, (uint32_t)s, orc::TAG_SPIN, 0, w);
+      c->spins[s] = (int)(w[0] & 1u);
+    }
+  }
+  return c;
+}
+void orc_sse_destroy(void* h) { delete static_cast<orc::sse_chain_t*>(h); }
+void orc_sse_sweep(void* h, int n) {
+  orc::sse_chain_t* c = static_cast<orc::sse_chain_t*>(h);
+  for (int i = 0; i < n; ++i) c->sweep_once();
+}
+int orc_sse_num_records(void* h) {
+  return (int)(static_cast<orc::sse_chain_t*>(h)->records.size() / orc::R_WORDS);
+}
+void orc_sse_get_records(void* h, uint64_t* out) {
+  auto& r = static_cast<orc::sse_chain_t*>(h)->records;
+  std::memcpy(out, r.data(), r.size() * sizeof(uint64_t));
+}
+void orc_sse_clear_records(void* h) { static_cast<orc::sse_chain_t*>(h)->records.clear(); }
+int orc_sse_get_state(void* h, int* spins, uint32_t* ops, int cap) {
+  orc::sse_chain_t* c = static_cast<orc::sse_chain_t*>(h);
+  for (int s = 0; s < c->lat.N; ++s) spins[s] = c->spins[s];
+  const int n = (int)c->ops.size();
+  for (int i = 0; i < n && i < cap; ++i) ops[i] = c->ops[i];
+  return n;
+}
+void orc_sse_set_state(void* h, const int* spins, const uint32_t* ops, int n, uint32_t sweep) {
+  orc::sse_chain_t* c = static_cast<orc::sse_chain_t*>(h);
+  for (int s = 0; s < c->lat.N; ++s) c->spins[s] = spins[s] & 1;
+  c->ops.assign(ops, ops + n);
+  c->sweep = sweep;
+}
 
 // Cluster labels of a given configuration (time-ordered vertex list), following the fragment
 // numbering of path_integral.C:482 / graph_impl.h:285-288: sites first, then one fragment per

@@ -3,7 +3,7 @@
 Sources:
   * standalone/loop.op            -> standalone_loop_op.json   (deterministic standalone run)
   * test/union_find.op            -> union_find_op.json        (100 unions + full listing)
-  * loop.op (diag + PI blocks)    -> loop_op.json              (known answers, L=4 chains,
+  * loop.op (diag, PI, SSE)      -> loop_op.json              (known answers, L=4 chains,
                                                                   with the correlation vectors)
   * oracle (philox mode) configs  -> uf_labels.json            (cluster-construction configs)
   * oracle/ed.py (momentum ED)    -> ed_chain16.json           (exact L=16 chain at T=0.1)
@@ -94,7 +94,7 @@ def loop_op(ref):
     for i, hdr in blocks:
         h = "\n".join(hdr)
         alg = lines[i].split("=", 1)[1].strip().rstrip(";").strip('"')
-        if alg not in ("diagonalization", "loop; path integral"):
+        if alg not in ("diagonalization", "loop; path integral", "loop; sse"):
             continue
         lat = re.findall(r'LATTICE = "?([^";]+)"?;', h)
         if not lat or lat[-1] != "chain lattice":

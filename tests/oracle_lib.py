@@ -141,6 +141,58 @@ class Oracle:
         return lab[:n].copy(), lib().orc_last_nc(self._h)
 
 
+class SseOracle:
+    """One SSE chain (sse.C) in philox mode: the random source of the GPU's SSE form."""
+
+    def __init__(self, dim, L, beta, jxy=1.0, jz=1.0, seed=1, random_spins=True):
+        self.dim, self.L, self.beta = dim, L, beta
+        p = _P(dim, L, beta, jxy, jz, 0.0, 0.0, seed, 1 if random_spins else 0, 1, 1)
+        L_ = lib()
+        L_.orc_sse_create.restype = ctypes.c_void_p
+        L_.orc_sse_create.argtypes = [ctypes.c_void_p]
+        self._h = ctypes.c_void_p(L_.orc_sse_create(ctypes.byref(p)))
+        assert self._h.value
+        self.N = L ** dim
+
+    def close(self):
+        if self._h:
+            lib().orc_sse_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sweep(self, n=1):
+        lib().orc_sse_sweep(self._h, ctypes.c_int(n))
+
+    def records(self):
+        n = lib().orc_sse_num_records(self._h)
+        r = np.zeros(n * RECORD_WORDS, dtype=np.uint64)
+        if n:
+            lib().orc_sse_get_records(self._h, _ptr(r))
+        return r.reshape(n, RECORD_WORDS)
+
+    def clear_records(self):
+        lib().orc_sse_clear_records(self._h)
+
+    def state(self):
+        """(spins at the bottom, operator codes bond << 1 | off-diagonal in string order)"""
+        cap = 1 << 22
+        spins = np.zeros(self.N, dtype=np.int32)
+        ops = np.zeros(cap, dtype=np.uint32)
+        n = lib().orc_sse_get_state(self._h, _ptr(spins), _ptr(ops), ctypes.c_int(cap))
+        return spins, ops[:n].copy()
+
+    def set_state(self, spins, ops, sweep):
+        spins = np.ascontiguousarray(spins, dtype=np.int32)
+        ops = np.ascontiguousarray(ops, dtype=np.uint32)
+        lib().orc_sse_set_state(self._h, _ptr(spins), _ptr(ops), ctypes.c_int(len(ops)),
+                                ctypes.c_uint32(sweep))
+
+
 def standalone(L, T, sweeps, therm):
     out = np.zeros(10)
     speed = ctypes.c_double()
@@ -227,6 +279,36 @@ def observables(records, dim, L, beta, jxy=1.0, jz=1.0, h=0.0, spin2=1):
         out["Staggered Magnetization^2"] = ms ** 2
         out["Staggered Susceptibility"] = beta * sma ** 2 / N
     return out
+
+
+def sse_observables(records, dim, L, beta, jxy=1.0, jz=1.0, normal=False):
+    """Per-sweep observables from SSE oracle records: energy as on the path-integral form
+    (sse.C:383-384, energy.h:76-84) and the SSE susceptibilities of the improved estimator
+    (susceptibility.h:224-225, 231-232): beta (dip(integral, n) + tau0) / (n + 1) / V, with the
+    time-integrated sums in operator-index units."""
+    r = records
+    N = L ** dim
+    NB = N * dim
+    v, W = weights(jxy, jz)
+    nop = r[:, 0].astype(np.float64)
+    ene = NB * W / 2 - nop / beta
+    dip = lambda x: np.where(nop > 0, x / np.maximum(nop, 1), 0.0)  # noqa: E731
+    if normal:  # susceptibility.h:303-335: M at the bottom, its operator-index integral MA
+        s = lambda i: r[:, i].view(np.int64).astype(np.float64)  # noqa: E731
+        m, sm, ma, sma = s(2) / 2, s(3) / 2, s(25) / 2, s(26) / 2
+        return {"Energy": ene, "Energy^2": ene ** 2 - nop / beta ** 2,
+                "Magnetization^2": m ** 2,
+                "Susceptibility": beta * (dip(ma ** 2) + m ** 2) / (nop + 1) / N,
+                "Staggered Magnetization^2": sm ** 2,
+                "Staggered Susceptibility": beta * (dip(sma ** 2) + sm ** 2) / (nop + 1) / N}
+    m2 = r[:, 4].astype(np.float64) / 4
+    sm2 = r[:, 6].astype(np.float64) / 4
+    return {"Energy": ene, "Energy^2": ene ** 2 - nop / beta ** 2,
+            "Number of Clusters": r[:, 1].astype(np.float64),
+            "Magnetization^2": m2,
+            "Susceptibility": beta * (dip(u128(r, 18) / 4) + m2) / (nop + 1) / N,
+            "Staggered Magnetization^2": sm2,
+            "Staggered Susceptibility": beta * (dip(u128(r, 22) / 4) + sm2) / (nop + 1) / N}
 
 
 def binned(x, nbins=64):

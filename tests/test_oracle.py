@@ -250,6 +250,68 @@ def test_philox_xy_chain_vs_ed():
                   "Staggered Susceptibility"])
 
 
+def _check_sse_vs_ed(dim, L, T, jxy, jz, therm, sweeps, seed, keys, normal=False):
+    beta = 1.0 / T
+    o = orc.SseOracle(dim, L, beta, jxy, jz, seed=seed)
+    o.sweep(therm)
+    o.clear_records()
+    o.sweep(sweeps)
+    obs = orc.sse_observables(o.records(), dim, L, beta, jxy, jz, normal=normal)
+    ref = orc.ed.thermal(dim, L, T, jxy=jxy, jz=jz)
+    for k in keys:
+        if k == "Specific Heat":
+            m, e = orc.specific_heat(obs, beta, L ** dim)
+        else:
+            m, e = orc.binned(obs[k])
+        assert abs(m - ref[k]) <= 3.5 * e + 1e-12, (k, m, e, ref[k])
+
+
+SSE_KEYS = ["Energy", "Specific Heat", "Magnetization^2", "Susceptibility",
+            "Staggered Magnetization^2", "Staggered Susceptibility"]
+
+
+def test_sse_oracle_agrees_with_reference_sse_blocks(golden):
+    # every S = 1/2 "loop; sse" block of loop.op (Heisenberg ring T = 0.25 and Ising ring
+    # T = 0.5, L = 4, 4096 sweeps each) within 3 combined sigma of the restatement, the number of
+    # clusters included (it depends on the fragments the SSE string makes)
+    n = 0
+    for b in golden("loop_op.json"):
+        if b["algorithm"] != "loop; sse" or b.get("spin2", 1) != 1:
+            continue
+        beta = 1.0 / b["T"]
+        o = orc.SseOracle(1, b["L"], beta, b["jxy"], b["jz"], seed=31 + n)
+        o.sweep(1000)
+        o.clear_records()
+        o.sweep(1 << 16)
+        obs = orc.sse_observables(o.records(), 1, b["L"], beta, b["jxy"], b["jz"])
+        for k, (v, e) in b["values"].items():
+            if k == "Specific Heat":
+                m, err = orc.specific_heat(obs, beta, b["L"])
+            else:
+                m, err = orc.binned(obs[k])
+            assert abs(m - v) <= 3.0 * (err ** 2 + float(e) ** 2) ** 0.5, (b["T"], k, m, err, v, e)
+            n += 1
+    assert n == 14
+
+
+@pytest.mark.parametrize("case", [
+    (1, 8, 0.5, 1.0, 1.0),      # Heisenberg ring
+    (1, 6, 0.3, 1.0, 0.5),      # XXZ
+    (1, 6, 0.4, 1.0, 0.0),      # XY: graphs 0 and 1 at equal weight
+    (1, 6, 0.5, -1.0, -0.5),    # ferromagnetic: the crossed graph and its frozen form
+    (1, 4, 0.5, 0.0, 1.0),      # Ising: frozen graphs only
+    (2, 2, 0.5, 1.0, 1.0),      # 2x2 square (doubled bonds)
+    (3, 2, 0.5, 1.0, 0.5),      # 2x2x2 cube
+])
+def test_sse_oracle_vs_ed(case):
+    dim, L, T, jxy, jz = case
+    _check_sse_vs_ed(dim, L, T, jxy, jz, 1000, 40000, 40 + L + dim, SSE_KEYS)
+
+
+def test_sse_oracle_normal_estimator_vs_ed():
+    _check_sse_vs_ed(1, 6, 0.5, 1.0, 1.0, 1000, 60000, 77, SSE_KEYS, normal=True)
+
+
 def test_momentum_ed_matches_dense_ed():
     for (L, T, jxy, jz, h) in [(8, 0.3, 1.0, 0.5, 0.2), (8, 1.0, -1.0, 1.0, 0.0)]:
         a = orc.ed.thermal(1, L, T, jxy=jxy, jz=jz, h=h)
