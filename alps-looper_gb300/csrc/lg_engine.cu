@@ -124,7 +124,7 @@ struct Engine {
   int C = 0, N = 0, NB = 0;
   std::vector<DChain> hch;
   std::vector<int> h_bond_s0, h_bond_s1, h_inc_off, h_inc, h_inc_nbr;
-  std::vector<uint8_t> h_inc_side, h_bond_dir0, h_inc_dir;
+  std::vector<uint8_t> h_inc_side, h_bond_dir0, h_bond_dir1, h_inc_dir;  // dir0/1: incidence index at s0/s1
   std::vector<int> h_site_chain, h_bond_chain;
 
   DBuf<DChain> d_ch;
@@ -204,7 +204,7 @@ struct Engine {
   DBuf<uint8_t> rb_spin0, rb_sdir;
   DBuf<int> rb_off_base, rb_off_cnt;
   DBuf<uint64_t> rb_stime;
-  // ---- the SSE form (k_sse: one thread per chain): operator strings of sse_ocap entries per
+  // ---- the SSE form (k_sse: one chain per warp): operator strings of sse_ocap entries per
   // chain, double-buffered with the spins (rb_spin0) like the resident path's state
   bool sse = false;
   int sse_ocap = 0, sse_fcap = 0, sse_grid = 0;
@@ -279,6 +279,7 @@ struct Engine {
     N = (int)nsite; NB = (int)nbond;
     hch.resize(C);
     h_bond_s0.resize(NB); h_bond_s1.resize(NB); h_bond_chain.resize(NB); h_bond_dir0.resize(NB);
+    h_bond_dir1.resize(NB);
     h_site_chain.resize(N);
     std::vector<int8_t> h_gauge(N);
     h_inc_off.assign(N + 1, 0);
@@ -326,6 +327,9 @@ struct Engine {
       int a = h_bond_s0[b];
       for (int j = h_inc_off[a]; j < h_inc_off[a + 1]; ++j)
         if (h_inc[j] == b && h_inc_side[j] == 0) { h_bond_dir0[b] = (uint8_t)(j - h_inc_off[a]); break; }
+      const int t = h_bond_s1[b];
+      for (int j = h_inc_off[t]; j < h_inc_off[t + 1]; ++j)
+        if (h_inc[j] == b) { h_bond_dir1[b] = (uint8_t)(j - h_inc_off[t]); break; }
     }
     int rc;
     if ((rc = d_ch.alloc(C)) || (rc = d_bond_s0.alloc(NB)) || (rc = d_bond_s1.alloc(NB)) ||
@@ -373,7 +377,11 @@ struct Engine {
     sse = any_sse;
     if (sse) {
       if ((rc = setup_sse(res_vcap_for(1.0), false))) return rc;
-    } else if (allow_resident && res_fits(res_vcap_for(1.0), RES_SMEM_DEFAULT)) {
+    } else if (allow_resident && C >= nsm && res_fits(res_vcap_for(1.0), RES_SMEM_DEFAULT)) {
+      // chain-resident by default from one chain per SM on (1024 64-site chains at beta = 10:
+      // 0.21 against 0.33 ms per sweep); a few chains would leave most SMs idle while one CTA
+      // walks each chain's serial phases, and the grid path spreads them over the GPU (a lone
+      // such chain: 39 against 86 us).  The autotuner times both either way.
       if ((rc = setup_resident(res_vcap_for(1.0)))) return rc;
       shape = default_shape();
       shape.resident = 1;
@@ -434,7 +442,7 @@ struct Engine {
     } else {
       LG_CUDA(cudaMemset(sse_nop.p, 0, C * sizeof(int)));
     }
-    sse_grid = std::max(1, std::min((C + SSE_THREADS - 1) / SSE_THREADS, nsm * 16));
+    sse_grid = std::max(1, std::min((C + SSE_WARPS - 1) / SSE_WARPS, nsm * 16));
     return LG_OK;
   }
 
@@ -477,6 +485,8 @@ struct Engine {
         Ctl z0 = hc;
         z0.err = 0;
         LG_CUDA(lg_copy(d_ctl.p, &z0, sizeof(Ctl), cudaMemcpyHostToDevice));
+        if (hc.err == ERR_BOUNDARY)
+          return lg_fail(LG_EINVAL, "spin-S configuration not periodic in imaginary time");
         if (hc.err != ERR_OVERFLOW) return lg_fail(LG_EDEVICE, "SSE sweep failed (%d)", hc.err);
         const long long o2 = std::min<long long>(1ll << 28, ((long long)sse_ocap * 3 / 2 + 63) & ~31ll);
         if (o2 <= sse_ocap) return lg_fail(LG_EBUDGET, "SSE operator string too long");
@@ -516,7 +526,7 @@ struct Engine {
   }
 
   // Replace chain c's SSE state (checked first: bonds in range, and every site's spin periodic
-  // through the string).
+  // through the string; for S > 1/2 every real site's number of up virtual spins).
   int sse_set(int c, const int32_t* spins, const std::vector<uint32_t>& ops, uint64_t sweep) {
     const ChainSpec& s = spec[c];
     std::vector<uint8_t> sp(s.N), cur(s.N);
@@ -526,9 +536,12 @@ struct Engine {
       if ((int)b >= s.NB) return lg_fail(LG_EINVAL, "operator %zu out of range", i);
       if (ops[i] & 1u) { cur[s.s0[b]] ^= 1u; cur[s.s1[b]] ^= 1u; }
     }
-    for (int i = 0; i < s.N; ++i)
-      if (cur[i] != sp[i])
-        return lg_fail(LG_EINVAL, "site %d: the string is not periodic in imaginary time", i);
+    const int q = std::max(1, s.spin2);
+    for (int i = 0; i < s.N; i += q) {
+      int a = 0, b = 0;
+      for (int k = 0; k < q; ++k) { a += cur[i + k]; b += sp[i + k]; }
+      if (a != b) return lg_fail(LG_EINVAL, "site %d: the string is not periodic in imaginary time", i / q);
+    }
     if ((long long)ops.size() > sse_ocap) {
       int rc = setup_sse((int)std::min<long long>(1ll << 28, ((long long)ops.size() * 3 / 2 + 63) & ~31ll), true);
       if (rc) return rc;
@@ -1236,8 +1249,8 @@ struct Engine {
   // with the narrow / wide split, and the fastest shape is kept.  The timed sweeps are the
   // chains' own sweeps: no shape changes a result, so tuning costs no extra sweeps.
   int autotune(int trial, size_t flush_bytes, std::string& report) {
-    if (sse) {  // one thread per chain: nothing to choose
-      report = "chosen: SSE form (one thread per chain)\n";
+    if (sse) {  // one chain per warp: nothing to choose
+      report = "chosen: SSE form (one chain per warp)\n";
       return run(trial);
     }
     if (trial < 1) trial = 1;
@@ -1420,17 +1433,22 @@ struct Engine {
     LG_CUDA(lg_copy(oc.data(), d_off_cnt.p + so, s.N * sizeof(int), cudaMemcpyDeviceToHost));
     spins.assign(sp.begin(), sp.end());
     std::vector<std::pair<uint64_t, int>> ops;
+    // one copy of each list array over the span the chain's lists occupy
+    long long lo = -1, hi = 0;
+    for (int i = 0; i < s.N; ++i)
+      if (oc[i]) { lo = lo < 0 ? ob[i] : std::min<long long>(lo, ob[i]); hi = std::max<long long>(hi, (long long)ob[i] + oc[i]); }
+    std::vector<uint64_t> t(lo < 0 ? 0 : hi - lo);
+    std::vector<uint8_t> d(t.size());
+    if (!t.empty()) {
+      LG_CUDA(lg_copy(t.data(), d_stime.p + lo, t.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+      LG_CUDA(lg_copy(d.data(), d_sdir.p + lo, d.size(), cudaMemcpyDeviceToHost));
+    }
     for (int i = 0; i < s.N; ++i) {
-      if (!oc[i]) continue;
-      std::vector<uint64_t> t(oc[i]);
-      std::vector<uint8_t> d(oc[i]);
-      LG_CUDA(lg_copy(t.data(), d_stime.p + ob[i], oc[i] * sizeof(uint64_t), cudaMemcpyDeviceToHost));
-      LG_CUDA(lg_copy(d.data(), d_sdir.p + ob[i], oc[i], cudaMemcpyDeviceToHost));
-      int gs = so + i;
+      const int gs = so + i;
       for (int j = 0; j < oc[i]; ++j) {
-        int idx = h_inc_off[gs] + d[j];
+        const int idx = h_inc_off[gs] + d[ob[i] - lo + j];
         if (h_inc_side[idx] != 0) continue;  // take each operator once, from its source site
-        ops.push_back({t[j], h_inc[idx] - hch[c].bond_off});
+        ops.push_back({t[ob[i] - lo + j], h_inc[idx] - hch[c].bond_off});
       }
     }
     std::sort(ops.begin(), ops.end());
@@ -1468,16 +1486,28 @@ struct Engine {
 
   // Lay the lists out contiguously from segment 0 and upload them.
   int upload_lists(const SiteLists& L) {
-    std::vector<int> ob(N), oc(N);
+    std::vector<int> oc(N);
     long long total = 0;
-    for (int i = 0; i < N; ++i) { ob[i] = (int)total; oc[i] = (int)L[i].size(); total += oc[i]; }
+    for (int i = 0; i < N; ++i) { oc[i] = (int)L[i].size(); total += oc[i]; }
+    std::vector<uint64_t> t(total);
+    std::vector<uint8_t> d(total);
+    for (long long i = 0, k = 0; i < N; ++i)
+      for (const auto& e : L[i]) { t[k] = e.first; d[k] = e.second; ++k; }
+    return upload_flat(oc, t, d);
+  }
+
+  // The same from the lists of every site packed in site order (oc[i] entries for site i).
+  int upload_flat(const std::vector<int>& oc, const std::vector<uint64_t>& t, const std::vector<uint8_t>& d) {
+    std::vector<int> ob(N);
+    long long total = 0;
+    for (int i = 0; i < N; ++i) { ob[i] = (int)total; total += oc[i]; }
     if (resident) {
       // the list arrays hold res_lcap entries per chain; a chain with more grows the capacity
       long long need = 0;
       for (int c = 0; c < C; ++c) {
-        long long t = 0;
-        for (int i = 0; i < spec[c].N; ++i) t += (long long)L[hch[c].site_off + i].size();
-        need = std::max(need, t);
+        long long n = 0;
+        for (int i = 0; i < spec[c].N; ++i) n += oc[hch[c].site_off + i];
+        need = std::max(need, n);
       }
       if (need > res_lcap || total > (long long)d_stime.n) {
         const int v2 = (int)std::min<long long>(1ll << 24, ((std::max<long long>(need, res_lcap) * 3 / 4) + 63) & ~31ll);
@@ -1488,7 +1518,7 @@ struct Engine {
           rb_off_cnt.release();
           int rc = setup_grid();
           if (rc) return rc;
-          return upload_lists(L);
+          return upload_flat(oc, t, d);
         }
         int rc = setup_resident(v2);
         if (rc) return rc;
@@ -1497,10 +1527,6 @@ struct Engine {
       int rc = alloc_dynamic(total + 4096, false);
       if (rc) return rc;
     }
-    std::vector<uint64_t> t(total);
-    std::vector<uint8_t> d(total);
-    for (int i = 0; i < N; ++i)
-      for (int j = 0; j < oc[i]; ++j) { t[ob[i] + j] = L[i][j].first; d[ob[i] + j] = L[i][j].second; }
     LG_CUDA(lg_copy(d_off_base.p, ob.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     LG_CUDA(lg_copy(d_off_cnt.p, oc.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     if (total) {
@@ -1566,8 +1592,29 @@ struct Engine {
           return lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
                                     "(not periodic in imaginary time)", i);
     for (int i = 0; i < s.N; ++i) start[i + 1] += start[i];
-    std::vector<std::pair<uint64_t, int>> ep(2 * n);  // (time bits, global bond)
-    {
+    // the chain's lists, packed in site order: (time bits, incidence index)
+    std::vector<uint64_t> ft(2 * n);
+    std::vector<uint8_t> fd(2 * n);
+    bool ordered = true;  // (time, bond) ascending, as lg_save writes them
+    for (long long i = 1; i < n && ordered; ++i) {
+      uint64_t ta, tb;
+      std::memcpy(&ta, &times[i - 1], 8);
+      std::memcpy(&tb, &times[i], 8);
+      ordered = ta < tb || (ta == tb && bonds[i - 1] <= bonds[i]);
+    }
+    if (ordered) {  // every site's entries arrive in the order the sweep produces
+      std::vector<long long> fill(start.begin(), start.end() - 1);
+      const int bo = hch[c].bond_off;
+      for (long long i = 0; i < n; ++i) {
+        const int b = bonds[i];
+        uint64_t tb;
+        std::memcpy(&tb, &times[i], 8);
+        const long long k0 = fill[s.s0[b]]++, k1 = fill[s.s1[b]]++;
+        ft[k0] = tb; fd[k0] = h_bond_dir0[b + bo];
+        ft[k1] = tb; fd[k1] = h_bond_dir1[b + bo];
+      }
+    } else {
+      std::vector<std::pair<uint64_t, int>> ep(2 * n);  // (time bits, global bond)
       std::vector<long long> fill(start.begin(), start.end() - 1);
       for (long long i = 0; i < n; ++i) {
         const int b = bonds[i];
@@ -1576,25 +1623,24 @@ struct Engine {
         ep[fill[s.s0[b]]++] = {tb, b + hch[c].bond_off};
         ep[fill[s.s1[b]]++] = {tb, b + hch[c].bond_off};
       }
+      for (int i = 0; i < s.N; ++i) {
+        std::sort(ep.begin() + start[i], ep.begin() + start[i + 1]);  // the order the sweep produces
+        const int gs = so + i;
+        for (long long k = start[i]; k < start[i + 1]; ++k) {
+          const int gb = ep[k].second;
+          ft[k] = ep[k].first;
+          fd[k] = h_bond_s0[gb] == gs ? h_bond_dir0[gb] : h_bond_dir1[gb];
+        }
+      }
     }
     SiteLists L;
     int rc;
     if (C > 1) {  // the other chains' lists stay as they are
       if ((rc = download_lists(L))) return rc;
-    } else {
-      L.assign(N, {});
-    }
-    for (int i = 0; i < s.N; ++i) {
-      std::sort(ep.begin() + start[i], ep.begin() + start[i + 1]);  // the order the sweep produces
-      const int gs = so + i;
-      auto& Li = L[gs];
-      Li.clear();
-      Li.reserve(start[i + 1] - start[i]);
-      for (long long k = start[i]; k < start[i + 1]; ++k) {
-        int dir = -1;
-        for (int j = h_inc_off[gs]; j < h_inc_off[gs + 1]; ++j)
-          if (h_inc[j] == ep[k].second) { dir = j - h_inc_off[gs]; break; }
-        Li.push_back({ep[k].first, (uint8_t)dir});
+      for (int i = 0; i < s.N; ++i) {
+        auto& Li = L[so + i];
+        Li.clear();
+        for (long long k = start[i]; k < start[i + 1]; ++k) Li.push_back({ft[k], fd[k]});
       }
     }
     if (C == 1) {  // a complete, valid state: a union-find failure (LG_EITERCAP) no longer applies
@@ -1604,7 +1650,13 @@ struct Engine {
       hc.step = 0;
       LG_CUDA(lg_copy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
     }
-    if ((rc = upload_lists(L))) return rc;
+    if (C > 1) {
+      if ((rc = upload_lists(L))) return rc;
+    } else {
+      std::vector<int> oc(s.N);
+      for (int i = 0; i < s.N; ++i) oc[i] = (int)(start[i + 1] - start[i]);
+      if ((rc = upload_flat(oc, ft, fd))) return rc;
+    }
     std::vector<uint8_t> sp(s.N);
     for (int i = 0; i < s.N; ++i) sp[i] = (uint8_t)(spins[i] & 1);
     LG_CUDA(lg_copy(d_spin0.p + so, sp.data(), s.N, cudaMemcpyHostToDevice));

@@ -274,10 +274,9 @@ int ChainSpec::init(const lg_params& p) {
   if (p.algorithm != LG_PATH_INTEGRAL && p.algorithm != LG_SSE)
     return lg_fail(LG_EINVAL, "unknown ALGORITHM %d", p.algorithm);
   if (sse) {
-    // sse.C:139 checks the model without longitudinal field support; S > 1/2 and correlations
-    // are not built for the SSE form here
+    // sse.C:123 checks the model without longitudinal field support; correlations are not
+    // built for the SSE form here
     if (field) return lg_fail(LG_EUNSUPPORTED, "the SSE worker supports no longitudinal field");
-    if (spin2 > 1) return lg_fail(LG_EUNSUPPORTED, "the SSE form runs S = 1/2 only");
     if (p.measure_correlations || p.measure_structure_factor)
       return lg_fail(LG_EUNSUPPORTED, "correlations are measured by the path-integral form only");
   }
@@ -666,14 +665,22 @@ extern "C" const char* lg_obs_name(int i) {
 // ---------------------------------------------------------------------------------------------
 // Checkpoint: the worker's save/load content (path_integral.C:111-124: mcs, spins, operators).
 // Layout (little endian): "LGCK" u32 version, u32 dim, u32 L, u64 mcs, u64 n_ops,
-// N x u8 spins, n_ops x (i32 bond, f64 time), u64 FNV-1a of everything before it.  Version 1:
+// N x u8 spins, n_ops x (i32 bond, f64 time), u64 checksum of everything before it (FNV-1a over
+// its 64-bit little-endian words, then over its remaining bytes).  Version 1:
 // the path-integral form, its off-diagonal operators with their times.  Version 2: the SSE form
 // (sse.C save: mcs, spins, operators), every operator of the string as bond << 1 | off-diagonal,
 // with (index + 1/2) / n_ops as its time (the order).
 // ---------------------------------------------------------------------------------------------
 static uint64_t fnv1a(const uint8_t* p, size_t n) {
   uint64_t h = 1469598103934665603ull;
-  for (size_t i = 0; i < n; ++i) { h ^= p[i]; h *= 1099511628211ull; }
+  size_t i = 0;
+  for (; i + 8 <= n; i += 8) {  // 64-bit little-endian words (8x fewer dependent multiplies)
+    uint64_t w = 0;
+    for (int k = 7; k >= 0; --k) w = (w << 8) | p[i + k];
+    h ^= w;
+    h *= 1099511628211ull;
+  }
+  for (; i < n; ++i) { h ^= p[i]; h *= 1099511628211ull; }
   return h;
 }
 

@@ -1,4 +1,4 @@
-// The stochastic series expansion (SSE) loop worker of sse.C, batched: one GPU thread per chain.
+// The stochastic series expansion (SSE) loop worker of sse.C, batched: one chain per warp.
 //
 // The SSE representation keeps an ordered operator string without times.  Its diagonal update is
 // one sequential walk (sse.C:201-250): at every gap an insertion is tried with probability
@@ -7,8 +7,8 @@
 // n / (beta W) or re-draws its graph; off-diagonal operators re-draw theirs.  The acceptance
 // probabilities depend on the running count, so the walk cannot be split across threads; what
 // the GPU offers is thousands of such walks side by side, one per chain, which is the form here:
-// each thread owns a chain for a whole chunk of sweeps (k_sse), and the chains of an arena are
-// spread over the grid.
+// one thread (the first lane of a warp) owns a chain for a whole chunk of sweeps (k_sse), and
+// the chains of an arena are spread over the grid.
 //
 // Per sweep and chain the thread does what sse.C does, in the same order:
 //   walk           insertions / removals / graph choices (sse.C:201-250), the spin propagation and
@@ -16,7 +16,10 @@
 //                  and the improved estimator's contributions of every world-line piece
 //                  (susceptibility.h:116-150, stiffness.h:82-130), added to the fragment the piece
 //                  belongs to (the operator index is the SSE "time")
-//   closure        every site's top fragment joined to its bottom one (sse.C:275-277)
+//   closure        every site's top fragment joined to its bottom one (sse.C:275-277); for S > 1/2
+//                  the bottom of virtual site a joins the top of pair[a], a matching within each
+//                  spin sector of the real site (sse.C:278-296), the path-integral form's
+//                  boundary_pairs draw
 //   clusters       fragments summed into their roots (the smallest fragment index: deterministic
 //                  unify), a coin per cluster keyed by its root, the exact per-sweep sums
 //                  (susceptibility.h:182-198) into the record row
@@ -109,6 +112,7 @@ __device__ void sse_chain(const Arena& A, const SseArgs& S, int c) {
   int nop = S.nop_in[c];
   uint32_t sweep = A.ch_sweep[c];
   const double bw = ch.sse_bw;
+  const uint32_t q2 = (uint32_t)(ch.spin2 > 1 ? ch.spin2 * ch.spin2 : 1);
   for (int step = 0; step < S.m; ++step, ++sweep) {
     // strings: the launch's input, then alternating so that the last sweep writes ops_out
     const uint32_t* in = step == 0 ? S.ops_in + obase
@@ -161,7 +165,7 @@ __device__ void sse_chain(const Arena& A, const SseArgs& S, int c) {
       if (nn >= S.ocap || fid >= S.fcap) { atomicExch(&A.ctl->err, ERR_OVERFLOW); return; }
       const int s0 = A.bond_s0[bo + b] - so, s1 = A.bond_s1[bo + b] - so;
       const int gs0 = A.gauge[so + s0], gs1 = A.gauge[so + s1];
-      const int d = (int)(b % (uint32_t)dim);
+      const int d = (int)((b / q2) % (uint32_t)dim);   // bond = (site dim + d) (2S)^2 + pair
       const bool frozen = (g & 2u) != 0;
       const int a0 = cur[s0], a1 = cur[s1];
       const int c0 = spc[s0], c1 = spc[s1];
@@ -201,9 +205,19 @@ __device__ void sse_chain(const Arena& A, const SseArgs& S, int c) {
       ++nn;
     }
     nop = nn;
-    for (int s = 0; s < N; ++s) {  // stop_top, then the closure in imaginary time
-      sse_piece(est + 8 * cur[s], 1, nop, spc[s], A.gauge[so + s]);
-      sse_unify(frag, s, cur[s]);
+    for (int s = 0; s < N; ++s) sse_piece(est + 8 * cur[s], 1, nop, spc[s], A.gauge[so + s]);  // stop_top
+    const int sp2 = ch.spin2;
+    if (sp2 <= 1) {                // the closure in imaginary time
+      for (int s = 0; s < N; ++s) sse_unify(frag, s, cur[s]);
+    } else {
+      for (int off = 0, rs = 0; off < N; off += sp2, ++rs) {
+        int pair[8];
+        if (!boundary_pairs(ch.seed, sweep, (uint32_t)rs, sp2, spins + off, spc + off, pair)) {
+          atomicExch(&A.ctl->err, ERR_BOUNDARY);
+          return;
+        }
+        for (int a = 0; a < sp2; ++a) sse_unify(frag, off + a, cur[off + pair[a]]);
+      }
     }
     // clusters: fragment sums into their roots
     for (int f = 0; f < fid; ++f) {
@@ -270,11 +284,18 @@ __device__ void sse_chain(const Arena& A, const SseArgs& S, int c) {
   A.ch_sweep[c] = sweep;
 }
 
-constexpr int SSE_THREADS = 64;
+// One chain per warp, walked by its first lane: the walks are sequential and branchy, so lanes
+// of one warp walking different chains would serialise on every divergent branch, and a chain
+// per warp spreads an arena over every SM (1024 chains: 7 walks per SM instead of 64 lanes on
+// each of 16 SMs).
+constexpr int SSE_WARPS = 4;
+constexpr int SSE_THREADS = 32 * SSE_WARPS;
 
 __global__ void __launch_bounds__(SSE_THREADS) k_sse(Arena A, SseArgs S) {
   if (A.ctl->err) return;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < A.C; c += gridDim.x * blockDim.x) {
+  if ((threadIdx.x & 31) != 0) return;
+  const int warps = gridDim.x * SSE_WARPS;
+  for (int c = blockIdx.x * SSE_WARPS + (threadIdx.x >> 5); c < A.C; c += warps) {
     if (!A.all_active && !A.ch_active[c]) continue;
     sse_chain(A, S, c);
   }

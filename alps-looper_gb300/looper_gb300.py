@@ -377,8 +377,8 @@ class LoopWorker:
         return buf.raw[:n.value]
 
     def load(self, blob: bytes):
-        buf = ctypes.create_string_buffer(blob, len(blob))
-        check(lib().lg_load(self._h, buf, len(blob)))
+        blob = bytes(blob)  # read in place (lg_load copies nothing it keeps)
+        check(lib().lg_load(self._h, ctypes.c_char_p(blob), len(blob)))
 
     def time_sweeps(self, n, flush_bytes=0):
         """Device time (ms) of each of n sweeps, L2 flushed between sweeps."""

@@ -638,8 +638,9 @@ struct chain_t {
 };
 
 // ----------------------------------------------------------------------------------------------
-// SSE chain: restates the stochastic-series-expansion loop worker (sse.C:180-371) for S=1/2 XXZ
-// models without field, in philox mode.  The configuration is an ordered operator string with no
+// SSE chain: restates the stochastic-series-expansion loop worker (sse.C:180-371) for spin-S XXZ
+// models without field (sse.C:123 refuses a longitudinal field), in philox mode; S > 1/2 on the
+// virtual lattice of the path-integral chain.  The configuration is an ordered operator string with no
 // times; operator code = bond << 1 | off-diagonal.  One sweep:
 //   * diagonal update & labelling (sse.C:201-276): a walk over the old string; before every
 //     operator (and once more at the end) an insertion is tried with probability
@@ -647,7 +648,10 @@ struct chain_t {
 //     compatible; a diagonal operator is removed with probability n / (beta W_tot), otherwise its
 //     graph is re-chosen (choose_diagonal, graph_impl.h:297-312); an off-diagonal one re-chooses
 //     (choose_offdiagonal, :314-327).  Spins propagate and fragments reconnect (:280-295).
-//   * closure of every site's top onto its bottom (sse.C:275-277)
+//   * closure of every site's top onto its bottom (sse.C:275-277); for S > 1/2 the bottom of
+//     virtual site a joins the top of pair[a], a matching within each spin sector
+//     (sse.C:278-296, partitioned_random_shuffle), drawn as in the path-integral chain
+//     (boundary_matching)
 //   * cluster ids (sse.C:305-306) and the improved estimators in a second pass over the new string
 //     with the loop_l / loop_u fragments of each operator (sse.C:314-354; graph_impl.h:489-494);
 //     the operator index is the time.  The normal estimator's time-integrated magnetization is
@@ -672,6 +676,7 @@ struct sse_chain_t {
   std::vector<uint32_t> ops;
   uint32_t sweep = 0;
   std::vector<uint64_t> records;
+  int status = 0;  // 1: a boundary had spin sectors of different sizes
 
   void init_derived() {
     const double W = bw.W;
@@ -768,7 +773,19 @@ struct sse_chain_t {
       MA += (int64_t)(1 - 2 * sc[s]) * T;
       SMA += (int64_t)lat.gauge[s] * (1 - 2 * sc[s]) * T;
     }
-    for (int s = 0; s < N; ++s) frag.unify(s, current[s]);
+    if (lat.spin2 <= 1) {
+      for (int s = 0; s < N; ++s) frag.unify(s, current[s]);
+    } else {
+      for (int rs = 0; rs < lat.NR; ++rs) {
+        const int off = rs * lat.spin2;
+        int pair[8];
+        if (!boundary_matching(seed, sweep, (uint32_t)rs, lat.spin2, &spins[off], &sc[off], pair)) {
+          status = 1;
+          return;
+        }
+        for (int a = 0; a < lat.spin2; ++a) frag.unify(off + a, current[off + pair[a]]);
+      }
+    }
     const int nf = (int)frag.parent.size();
     const int nc = frag.set_ids();
 
@@ -1067,12 +1084,12 @@ int orc_last_labels(void* h, int* labels, int cap) {
 }
 int orc_last_nc(void* h) { return static_cast<orc::chain_t*>(h)->last_nc; }
 
-// SSE chains (sse_chain_t): create from the same parameters (h must be 0, spin2 1), sweep, the
+// SSE chains (sse_chain_t): create from the same parameters (h must be 0), sweep, the
 // per-sweep records, and the state (spins at the bottom and the operator codes in order).
 void* orc_sse_create(const orc_params* p) {
-  if (std::fabs(p->h) > 0 || p->spin2 > 1) return nullptr;
+  if (std::fabs(p->h) > 0) return nullptr;
   orc::sse_chain_t* c = new orc::sse_chain_t();
-  c->lat.build(p->dim, p->L, 1);
+  c->lat.build(p->dim, p->L, p->spin2 > 1 ? p->spin2 : 1);
   c->bw = orc::make_weight(p->jxy, p->jz, p->force_scatter);
   c->beta = p->beta;
   c->seed = p->seed;
@@ -1088,6 +1105,7 @@ void* orc_sse_create(const orc_params* p) {
   return c;
 }
 void orc_sse_destroy(void* h) { delete static_cast<orc::sse_chain_t*>(h); }
+int orc_sse_status(void* h) { return static_cast<orc::sse_chain_t*>(h)->status; }
 void orc_sse_sweep(void* h, int n) {
   orc::sse_chain_t* c = static_cast<orc::sse_chain_t*>(h);
   for (int i = 0; i < n; ++i) c->sweep_once();

@@ -29,7 +29,14 @@ int lg_fail(int code, const char* fmt, ...) {
 
 static uint64_t fnv1a(const uint8_t* p, size_t n) {
   uint64_t h = 1469598103934665603ull;
-  for (size_t i = 0; i < n; ++i) { h ^= p[i]; h *= 1099511628211ull; }
+  size_t i = 0;
+  for (; i + 8 <= n; i += 8) {
+    uint64_t w = 0;
+    for (int k = 7; k >= 0; --k) w = (w << 8) | p[i + k];
+    h ^= w;
+    h *= 1099511628211ull;
+  }
+  for (; i < n; ++i) { h ^= p[i]; h *= 1099511628211ull; }
   return h;
 }
 

@@ -144,15 +144,15 @@ class Oracle:
 class SseOracle:
     """One SSE chain (sse.C) in philox mode: the random source of the GPU's SSE form."""
 
-    def __init__(self, dim, L, beta, jxy=1.0, jz=1.0, seed=1, random_spins=True):
+    def __init__(self, dim, L, beta, jxy=1.0, jz=1.0, seed=1, random_spins=True, spin2=1):
         self.dim, self.L, self.beta = dim, L, beta
-        p = _P(dim, L, beta, jxy, jz, 0.0, 0.0, seed, 1 if random_spins else 0, 1, 1)
+        p = _P(dim, L, beta, jxy, jz, 0.0, 0.0, seed, 1 if random_spins else 0, 1, spin2)
         L_ = lib()
         L_.orc_sse_create.restype = ctypes.c_void_p
         L_.orc_sse_create.argtypes = [ctypes.c_void_p]
         self._h = ctypes.c_void_p(L_.orc_sse_create(ctypes.byref(p)))
         assert self._h.value
-        self.N = L ** dim
+        self.N = L ** dim * spin2
 
     def close(self):
         if self._h:
@@ -167,6 +167,7 @@ class SseOracle:
 
     def sweep(self, n=1):
         lib().orc_sse_sweep(self._h, ctypes.c_int(n))
+        assert lib().orc_sse_status(self._h) == 0, "boundary spin sectors differ"
 
     def records(self):
         n = lib().orc_sse_num_records(self._h)
@@ -281,14 +282,14 @@ def observables(records, dim, L, beta, jxy=1.0, jz=1.0, h=0.0, spin2=1):
     return out
 
 
-def sse_observables(records, dim, L, beta, jxy=1.0, jz=1.0, normal=False):
+def sse_observables(records, dim, L, beta, jxy=1.0, jz=1.0, normal=False, spin2=1):
     """Per-sweep observables from SSE oracle records: energy as on the path-integral form
     (sse.C:383-384, energy.h:76-84) and the SSE susceptibilities of the improved estimator
     (susceptibility.h:224-225, 231-232): beta (dip(integral, n) + tau0) / (n + 1) / V, with the
     time-integrated sums in operator-index units."""
     r = records
     N = L ** dim
-    NB = N * dim
+    NB = N * dim * spin2 * spin2
     v, W = weights(jxy, jz)
     nop = r[:, 0].astype(np.float64)
     ene = NB * W / 2 - nop / beta

@@ -39,12 +39,18 @@ MODELS = {
     "square8": dict(dim=2, L=8, beta=2.0, jxy=1.0, jz=1.0),
     "square6_xxz_cold": dict(dim=2, L=6, beta=8.0, jxy=1.0, jz=0.7),
     "cubic4_xxz": dict(dim=3, L=4, beta=1.0, jxy=1.0, jz=0.5),
+    # spin S on the virtual lattice, closed in imaginary time by the boundary matching
+    "chain6_s1": dict(dim=1, L=6, beta=3.0, jxy=1.0, jz=1.0, spin2=2),
+    "chain5_s3half_ferro": dict(dim=1, L=5, beta=1.5, jxy=-1.0, jz=-0.5, spin2=3),
+    "square4_s1_xxz": dict(dim=2, L=4, beta=1.5, jxy=1.0, jz=0.5, spin2=2),
+    "cubic2_s2": dict(dim=3, L=2, beta=0.7, jxy=1.0, jz=1.0, spin2=4),
 }
 
 
 def _params(lg, m, seed, **kw):
     base = dict(LATTICE=m["dim"], L=m["L"], BETA=m["beta"], Jxy=m["jxy"], Jz=m["jz"], SEED=seed,
-                SWEEPS=1000, THERMALIZATION=0, INITIAL_SPINS="random", ALGORITHM="loop; sse")
+                SWEEPS=1000, THERMALIZATION=0, INITIAL_SPINS="random", ALGORITHM="loop; sse",
+                local_S=m.get("spin2", 1) / 2)
     base.update(kw)
     return lg.make_params(**base)
 
@@ -73,8 +79,9 @@ def test_sse_trajectory_bit_exact_vs_oracle(lg, name):
     seed = 4321 + len(name)
     g = lg.LoopWorker(_params(lg, m, seed))
     g.keep_records(True)
-    o = orc.SseOracle(m["dim"], m["L"], m["beta"], m["jxy"], m["jz"], seed=seed)
-    n = m["L"] ** m["dim"]
+    o = orc.SseOracle(m["dim"], m["L"], m["beta"], m["jxy"], m["jz"], seed=seed,
+                      spin2=m.get("spin2", 1))
+    n = m["L"] ** m["dim"] * m.get("spin2", 1)
     _assert_same_state(g, o, n)
     for k in (1, 9, 30, 64, 96):         # chunks of one launch and of several
         g.run(k)
@@ -159,8 +166,12 @@ def test_sse_checkpoint_round_trip(lg):
     j = 32 + 36
     code = struct.unpack_from("<i", bad, j)[0]
     struct.pack_into("<i", bad, j, code ^ 1)
-    h = 1469598103934665603                     # the trailing FNV-1a checksum, recomputed
-    for x in bytes(bad[:-8]):
+    h = 1469598103934665603                     # the trailing checksum, recomputed
+    body = bytes(bad[:-8])
+    n8 = len(body) // 8 * 8
+    for (w,) in struct.iter_unpack("<Q", body[:n8]):
+        h = ((h ^ w) * 1099511628211) & (2 ** 64 - 1)
+    for x in body[n8:]:
         h = ((h ^ x) * 1099511628211) & (2 ** 64 - 1)
     struct.pack_into("<Q", bad, len(bad) - 8, h)
     with pytest.raises(lg.LoopError) as e:
@@ -174,21 +185,22 @@ def test_sse_checkpoint_round_trip(lg):
         w.close()
 
 
-ED_CASES = [(1, 8, 0.5, 1.0, 1.0, False), (1, 6, 0.3, 1.0, 0.5, False),
-            (2, 2, 0.5, 1.0, 1.0, False), (3, 2, 0.5, 1.0, 0.5, False),
-            (1, 6, 0.5, 1.0, 1.0, True)]
+ED_CASES = [(1, 8, 0.5, 1.0, 1.0, False, 1), (1, 6, 0.3, 1.0, 0.5, False, 1),
+            (2, 2, 0.5, 1.0, 1.0, False, 1), (3, 2, 0.5, 1.0, 0.5, False, 1),
+            (1, 6, 0.5, 1.0, 1.0, True, 1), (1, 4, 0.5, 1.0, 1.0, False, 2),
+            (1, 4, 1.0, 1.0, 0.5, False, 3), (2, 2, 0.5, 1.0, 1.0, False, 2)]
 
 
 @pytest.mark.parametrize("case", ED_CASES)
 def test_sse_observables_vs_exact_diagonalization(lg, case):
-    dim, L, T, jxy, jz, normal = case
+    dim, L, T, jxy, jz, normal, spin2 = case
     kw = dict(DISABLE_IMPROVED_ESTIMATOR=True) if normal else {}
     g = lg.LoopWorker(lg.make_params(LATTICE=dim, L=L, T=T, Jxy=jxy, Jz=jz, SEED=17,
-                                     SWEEPS=1 << 16, THERMALIZATION=1 << 10,
+                                     SWEEPS=1 << 16, THERMALIZATION=1 << 10, local_S=spin2 / 2,
                                      INITIAL_SPINS="random", ALGORITHM="loop; sse", **kw))
     g.run((1 << 16) + (1 << 10))
     obs = g.observables()
-    ref = orc.ed.thermal(dim, L, T, jxy=jxy, jz=jz)
+    ref = orc.ed.thermal(dim, L, T, jxy=jxy, jz=jz, spin2=spin2)
     for k in ["Energy", "Specific Heat", "Susceptibility", "Magnetization^2",
               "Staggered Magnetization^2", "Staggered Susceptibility"]:
         mean, err = obs[k]
@@ -197,16 +209,17 @@ def test_sse_observables_vs_exact_diagonalization(lg, case):
 
 
 def test_sse_agrees_with_reference_sse_blocks(lg, golden):
-    """The S = 1/2 "loop; sse" blocks of loop.op (L = 4 rings, 4096 sweeps each): every printed
-    value within 3 combined standard errors, the number of clusters included."""
+    """The "loop; sse" blocks of loop.op without single-ion anisotropy (L = 4 rings: S = 1/2
+    Heisenberg and Ising, S = 1 Heisenberg; 4096 sweeps each): every printed value within 3
+    combined standard errors, the number of clusters included."""
     n = 0
     for blk in golden("loop_op.json"):
-        if blk["algorithm"] != "loop; sse" or blk.get("spin2", 1) != 1:
+        if blk["algorithm"] != "loop; sse":
             continue
         w = lg.LoopWorker(lg.make_params(LATTICE="chain", L=blk["L"], T=blk["T"], Jxy=blk["jxy"],
                                          Jz=blk["jz"], SEED=2718 + n, SWEEPS=1 << 16,
                                          THERMALIZATION=1 << 10, INITIAL_SPINS="random",
-                                         ALGORITHM="loop; sse"))
+                                         local_S=blk.get("spin2", 1) / 2, ALGORITHM="loop; sse"))
         w.run((1 << 16) + (1 << 10))
         obs = w.observables()
         for k, (v, e) in blk["values"].items():
@@ -215,7 +228,7 @@ def test_sse_agrees_with_reference_sse_blocks(lg, golden):
             assert abs(mean - v) <= tol + 1e-9, (blk["T"], k, mean, err, v, e)
             n += 1
         w.close()
-    assert n == 14
+    assert n == 21
 
 
 def test_sse_exchange_vs_exact_diagonalization(lg):
@@ -259,7 +272,7 @@ def test_sse_values_reproduce_observables(lg):
 
 def test_sse_unsupported_inputs(lg):
     m = MODELS["chain6_xxz"]
-    for kw in (dict(h=0.1), dict(local_S=1.0), dict(MEASURE_CORRELATIONS=True)):
+    for kw in (dict(h=0.1), dict(MEASURE_CORRELATIONS=True), dict(local_S=4.5)):
         with pytest.raises(lg.LoopError) as e:
             lg.LoopWorker(_params(lg, m, 1, **kw))
         assert e.value.code == -4, kw

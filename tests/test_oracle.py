@@ -250,14 +250,14 @@ def test_philox_xy_chain_vs_ed():
                   "Staggered Susceptibility"])
 
 
-def _check_sse_vs_ed(dim, L, T, jxy, jz, therm, sweeps, seed, keys, normal=False):
+def _check_sse_vs_ed(dim, L, T, jxy, jz, therm, sweeps, seed, keys, normal=False, spin2=1):
     beta = 1.0 / T
-    o = orc.SseOracle(dim, L, beta, jxy, jz, seed=seed)
+    o = orc.SseOracle(dim, L, beta, jxy, jz, seed=seed, spin2=spin2)
     o.sweep(therm)
     o.clear_records()
     o.sweep(sweeps)
-    obs = orc.sse_observables(o.records(), dim, L, beta, jxy, jz, normal=normal)
-    ref = orc.ed.thermal(dim, L, T, jxy=jxy, jz=jz)
+    obs = orc.sse_observables(o.records(), dim, L, beta, jxy, jz, normal=normal, spin2=spin2)
+    ref = orc.ed.thermal(dim, L, T, jxy=jxy, jz=jz, spin2=spin2)
     for k in keys:
         if k == "Specific Heat":
             m, e = orc.specific_heat(obs, beta, L ** dim)
@@ -271,19 +271,21 @@ SSE_KEYS = ["Energy", "Specific Heat", "Magnetization^2", "Susceptibility",
 
 
 def test_sse_oracle_agrees_with_reference_sse_blocks(golden):
-    # every S = 1/2 "loop; sse" block of loop.op (Heisenberg ring T = 0.25 and Ising ring
-    # T = 0.5, L = 4, 4096 sweeps each) within 3 combined sigma of the restatement, the number of
-    # clusters included (it depends on the fragments the SSE string makes)
+    # every "loop; sse" block of loop.op without single-ion anisotropy (S = 1/2 Heisenberg ring
+    # T = 0.25, Ising ring T = 0.5, S = 1 Heisenberg ring T = 0.25; L = 4, 4096 sweeps each)
+    # within 3 combined sigma of the restatement, the number of clusters included (it depends on
+    # the fragments the SSE string makes)
     n = 0
     for b in golden("loop_op.json"):
-        if b["algorithm"] != "loop; sse" or b.get("spin2", 1) != 1:
+        if b["algorithm"] != "loop; sse":
             continue
         beta = 1.0 / b["T"]
-        o = orc.SseOracle(1, b["L"], beta, b["jxy"], b["jz"], seed=31 + n)
+        sp2 = b.get("spin2", 1)
+        o = orc.SseOracle(1, b["L"], beta, b["jxy"], b["jz"], seed=31 + n, spin2=sp2)
         o.sweep(1000)
         o.clear_records()
         o.sweep(1 << 16)
-        obs = orc.sse_observables(o.records(), 1, b["L"], beta, b["jxy"], b["jz"])
+        obs = orc.sse_observables(o.records(), 1, b["L"], beta, b["jxy"], b["jz"], spin2=sp2)
         for k, (v, e) in b["values"].items():
             if k == "Specific Heat":
                 m, err = orc.specific_heat(obs, beta, b["L"])
@@ -291,7 +293,7 @@ def test_sse_oracle_agrees_with_reference_sse_blocks(golden):
                 m, err = orc.binned(obs[k])
             assert abs(m - v) <= 3.0 * (err ** 2 + float(e) ** 2) ** 0.5, (b["T"], k, m, err, v, e)
             n += 1
-    assert n == 14
+    assert n == 21
 
 
 @pytest.mark.parametrize("case", [
@@ -310,6 +312,17 @@ def test_sse_oracle_vs_ed(case):
 
 def test_sse_oracle_normal_estimator_vs_ed():
     _check_sse_vs_ed(1, 6, 0.5, 1.0, 1.0, 1000, 60000, 77, SSE_KEYS, normal=True)
+
+
+@pytest.mark.parametrize("case", [
+    (1, 4, 0.5, 1.0, 1.0, 2),    # S = 1 ring
+    (1, 4, 1.0, 1.0, 0.5, 3),    # S = 3/2 XXZ ring
+    (1, 5, 0.7, -1.0, -0.5, 2),  # S = 1 ferromagnet on an odd ring
+    (2, 2, 0.5, 1.0, 1.0, 2),    # S = 1 on the 2x2 square
+])
+def test_sse_oracle_spin_s_vs_ed(case):
+    dim, L, T, jxy, jz, spin2 = case
+    _check_sse_vs_ed(dim, L, T, jxy, jz, 1000, 40000, 90 + spin2 + L, SSE_KEYS, spin2=spin2)
 
 
 def test_momentum_ed_matches_dense_ed():
