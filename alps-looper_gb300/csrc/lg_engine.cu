@@ -22,6 +22,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/looper_gpu.h"
@@ -102,6 +103,10 @@ struct DBuf {
 //   resident  run the arena's sweeps as chain-resident launches (k_resident: one CTA per chain,
 //             a chunk of sweeps per launch) where every chain fits in shared memory; the fields
 //             above then wait for the arena to return to the grid path
+//   union_mode  0: every union in k_union, a lane per vertex; 1: the lower-leg pairs of the
+//             non-crossing vertices hooked first (k_union_pairs, spin-1/2 arenas only), the rest in
+//             k_union; 2: the pairs first where allowed, the rest in k_union_bal (each warp's
+//             unions balanced over its lanes)
 struct Shape {
   double insert_k = 32.0;
   double narrow_k = 32.0;
@@ -109,6 +114,7 @@ struct Shape {
   int cl_tile = 4096;
   int un_warps = 8;
   int resident = 0;
+  int union_mode = 2;
 };
 
 // Shared memory a chain-resident CTA may use by default: at most this much keeps two CTAs per SM.
@@ -260,9 +266,8 @@ struct Engine {
     for (int c = 0; c < C; ++c) acc_of_chain[c] = c;
     int dev = 0;
     LG_CUDA(cudaGetDevice(&dev));
-    cudaDeviceProp prop;
-    LG_CUDA(cudaGetDeviceProperties(&prop, dev));
-    nsm = prop.multiProcessorCount;
+    // one attribute, not cudaGetDeviceProperties (which queries every property, slowly)
+    LG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     LG_CUDA(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, stream_priority));
     LG_CUDA(cudaStreamCreateWithPriority(&st2, cudaStreamNonBlocking, stream_priority));
     LG_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
@@ -914,7 +919,8 @@ struct Engine {
     if (!(sh.acc_tile == 512 || sh.acc_tile == 1024 || sh.acc_tile == 2048) ||
         !(sh.cl_tile == 2048 || sh.cl_tile == 4096 || sh.cl_tile == 8192) ||
         !(sh.un_warps == 4 || sh.un_warps == 8 || sh.un_warps == 16) || !(sh.narrow_k >= 0) ||
-        !(sh.insert_k >= 0) || !(sh.resident == 0 || sh.resident == 1))
+        !(sh.insert_k >= 0) || !(sh.resident == 0 || sh.resident == 1) ||
+        !(sh.union_mode >= 0 && sh.union_mode <= 2))
       return lg_fail(LG_EINVAL, "bad launch shape");
     if (sh.resident && !resident) {
       int rc = to_resident();
@@ -1047,9 +1053,26 @@ struct Engine {
     {
       const int w = shape.un_warps, per = w * UN_CHUNK;
       const int g = (ns_cap + per - 1) / per;  // one chunk per warp: no straggler tail
-      if (w == 4) k_union<4><<<g, 4 * 32, 0, st>>>(A);
-      else if (w == 16) k_union<16><<<g, 16 * 32, 0, st>>>(A);
-      else k_union<8><<<g, 8 * 32, 0, st>>>(A);
+      const bool pairs = shape.union_mode >= 1 && !any_spin_s;
+      if (pairs) {
+        k_union_pairs<<<grid_for(ns_cap, 256, 16), 256, 0, st>>>(A);
+        ++launches;
+      }
+      if (shape.union_mode == 2) {
+        // persistent: at most eight CTAs per SM, no more warps than chunks
+        const int gb = (int)std::max<long long>(1, std::min<long long>(
+            (long long)nsm * 8, ((long long)ns_cap + UB_WARPS * UN_CHUNK - 1) / (UB_WARPS * UN_CHUNK)));
+        if (pairs) k_union_bal<true><<<gb, UB_WARPS * 32, 0, st>>>(A);
+        else k_union_bal<false><<<gb, UB_WARPS * 32, 0, st>>>(A);
+      } else if (pairs) {
+        if (w == 4) k_union<4, true><<<g, 4 * 32, 0, st>>>(A);
+        else if (w == 16) k_union<16, true><<<g, 16 * 32, 0, st>>>(A);
+        else k_union<8, true><<<g, 8 * 32, 0, st>>>(A);
+      } else {
+        if (w == 4) k_union<4><<<g, 4 * 32, 0, st>>>(A);
+        else if (w == 16) k_union<16><<<g, 16 * 32, 0, st>>>(A);
+        else k_union<8><<<g, 8 * 32, 0, st>>>(A);
+      }
     }
     mark(3);
     {
@@ -1254,7 +1277,7 @@ struct Engine {
       return run(trial);
     }
     if (trial < 1) trial = 1;
-    char line[160];
+    char line[224];
     report.clear();
     // the chain-resident path, where the arena qualifies: timed first, over whole chunks
     const int trial2 = std::max(trial, 8);
@@ -1290,8 +1313,8 @@ struct Engine {
       double t = 0;
       for (double x : km) t += x;
       *ms = t / trial;
-      std::snprintf(line, sizeof(line), "insert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d: %.4f ms\n",
-                    sh.insert_k, sh.narrow_k, sh.acc_tile, sh.cl_tile, sh.un_warps, *ms);
+      std::snprintf(line, sizeof(line), "insert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d union_mode=%d: %.4f ms\n",
+                    sh.insert_k, sh.narrow_k, sh.acc_tile, sh.cl_tile, sh.un_warps, sh.union_mode, *ms);
       report += line;
       return LG_OK;
     };
@@ -1346,6 +1369,11 @@ struct Engine {
       Shape c = best; c.un_warps = w;
       if ((rc = consider(c))) return rc;
     }
+    for (int m : {0, 1, 2}) {
+      if (m == best.union_mode || (m == 1 && any_spin_s)) continue;
+      Shape c = best; c.union_mode = m;
+      if ((rc = consider(c))) return rc;
+    }
     if ((rc = set_shape(best))) return rc;
     if (res_ms > 0) {
       // the best grid shape timed as it runs (CUDA graph), against the resident time
@@ -1361,9 +1389,9 @@ struct Engine {
         best_ms = res_ms;
       }
     }
-    std::snprintf(line, sizeof(line), "chosen: %sinsert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d (%.4f ms)\n",
+    std::snprintf(line, sizeof(line), "chosen: %sinsert_k=%g narrow_k=%g acc_tile=%d cl_tile=%d union_warps=%d union_mode=%d (%.4f ms)\n",
                   best.resident ? "resident; " : "", best.insert_k, best.narrow_k, best.acc_tile,
-                  best.cl_tile, best.un_warps, best_ms);
+                  best.cl_tile, best.un_warps, best.union_mode, best_ms);
     report += line;
     return set_shape(best);
   }
@@ -1570,100 +1598,224 @@ struct Engine {
     return LG_OK;
   }
 
-  int set_state(int c, const int32_t* spins, const int32_t* bonds, const double* times, long long n,
-                uint64_t sweep) {
-    if (sse) return lg_fail(LG_EUNSUPPORTED, "an SSE chain takes its state from lg_load (diagonal operators included)");
+  // A chain's off-diagonal operators as the sweep keeps them: per site, its endpoints in (time,
+  // bond) order as (time bits, incidence index), packed in site order (oc[i] entries of site i).
+  struct Packed {
+    std::vector<int> oc;
+    std::vector<uint64_t> t;
+    std::vector<uint8_t> d;
+    long long bad = -1;     // first operator out of range (bond or time), or -1
+    int odd_site = -1;      // first spin-1/2 site with an odd number of endpoints, or -1
+  };
+
+  // Packs n operators of chain c, operator i given by get(i, &bond, &time bits).  Input in
+  // (time, bond) order, as lg_save writes it, is placed by a stable counting sort split over up to
+  // eight host threads (per-thread site counts, then each thread places its range); other input is
+  // sorted per site.  A time is accepted in [0, 1) (-0 is read as +0).
+  template <class Get>
+  void pack_ops(int c, long long n, const Get& get, Packed& P) {
     const ChainSpec& s = spec[c];
-    const int so = hch[c].site_off;
-    // the chain's endpoints by counting sort: per site, then (time, bond) within each site
-    std::vector<long long> start(s.N + 1, 0);
-    for (long long i = 0; i < n; ++i) {
-      const int b = bonds[i];
-      if (b < 0 || b >= s.NB || !(times[i] >= 0.0 && times[i] < 1.0))
-        return lg_fail(LG_EINVAL, "operator %lld out of range", i);
-      ++start[s.s0[b] + 1];
-      ++start[s.s1[b] + 1];
+    const int so = hch[c].site_off, bo = hch[c].bond_off;
+    // threads: at most 8, one per 64k operators, and no more count arrays than operators per site
+    const long long hw = std::max(1u, std::thread::hardware_concurrency());
+    const int T = (int)std::max<long long>(1, std::min<long long>({8ll, hw, n / 65536, 2 * n / std::max(1, s.N)}));
+    const long long per = (n + T - 1) / T;
+    std::vector<std::vector<int>> cnt(T, std::vector<int>(s.N, 0));
+    std::vector<long long> bad(T, -1);
+    std::vector<char> ord(T, 1);
+    auto count = [&](int t) {
+      const long long i0 = t * per, i1 = std::min(n, i0 + per);
+      int* ct = cnt[t].data();
+      int pb = -1;
+      uint64_t pt = 0;
+      for (long long i = i0; i < i1; ++i) {
+        int b;
+        uint64_t tb;
+        get(i, &b, &tb);
+        double tv;
+        std::memcpy(&tv, &tb, 8);
+        if (b < 0 || b >= s.NB || !(tv >= 0.0 && tv < 1.0)) { bad[t] = i; return; }
+        if (tv == 0.0) tb = 0;
+        ++ct[s.s0[b]];
+        ++ct[s.s1[b]];
+        if (i > i0 && !(pt < tb || (pt == tb && pb <= b))) ord[t] = 0;
+        pb = b;
+        pt = tb;
+      }
+    };
+    auto run_par = [&](auto&& f) {  // ranges 1.. on threads (on this one where none starts), 0 here
+      std::vector<std::thread> th;
+      int t = 1;
+      try {
+        th.reserve(T);
+        for (; t < T; ++t) th.emplace_back(f, t);
+      } catch (...) {
+      }
+      for (int u = t; u < T; ++u) f(u);
+      f(0);
+      for (auto& x : th) x.join();
+    };
+    run_par(count);
+    for (int t = 0; t < T; ++t)
+      if (bad[t] >= 0) { P.bad = bad[t]; return; }
+    bool ordered = true;
+    for (int t = 0; t < T; ++t) ordered &= ord[t] != 0;
+    for (int t = 1; t < T && ordered; ++t) {  // across the ranges' boundaries
+      const long long i = t * per;
+      if (i >= n) break;
+      int ba, bb;
+      uint64_t ta, tb;
+      get(i - 1, &ba, &ta);
+      get(i, &bb, &tb);
+      double va, vb;
+      std::memcpy(&va, &ta, 8);
+      std::memcpy(&vb, &tb, 8);
+      if (va == 0.0) ta = 0;
+      if (vb == 0.0) tb = 0;
+      ordered = ta < tb || (ta == tb && ba <= bb);
     }
+    P.oc.assign(s.N, 0);
+    for (int t = 0; t < T; ++t)
+      for (int i = 0; i < s.N; ++i) P.oc[i] += cnt[t][i];
     // a spin-1/2 world line is periodic in imaginary time: an even number of flips per site
     // (spin-S chains close through the boundary matching, which checks its own sectors)
     if (s.spin2 <= 1)
       for (int i = 0; i < s.N; ++i)
-        if (start[i + 1] & 1)
-          return lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
-                                    "(not periodic in imaginary time)", i);
-    for (int i = 0; i < s.N; ++i) start[i + 1] += start[i];
-    // the chain's lists, packed in site order: (time bits, incidence index)
-    std::vector<uint64_t> ft(2 * n);
-    std::vector<uint8_t> fd(2 * n);
-    bool ordered = true;  // (time, bond) ascending, as lg_save writes them
-    for (long long i = 1; i < n && ordered; ++i) {
-      uint64_t ta, tb;
-      std::memcpy(&ta, &times[i - 1], 8);
-      std::memcpy(&tb, &times[i], 8);
-      ordered = ta < tb || (ta == tb && bonds[i - 1] <= bonds[i]);
-    }
+        if (P.oc[i] & 1) { P.odd_site = i; return; }
+    std::vector<long long> start(s.N + 1, 0);
+    for (int i = 0; i < s.N; ++i) start[i + 1] = start[i] + P.oc[i];
+    P.t.resize(2 * n);
+    P.d.resize(2 * n);
     if (ordered) {  // every site's entries arrive in the order the sweep produces
-      std::vector<long long> fill(start.begin(), start.end() - 1);
-      const int bo = hch[c].bond_off;
-      for (long long i = 0; i < n; ++i) {
-        const int b = bonds[i];
-        uint64_t tb;
-        std::memcpy(&tb, &times[i], 8);
-        const long long k0 = fill[s.s0[b]]++, k1 = fill[s.s1[b]]++;
-        ft[k0] = tb; fd[k0] = h_bond_dir0[b + bo];
-        ft[k1] = tb; fd[k1] = h_bond_dir1[b + bo];
+      for (int i = 0; i < s.N; ++i) {  // cnt[t][i] := where thread t's first entry of site i goes
+        long long run = start[i];
+        for (int t = 0; t < T; ++t) { const int k = cnt[t][i]; cnt[t][i] = (int)run; run += k; }
       }
-    } else {
-      std::vector<std::pair<uint64_t, int>> ep(2 * n);  // (time bits, global bond)
-      std::vector<long long> fill(start.begin(), start.end() - 1);
-      for (long long i = 0; i < n; ++i) {
-        const int b = bonds[i];
-        uint64_t tb;
-        std::memcpy(&tb, &times[i], 8);
-        ep[fill[s.s0[b]]++] = {tb, b + hch[c].bond_off};
-        ep[fill[s.s1[b]]++] = {tb, b + hch[c].bond_off};
-      }
-      for (int i = 0; i < s.N; ++i) {
-        std::sort(ep.begin() + start[i], ep.begin() + start[i + 1]);  // the order the sweep produces
-        const int gs = so + i;
-        for (long long k = start[i]; k < start[i + 1]; ++k) {
-          const int gb = ep[k].second;
-          ft[k] = ep[k].first;
-          fd[k] = h_bond_s0[gb] == gs ? h_bond_dir0[gb] : h_bond_dir1[gb];
+      auto place = [&](int t) {
+        const long long i0 = t * per, i1 = std::min(n, i0 + per);
+        int* at = cnt[t].data();
+        for (long long i = i0; i < i1; ++i) {
+          int b;
+          uint64_t tb;
+          get(i, &b, &tb);
+          double tv;
+          std::memcpy(&tv, &tb, 8);
+          if (tv == 0.0) tb = 0;
+          const int k0 = at[s.s0[b]]++, k1 = at[s.s1[b]]++;
+          P.t[k0] = tb; P.d[k0] = h_bond_dir0[b + bo];
+          P.t[k1] = tb; P.d[k1] = h_bond_dir1[b + bo];
         }
+      };
+      run_par(place);
+      return;
+    }
+    std::vector<std::pair<uint64_t, int>> ep(2 * n);  // (time bits, global bond)
+    std::vector<long long> fill(start.begin(), start.end() - 1);
+    for (long long i = 0; i < n; ++i) {
+      int b;
+      uint64_t tb;
+      get(i, &b, &tb);
+      double tv;
+      std::memcpy(&tv, &tb, 8);
+      if (tv == 0.0) tb = 0;
+      ep[fill[s.s0[b]]++] = {tb, b + bo};
+      ep[fill[s.s1[b]]++] = {tb, b + bo};
+    }
+    for (int i = 0; i < s.N; ++i) {
+      std::sort(ep.begin() + start[i], ep.begin() + start[i + 1]);  // the order the sweep produces
+      const int gs = so + i;
+      for (long long k = start[i]; k < start[i + 1]; ++k) {
+        const int gb = ep[k].second;
+        P.t[k] = ep[k].first;
+        P.d[k] = h_bond_s0[gb] == gs ? h_bond_dir0[gb] : h_bond_dir1[gb];
       }
     }
-    SiteLists L;
+  }
+
+  // Makes a packed, checked state chain c's state (spins sp[i] in {0, 1}, sweeps done).
+  int commit_state(int c, const Packed& P, const std::vector<uint8_t>& sp, uint64_t sweep) {
+    const ChainSpec& s = spec[c];
+    const int so = hch[c].site_off;
     int rc;
     if (C > 1) {  // the other chains' lists stay as they are
+      SiteLists L;
       if ((rc = download_lists(L))) return rc;
-      for (int i = 0; i < s.N; ++i) {
+      for (int i = 0, k = 0; i < s.N; ++i) {
         auto& Li = L[so + i];
         Li.clear();
-        for (long long k = start[i]; k < start[i + 1]; ++k) Li.push_back({ft[k], fd[k]});
+        for (int j = 0; j < P.oc[i]; ++j, ++k) Li.push_back({P.t[k], P.d[k]});
       }
-    }
-    if (C == 1) {  // a complete, valid state: a union-find failure (LG_EITERCAP) no longer applies
-      Ctl hc;
-      LG_CUDA(lg_copy(&hc, d_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
-      hc.err = 0;
-      hc.step = 0;
-      LG_CUDA(lg_copy(d_ctl.p, &hc, sizeof(Ctl), cudaMemcpyHostToDevice));
-    }
-    if (C > 1) {
       if ((rc = upload_lists(L))) return rc;
     } else {
-      std::vector<int> oc(s.N);
-      for (int i = 0; i < s.N; ++i) oc[i] = (int)(start[i + 1] - start[i]);
-      if ((rc = upload_flat(oc, ft, fd))) return rc;
+      // a complete, valid state: a union-find failure (LG_EITERCAP) no longer applies
+      const int zero = 0;
+      LG_CUDA(lg_copy(&d_ctl.p->err, &zero, sizeof(int), cudaMemcpyHostToDevice));
+      LG_CUDA(lg_copy(&d_ctl.p->step, &zero, sizeof(uint32_t), cudaMemcpyHostToDevice));
+      if ((rc = upload_flat(P.oc, P.t, P.d))) return rc;
     }
-    std::vector<uint8_t> sp(s.N);
-    for (int i = 0; i < s.N; ++i) sp[i] = (uint8_t)(spins[i] & 1);
     LG_CUDA(lg_copy(d_spin0.p + so, sp.data(), s.N, cudaMemcpyHostToDevice));
     uint32_t sw = (uint32_t)sweep;
     LG_CUDA(lg_copy(d_sweep.p + c, &sw, sizeof(uint32_t), cudaMemcpyHostToDevice));
     spec[c].mcs = sweep;
     return LG_OK;
+  }
+
+  int set_state(int c, const int32_t* spins, const int32_t* bonds, const double* times, long long n,
+                uint64_t sweep) {
+    if (sse) return lg_fail(LG_EUNSUPPORTED, "an SSE chain takes its state from lg_load (diagonal operators included)");
+    const ChainSpec& s = spec[c];
+    Packed P;
+    pack_ops(c, n, [&](long long i, int* b, uint64_t* tb) { *b = bonds[i]; std::memcpy(tb, &times[i], 8); }, P);
+    if (P.bad >= 0) return lg_fail(LG_EINVAL, "operator %lld out of range", P.bad);
+    if (P.odd_site >= 0)
+      return lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
+                                "(not periodic in imaginary time)", P.odd_site);
+    std::vector<uint8_t> sp(s.N);
+    for (int i = 0; i < s.N; ++i) sp[i] = (uint8_t)(spins[i] & 1);
+    return commit_state(c, P, sp, sweep);
+  }
+
+  // lg_load of a path-integral checkpoint: the operators are read in place from the blob, packed
+  // by pack_ops while a second thread checks the checksum; nothing reaches the device before
+  // both are done.
+  int load_checkpoint(int c, const uint8_t* buf, size_t size) {
+    const ChainSpec& s = spec[c];
+    if (!buf || size < CHECKPOINT_HEAD + 8) return lg_fail(LG_ECORRUPT, "checkpoint too short");
+    bool sum_ok = false;
+    std::thread sum;
+    try {
+      sum = std::thread([&] { sum_ok = checkpoint_checksum_ok(buf, size); });
+    } catch (...) {
+      sum_ok = checkpoint_checksum_ok(buf, size);
+    }
+    uint64_t n = 0, mcs = 0;
+    int hrc = LG_OK;
+    Packed P;
+    std::vector<uint8_t> sp;
+    try {
+      hrc = checkpoint_header(s, buf, size, &n, &mcs);
+      if (hrc == LG_OK) {
+        const uint8_t* ops = buf + CHECKPOINT_HEAD + s.N;
+        pack_ops(c, (long long)n, [&](long long i, int* b, uint64_t* tb) {
+          std::memcpy(b, ops + 12 * i, 4);
+          std::memcpy(tb, ops + 12 * i + 4, 8);
+        }, P);
+        sp.resize(s.N);
+        for (int i = 0; i < s.N; ++i) sp[i] = (uint8_t)(buf[CHECKPOINT_HEAD + i] & 1);
+      }
+    } catch (...) {
+      if (sum.joinable()) sum.join();
+      throw;
+    }
+    if (sum.joinable()) sum.join();
+    // the checksum is reported first, then the header (its message is already set), then the rest
+    if (!sum_ok) return lg_fail(LG_ECORRUPT, "checkpoint checksum mismatch");
+    if (hrc) return checkpoint_header(s, buf, size, &n, &mcs);
+    if (P.bad >= 0) return lg_fail(LG_ECORRUPT, "checkpoint operator %lld out of range", P.bad);
+    if (P.odd_site >= 0)
+      return lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
+                                "(not periodic in imaginary time)", P.odd_site);
+    return commit_state(c, P, sp, mcs);
   }
 
   // Cluster labels of an explicit configuration (single-chain engine): fills the bond vertex
@@ -2165,6 +2317,8 @@ int lg_set_iteration_cap(lg_chain* c, int cap) {
 
 int lg_load(lg_chain* c, const void* buf, size_t size) {
   return lg_guard([&]() -> int {
+    if (!c) return lg_fail(LG_EINVAL, "null argument");
+    if (!c->eng->sse) return c->eng->load_checkpoint(c->index, (const uint8_t*)buf, size);
     std::vector<int32_t> sp, bd;
     std::vector<double> tm;
     uint64_t mcs = 0;
@@ -2267,7 +2421,7 @@ static void shape_out(const Shape& s, lg_shape* out) {
   out->cl_tile = s.cl_tile;
   out->union_warps = s.un_warps;
   out->resident = s.resident;
-  out->reserved = 0;
+  out->union_mode = s.union_mode;
 }
 
 static int autotune_engine(Engine& e, int trial, size_t flush_bytes, lg_shape* chosen, char* report,
@@ -2305,6 +2459,7 @@ static int set_shape_engine(Engine& e, const lg_shape* in) {
   s.cl_tile = in->cl_tile;
   s.un_warps = in->union_warps;
   s.resident = in->resident;
+  s.union_mode = in->union_mode;
   return e.set_shape(s);
 }
 

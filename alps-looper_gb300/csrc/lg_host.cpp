@@ -684,35 +684,45 @@ static uint64_t fnv1a(const uint8_t* p, size_t n) {
   return h;
 }
 
-template <class T>
-static void put_raw(std::vector<uint8_t>& b, const T& x) {
-  const uint8_t* p = reinterpret_cast<const uint8_t*>(&x);
-  b.insert(b.end(), p, p + sizeof(T));
+uint64_t checkpoint_checksum(const uint8_t* buf, size_t size) {
+  return size < 8 ? 0 : fnv1a(buf, size - 8);
+}
+
+bool checkpoint_checksum_ok(const uint8_t* buf, size_t size) {
+  if (!buf || size < 8) return false;
+  uint64_t h;
+  std::memcpy(&h, buf + size - 8, 8);
+  return h == checkpoint_checksum(buf, size);
 }
 
 void checkpoint_encode(const ChainSpec& s, const std::vector<int32_t>& spins,
                        const std::vector<int32_t>& bonds, const std::vector<double>& times,
                        std::vector<uint8_t>& blob) {
-  blob.clear();
-  blob.insert(blob.end(), {'L', 'G', 'C', 'K'});
-  put_raw(blob, (uint32_t)(s.sse ? 2 : 1));  // 2: the SSE form, operators as bond << 1 | type
-  put_raw(blob, (uint32_t)s.dim);
-  put_raw(blob, (uint32_t)s.L);
-  put_raw(blob, (uint64_t)s.mcs);
-  put_raw(blob, (uint64_t)bonds.size());
-  for (int x : spins) blob.push_back((uint8_t)(x & 1));
-  for (size_t i = 0; i < bonds.size(); ++i) { put_raw(blob, bonds[i]); put_raw(blob, times[i]); }
-  put_raw(blob, fnv1a(blob.data(), blob.size()));
+  const size_t head = 4 + 4 + 4 + 4 + 8 + 8;
+  blob.resize(head + spins.size() + 12 * bonds.size() + 8);
+  uint8_t* p = blob.data();
+  const uint32_t ver = s.sse ? 2 : 1, dim = (uint32_t)s.dim, L = (uint32_t)s.L;
+  const uint64_t mcs = s.mcs, n = bonds.size();
+  std::memcpy(p, "LGCK", 4);
+  std::memcpy(p + 4, &ver, 4);  // 2: the SSE form, operators as bond << 1 | type
+  std::memcpy(p + 8, &dim, 4);
+  std::memcpy(p + 12, &L, 4);
+  std::memcpy(p + 16, &mcs, 8);
+  std::memcpy(p + 24, &n, 8);
+  p += head;
+  for (int x : spins) *p++ = (uint8_t)(x & 1);
+  for (size_t i = 0; i < bonds.size(); ++i, p += 12) {
+    std::memcpy(p, &bonds[i], 4);
+    std::memcpy(p + 4, &times[i], 8);
+  }
+  const uint64_t h = checkpoint_checksum(blob.data(), blob.size());
+  std::memcpy(p, &h, 8);
 }
 
-int checkpoint_decode(const ChainSpec& s, const uint8_t* buf, size_t size,
-                      std::vector<int32_t>& spins, std::vector<int32_t>& bonds,
-                      std::vector<double>& times, uint64_t* mcs) {
-  const size_t head = 4 + 4 + 4 + 4 + 8 + 8;
+int checkpoint_header(const ChainSpec& s, const uint8_t* buf, size_t size, uint64_t* nops,
+                      uint64_t* mcs) {
+  const size_t head = CHECKPOINT_HEAD;
   if (!buf || size < head + 8) return lg_fail(LG_ECORRUPT, "checkpoint too short");
-  uint64_t h;
-  std::memcpy(&h, buf + size - 8, 8);
-  if (h != fnv1a(buf, size - 8)) return lg_fail(LG_ECORRUPT, "checkpoint checksum mismatch");
   if (std::memcmp(buf, "LGCK", 4) != 0) return lg_fail(LG_ECORRUPT, "not a checkpoint");
   uint32_t ver, dim, L;
   uint64_t m, n;
@@ -727,7 +737,20 @@ int checkpoint_decode(const ChainSpec& s, const uint8_t* buf, size_t size,
   const size_t fixed = head + (size_t)s.N + 8;
   if (size < fixed || (size - fixed) % 12 != 0 || n != (uint64_t)((size - fixed) / 12))
     return lg_fail(LG_ECORRUPT, "checkpoint size mismatch");
-  const uint8_t* p = buf + head;
+  *nops = n;
+  *mcs = m;
+  return LG_OK;
+}
+
+int checkpoint_decode(const ChainSpec& s, const uint8_t* buf, size_t size,
+                      std::vector<int32_t>& spins, std::vector<int32_t>& bonds,
+                      std::vector<double>& times, uint64_t* mcs) {
+  if (!buf || size < CHECKPOINT_HEAD + 8) return lg_fail(LG_ECORRUPT, "checkpoint too short");
+  if (!checkpoint_checksum_ok(buf, size)) return lg_fail(LG_ECORRUPT, "checkpoint checksum mismatch");
+  uint64_t n = 0, m = 0;
+  int rc = checkpoint_header(s, buf, size, &n, &m);
+  if (rc) return rc;
+  const uint8_t* p = buf + CHECKPOINT_HEAD;
   spins.resize(s.N);
   for (int i = 0; i < s.N; ++i) spins[i] = p[i];
   p += s.N;

@@ -97,6 +97,15 @@ void record_values(const ChainSpec& s, const uint64_t* rec, double* v);
 void record_scalars(const ChainSpec& s, const uint64_t* rec, double* v);
 uint64_t value_mask(const ChainSpec& s);
 
+// Checkpoint blob (path_integral.C:111-124 save/load content): a 32-byte header ("LGCK", version,
+// dim, L, mcs, operator count), the spins, 12 bytes per operator, a trailing checksum.
+constexpr size_t CHECKPOINT_HEAD = 32;
+// FNV-1a of everything before the trailing checksum, and whether the stored one matches.
+uint64_t checkpoint_checksum(const uint8_t* buf, size_t size);
+bool checkpoint_checksum_ok(const uint8_t* buf, size_t size);
+// The header and size of a blob for chain s (no checksum): operator count and sweeps done.
+int checkpoint_header(const ChainSpec& s, const uint8_t* buf, size_t size, uint64_t* nops,
+                      uint64_t* mcs);
 void checkpoint_encode(const ChainSpec& s, const std::vector<int32_t>& spins,
                        const std::vector<int32_t>& bonds, const std::vector<double>& times,
                        std::vector<uint8_t>& blob);

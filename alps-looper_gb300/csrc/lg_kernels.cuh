@@ -1088,7 +1088,34 @@ __global__ void __launch_bounds__(256) k_boundary(Arena A) {
 constexpr int UN_WARPS = 8;   // default warps per block
 constexpr int UN_CHUNK = 64;
 
-template <int WARPS = UN_WARPS>
+// The lower-leg pairs first (arenas of spin-1/2 chains only).  Every segment ends at exactly one
+// vertex (the top segment of a site at tau = 1 instead), so the lower-leg unions (a-1, b-1) of the
+// non-crossing vertices (g != 1) form a matching, and every segment in it is still a root when this
+// kernel runs: k_merge hooks only top segments (the closure), which end at no vertex.  Each pair is
+// therefore hooked with one plain store, P[max] = min, no find and no CAS.  This is half of the
+// unions of a loop model with g = 0 graphs (the antiferromagnetic Heisenberg model); k_union<W,
+// true> then makes the rest on a forest of depth-one trees.  The pass also replaces svert[x] of
+// every source-side segment x by the target-side segment b of its vertex (nothing after the
+// unions reads svert), so that k_union<W, true> finds b in the same round trip as the segment's
+// info.  With spin S > 1/2, k_boundary unites bottom segments before k_union, so the matching's
+// segments need not be roots and this pass is not used.
+__global__ void __launch_bounds__(256) k_union_pairs(Arena A) {
+  if (A.ctl->err) return;
+  const int ns = A.ctl->ns_total;
+  LG_GRID_STRIDE(x, ns) {
+    const uint8_t info = A.sinfo[x];
+    if (!(info & SI_SRC)) continue;
+    const int b = A.vslot[2 * A.svert[x] + 1];
+    A.svert[x] = b;
+    if (((info >> SI_GSHIFT) & 3) == 1) continue;
+    const int lo = min(x, b) - 1, hi = max(x, b) - 1;
+    A.parent[hi] = lo;
+  }
+}
+
+// PAIRS_DONE: k_union_pairs has made the lower-leg unions of the non-crossing vertices and left
+// the target-side segment of each source-side segment's vertex in svert.
+template <int WARPS = UN_WARPS, bool PAIRS_DONE = false>
 __global__ void __launch_bounds__(WARPS * 32) k_union(Arena A) {
   if (A.ctl->err) return;
   __shared__ int pend[WARPS][UN_CHUNK];   // source-side segment a
@@ -1109,8 +1136,9 @@ __global__ void __launch_bounds__(WARPS * 32) k_union(Arena A) {
     const int v0 = x0 < ns ? A.svert[x0] : 0;
     const int v1 = x1 < ns ? A.svert[x1] : 0;
     const bool s0 = (i0 & SI_SRC) != 0, s1 = (i1 & SI_SRC) != 0;
-    const int b0 = s0 ? A.vslot[2 * v0 + 1] : 0;
-    const int b1 = s1 ? A.vslot[2 * v1 + 1] : 0;
+    // after k_union_pairs, svert of a source-side segment is already the target-side segment
+    const int b0 = s0 ? (PAIRS_DONE ? v0 : A.vslot[2 * v0 + 1]) : 0;
+    const int b1 = s1 ? (PAIRS_DONE ? v1 : A.vslot[2 * v1 + 1]) : 0;
     const unsigned m0 = __ballot_sync(0xFFFFFFFFu, s0), m1 = __ballot_sync(0xFFFFFFFFu, s1);
     const int n0 = __popc(m0), tot = n0 + __popc(m1);
     if (s0) { const int q = __popc(m0 & lt); pend[w][q] = x0; pb[w][q] = b0; pg[w][q] = (i0 >> SI_GSHIFT) & 3; }
@@ -1123,12 +1151,136 @@ __global__ void __launch_bounds__(WARPS * 32) k_union(Arena A) {
         ok &= uf_union(P, a - 1, b, cap);
         ok &= uf_union(P, b - 1, a, cap);
       } else {
-        ok &= uf_union(P, a - 1, b - 1, cap);
+        if (!PAIRS_DONE) ok &= uf_union(P, a - 1, b - 1, cap);
         ok &= uf_union(P, a, b, cap);
         if (g & 2) ok &= uf_union(P, a - 1, a, cap);
       }
     }
     __syncwarp();
+  }
+  if (!ok) atomicExch(&A.ctl->err, ERR_ITERCAP);
+}
+
+// The same unions with the work of a warp balanced over its lanes.  In k_union every lane makes the
+// unions of one vertex, and the warp runs until its slowest lane is done: the longest find path of
+// 32.  Here each warp keeps the unions of its chunks in a shared-memory queue, and every step a
+// lane that has finished takes the next one, so a long path holds up one lane, not 32.  A step is
+// one round trip: the parents of both current nodes are read together; a node whose parent is
+// not itself moves to it, and the node it came from is pointed at that parent (path splitting:
+// every pointer only moves to an ancestor, which keeps parents below their children); when both
+// are roots, the larger is hooked under the smaller with a CAS (a failed CAS continues from the
+// root that won).  The warps are persistent (one grid over the GPU) and stride over the chunks.
+// PAIRS_DONE: k_union_pairs has run (the lower-leg pairs are hooked, svert holds the target-side
+// segment of each source-side one).
+constexpr int UB_WARPS = 8;
+// Pending unions per warp: fewer than 32 before a chunk is added, and a chunk adds at most 3 per
+// source-side segment, 3 * UN_CHUNK = 192: never more than 223 at once.
+constexpr int UB_QUEUE = 256;
+
+template <bool PAIRS_DONE>
+__global__ void __launch_bounds__(UB_WARPS * 32, 8) k_union_bal(Arena A) {
+  if (A.ctl->err) return;
+  __shared__ int qa[UB_WARPS][UB_QUEUE];
+  __shared__ int qb[UB_WARPS][UB_QUEUE];
+  const int ns = A.ctl->ns_total;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const int nwarps = gridDim.x * UB_WARPS;
+  const int nchunks = (ns + UN_CHUNK - 1) / UN_CHUNK;
+  const int cap = iter_cap_of(A.ctl);
+  int* P = A.parent;
+  int chunk = blockIdx.x * UB_WARPS + w;
+  unsigned head = 0, tail = 0;  // the warp's queue is [head, tail), indices mod UB_QUEUE
+  int x = 0, y = 0, prevx = -1, prevy = -1, iters = 0;
+  bool busy = false, ok = true;
+  while (true) {
+    // refill while the queue cannot feed every lane and chunks remain (warp-uniform)
+    while (tail - head < 32u && chunk < nchunks) {
+      // both halves of the chunk: info and vertex (or, after k_union_pairs, the target-side
+      // segment) in one round trip
+      const int xh0 = chunk * UN_CHUNK + lane, xh1 = xh0 + 32;
+      const uint8_t ih0 = xh0 < ns ? A.sinfo[xh0] : 0, ih1 = xh1 < ns ? A.sinfo[xh1] : 0;
+      const int vh0 = xh0 < ns ? A.svert[xh0] : 0, vh1 = xh1 < ns ? A.svert[xh1] : 0;
+      int bh0 = vh0, bh1 = vh1;
+      if (!PAIRS_DONE) {
+        bh0 = (ih0 & SI_SRC) ? A.vslot[2 * vh0 + 1] : 0;
+        bh1 = (ih1 & SI_SRC) ? A.vslot[2 * vh1 + 1] : 0;
+      }
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int xs = half ? xh1 : xh0;
+        const uint8_t info = half ? ih1 : ih0;
+        int n = 0, u0a = 0, u0b = 0, u1a = 0, u1b = 0, u2a = 0, u2b = 0;
+        if (info & SI_SRC) {
+          const int a = xs;
+          const int b = half ? bh1 : bh0;
+          const int g = (info >> SI_GSHIFT) & 3;
+          if (g == 1) {
+            u0a = a - 1; u0b = b; u1a = b - 1; u1b = a; n = 2;
+          } else {
+            u0a = a; u0b = b; n = 1;
+            if (g & 2) { u1a = a - 1; u1b = a; n = 2; }
+            if (!PAIRS_DONE) {
+              if (n == 1) { u1a = a - 1; u1b = b - 1; } else { u2a = a - 1; u2b = b - 1; }
+              ++n;
+            }
+          }
+        }
+        // exclusive prefix of n over the warp
+        int pre = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xFFFFFFFFu, pre, o);
+          if (lane >= o) pre += v;
+        }
+        const int tot = __shfl_sync(0xFFFFFFFFu, pre, 31);
+        const unsigned at = tail + (unsigned)(pre - n);
+        if (n > 0) { qa[w][at % UB_QUEUE] = u0a; qb[w][at % UB_QUEUE] = u0b; }
+        if (n > 1) { qa[w][(at + 1) % UB_QUEUE] = u1a; qb[w][(at + 1) % UB_QUEUE] = u1b; }
+        if (n > 2) { qa[w][(at + 2) % UB_QUEUE] = u2a; qb[w][(at + 2) % UB_QUEUE] = u2b; }
+        tail += (unsigned)tot;
+      }
+      chunk += nwarps;
+    }
+    __syncwarp();
+    // lanes without a union take the next pending ones, in queue order
+    const unsigned idle = __ballot_sync(0xFFFFFFFFu, !busy);
+    const unsigned avail = tail - head;
+    if (!busy) {
+      const unsigned r = (unsigned)__popc(idle & lt);
+      if (r < avail) {
+        x = qa[w][(head + r) % UB_QUEUE];
+        y = qb[w][(head + r) % UB_QUEUE];
+        prevx = prevy = -1;
+        iters = 0;
+        busy = true;
+      }
+    }
+    head += min(avail, (unsigned)__popc(idle));
+    if (!__any_sync(0xFFFFFFFFu, busy)) break;  // queue empty and no chunk left
+    __syncwarp();
+    if (busy) {
+      const int px = __ldcg(P + x), py = __ldcg(P + y);
+      // path splitting: the node a step came from now points at its grandparent
+      if (prevx >= 0 && px != x) P[prevx] = px;
+      if (prevy >= 0 && py != y) P[prevy] = py;
+      if (x == y || px == py || px == y || py == x) {
+        busy = false;  // a common ancestor: already one set
+      } else if (px == x && py == y) {
+        const int lo = x < y ? x : y, hi = x < y ? y : x;
+        const int old = atomicCAS(P + hi, hi, lo);
+        if (old == hi) {
+          busy = false;
+        } else {  // hi was hooked meanwhile: go on from the root it went under
+          x = lo; y = old;
+          prevx = prevy = -1;
+        }
+      } else {
+        if (px != x) { prevx = x; x = px; } else prevx = -1;
+        if (py != y) { prevy = y; y = py; } else prevy = -1;
+      }
+      if (busy && ++iters >= cap) { ok = false; busy = false; }
+    }
   }
   if (!ok) atomicExch(&A.ctl->err, ERR_ITERCAP);
 }
@@ -1156,9 +1308,11 @@ __global__ void __launch_bounds__(256) k_compress(Arena A) {
 // cluster.h:54-59.
 //
 // At low temperature a few clusters own a large share of all segments, so the additions are
-// combined before they reach global memory: lanes of a warp with the same (root, class) are
-// summed with match_any + redux, and each block keeps a shared-memory hash of (root, class) sums
-// for its tile of ACC_TILE consecutive segments, flushed with one global atomic per entry.
+// combined before they reach global memory: each block keeps a shared-memory hash of (root,
+// class) sums for its tile of ACC_TILE consecutive segments, flushed with one global atomic per
+// entry.  (Summing the lanes of a warp with the same (root, class) first, with match_any and
+// reductions, removes most same-address conflicts of the shared atomics but doubles the
+// instructions; it measured 76 -> 137 us on the 128^2, beta = 64 sweep.)
 // The class sums are zero on entry: k_cluster clears what it consumes.
 constexpr int ACC_TILE = 1024;
 constexpr int ACC_HASH = 1024;   // power of two
@@ -1191,7 +1345,7 @@ __device__ __forceinline__ SegContrib seg_contrib(uint8_t info, uint8_t info1, u
 }
 
 template <int TILE = ACC_TILE>
-__global__ void __launch_bounds__(256) k_accumulate(Arena A) {
+__global__ void __launch_bounds__(256, 4) k_accumulate(Arena A) {
   if (A.ctl->err) return;
   __shared__ int hkey[ACC_HASH];
   // class sums of the hash entries as two 32-bit words: 32-bit shared-memory atomics are
@@ -1215,32 +1369,39 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
     __syncthreads();
     const int t0 = tile * TILE;
     constexpr int PER = TILE / 256;  // segments per thread (blockDim.x == 256)
-    int xs[PER], par[PER];
-    uint8_t info[PER], info1[PER], dir[PER], dir1[PER];
-    uint64_t ta[PER], tb[PER];
+    // Each segment is reduced to what it adds as soon as its loads arrive: its length (u64) and
+    // one packed word, class q (bits 0-1), first segment (bit 2), winding + 2 per direction (3
+    // bits each from bit 3; each is in [-2, 2]).  Eight segments then keep 4 registers each
+    // instead of their raw fields, so the 2048-segment tile does not halve the occupancy.
+    int par[PER];
+    unsigned long long len[PER];
+    unsigned meta[PER];
     // issue every load of this thread's segments first, then walk and add
 #pragma unroll
     for (int j = 0; j < PER; ++j) {
       const int x = t0 + threadIdx.x + j * 256;
-      xs[j] = x;
+      par[j] = x;
+      len[j] = 0;
+      meta[j] = 0;
       if (x < ns) {
         par[j] = A.parent[x];
-        info[j] = A.sinfo[x];
-        dir[j] = A.sdir[x];
-        ta[j] = A.stime[x];
-        const bool last = info[j] & SI_LAST;
-        tb[j] = last ? 0ull : A.stime[x + 1];
-        info1[j] = last ? 0 : A.sinfo[x + 1];
-        dir1[j] = last ? 0 : A.sdir[x + 1];
+        const uint8_t info = A.sinfo[x];
+        const uint8_t dir = A.sdir[x];
+        const uint64_t ta = A.stime[x];
+        const bool last = info & SI_LAST;
+        const uint64_t tb = last ? 0ull : A.stime[x + 1];
+        const uint8_t info1 = last ? 0 : A.sinfo[x + 1];
+        const uint8_t dir1 = last ? 0 : A.sdir[x + 1];
+        const SegContrib sc = seg_contrib(info, info1, ta, tb, dir, dir1);
+        len[j] = sc.len;
+        meta[j] = (unsigned)sc.q | ((info & SI_FIRST) ? 4u : 0u) | ((unsigned)(sc.w[0] + 2) << 3) |
+                  ((unsigned)(sc.w[1] + 2) << 6) | ((unsigned)(sc.w[2] + 2) << 9);
       }
     }
     // root walks of this thread's segments in lockstep (their parent reads in flight together)
     int rt[PER];
 #pragma unroll
-    for (int j = 0; j < PER; ++j) {
-      rt[j] = xs[j];
-      if (xs[j] >= ns) par[j] = xs[j];
-    }
+    for (int j = 0; j < PER; ++j) rt[j] = t0 + threadIdx.x + j * 256;
     for (int it = 0; it < ITER_CAP; ++it) {
       unsigned moved = 0;
 #pragma unroll
@@ -1253,17 +1414,17 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
     }
 #pragma unroll
     for (int j = 0; j < PER; ++j) {
-      const int x = xs[j];
+      const int x = t0 + threadIdx.x + j * 256;
       if (x >= ns) continue;
       const int r = rt[j];
       if (r != x) A.parent[x] = r;
-      const SegContrib sc = seg_contrib(info[j], info1[j], ta[j], tb[j], dir[j], dir1[j]);
-      const unsigned long long len = sc.len;
-      const int q = sc.q;
-      const int* w = sc.w;
-      if (info[j] & SI_FIRST) atomicAdd(&A.rkw[r].K[q], 1u);
+      const unsigned long long ln = len[j];
+      const unsigned mt = meta[j];
+      const int q = (int)(mt & 3u);
+      const int w[3] = {(int)((mt >> 3) & 7u) - 2, (int)((mt >> 6) & 7u) - 2, (int)((mt >> 9) & 7u) - 2};
+      if (mt & 4u) atomicAdd(&A.rkw[r].K[q], 1u);
       const bool wnz = (w[0] | w[1] | w[2]) != 0;
-      if (len || wnz) {
+      if (ln || wnz) {
         unsigned h = ((unsigned)r * 2654435761u) >> 22;  // 10-bit hash
         bool done = false;
         for (int probe = 0; probe < 32; ++probe) {
@@ -1271,8 +1432,8 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
           int k = hkey[h];
           if (k == -1) k = atomicCAS(hkey + h, -1, r);
           if (k == -1 || k == r) {
-            if (len) {
-              const unsigned lo = (unsigned)len, hi = (unsigned)(len >> 32);
+            if (ln) {
+              const unsigned lo = (unsigned)ln, hi = (unsigned)(ln >> 32);
               const unsigned old = atomicAdd(hlo + 4 * h + q, lo);
               const unsigned carry = (old + lo < old) ? 1u : 0u;
               if (hi + carry) atomicAdd(hhi + 4 * h + q, hi + carry);
@@ -1285,7 +1446,7 @@ __global__ void __launch_bounds__(256) k_accumulate(Arena A) {
           h = (h + 1) & (ACC_HASH - 1);
         }
         if (!done) {
-          if (len) atomicAdd(A.cls + 4 * (size_t)r + q, len);
+          if (ln) atomicAdd(A.cls + 4 * (size_t)r + q, ln);
 #pragma unroll
           for (int d = 0; d < 3; ++d)
             if (w[d]) atomicAdd(&A.rkw[r].W[d], w[d]);

@@ -70,12 +70,12 @@ class Shape(ctypes.Structure):
     _fields_ = [("insert_k", ctypes.c_double), ("narrow_k", ctypes.c_double),
                 ("acc_tile", ctypes.c_int), ("cl_tile", ctypes.c_int),
                 ("union_warps", ctypes.c_int), ("resident", ctypes.c_int),
-                ("reserved", ctypes.c_int)]
+                ("union_mode", ctypes.c_int)]
 
     def as_dict(self):
         return {"insert_k": self.insert_k, "narrow_k": self.narrow_k, "acc_tile": self.acc_tile,
                 "cl_tile": self.cl_tile, "union_warps": self.union_warps,
-                "resident": self.resident}
+                "resident": self.resident, "union_mode": self.union_mode}
 
 
 class ServerStats(ctypes.Structure):

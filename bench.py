@@ -472,7 +472,9 @@ def run_ours(args, dist, ws, rank, local):
     w.run(PRE_THERM // 2)
     if args.shape == "auto":
         # launch shape chosen by the autotuner on the chain's own pre-thermalization sweeps
-        shape, _ = w.autotune(8, args.flush_bytes)
+        shape, report = w.autotune(8, args.flush_bytes)
+        if rank == 0:
+            sys.stderr.write(report)
     else:
         w.shape = json.loads(args.shape)  # a fixed shape (e.g. to profile the tuned one)
         shape = w.shape
@@ -527,18 +529,24 @@ def run_ours(args, dist, ws, rank, local):
     h0, d0 = lg.copy_bytes()
     t0 = time.perf_counter()
     e = lg.LoopWorker(_params(lg, seed=SEED + 31 + rank, sweeps=1 << 13, therm=0))
+    t1 = time.perf_counter()
     e.load(blob)
+    t2 = time.perf_counter()
     e.run(args.steps)
+    t3 = time.perf_counter()
     obs = e.observables()
     e2e_s = time.perf_counter() - t0
     h1, d1 = lg.copy_bytes()
+    split_ms = {"lg_create": (t1 - t0) * 1e3, "lg_load": (t2 - t1) * 1e3,
+                "lg_run": (t3 - t2) * 1e3, "lg_observables": (t0 + e2e_s - t3) * 1e3}
     e.close()
     e2e_s = _reduce_max(dist, e2e_s)
     e_nop = obs["Number of Operators"][0]
     e2e = {"value": ws * args.steps * N_SITES / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": round((h1 - h0) / args.steps, 1),
            "d2h_bytes_per_step": round((d1 - d0) / args.steps, 1),
-           "seconds": e2e_s, "checkpoint_bytes": len(blob),
+           "seconds": e2e_s, "split_ms": {k: round(v, 3) for k, v in split_ms.items()},
+           "checkpoint_bytes": len(blob),
            "operators_per_sweep": e_nop, "operators_vs_device_timed": e_nop / nv_mean,
            "scope": "lg_create + lg_load(equilibrated checkpoint) + lg_run(steps) + "
                     "lg_observables, host wall clock; bytes counted by the library's copies"}

@@ -328,14 +328,19 @@ int lg_batch_validate_sweeps(lg_batch* b, int64_t n);
  *   narrow_k     the same split for the per-site merge and list compaction
  *   acc_tile     segments per CTA of the cluster-sum accumulation: 512, 1024 or 2048
  *   cl_tile      segments per CTA of the cluster flip / estimator kernel: 2048, 4096 or 8192
- *   union_warps  warps per CTA of the union-find kernel: 4, 8 or 16
+ *   union_warps  warps per CTA of the union-find kernel of union_mode 0 and 1: 4, 8 or 16
  *   resident     1: the chain-resident path, where every chain of the arena qualifies (S = 1/2,
  *                no correlation measurement, a sweep's operators within one CTA's shared memory):
  *                one CTA per chain runs a whole chunk of up to 64 sweeps in one launch, with the
  *                sweep's vertices, segments and union-find forest in shared memory; 0: the grid
  *                path (one CUDA graph of grid-wide kernels per sweep).  lg_create and
  *                lg_batch_create start small arenas on the resident path; a chain that outgrows a
- *                CTA moves to the grid path by itself. */
+ *                CTA moves to the grid path by itself.
+ *   union_mode   how the union-find runs: 0, every union in one lock-free pass with a lane per
+ *                vertex; 1, in arenas of spin-1/2 chains the lower-leg unions of the non-crossing
+ *                vertices (a matching of segments that are all still roots) first, one plain
+ *                store each, then the rest as in 0; 2 (default), those pairs first where 1 allows
+ *                them, then the rest with each warp's unions balanced over its lanes. */
 typedef struct lg_shape {
   double insert_k;
   double narrow_k;
@@ -343,7 +348,7 @@ typedef struct lg_shape {
   int cl_tile;
   int union_warps;
   int resident;
-  int reserved;
+  int union_mode;
 } lg_shape;
 
 /* Autotuner: times trial_sweeps sweeps per candidate shape (device events, flush_bytes of L2

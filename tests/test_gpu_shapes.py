@@ -34,8 +34,12 @@ MODELS = [
 SHAPES = [
     dict(insert_k=0.0, narrow_k=0.0, resident=0),                 # every chain warp-per-site
     dict(insert_k=1e300, narrow_k=1e300, resident=0),             # every chain thread-per-site
-    dict(insert_k=1e300, narrow_k=10.0, acc_tile=512, cl_tile=2048, union_warps=4, resident=0),
-    dict(insert_k=10.0, narrow_k=32.0, acc_tile=2048, cl_tile=8192, union_warps=16, resident=0),
+    dict(insert_k=1e300, narrow_k=10.0, acc_tile=512, cl_tile=2048, union_warps=4, resident=0,
+         union_mode=0),                                           # a lane per vertex
+    dict(insert_k=10.0, narrow_k=32.0, acc_tile=2048, cl_tile=8192, union_warps=16, resident=0,
+         union_mode=1),                                           # lower-leg pairs first
+    dict(insert_k=0.0, narrow_k=1e300, acc_tile=1024, cl_tile=4096, resident=0,
+         union_mode=2),                                           # pairs, then lane-balanced
     dict(resident=1),                                             # one CTA per chain
 ]
 
