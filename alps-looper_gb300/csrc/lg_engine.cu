@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -57,6 +58,36 @@ static cudaError_t lg_copy_async(void* dst, const void* src, size_t n, cudaMemcp
   return cudaMemcpyAsync(dst, src, n, k, st);
 }
 static thread_local std::string g_err;
+
+// A process-wide page-locked host buffer for the operator lists that lg_load and lg_set_state
+// upload: a pinned source copies to the device at the link's rate, a pageable one goes through the
+// driver's bounce buffer.  The first engine built in a process reserves it (cudaHostAlloc is slow
+// enough to matter once per load), later loads grow it when they need more; a user holds the lock
+// from packing until its copies have finished.  It lives until the process exits.
+struct HostStage {
+  std::mutex m;
+  unsigned char* p = nullptr;
+  size_t cap = 0;
+  // (under the lock) at least n bytes; false when page-locked memory cannot be had (the caller
+  // then packs into pageable memory)
+  bool reserve(size_t n) {
+    if (n <= cap) return true;
+    const size_t want = std::max(n, 2 * cap);
+    void* q = nullptr;
+    if (cudaHostAlloc(&q, want, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (p) cudaFreeHost(p);
+    p = static_cast<unsigned char*>(q);
+    cap = want;
+    return true;
+  }
+};
+static HostStage& host_stage() {
+  static HostStage* s = new HostStage();  // never destroyed: no CUDA call after the runtime is gone
+  return *s;
+}
 
 int lg_fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -380,6 +411,11 @@ struct Engine {
     if (any_sse && !all_sse)
       return lg_fail(LG_EINVAL, "an arena holds either path-integral or SSE chains, not both");
     sse = any_sse;
+    if (!sse) {  // the pinned buffer of lg_load / lg_set_state, once per process (16 MiB: 900k operators)
+      HostStage& hs = host_stage();
+      std::lock_guard<std::mutex> lock(hs.m);
+      hs.reserve(16u << 20);
+    }
     if (sse) {
       if ((rc = setup_sse(res_vcap_for(1.0), false))) return rc;
     } else if (allow_resident && C >= nsm && res_fits(res_vcap_for(1.0), RES_SMEM_DEFAULT)) {
@@ -1055,7 +1091,7 @@ struct Engine {
       const int g = (ns_cap + per - 1) / per;  // one chunk per warp: no straggler tail
       const bool pairs = shape.union_mode >= 1 && !any_spin_s;
       if (pairs) {
-        k_union_pairs<<<grid_for(ns_cap, 256, 16), 256, 0, st>>>(A);
+        k_union_pairs<<<grid_for((ns_cap + UP_PER - 1) / UP_PER, 256, 16), 256, 0, st>>>(A);
         ++launches;
       }
       if (shape.union_mode == 2) {
@@ -1521,11 +1557,11 @@ struct Engine {
     std::vector<uint8_t> d(total);
     for (long long i = 0, k = 0; i < N; ++i)
       for (const auto& e : L[i]) { t[k] = e.first; d[k] = e.second; ++k; }
-    return upload_flat(oc, t, d);
+    return upload_flat(oc, t.data(), d.data());
   }
 
   // The same from the lists of every site packed in site order (oc[i] entries for site i).
-  int upload_flat(const std::vector<int>& oc, const std::vector<uint64_t>& t, const std::vector<uint8_t>& d) {
+  int upload_flat(const std::vector<int>& oc, const uint64_t* t, const uint8_t* d) {
     std::vector<int> ob(N);
     long long total = 0;
     for (int i = 0; i < N; ++i) { ob[i] = (int)total; total += oc[i]; }
@@ -1558,8 +1594,8 @@ struct Engine {
     LG_CUDA(lg_copy(d_off_base.p, ob.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     LG_CUDA(lg_copy(d_off_cnt.p, oc.data(), N * sizeof(int), cudaMemcpyHostToDevice));
     if (total) {
-      LG_CUDA(lg_copy(d_stime.p, t.data(), total * sizeof(uint64_t), cudaMemcpyHostToDevice));
-      LG_CUDA(lg_copy(d_sdir.p, d.data(), total, cudaMemcpyHostToDevice));
+      LG_CUDA(lg_copy(d_stime.p, t, total * sizeof(uint64_t), cudaMemcpyHostToDevice));
+      LG_CUDA(lg_copy(d_sdir.p, d, total, cudaMemcpyHostToDevice));
     }
     return LG_OK;
   }
@@ -1602,8 +1638,10 @@ struct Engine {
   // bond) order as (time bits, incidence index), packed in site order (oc[i] entries of site i).
   struct Packed {
     std::vector<int> oc;
-    std::vector<uint64_t> t;
-    std::vector<uint8_t> d;
+    uint64_t* t = nullptr;  // 2n endpoints: time bits
+    uint8_t* d = nullptr;   // and incidence index
+    std::unique_ptr<uint64_t[]> own_t;  // when t, d are not in the pinned stage
+    std::unique_ptr<uint8_t[]> own_d;
     long long bad = -1;     // first operator out of range (bond or time), or -1
     int odd_site = -1;      // first spin-1/2 site with an odd number of endpoints, or -1
   };
@@ -1612,8 +1650,9 @@ struct Engine {
   // (time, bond) order, as lg_save writes it, is placed by a stable counting sort split over up to
   // eight host threads (per-thread site counts, then each thread places its range); other input is
   // sorted per site.  A time is accepted in [0, 1) (-0 is read as +0).
+  // With `stage` (held under its lock) the endpoints are packed into the pinned buffer.
   template <class Get>
-  void pack_ops(int c, long long n, const Get& get, Packed& P) {
+  void pack_ops(int c, long long n, const Get& get, Packed& P, HostStage* stage) {
     const ChainSpec& s = spec[c];
     const int so = hch[c].site_off, bo = hch[c].bond_off;
     // threads: at most 8, one per 64k operators, and no more count arrays than operators per site
@@ -1684,8 +1723,15 @@ struct Engine {
         if (P.oc[i] & 1) { P.odd_site = i; return; }
     std::vector<long long> start(s.N + 1, 0);
     for (int i = 0; i < s.N; ++i) start[i + 1] = start[i] + P.oc[i];
-    P.t.resize(2 * n);
-    P.d.resize(2 * n);
+    if (stage && stage->reserve((size_t)n * 18 + 64)) {
+      P.t = reinterpret_cast<uint64_t*>(stage->p);
+      P.d = stage->p + (size_t)n * 16;
+    } else {
+      P.own_t.reset(new uint64_t[2 * n + 1]);  // no zero fill: every entry is written below
+      P.own_d.reset(new uint8_t[2 * n + 1]);
+      P.t = P.own_t.get();
+      P.d = P.own_d.get();
+    }
     if (ordered) {  // every site's entries arrive in the order the sweep produces
       for (int i = 0; i < s.N; ++i) {  // cnt[t][i] := where thread t's first entry of site i goes
         long long run = start[i];
@@ -1764,8 +1810,10 @@ struct Engine {
                 uint64_t sweep) {
     if (sse) return lg_fail(LG_EUNSUPPORTED, "an SSE chain takes its state from lg_load (diagonal operators included)");
     const ChainSpec& s = spec[c];
+    HostStage& hs = host_stage();
+    std::lock_guard<std::mutex> lock(hs.m);
     Packed P;
-    pack_ops(c, n, [&](long long i, int* b, uint64_t* tb) { *b = bonds[i]; std::memcpy(tb, &times[i], 8); }, P);
+    pack_ops(c, n, [&](long long i, int* b, uint64_t* tb) { *b = bonds[i]; std::memcpy(tb, &times[i], 8); }, P, &hs);
     if (P.bad >= 0) return lg_fail(LG_EINVAL, "operator %lld out of range", P.bad);
     if (P.odd_site >= 0)
       return lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
@@ -1781,15 +1829,29 @@ struct Engine {
   int load_checkpoint(int c, const uint8_t* buf, size_t size) {
     const ChainSpec& s = spec[c];
     if (!buf || size < CHECKPOINT_HEAD + 8) return lg_fail(LG_ECORRUPT, "checkpoint too short");
-    bool sum_ok = false;
-    std::thread sum;
+    // the checksum's blocks on up to four threads beside the packing
+    const size_t nblk = checkpoint_blocks(size);
+    std::vector<uint64_t> bh(nblk, 0);
+    const int K = (int)std::min<size_t>(4, nblk);
+    std::vector<std::thread> sum;
+    auto hash_blocks = [&](int k) {
+      for (size_t b = (size_t)k; b < nblk; b += (size_t)K) bh[b] = checkpoint_block_hash(buf, size, b);
+    };
+    int started = 0;
     try {
-      sum = std::thread([&] { sum_ok = checkpoint_checksum_ok(buf, size); });
+      sum.reserve(K);
+      for (; started < K; ++started) sum.emplace_back(hash_blocks, started);
     } catch (...) {
-      sum_ok = checkpoint_checksum_ok(buf, size);
     }
+    auto join_sum = [&]() {
+      for (auto& t : sum) t.join();
+      sum.clear();
+      for (int k = started; k < K; ++k) hash_blocks(k);  // blocks no thread could be started for
+    };
     uint64_t n = 0, mcs = 0;
     int hrc = LG_OK;
+    HostStage& hs = host_stage();
+    std::unique_lock<std::mutex> lock(hs.m);
     Packed P;
     std::vector<uint8_t> sp;
     try {
@@ -1799,15 +1861,16 @@ struct Engine {
         pack_ops(c, (long long)n, [&](long long i, int* b, uint64_t* tb) {
           std::memcpy(b, ops + 12 * i, 4);
           std::memcpy(tb, ops + 12 * i + 4, 8);
-        }, P);
+        }, P, &hs);
         sp.resize(s.N);
         for (int i = 0; i < s.N; ++i) sp[i] = (uint8_t)(buf[CHECKPOINT_HEAD + i] & 1);
       }
     } catch (...) {
-      if (sum.joinable()) sum.join();
+      join_sum();
       throw;
     }
-    if (sum.joinable()) sum.join();
+    join_sum();
+    const bool sum_ok = checkpoint_combine(bh.data(), nblk) == checkpoint_stored_checksum(buf, size);
     // the checksum is reported first, then the header (its message is already set), then the rest
     if (!sum_ok) return lg_fail(LG_ECORRUPT, "checkpoint checksum mismatch");
     if (hrc) return checkpoint_header(s, buf, size, &n, &mcs);

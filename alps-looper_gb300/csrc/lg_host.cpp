@@ -665,11 +665,13 @@ extern "C" const char* lg_obs_name(int i) {
 // ---------------------------------------------------------------------------------------------
 // Checkpoint: the worker's save/load content (path_integral.C:111-124: mcs, spins, operators).
 // Layout (little endian): "LGCK" u32 version, u32 dim, u32 L, u64 mcs, u64 n_ops,
-// N x u8 spins, n_ops x (i32 bond, f64 time), u64 checksum of everything before it (FNV-1a over
-// its 64-bit little-endian words, then over its remaining bytes).  Version 1:
-// the path-integral form, its off-diagonal operators with their times.  Version 2: the SSE form
+// N x u8 spins, n_ops x (i32 bond, f64 time), u64 checksum of everything before it.  Version 3:
+// the path-integral form, its off-diagonal operators with their times.  Version 4: the SSE form
 // (sse.C save: mcs, spins, operators), every operator of the string as bond << 1 | off-diagonal,
 // with (index + 1/2) / n_ops as its time (the order).
+// The checksum is blocked so that several threads can compute it: FNV-1a (64-bit) of each 1 MiB
+// block (over its 64-bit little-endian words, then its remaining bytes), then FNV-1a of those
+// block hashes in order.
 // ---------------------------------------------------------------------------------------------
 static uint64_t fnv1a(const uint8_t* p, size_t n) {
   uint64_t h = 1469598103934665603ull;
@@ -684,15 +686,43 @@ static uint64_t fnv1a(const uint8_t* p, size_t n) {
   return h;
 }
 
+size_t checkpoint_blocks(size_t size) {
+  const size_t n = size < 8 ? 0 : size - 8;
+  return (n + CHECKPOINT_BLOCK - 1) / CHECKPOINT_BLOCK;
+}
+
+uint64_t checkpoint_block_hash(const uint8_t* buf, size_t size, size_t block) {
+  const size_t n = size < 8 ? 0 : size - 8;
+  const size_t b0 = block * CHECKPOINT_BLOCK;
+  if (b0 >= n) return 0;
+  return fnv1a(buf + b0, std::min(CHECKPOINT_BLOCK, n - b0));
+}
+
+uint64_t checkpoint_combine(const uint64_t* block_hash, size_t nblocks) {
+  uint64_t h = 1469598103934665603ull;
+  for (size_t i = 0; i < nblocks; ++i) {
+    h ^= block_hash[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
 uint64_t checkpoint_checksum(const uint8_t* buf, size_t size) {
-  return size < 8 ? 0 : fnv1a(buf, size - 8);
+  const size_t nb = checkpoint_blocks(size);
+  std::vector<uint64_t> h(nb);
+  for (size_t i = 0; i < nb; ++i) h[i] = checkpoint_block_hash(buf, size, i);
+  return checkpoint_combine(h.data(), nb);
+}
+
+uint64_t checkpoint_stored_checksum(const uint8_t* buf, size_t size) {
+  uint64_t h = 0;
+  if (buf && size >= 8) std::memcpy(&h, buf + size - 8, 8);
+  return h;
 }
 
 bool checkpoint_checksum_ok(const uint8_t* buf, size_t size) {
   if (!buf || size < 8) return false;
-  uint64_t h;
-  std::memcpy(&h, buf + size - 8, 8);
-  return h == checkpoint_checksum(buf, size);
+  return checkpoint_stored_checksum(buf, size) == checkpoint_checksum(buf, size);
 }
 
 void checkpoint_encode(const ChainSpec& s, const std::vector<int32_t>& spins,
@@ -701,10 +731,11 @@ void checkpoint_encode(const ChainSpec& s, const std::vector<int32_t>& spins,
   const size_t head = 4 + 4 + 4 + 4 + 8 + 8;
   blob.resize(head + spins.size() + 12 * bonds.size() + 8);
   uint8_t* p = blob.data();
-  const uint32_t ver = s.sse ? 2 : 1, dim = (uint32_t)s.dim, L = (uint32_t)s.L;
+  const uint32_t ver = s.sse ? CHECKPOINT_VERSION_SSE : CHECKPOINT_VERSION_PI, dim = (uint32_t)s.dim,
+                 L = (uint32_t)s.L;
   const uint64_t mcs = s.mcs, n = bonds.size();
   std::memcpy(p, "LGCK", 4);
-  std::memcpy(p + 4, &ver, 4);  // 2: the SSE form, operators as bond << 1 | type
+  std::memcpy(p + 4, &ver, 4);
   std::memcpy(p + 8, &dim, 4);
   std::memcpy(p + 12, &L, 4);
   std::memcpy(p + 16, &mcs, 8);
@@ -731,7 +762,8 @@ int checkpoint_header(const ChainSpec& s, const uint8_t* buf, size_t size, uint6
   std::memcpy(&L, buf + 12, 4);
   std::memcpy(&m, buf + 16, 8);
   std::memcpy(&n, buf + 24, 8);
-  if (ver != (s.sse ? 2u : 1u)) return lg_fail(LG_ECORRUPT, "checkpoint version %u", ver);
+  if (ver != (s.sse ? CHECKPOINT_VERSION_SSE : CHECKPOINT_VERSION_PI))
+    return lg_fail(LG_ECORRUPT, "checkpoint version %u", ver);
   if ((int)dim != s.dim || (int)L != s.L) return lg_fail(LG_ECORRUPT, "checkpoint lattice mismatch");
   // n is checked against the size without multiplying it (a forged count must not wrap)
   const size_t fixed = head + (size_t)s.N + 8;

@@ -98,10 +98,17 @@ void record_scalars(const ChainSpec& s, const uint64_t* rec, double* v);
 uint64_t value_mask(const ChainSpec& s);
 
 // Checkpoint blob (path_integral.C:111-124 save/load content): a 32-byte header ("LGCK", version,
-// dim, L, mcs, operator count), the spins, 12 bytes per operator, a trailing checksum.
+// dim, L, mcs, operator count), the spins, 12 bytes per operator, a trailing checksum: FNV-1a of
+// each CHECKPOINT_BLOCK bytes before it, then FNV-1a of those block hashes.
 constexpr size_t CHECKPOINT_HEAD = 32;
-// FNV-1a of everything before the trailing checksum, and whether the stored one matches.
+constexpr size_t CHECKPOINT_BLOCK = 1u << 20;
+constexpr uint32_t CHECKPOINT_VERSION_PI = 3;   // path integral: off-diagonal operators and times
+constexpr uint32_t CHECKPOINT_VERSION_SSE = 4;  // SSE: the whole operator string
+size_t checkpoint_blocks(size_t size);
+uint64_t checkpoint_block_hash(const uint8_t* buf, size_t size, size_t block);
+uint64_t checkpoint_combine(const uint64_t* block_hash, size_t nblocks);
 uint64_t checkpoint_checksum(const uint8_t* buf, size_t size);
+uint64_t checkpoint_stored_checksum(const uint8_t* buf, size_t size);
 bool checkpoint_checksum_ok(const uint8_t* buf, size_t size);
 // The header and size of a blob for chain s (no checksum): operator count and sweeps done.
 int checkpoint_header(const ChainSpec& s, const uint8_t* buf, size_t size, uint64_t* nops,

@@ -665,6 +665,32 @@ def uf_label_static(lattice, L, nops, d_bonds, d_graphs, d_labels, stream=0):
     return nf.value, nc.value
 
 
+CHECKPOINT_BLOCK = 1 << 20
+
+
+def checkpoint_checksum(blob) -> int:
+    """The checksum lg_save stores in a checkpoint's last 8 bytes, computed over everything before
+    them: FNV-1a (64-bit) of each 1 MiB block, over its 64-bit little-endian words and then its
+    remaining bytes, and FNV-1a of those block hashes in order.  For tools that edit a blob."""
+    body = bytes(blob)[:-8]
+    mask = (1 << 64) - 1
+
+    def fnv(data):
+        h = 1469598103934665603
+        n8 = len(data) // 8 * 8
+        words = np.frombuffer(data[:n8], dtype="<u8").tolist()
+        for w in words:
+            h = ((h ^ w) * 1099511628211) & mask
+        for x in data[n8:]:
+            h = ((h ^ x) * 1099511628211) & mask
+        return h
+
+    h = 1469598103934665603
+    for b0 in range(0, len(body), CHECKPOINT_BLOCK):
+        h = ((h ^ fnv(body[b0:b0 + CHECKPOINT_BLOCK])) * 1099511628211) & mask
+    return h
+
+
 def kernel_launches() -> int:
     return lib().lg_kernel_launches()
 

@@ -27,19 +27,6 @@ int lg_fail(int code, const char* fmt, ...) {
   return code;
 }
 
-static uint64_t fnv1a(const uint8_t* p, size_t n) {
-  uint64_t h = 1469598103934665603ull;
-  size_t i = 0;
-  for (; i + 8 <= n; i += 8) {
-    uint64_t w = 0;
-    for (int k = 7; k >= 0; --k) w = (w << 8) | p[i + k];
-    h ^= w;
-    h *= 1099511628211ull;
-  }
-  for (; i < n; ++i) { h ^= p[i]; h *= 1099511628211ull; }
-  return h;
-}
-
 static int fuzz_parser(std::mt19937_64& g, int iterations) {
   const std::string base =
       "LATTICE = \"square lattice\"; L = 16\nT = 1/4 # comment\nJz = 0.5; Jxy = 1; h = 0.2\n"
@@ -135,7 +122,7 @@ static int fuzz_model_records_checkpoints(std::mt19937_64& g, int iterations, in
         std::memcpy(b.data() + 24, &big, 8);
       }
       if (g() % 4 == 0) b.resize(g() % (b.size() + 1) + 8);
-      const uint64_t h = fnv1a(b.data(), b.size() - 8);
+      const uint64_t h = checkpoint_checksum(b.data(), b.size());
       std::memcpy(b.data() + b.size() - 8, &h, 8);
       const int rc = checkpoint_decode(s, b.data(), b.size(), sp2, bd2, tm2, &mcs);
       if (rc != LG_OK && rc != LG_ECORRUPT) {

@@ -56,10 +56,10 @@ def _params(lg, m, seed, **kw):
 
 
 def sse_state(blob, nsites):
-    """(sweeps done, spins, operator codes) of an SSE checkpoint (version 2)."""
+    """(sweeps done, spins, operator codes) of an SSE checkpoint (version 4)."""
     assert blob[:4] == b"LGCK"
     ver, _, _, mcs, n = struct.unpack_from("<IIIQQ", blob, 4)
-    assert ver == 2
+    assert ver == 4
     spins = np.frombuffer(blob, dtype=np.uint8, count=nsites, offset=32).astype(np.int32)
     rows = np.frombuffer(blob, dtype=np.dtype([("op", "<i4"), ("t", "<f8")]), count=n,
                          offset=32 + nsites)
@@ -166,14 +166,7 @@ def test_sse_checkpoint_round_trip(lg):
     j = 32 + 36
     code = struct.unpack_from("<i", bad, j)[0]
     struct.pack_into("<i", bad, j, code ^ 1)
-    h = 1469598103934665603                     # the trailing checksum, recomputed
-    body = bytes(bad[:-8])
-    n8 = len(body) // 8 * 8
-    for (w,) in struct.iter_unpack("<Q", body[:n8]):
-        h = ((h ^ w) * 1099511628211) & (2 ** 64 - 1)
-    for x in body[n8:]:
-        h = ((h ^ x) * 1099511628211) & (2 ** 64 - 1)
-    struct.pack_into("<Q", bad, len(bad) - 8, h)
+    struct.pack_into("<Q", bad, len(bad) - 8, lg.checkpoint_checksum(bad))  # re-signed
     with pytest.raises(lg.LoopError) as e:
         b.load(bytes(bad))
     assert e.value.code == -1
