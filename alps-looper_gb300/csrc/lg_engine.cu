@@ -28,6 +28,7 @@
 
 #include "../../include/looper_gpu.h"
 #include "lg_kernels.cuh"
+#include "lg_pack.h"
 #include "lg_host.h"
 #include "lg_resident.cuh"
 #include "lg_sse.cuh"
@@ -411,10 +412,10 @@ struct Engine {
     if (any_sse && !all_sse)
       return lg_fail(LG_EINVAL, "an arena holds either path-integral or SSE chains, not both");
     sse = any_sse;
-    if (!sse) {  // the pinned buffer of lg_load / lg_set_state, once per process (16 MiB: 900k operators)
+    if (!sse) {  // the pinned buffer of lg_load / lg_set_state, once per process (32 MiB: 670k operators)
       HostStage& hs = host_stage();
       std::lock_guard<std::mutex> lock(hs.m);
-      hs.reserve(16u << 20);
+      hs.reserve(32u << 20);
     }
     if (sse) {
       if ((rc = setup_sse(res_vcap_for(1.0), false))) return rc;
@@ -1635,147 +1636,42 @@ struct Engine {
   }
 
   // A chain's off-diagonal operators as the sweep keeps them: per site, its endpoints in (time,
-  // bond) order as (time bits, incidence index), packed in site order (oc[i] entries of site i).
+  // bond) order as (time bits, incidence index), packed in site order (R.oc[i] entries of site i).
   struct Packed {
-    std::vector<int> oc;
+    PackResult R;
     uint64_t* t = nullptr;  // 2n endpoints: time bits
     uint8_t* d = nullptr;   // and incidence index
-    std::unique_ptr<uint64_t[]> own_t;  // when t, d are not in the pinned stage
-    std::unique_ptr<uint8_t[]> own_d;
-    long long bad = -1;     // first operator out of range (bond or time), or -1
-    int odd_site = -1;      // first spin-1/2 site with an odd number of endpoints, or -1
+    std::unique_ptr<unsigned char[]> own;  // when they are not in the pinned stage
   };
 
-  // Packs n operators of chain c, operator i given by get(i, &bond, &time bits).  Input in
-  // (time, bond) order, as lg_save writes it, is placed by a stable counting sort split over up to
-  // eight host threads (per-thread site counts, then each thread places its range); other input is
-  // sorted per site.  A time is accepted in [0, 1) (-0 is read as +0).
-  // With `stage` (held under its lock) the endpoints are packed into the pinned buffer.
+  // Packs n operators of chain c (operator i given by get(i, &bond, &time bits)) with
+  // pack_site_lists, into the pinned stage when `stage` (held under its lock) can hold them.
   template <class Get>
   void pack_ops(int c, long long n, const Get& get, Packed& P, HostStage* stage) {
     const ChainSpec& s = spec[c];
-    const int so = hch[c].site_off, bo = hch[c].bond_off;
-    // threads: at most 8, one per 64k operators, and no more count arrays than operators per site
-    const long long hw = std::max(1u, std::thread::hardware_concurrency());
-    const int T = (int)std::max<long long>(1, std::min<long long>({8ll, hw, n / 65536, 2 * n / std::max(1, s.N)}));
-    const long long per = (n + T - 1) / T;
-    std::vector<std::vector<int>> cnt(T, std::vector<int>(s.N, 0));
-    std::vector<long long> bad(T, -1);
-    std::vector<char> ord(T, 1);
-    auto count = [&](int t) {
-      const long long i0 = t * per, i1 = std::min(n, i0 + per);
-      int* ct = cnt[t].data();
-      int pb = -1;
-      uint64_t pt = 0;
-      for (long long i = i0; i < i1; ++i) {
-        int b;
-        uint64_t tb;
-        get(i, &b, &tb);
-        double tv;
-        std::memcpy(&tv, &tb, 8);
-        if (b < 0 || b >= s.NB || !(tv >= 0.0 && tv < 1.0)) { bad[t] = i; return; }
-        if (tv == 0.0) tb = 0;
-        ++ct[s.s0[b]];
-        ++ct[s.s1[b]];
-        if (i > i0 && !(pt < tb || (pt == tb && pb <= b))) ord[t] = 0;
-        pb = b;
-        pt = tb;
-      }
-    };
-    auto run_par = [&](auto&& f) {  // ranges 1.. on threads (on this one where none starts), 0 here
-      std::vector<std::thread> th;
-      int t = 1;
-      try {
-        th.reserve(T);
-        for (; t < T; ++t) th.emplace_back(f, t);
-      } catch (...) {
-      }
-      for (int u = t; u < T; ++u) f(u);
-      f(0);
-      for (auto& x : th) x.join();
-    };
-    run_par(count);
-    for (int t = 0; t < T; ++t)
-      if (bad[t] >= 0) { P.bad = bad[t]; return; }
-    bool ordered = true;
-    for (int t = 0; t < T; ++t) ordered &= ord[t] != 0;
-    for (int t = 1; t < T && ordered; ++t) {  // across the ranges' boundaries
-      const long long i = t * per;
-      if (i >= n) break;
-      int ba, bb;
-      uint64_t ta, tb;
-      get(i - 1, &ba, &ta);
-      get(i, &bb, &tb);
-      double va, vb;
-      std::memcpy(&va, &ta, 8);
-      std::memcpy(&vb, &tb, 8);
-      if (va == 0.0) ta = 0;
-      if (vb == 0.0) tb = 0;
-      ordered = ta < tb || (ta == tb && ba <= bb);
-    }
-    P.oc.assign(s.N, 0);
-    for (int t = 0; t < T; ++t)
-      for (int i = 0; i < s.N; ++i) P.oc[i] += cnt[t][i];
-    // a spin-1/2 world line is periodic in imaginary time: an even number of flips per site
-    // (spin-S chains close through the boundary matching, which checks its own sectors)
-    if (s.spin2 <= 1)
-      for (int i = 0; i < s.N; ++i)
-        if (P.oc[i] & 1) { P.odd_site = i; return; }
-    std::vector<long long> start(s.N + 1, 0);
-    for (int i = 0; i < s.N; ++i) start[i + 1] = start[i] + P.oc[i];
-    if (stage && stage->reserve((size_t)n * 18 + 64)) {
-      P.t = reinterpret_cast<uint64_t*>(stage->p);
-      P.d = stage->p + (size_t)n * 16;
+    const int bo = hch[c].bond_off;
+    PackTables tab;
+    tab.N = s.N;
+    tab.NB = s.NB;
+    tab.s0 = s.s0.data();
+    tab.s1 = s.s1.data();
+    tab.dir0 = h_bond_dir0.data() + bo;
+    tab.dir1 = h_bond_dir1.data() + bo;
+    tab.check_parity = s.spin2 <= 1;  // spin-S chains close through the matching, which checks its sectors
+    const size_t td = ((size_t)n * 18 + 63) & ~(size_t)63;  // 2n time words and 2n incidence bytes
+    const size_t need = td + pack_scratch_bytes(n) + 64;
+    unsigned char* base = nullptr;
+    if (stage && stage->reserve(need)) {
+      base = stage->p;
     } else {
-      P.own_t.reset(new uint64_t[2 * n + 1]);  // no zero fill: every entry is written below
-      P.own_d.reset(new uint8_t[2 * n + 1]);
-      P.t = P.own_t.get();
-      P.d = P.own_d.get();
+      P.own.reset(new unsigned char[need]);  // no zero fill: every byte used is written
+      base = P.own.get();
     }
-    if (ordered) {  // every site's entries arrive in the order the sweep produces
-      for (int i = 0; i < s.N; ++i) {  // cnt[t][i] := where thread t's first entry of site i goes
-        long long run = start[i];
-        for (int t = 0; t < T; ++t) { const int k = cnt[t][i]; cnt[t][i] = (int)run; run += k; }
-      }
-      auto place = [&](int t) {
-        const long long i0 = t * per, i1 = std::min(n, i0 + per);
-        int* at = cnt[t].data();
-        for (long long i = i0; i < i1; ++i) {
-          int b;
-          uint64_t tb;
-          get(i, &b, &tb);
-          double tv;
-          std::memcpy(&tv, &tb, 8);
-          if (tv == 0.0) tb = 0;
-          const int k0 = at[s.s0[b]]++, k1 = at[s.s1[b]]++;
-          P.t[k0] = tb; P.d[k0] = h_bond_dir0[b + bo];
-          P.t[k1] = tb; P.d[k1] = h_bond_dir1[b + bo];
-        }
-      };
-      run_par(place);
-      return;
-    }
-    std::vector<std::pair<uint64_t, int>> ep(2 * n);  // (time bits, global bond)
-    std::vector<long long> fill(start.begin(), start.end() - 1);
-    for (long long i = 0; i < n; ++i) {
-      int b;
-      uint64_t tb;
-      get(i, &b, &tb);
-      double tv;
-      std::memcpy(&tv, &tb, 8);
-      if (tv == 0.0) tb = 0;
-      ep[fill[s.s0[b]]++] = {tb, b + bo};
-      ep[fill[s.s1[b]]++] = {tb, b + bo};
-    }
-    for (int i = 0; i < s.N; ++i) {
-      std::sort(ep.begin() + start[i], ep.begin() + start[i + 1]);  // the order the sweep produces
-      const int gs = so + i;
-      for (long long k = start[i]; k < start[i + 1]; ++k) {
-        const int gb = ep[k].second;
-        P.t[k] = ep[k].first;
-        P.d[k] = h_bond_s0[gb] == gs ? h_bond_dir0[gb] : h_bond_dir1[gb];
-      }
-    }
+    P.t = reinterpret_cast<uint64_t*>(base);
+    P.d = base + (size_t)n * 16;
+    PackRec* scratch = reinterpret_cast<PackRec*>(base + td);
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    pack_site_lists(tab, n, get, P.t, P.d, scratch, P.R, std::min(8, hw));
   }
 
   // Makes a packed, checked state chain c's state (spins sp[i] in {0, 1}, sweeps done).
@@ -1789,7 +1685,7 @@ struct Engine {
       for (int i = 0, k = 0; i < s.N; ++i) {
         auto& Li = L[so + i];
         Li.clear();
-        for (int j = 0; j < P.oc[i]; ++j, ++k) Li.push_back({P.t[k], P.d[k]});
+        for (int j = 0; j < P.R.oc[i]; ++j, ++k) Li.push_back({P.t[k], P.d[k]});
       }
       if ((rc = upload_lists(L))) return rc;
     } else {
@@ -1797,7 +1693,7 @@ struct Engine {
       const int zero = 0;
       LG_CUDA(lg_copy(&d_ctl.p->err, &zero, sizeof(int), cudaMemcpyHostToDevice));
       LG_CUDA(lg_copy(&d_ctl.p->step, &zero, sizeof(uint32_t), cudaMemcpyHostToDevice));
-      if ((rc = upload_flat(P.oc, P.t, P.d))) return rc;
+      if ((rc = upload_flat(P.R.oc, P.t, P.d))) return rc;
     }
     LG_CUDA(lg_copy(d_spin0.p + so, sp.data(), s.N, cudaMemcpyHostToDevice));
     uint32_t sw = (uint32_t)sweep;
@@ -1814,10 +1710,10 @@ struct Engine {
     std::lock_guard<std::mutex> lock(hs.m);
     Packed P;
     pack_ops(c, n, [&](long long i, int* b, uint64_t* tb) { *b = bonds[i]; std::memcpy(tb, &times[i], 8); }, P, &hs);
-    if (P.bad >= 0) return lg_fail(LG_EINVAL, "operator %lld out of range", P.bad);
-    if (P.odd_site >= 0)
+    if (P.R.bad >= 0) return lg_fail(LG_EINVAL, "operator %lld out of range", P.R.bad);
+    if (P.R.odd_site >= 0)
       return lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
-                                "(not periodic in imaginary time)", P.odd_site);
+                                "(not periodic in imaginary time)", P.R.odd_site);
     std::vector<uint8_t> sp(s.N);
     for (int i = 0; i < s.N; ++i) sp[i] = (uint8_t)(spins[i] & 1);
     return commit_state(c, P, sp, sweep);
@@ -1874,10 +1770,10 @@ struct Engine {
     // the checksum is reported first, then the header (its message is already set), then the rest
     if (!sum_ok) return lg_fail(LG_ECORRUPT, "checkpoint checksum mismatch");
     if (hrc) return checkpoint_header(s, buf, size, &n, &mcs);
-    if (P.bad >= 0) return lg_fail(LG_ECORRUPT, "checkpoint operator %lld out of range", P.bad);
-    if (P.odd_site >= 0)
+    if (P.R.bad >= 0) return lg_fail(LG_ECORRUPT, "checkpoint operator %lld out of range", P.R.bad);
+    if (P.R.odd_site >= 0)
       return lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
-                                "(not periodic in imaginary time)", P.odd_site);
+                                "(not periodic in imaginary time)", P.R.odd_site);
     return commit_state(c, P, sp, mcs);
   }
 
