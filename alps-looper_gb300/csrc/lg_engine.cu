@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -29,6 +30,7 @@
 #include "../../include/looper_gpu.h"
 #include "lg_kernels.cuh"
 #include "lg_pack.h"
+#include "lg_load.cuh"
 #include "lg_host.h"
 #include "lg_resident.cuh"
 #include "lg_sse.cuh"
@@ -1722,6 +1724,106 @@ struct Engine {
   // lg_load of a path-integral checkpoint: the operators are read in place from the blob, packed
   // by pack_ops while a second thread checks the checksum; nothing reaches the device before
   // both are done.
+  // Whether lg_load of n operators can pack on the device: a single chain on the grid path, the
+  // path-integral form, site offsets in one two-level scan, operator indices below 2^31.
+  bool device_load_ok(long long n) const {
+    return C == 1 && !sse && !resident && N <= SITE_SCAN_MAX && n > 0 && n < (1ll << 30);
+  }
+
+  // The device pass of lg_load (lg_load.cuh).  Stages the spins, operators and the bonds' target
+  // incidence indices into the pinned buffer (held by the caller), copies them into the class-sum
+  // array (scratch between sweeps, cleared again before returning), runs the checks and the
+  // packing, and reads back the status.  *bad, *flags, *odd receive the device checks.  The lists
+  // are written only by device_load_commit.
+  int device_load_pack(const uint8_t* buf, long long n, HostStage& hs, LoadArgs& L, int* bad,
+                       int* flags, int* odd, size_t* scratch_used) {
+    if (n > nv_cap) {  // the lists and the scratch need room for 2n endpoints; keep the current ones
+      int rc = alloc_dynamic(n + 4096, true);
+      if (rc) return rc;
+    }
+    const size_t npad = ((size_t)N + 15) & ~(size_t)15;
+    const size_t ops_b = (size_t)n * 12, dir_b = ((size_t)NB + 15) & ~(size_t)15;
+    const size_t stage_b = npad + ops_b + dir_b + 16;  // spins, operators, target incidences, status
+    const size_t rec_b = ((size_t)(2 * n) * 4 + 15) & ~(size_t)15;
+    const size_t fill_b = ((size_t)N * 4 + 15) & ~(size_t)15;
+    const size_t used = stage_b + rec_b + fill_b;
+    if (used > (size_t)ns_cap * 4 * sizeof(unsigned long long) || !hs.reserve(stage_b)) {
+      *bad = INT_MAX;  // no room: the host packs instead
+      *flags = LD_FLAG_LONG;
+      *odd = INT_MAX;
+      return LG_OK;
+    }
+    unsigned char* h = hs.p;
+    // staging: spins, operator records (4-byte aligned), then dir1; several threads copy the
+    // operators
+    std::memcpy(h, buf + CHECKPOINT_HEAD, N);
+    const unsigned char* ops = buf + CHECKPOINT_HEAD + N;
+    const int T = (int)std::max<size_t>(1, std::min<size_t>(4, ops_b >> 20));
+    pack_parallel(T, [&](int k) {
+      const size_t a = ops_b * k / T, b = ops_b * (k + 1) / T;
+      std::memcpy(h + npad + a, ops + a, b - a);
+    });
+    std::memcpy(h + npad + ops_b, h_bond_dir1.data(), NB);
+    int* hstat = reinterpret_cast<int*>(h + npad + ops_b + dir_b);
+    hstat[0] = INT_MAX; hstat[1] = 0; hstat[2] = INT_MAX; hstat[3] = 0;
+    unsigned char* d = reinterpret_cast<unsigned char*>(d_cls.p);
+    LG_CUDA(lg_copy_async(d, h, stage_b, cudaMemcpyHostToDevice, st));
+    *scratch_used = used;
+    L.spins = d;
+    L.ops = reinterpret_cast<const uint32_t*>(d + npad);
+    L.n = n;
+    L.N = N;
+    L.NB = NB;
+    L.s0 = d_bond_s0.p;
+    L.s1 = d_bond_s1.p;
+    L.dir0 = d_bond_dir0.p;
+    L.dir1 = d + npad + ops_b;
+    L.status = reinterpret_cast<int*>(d + npad + ops_b + dir_b);
+    L.rec = reinterpret_cast<uint32_t*>(d + stage_b);
+    L.fill = reinterpret_cast<int*>(d + stage_b + rec_b);
+    L.cnt = d_site_cnt.p;
+    L.off = d_sbase.p;
+    L.partial = d_partial.p;
+    L.parity = spec[0].spin2 <= 1;
+    LG_CUDA(cudaMemsetAsync(L.cnt, 0, (size_t)N * sizeof(int), st));
+    LG_CUDA(cudaMemsetAsync(L.fill, 0, (size_t)N * sizeof(int), st));
+    const int gops = grid_for(n, 256, 8);
+    const int gsites = (N + 1023) / 1024;
+    k_ld_count<<<gops, 256, 0, st>>>(L);
+    k_ld_scan_blocks<<<gsites, 1024, 0, st>>>(L);
+    k_ld_scan_offsets<<<gsites, 1024, 0, st>>>(L);
+    k_ld_place<<<gops, 256, 0, st>>>(L);
+    k_ld_sort<<<grid_for(N, LD_SORT_WARPS, 8), LD_SORT_WARPS * 32, 0, st>>>(L);
+    g_launches += 5;
+    LG_CUDA(cudaGetLastError());
+    LG_CUDA(lg_copy_async(hstat, L.status, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    LG_CUDA(cudaStreamSynchronize(st));
+    *bad = hstat[0];
+    *flags = hstat[1];
+    *odd = hstat[2];
+    return LG_OK;
+  }
+
+  // The checked, packed state becomes the chain's (device_load_pack ran and every check passed).
+  int device_load_commit(const LoadArgs& L, uint64_t mcs) {
+    k_ld_commit_lists<<<grid_for(2 * L.n, 256, 8), 256, 0, st>>>(L, d_stime.p, d_sdir.p);
+    k_ld_commit_sites<<<grid_for(N, 256, 8), 256, 0, st>>>(L, d_off_base.p, d_off_cnt.p, d_spin0.p);
+    g_launches += 2;
+    LG_CUDA(cudaGetLastError());
+    // a complete, valid state: a union-find failure (LG_EITERCAP) no longer applies
+    LG_CUDA(cudaMemsetAsync(&d_ctl.p->err, 0, sizeof(int), st));
+    LG_CUDA(cudaMemsetAsync(&d_ctl.p->step, 0, sizeof(uint32_t), st));
+    const uint32_t sw = (uint32_t)mcs;
+    LG_CUDA(lg_copy_async(d_sweep.p, &sw, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    LG_CUDA(cudaStreamSynchronize(st));
+    spec[0].mcs = mcs;
+    return LG_OK;
+  }
+
+  // lg_load of a path-integral checkpoint.  The checksum's blocks are hashed on host threads
+  // while the operators are checked and packed: on the device (device_load_ok), else by
+  // pack_site_lists on host threads.  Nothing reaches the chain's state before every check has
+  // passed.
   int load_checkpoint(int c, const uint8_t* buf, size_t size) {
     const ChainSpec& s = spec[c];
     if (!buf || size < CHECKPOINT_HEAD + 8) return lg_fail(LG_ECORRUPT, "checkpoint too short");
@@ -1750,9 +1852,19 @@ struct Engine {
     std::unique_lock<std::mutex> lock(hs.m);
     Packed P;
     std::vector<uint8_t> sp;
+    bool on_device = false, device_flags = false;
+    int dbad = INT_MAX, dflags = 0, dodd = INT_MAX;
+    LoadArgs L{};
+    size_t scratch = 0;
+    int drc = LG_OK;
     try {
       hrc = checkpoint_header(s, buf, size, &n, &mcs);
-      if (hrc == LG_OK) {
+      if (hrc == LG_OK && device_load_ok((long long)n)) {
+        on_device = true;
+        drc = device_load_pack(buf, (long long)n, hs, L, &dbad, &dflags, &dodd, &scratch);
+        device_flags = drc == LG_OK && dbad == INT_MAX && dflags != 0;
+      }
+      if (hrc == LG_OK && (!on_device || device_flags)) {  // unordered input or a very long list
         const uint8_t* ops = buf + CHECKPOINT_HEAD + s.N;
         pack_ops(c, (long long)n, [&](long long i, int* b, uint64_t* tb) {
           std::memcpy(b, ops + 12 * i, 4);
@@ -1763,18 +1875,32 @@ struct Engine {
       }
     } catch (...) {
       join_sum();
+      if (scratch) cudaMemsetAsync(d_cls.p, 0, scratch, st);
       throw;
     }
     join_sum();
     const bool sum_ok = checkpoint_combine(bh.data(), nblk) == checkpoint_stored_checksum(buf, size);
+    auto finish = [&](int rc) {  // the class sums were scratch: zero again for the next sweep
+      if (scratch && cudaMemsetAsync(d_cls.p, 0, scratch, st) != cudaSuccess && rc == LG_OK)
+        rc = lg_fail(LG_EDEVICE, "cudaMemsetAsync failed");
+      return rc;
+    };
     // the checksum is reported first, then the header (its message is already set), then the rest
-    if (!sum_ok) return lg_fail(LG_ECORRUPT, "checkpoint checksum mismatch");
-    if (hrc) return checkpoint_header(s, buf, size, &n, &mcs);
-    if (P.R.bad >= 0) return lg_fail(LG_ECORRUPT, "checkpoint operator %lld out of range", P.R.bad);
+    if (!sum_ok) return finish(lg_fail(LG_ECORRUPT, "checkpoint checksum mismatch"));
+    if (hrc) return finish(checkpoint_header(s, buf, size, &n, &mcs));
+    if (drc) return finish(drc);
+    if (on_device && !device_flags) {
+      if (dbad != INT_MAX) return finish(lg_fail(LG_ECORRUPT, "checkpoint operator %d out of range", dbad));
+      if (dodd != INT_MAX)
+        return finish(lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
+                                         "(not periodic in imaginary time)", dodd));
+      return finish(device_load_commit(L, mcs));
+    }
+    if (P.R.bad >= 0) return finish(lg_fail(LG_ECORRUPT, "checkpoint operator %lld out of range", P.R.bad));
     if (P.R.odd_site >= 0)
-      return lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
-                                "(not periodic in imaginary time)", P.R.odd_site);
-    return commit_state(c, P, sp, mcs);
+      return finish(lg_fail(LG_EINVAL, "site %d has an odd number of off-diagonal operators "
+                                       "(not periodic in imaginary time)", P.R.odd_site));
+    return finish(commit_state(c, P, sp, mcs));
   }
 
   // Cluster labels of an explicit configuration (single-chain engine): fills the bond vertex
