@@ -292,16 +292,247 @@ __device__ __forceinline__ int count_lt(const uint64_t* T, int n, uint64_t t) {
 // The vertex count n of a bond is known once its proposals are drawn, so the warp claims its
 // range of n vertices (claim_vertices) before it writes the list there: one pass, no scan.
 // The warps run over `sites` (nullptr: every site of the arena, in order).
+//
+// A site that owns two or more bonds (square and cubic lattices) inserts them two at a time, one
+// per half-warp: 16 proposals per bond and step instead of 32 for one bond, so two bonds of about
+// 32 proposals take about 2.6 steps instead of 3.2, and the staging, the claim and the output of
+// the two run side by side.  A proposal's random words, its time and its fate do not depend on the
+// lanes it ran on, so both forms produce the same list.
+
+// Staging of one warp: the site's own off-diagonal list, and per half-warp a partner list, the
+// bond's own off-diagonal operators and its accepted proposals.
+struct InsStage {
+  uint64_t offS[INS_CAP];
+  uint8_t dirS[INS_CAP];
+  uint64_t offT[2][INS_CAP];
+  uint64_t ownT[2][INS_CAP];
+  uint64_t accT[2][INS_ACC];
+  uint8_t accG[2][INS_ACC];
+};
+
+// The site's bond of incidence d (its source is the site): the whole warp, staging slot 0.
+__device__ __forceinline__ void insert_one(const Arena& A, InsStage& S, int d, int lane, int c,
+                                           int reg, int ns_off, uint32_t ps0, int my_b, int my_nt,
+                                           int my_tb, uint32_t my_pt, bool s_fits) {
+  const unsigned lt = (1u << lane) - 1u;
+  const int b = __shfl_sync(0xFFFFFFFFu, my_b, d);
+  const int nt_off = __shfl_sync(0xFFFFFFFFu, my_nt, d);
+  const int tb_ = __shfl_sync(0xFFFFFFFFu, my_tb, d);
+  const uint32_t pt0 = __shfl_sync(0xFFFFFFFFu, my_pt, d);
+  if (!s_fits || nt_off > INS_CAP) {
+    if (lane == 0) insert_bond_alone(A, b);
+    __syncwarp();
+    return;
+  }
+  __syncwarp();
+  for (int i = lane; i < nt_off; i += 32) S.offT[0][i] = A.stime[tb_ + i];
+  // own off-diagonal operators of bond b, in time order
+  int nown = 0;
+  for (int i0 = 0; i0 < ns_off; i0 += 32) {
+    const int i = i0 + lane;
+    const bool own = i < ns_off && S.dirS[i] == (uint8_t)d;
+    const unsigned ball = __ballot_sync(0xFFFFFFFFu, own);
+    if (own) S.ownT[0][nown + __popc(ball & lt)] = S.offS[i];
+    nown += __popc(ball);
+  }
+  __syncwarp();
+  const DChain ch = A.ch[c];
+  const uint32_t sweep = A.ch_sweep[c];
+  const uint32_t bl = (uint32_t)(b - ch.bond_off);
+  // diagonal proposals, 32 at a time
+  int nacc = 0;
+  bool more = ch.inv_rate > 0.0f;
+  uint64_t tbase = 0;
+  uint32_t k0 = 0;
+  while (more) {
+    const uint32_t k = k0 + lane;  // k0 is a multiple of 32: lanes 2i, 2i+1 share a block
+    rnd4 r = {0, 0, 0, 0};
+    if ((lane & 1) == 0) r = philox(ch.seed, sweep, bl, TAG_PROPOSAL, k >> 1);
+    const uint32_t rz = __shfl_xor_sync(0xFFFFFFFFu, r.z, 1);
+    const uint32_t rw = __shfl_xor_sync(0xFFFFFFFFu, r.w, 1);
+    const uint32_t wu = (k & 1u) ? rz : r.x;
+    const uint32_t wg = (k & 1u) ? rw : r.y;
+    const uint32_t tail = (wu >> 9) ? 0u : gap_tail_word(ch.seed, sweep, bl, k);
+    const float gap = __fmul_rn(-log_open(gap_uniform(wu, tail)), ch.inv_rate);
+    uint64_t q = gap_fix52(gap, ((uint64_t)(wu & 0x1FFu) << 16) | (wg & 0xFFFFu));
+    const bool stop = q >= FIX52_ONE;
+    if (stop) q = 0;
+    uint64_t incl = q;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const uint64_t tq = tbase + incl;
+    const unsigned stops = __ballot_sync(0xFFFFFFFFu, stop);
+    const bool valid = ((stops & (lt | (1u << lane))) == 0) && tq < FIX52_ONE;
+    const unsigned vb = __ballot_sync(0xFFFFFFFFu, valid);
+    bool accept = false;
+    uint64_t tp = 0;
+    uint32_t g = 0;
+    if (valid) {
+      tp = fix52_bits(tq);
+      g = (uint32_t)((uint64_t)wg >= ch.T0) + (uint32_t)((uint64_t)wg >= ch.T1) +
+          (uint32_t)((uint64_t)wg >= ch.T2);
+      const uint32_t ps = ps0 ^ (uint32_t)(count_le(S.offS, ns_off, tp) & 1);
+      const uint32_t pt = pt0 ^ (uint32_t)(count_le(S.offT[0], nt_off, tp) & 1);
+      accept = (((g & 1u) ^ ps ^ pt) & 1u) != 0;
+    }
+    const unsigned ab = __ballot_sync(0xFFFFFFFFu, accept);
+    if (accept) {
+      const int pos = nacc + __popc(ab & lt);
+      if (pos < INS_ACC) { S.accT[0][pos] = tp; S.accG[0][pos] = (uint8_t)g; }
+    }
+    nacc += __popc(ab);
+    more = vb == 0xFFFFFFFFu;
+    tbase = __shfl_sync(0xFFFFFFFFu, tq, 31);
+    k0 += 32;
+  }
+  const int n = nacc + nown;
+  int out0 = 0;
+  if (lane == 0) out0 = claim_vertices(A, b, n, reg);
+  out0 = __shfl_sync(0xFFFFFFFFu, out0, 0);
+  if (out0 >= 0 && nacc > INS_ACC) {
+    // more accepted proposals than the staging holds: the one-thread form writes the list
+    if (lane == 0) insert_bond_serial<true>(A, b, out0);
+  } else if (out0 >= 0) {
+    for (int j = lane; j < nacc; j += 32) {
+      const uint64_t tp = S.accT[0][j];
+      const int pos = j + count_le(S.ownT[0], nown, tp);
+      A.vtime[out0 + pos] = tp;
+      A.vcode[out0 + pos] = (uint8_t)(S.accG[0][j] << 1);
+    }
+    for (int i = lane; i < nown; i += 32) {
+      const uint64_t to = S.ownT[0][i];
+      const int pos = i + count_lt(S.accT[0], nacc, to);
+      const rnd4 ro = philox(ch.seed, sweep, bl, TAG_OFFDIAG, (uint32_t)i >> 2);
+      const uint32_t wv = (i & 3) == 0 ? ro.x : (i & 3) == 1 ? ro.y : (i & 3) == 2 ? ro.z : ro.w;
+      const uint32_t g = ((uint64_t)wv < ch.Poff) ? 0u : 1u;
+      A.vtime[out0 + pos] = to;
+      A.vcode[out0 + pos] = (uint8_t)((g << 1) | 1u);
+    }
+  }
+  __syncwarp();
+}
+
+// The site's bonds of incidences da (lanes 0-15, staging slot 0) and db (lanes 16-31, slot 1),
+// both with lists that fit the staging.  The same steps as insert_one, 16 proposals per bond and
+// step, prefix sums and ballots restricted to the half.
+__device__ __forceinline__ void insert_two(const Arena& A, InsStage& S, int da, int db, int lane,
+                                           int c, int reg, int ns_off, uint32_t ps0, int my_b,
+                                           int my_nt, int my_tb, uint32_t my_pt) {
+  const int h = lane >> 4, hl = lane & 15;
+  const unsigned hshift = 16u * (unsigned)h;
+  const unsigned hlt = (1u << hl) - 1u;
+  const int d = h ? db : da;
+  const int b = __shfl_sync(0xFFFFFFFFu, my_b, d);
+  const int nt_off = __shfl_sync(0xFFFFFFFFu, my_nt, d);
+  const int tb_ = __shfl_sync(0xFFFFFFFFu, my_tb, d);
+  const uint32_t pt0 = __shfl_sync(0xFFFFFFFFu, my_pt, d);
+  uint64_t* offT = S.offT[h];
+  uint64_t* ownT = S.ownT[h];
+  uint64_t* accT = S.accT[h];
+  uint8_t* accG = S.accG[h];
+  __syncwarp();
+  for (int i = hl; i < nt_off; i += 16) offT[i] = A.stime[tb_ + i];
+  // own off-diagonal operators of each half's bond, in time order
+  int nown = 0;
+  for (int i0 = 0; i0 < ns_off; i0 += 16) {
+    const int i = i0 + hl;
+    const bool own = i < ns_off && S.dirS[i] == (uint8_t)d;
+    const unsigned hb = (__ballot_sync(0xFFFFFFFFu, own) >> hshift) & 0xFFFFu;
+    if (own) ownT[nown + __popc(hb & hlt)] = S.offS[i];
+    nown += __popc(hb);
+  }
+  __syncwarp();
+  const DChain ch = A.ch[c];
+  const uint32_t sweep = A.ch_sweep[c];
+  const uint32_t bl = (uint32_t)(b - ch.bond_off);
+  int nacc = 0;
+  bool more = ch.inv_rate > 0.0f;  // this half's bond still proposes
+  uint64_t tbase = 0;
+  uint32_t k0 = 0;
+  while (__any_sync(0xFFFFFFFFu, more)) {
+    const uint32_t k = k0 + (uint32_t)hl;  // k0 is a multiple of 16: lanes 2i, 2i+1 share a block
+    rnd4 r = {0, 0, 0, 0};
+    if (more && (hl & 1) == 0) r = philox(ch.seed, sweep, bl, TAG_PROPOSAL, k >> 1);
+    const uint32_t rz = __shfl_xor_sync(0xFFFFFFFFu, r.z, 1);
+    const uint32_t rw = __shfl_xor_sync(0xFFFFFFFFu, r.w, 1);
+    const uint32_t wu = (k & 1u) ? rz : r.x;
+    const uint32_t wg = (k & 1u) ? rw : r.y;
+    uint64_t q = 0;
+    bool stop = true;
+    if (more) {
+      const uint32_t tail = (wu >> 9) ? 0u : gap_tail_word(ch.seed, sweep, bl, k);
+      const float gap = __fmul_rn(-log_open(gap_uniform(wu, tail)), ch.inv_rate);
+      q = gap_fix52(gap, ((uint64_t)(wu & 0x1FFu) << 16) | (wg & 0xFFFFu));
+      stop = q >= FIX52_ONE;
+      if (stop) q = 0;
+    }
+    uint64_t incl = q;
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o, 16);
+      if (hl >= o) incl += y;
+    }
+    const uint64_t tq = tbase + incl;
+    const unsigned stops = (__ballot_sync(0xFFFFFFFFu, stop) >> hshift) & 0xFFFFu;
+    const bool valid = more && ((stops & (hlt | (1u << hl))) == 0) && tq < FIX52_ONE;
+    const unsigned vb = (__ballot_sync(0xFFFFFFFFu, valid) >> hshift) & 0xFFFFu;
+    bool accept = false;
+    uint64_t tp = 0;
+    uint32_t g = 0;
+    if (valid) {
+      tp = fix52_bits(tq);
+      g = (uint32_t)((uint64_t)wg >= ch.T0) + (uint32_t)((uint64_t)wg >= ch.T1) +
+          (uint32_t)((uint64_t)wg >= ch.T2);
+      const uint32_t ps = ps0 ^ (uint32_t)(count_le(S.offS, ns_off, tp) & 1);
+      const uint32_t pt = pt0 ^ (uint32_t)(count_le(offT, nt_off, tp) & 1);
+      accept = (((g & 1u) ^ ps ^ pt) & 1u) != 0;
+    }
+    const unsigned ab = (__ballot_sync(0xFFFFFFFFu, accept) >> hshift) & 0xFFFFu;
+    if (accept) {
+      const int pos = nacc + __popc(ab & hlt);
+      if (pos < INS_ACC) { accT[pos] = tp; accG[pos] = (uint8_t)g; }
+    }
+    nacc += __popc(ab);
+    more = more && vb == 0xFFFFu;
+    tbase = __shfl_sync(0xFFFFFFFFu, tq, 15, 16);
+    k0 += 16;
+  }
+  const int n = nacc + nown;
+  int out0 = 0;
+  if (hl == 0) out0 = claim_vertices(A, b, n, reg);
+  out0 = __shfl_sync(0xFFFFFFFFu, out0, 0, 16);
+  __syncwarp();
+  if (out0 >= 0 && nacc > INS_ACC) {
+    // more accepted proposals than the staging holds: the one-thread form writes the list
+    if (hl == 0) insert_bond_serial<true>(A, b, out0);
+  } else if (out0 >= 0) {
+    for (int j = hl; j < nacc; j += 16) {
+      const uint64_t tp = accT[j];
+      const int pos = j + count_le(ownT, nown, tp);
+      A.vtime[out0 + pos] = tp;
+      A.vcode[out0 + pos] = (uint8_t)(accG[j] << 1);
+    }
+    for (int i = hl; i < nown; i += 16) {
+      const uint64_t to = ownT[i];
+      const int pos = i + count_lt(accT, nacc, to);
+      const rnd4 ro = philox(ch.seed, sweep, bl, TAG_OFFDIAG, (uint32_t)i >> 2);
+      const uint32_t wv = (i & 3) == 0 ? ro.x : (i & 3) == 1 ? ro.y : (i & 3) == 2 ? ro.z : ro.w;
+      const uint32_t g = ((uint64_t)wv < ch.Poff) ? 0u : 1u;
+      A.vtime[out0 + pos] = to;
+      A.vcode[out0 + pos] = (uint8_t)((g << 1) | 1u);
+    }
+  }
+  __syncwarp();
+}
+
 __global__ void __launch_bounds__(INS_WARPS * 32, 7) k_insert(Arena A, const int* sites, int nsites) {
   if (A.ctl->err) return;
-  __shared__ uint64_t offS[INS_WARPS][INS_CAP];
-  __shared__ uint8_t dirS[INS_WARPS][INS_CAP];
-  __shared__ uint64_t offT[INS_WARPS][INS_CAP];
-  __shared__ uint64_t ownT[INS_WARPS][INS_CAP];
-  __shared__ uint64_t accT[INS_WARPS][INS_ACC];
-  __shared__ uint8_t accG[INS_WARPS][INS_ACC];
+  __shared__ InsStage stage[INS_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const unsigned lt = (1u << lane) - 1u;
+  InsStage& S = stage[w];
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; si < nsites; si += warps) {
     const int s = sites ? sites[si] : si;
@@ -314,12 +545,12 @@ __global__ void __launch_bounds__(INS_WARPS * 32, 7) k_insert(Arena A, const int
     const int ns_off = A.off_cnt[s];
     const int sb = A.off_base[s];
     const uint32_t ps0 = A.spin0[s];
-    int my_b = 0, my_t = 0, my_side = 1, my_nt = 0, my_tb = 0;
+    int my_b = 0, my_side = 1, my_nt = 0, my_tb = 0;
     uint32_t my_pt = 0;
     if (lane < z) {
       my_b = A.inc[j0 + lane];
       my_side = A.inc_side[j0 + lane];
-      my_t = A.inc_nbr[j0 + lane];
+      const int my_t = A.inc_nbr[j0 + lane];
       if (my_side == 0) { my_nt = A.off_cnt[my_t]; my_tb = A.off_base[my_t]; my_pt = A.spin0[my_t]; }
     }
     if (!A.all_active && !A.ch_active[c]) {
@@ -328,108 +559,23 @@ __global__ void __launch_bounds__(INS_WARPS * 32, 7) k_insert(Arena A, const int
     }
     const bool s_fits = ns_off <= INS_CAP;
     if (s_fits) {
-      for (int i = lane; i < ns_off; i += 32) { offS[w][i] = A.stime[sb + i]; dirS[w][i] = A.sdir[sb + i]; }
+      for (int i = lane; i < ns_off; i += 32) { S.offS[i] = A.stime[sb + i]; S.dirS[i] = A.sdir[sb + i]; }
     }
-    for (int d = 0; d < z; ++d) {
-      if (__shfl_sync(0xFFFFFFFFu, my_side, d) != 0) continue;  // bonds owned by s: s is the source
-      const int b = __shfl_sync(0xFFFFFFFFu, my_b, d);
-      const int nt_off = __shfl_sync(0xFFFFFFFFu, my_nt, d);
-      const int tb_ = __shfl_sync(0xFFFFFFFFu, my_tb, d);
-      const uint32_t pt0 = __shfl_sync(0xFFFFFFFFu, my_pt, d);
-      if (!s_fits || nt_off > INS_CAP) {
-        if (lane == 0) insert_bond_alone(A, b);
-        __syncwarp();
-        continue;
+    // bonds owned by s (s is the source), two at a time where both partner lists fit
+    const unsigned owned = __ballot_sync(0xFFFFFFFFu, lane < z && my_side == 0);
+    const unsigned fits = __ballot_sync(0xFFFFFFFFu, lane < z && my_side == 0 && my_nt <= INS_CAP);
+    unsigned rest = owned;
+    while (rest) {
+      const int da = __ffs(rest) - 1;
+      rest &= rest - 1;
+      const unsigned pair_ok = s_fits && rest && ((fits >> da) & 1u) ? rest & fits : 0u;
+      if (pair_ok) {
+        const int db = __ffs(pair_ok) - 1;
+        rest &= ~(1u << db);
+        insert_two(A, S, da, db, lane, c, reg, ns_off, ps0, my_b, my_nt, my_tb, my_pt);
+      } else {
+        insert_one(A, S, da, lane, c, reg, ns_off, ps0, my_b, my_nt, my_tb, my_pt, s_fits);
       }
-      __syncwarp();
-      for (int i = lane; i < nt_off; i += 32) offT[w][i] = A.stime[tb_ + i];
-      // own off-diagonal operators of bond b, in time order
-      int nown = 0;
-      for (int i0 = 0; i0 < ns_off; i0 += 32) {
-        const int i = i0 + lane;
-        const bool own = i < ns_off && dirS[w][i] == (uint8_t)d;
-        const unsigned ball = __ballot_sync(0xFFFFFFFFu, own);
-        if (own) ownT[w][nown + __popc(ball & lt)] = offS[w][i];
-        nown += __popc(ball);
-      }
-      __syncwarp();
-      const DChain ch = A.ch[c];
-      const uint32_t sweep = A.ch_sweep[c];
-      const uint32_t bl = (uint32_t)(b - ch.bond_off);
-      // diagonal proposals, 32 at a time
-      int nacc = 0;
-      bool more = ch.inv_rate > 0.0f;
-      uint64_t tbase = 0;
-      uint32_t k0 = 0;
-      while (more) {
-        const uint32_t k = k0 + lane;  // k0 is a multiple of 32: lanes 2i, 2i+1 share a block
-        rnd4 r = {0, 0, 0, 0};
-        if ((lane & 1) == 0) r = philox(ch.seed, sweep, bl, TAG_PROPOSAL, k >> 1);
-        const uint32_t rz = __shfl_xor_sync(0xFFFFFFFFu, r.z, 1);
-        const uint32_t rw = __shfl_xor_sync(0xFFFFFFFFu, r.w, 1);
-        const uint32_t wu = (k & 1u) ? rz : r.x;
-        const uint32_t wg = (k & 1u) ? rw : r.y;
-        const uint32_t tail = (wu >> 9) ? 0u : gap_tail_word(ch.seed, sweep, bl, k);
-        const float gap = __fmul_rn(-log_open(gap_uniform(wu, tail)), ch.inv_rate);
-        uint64_t q = gap_fix52(gap, ((uint64_t)(wu & 0x1FFu) << 16) | (wg & 0xFFFFu));
-        const bool stop = q >= FIX52_ONE;
-        if (stop) q = 0;
-        uint64_t incl = q;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint64_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        const uint64_t tq = tbase + incl;
-        const unsigned stops = __ballot_sync(0xFFFFFFFFu, stop);
-        const bool valid = ((stops & (lt | (1u << lane))) == 0) && tq < FIX52_ONE;
-        const unsigned vb = __ballot_sync(0xFFFFFFFFu, valid);
-        bool accept = false;
-        uint64_t tp = 0;
-        uint32_t g = 0;
-        if (valid) {
-          tp = fix52_bits(tq);
-          g = (uint32_t)((uint64_t)wg >= ch.T0) + (uint32_t)((uint64_t)wg >= ch.T1) +
-              (uint32_t)((uint64_t)wg >= ch.T2);
-          const uint32_t ps = ps0 ^ (uint32_t)(count_le(offS[w], ns_off, tp) & 1);
-          const uint32_t pt = pt0 ^ (uint32_t)(count_le(offT[w], nt_off, tp) & 1);
-          accept = (((g & 1u) ^ ps ^ pt) & 1u) != 0;
-        }
-        const unsigned ab = __ballot_sync(0xFFFFFFFFu, accept);
-        if (accept) {
-          const int pos = nacc + __popc(ab & lt);
-          if (pos < INS_ACC) { accT[w][pos] = tp; accG[w][pos] = (uint8_t)g; }
-        }
-        nacc += __popc(ab);
-        more = vb == 0xFFFFFFFFu;
-        tbase = __shfl_sync(0xFFFFFFFFu, tq, 31);
-        k0 += 32;
-      }
-      const int n = nacc + nown;
-      int out0 = 0;
-      if (lane == 0) out0 = claim_vertices(A, b, n, reg);
-      out0 = __shfl_sync(0xFFFFFFFFu, out0, 0);
-      if (out0 >= 0 && nacc > INS_ACC) {
-        // more accepted proposals than the staging holds: the one-thread form writes the list
-        if (lane == 0) insert_bond_serial<true>(A, b, out0);
-      } else if (out0 >= 0) {
-        for (int j = lane; j < nacc; j += 32) {
-          const uint64_t tp = accT[w][j];
-          const int pos = j + count_le(ownT[w], nown, tp);
-          A.vtime[out0 + pos] = tp;
-          A.vcode[out0 + pos] = (uint8_t)(accG[w][j] << 1);
-        }
-        for (int i = lane; i < nown; i += 32) {
-          const uint64_t to = ownT[w][i];
-          const int pos = i + count_lt(accT[w], nacc, to);
-          const rnd4 ro = philox(ch.seed, sweep, bl, TAG_OFFDIAG, (uint32_t)i >> 2);
-          const uint32_t wv = (i & 3) == 0 ? ro.x : (i & 3) == 1 ? ro.y : (i & 3) == 2 ? ro.z : ro.w;
-          const uint32_t g = ((uint64_t)wv < ch.Poff) ? 0u : 1u;
-          A.vtime[out0 + pos] = to;
-          A.vcode[out0 + pos] = (uint8_t)((g << 1) | 1u);
-        }
-      }
-      __syncwarp();
     }
   }
 }
