@@ -640,7 +640,9 @@ def run_reference(args, dist, ws, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp64 times", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "lattice": "square", "L": L_SIDE, "beta": BETA,
-                   "step": "one sweep per thread"},
+                   "J": 1.0, "seed": SEED, "step": "one sweep",
+                   "parallelism": "one chain per host thread (%d threads, seeds %d + 1000 i)"
+                                  % (threads, SEED)},
         "operators_per_s": ops / el, "mean_operators": ops / (threads * steps),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "cpu_model": cpu_model(),
