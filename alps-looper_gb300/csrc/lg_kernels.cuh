@@ -1250,6 +1250,7 @@ constexpr int UP_PER = 4;  // segments per thread and step of k_union_pairs, loa
 
 __global__ void __launch_bounds__(256) k_union_pairs(Arena A) {
   if (A.ctl->err) return;
+  if (iter_cap_of(A.ctl) == 0) return;  // the test seam that lets no union run
   const int ns = A.ctl->ns_total;
   const long long step = (long long)gridDim.x * 256 * UP_PER;
   for (long long x0 = (long long)blockIdx.x * 256 * UP_PER + threadIdx.x; x0 < ns; x0 += step) {
@@ -1350,6 +1351,10 @@ __global__ void __launch_bounds__(UB_WARPS * 32, 8) k_union_bal(Arena A) {
   const int nwarps = gridDim.x * UB_WARPS;
   const int nchunks = (ns + UN_CHUNK - 1) / UN_CHUNK;
   const int cap = iter_cap_of(A.ctl);
+  if (cap == 0) {  // the test seam that lets no union run: the sweep stops with LG_EITERCAP
+    if (blockIdx.x == 0 && threadIdx.x == 0 && nchunks > 0) atomicExch(&A.ctl->err, ERR_ITERCAP);
+    return;
+  }
   int* P = A.parent;
   int chunk = blockIdx.x * UB_WARPS + w;
   unsigned head = 0, tail = 0;  // the warp's queue is [head, tail), indices mod UB_QUEUE

@@ -2,7 +2,8 @@
 
 Every device loop whose trip count depends on the data has a cap and reports LG_EITERCAP
 instead of hanging.  These tests:
-* lower the union-find cap through a test seam, so that the sweep gives up at once;
+* lower the union-find cap through a test seam, so that the sweep gives up at once (on the
+  chain-resident path and on the grid path with each way of making the unions);
 * check that the error is reported, stays reported (the sweep had already overwritten the
   chain's operator lists), and is cleared by loading a checkpoint, after which the chain
   continues exactly like an undisturbed one;
@@ -29,8 +30,13 @@ def _params(lg):
                           THERMALIZATION=0, INITIAL_SPINS="random")
 
 
-def test_union_find_cap_is_reported_and_recoverable(lg):
+@pytest.mark.parametrize("shape", [None, dict(resident=0, union_mode=0),
+                                   dict(resident=0, union_mode=1), dict(resident=0, union_mode=2)],
+                         ids=["default", "grid-lanes", "grid-pairs", "grid-balanced"])
+def test_union_find_cap_is_reported_and_recoverable(lg, shape):
     w = lg.LoopWorker(_params(lg))
+    if shape is not None:
+        w.shape = shape
     w.run(5)
     blob = w.save()
     w.set_iteration_cap(-1)          # no union may run: the next sweep stops
