@@ -831,16 +831,19 @@ __device__ __forceinline__ void warp_merge2(const uint64_t* XK, const uint16_t* 
     if (XK[i] <= YK[d0 - i - 1]) lo = i + 1; else hi = i;
   }
   int i = lo, j = d0 - lo;
+  // the head key of each side in a register; an exhausted side reads as ~0 (keys are below 2^63)
+  uint64_t xk = i < nx ? XK[i] : ~0ull, yk = j < ny ? YK[j] : ~0ull;
   for (int d = d0; d < d1; ++d) {
-    const bool tx = j >= ny || (i < nx && XK[i] <= YK[j]);
-    if (tx) {
-      OK[d] = XK[i];
+    if (xk <= yk) {
+      OK[d] = xk;
       OI[d] = XI ? XI[i] : (uint16_t)(xb + i);
       ++i;
+      xk = i < nx ? XK[i] : ~0ull;
     } else {
-      OK[d] = YK[j];
+      OK[d] = yk;
       OI[d] = YI ? YI[j] : (uint16_t)(yb + j);
       ++j;
+      yk = j < ny ? YK[j] : ~0ull;
     }
   }
 }
@@ -957,13 +960,17 @@ __global__ void __launch_bounds__(MERGE_WARPS * 32, 8) k_merge(Arena A, const in
         ptr[d] = 0; off[d + 1] = off[d]; sdv[d] = 0;
       }
     }
+    // one pass over the site's endpoints, list after list (no lane idles at the end of a list)
+    for (int i = lane; i < off[Z]; i += 32) {
+      int d = 0;
 #pragma unroll
-    for (int d = 0; d < Z; ++d) {
-      for (int i = lane; i < off[d + 1] - off[d]; i += 32) {
-        const uint8_t c = A.vcode[ptr[d] + i];
-        wsK[off[d] + i] = merge_key(A.vtime[ptr[d] + i], c);
-        wsC[off[d] + i] = c;
-      }
+      for (int q = 1; q < Z; ++q) if (i >= off[q]) d = q;
+      int v = 0;
+#pragma unroll
+      for (int q = 0; q < Z; ++q) if (q == d) v = ptr[q] + (i - off[q]);
+      const uint8_t c = A.vcode[v];
+      wsK[i] = merge_key(A.vtime[v], c);
+      wsC[i] = c;
     }
     __syncwarp();
     // The merged order is (time, off-diagonal first, list).  Up to 32 endpoints: every lane
