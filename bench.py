@@ -232,46 +232,46 @@ def cpu_port_rate(seconds=12.0, threads=1, state=None, warm=3):
 
 
 # ---- the CPU-runnable chain workload: S=1/2 Heisenberg AF chain, L=64, beta=10, seed 1234 ----
-C0_L, C0_BETA, C0_SEED, C0_THERM, C0_SWEEPS = 64, 10.0, 1234, 1 << 12, 1 << 14
+SMALL_L, SMALL_BETA, SMALL_SEED, SMALL_THERM, SMALL_SWEEPS = 64, 10.0, 1234, 1 << 12, 1 << 14
 
 
-def _c0_standalone(_):
+def _small_standalone(_):
     import oracle_lib as orc
-    out, speed = orc.standalone(C0_L, 1.0 / C0_BETA, C0_SWEEPS, C0_SWEEPS >> 3)
+    out, speed = orc.standalone(SMALL_L, 1.0 / SMALL_BETA, SMALL_SWEEPS, SMALL_SWEEPS >> 3)
     return speed
 
 
-def run_config0(lg, batch_chains=1024, batch_steps=256):
+def run_small_chain(lg, batch_chains=1024, batch_steps=256):
     """The CPU-runnable chain workload on the plain GPU path (lg_create + lg_run of the whole
     2^12 + 2^14 sweeps + lg_observables, host wall clock), as a batch of such chains (one arena,
     device time), and on the host: the oracle's restatement of standalone/loop.C (which
     reproduces that program's output digit for digit: same draws, same arithmetic) with its
     options -l 64 -t 0.1 -n 16384, on one core and as one process per core."""
     import multiprocessing as mp
-    p = lg.make_params(LATTICE="chain", L=C0_L, BETA=C0_BETA, J=1.0, SEED=C0_SEED,
-                       SWEEPS=C0_SWEEPS, THERMALIZATION=C0_THERM, INITIAL_SPINS="random")
+    p = lg.make_params(LATTICE="chain", L=SMALL_L, BETA=SMALL_BETA, J=1.0, SEED=SMALL_SEED,
+                       SWEEPS=SMALL_SWEEPS, THERMALIZATION=SMALL_THERM, INITIAL_SPINS="random")
     t0 = time.perf_counter()
     w = lg.LoopWorker(p)
-    w.run(C0_THERM + C0_SWEEPS)
+    w.run(SMALL_THERM + SMALL_SWEEPS)
     obs = w.observables()
     el = time.perf_counter() - t0
     w.close()
-    plain = (C0_THERM + C0_SWEEPS) * C0_L / el
-    ps = [lg.make_params(LATTICE="chain", L=C0_L, BETA=C0_BETA, J=1.0, SEED=C0_SEED + i,
-                         SWEEPS=C0_SWEEPS, THERMALIZATION=C0_THERM, INITIAL_SPINS="random")
+    plain = (SMALL_THERM + SMALL_SWEEPS) * SMALL_L / el
+    ps = [lg.make_params(LATTICE="chain", L=SMALL_L, BETA=SMALL_BETA, J=1.0, SEED=SMALL_SEED + i,
+                         SWEEPS=SMALL_SWEEPS, THERMALIZATION=SMALL_THERM, INITIAL_SPINS="random")
           for i in range(batch_chains)]
     b = lg.Batch(ps)
     b.run(64)
     b.time_sweeps(3)
     ms = b.time_sweeps(batch_steps)
-    batched = batch_chains * C0_L * batch_steps / (float(ms.sum()) / 1e3)
+    batched = batch_chains * SMALL_L * batch_steps / (float(ms.sum()) / 1e3)
     b.close()
     # host: one process, then one process per core (spawned: no GPU context is forked)
-    speed1 = _c0_standalone(0)
+    speed1 = _small_standalone(0)
     cores = os.cpu_count() or 1
     with mp.get_context("spawn").Pool(cores) as pool:
         t1 = time.perf_counter()
-        speeds = pool.map(_c0_standalone, range(cores))
+        speeds = pool.map(_small_standalone, range(cores))
         el_all = time.perf_counter() - t1
     return {"workload": "S=1/2 Heisenberg AF chain, L=64, J=1, beta=10, seed 1234, 2^12 + 2^14 "
                         "sweeps, iid random initial spins",
@@ -283,7 +283,7 @@ def run_config0(lg, batch_chains=1024, batch_steps=256):
                         "ms_per_sweep": float(ms.mean()), "steps": batch_steps,
                         "scope": "one arena of %d such chains (seeds 1234 + i), device time"
                                  % batch_chains},
-            "cpu": {"value_1core": speed1 * C0_L, "value_all_cores": sum(speeds) * C0_L,
+            "cpu": {"value_1core": speed1 * SMALL_L, "value_all_cores": sum(speeds) * SMALL_L,
                     "unit": UNIT, "cores": cores, "cpu_model": cpu_model(), "kind": "port",
                     "program": "oracle restatement of standalone/loop.C, options -l 64 -t 0.1 "
                                "-n 16384 (its own thermalization n/8 = 2048, seed 29833, spins "
@@ -561,7 +561,7 @@ def run_ours(args, dist, ws, rank, local):
                          "equilibrated state, %.1f s, 1 thread (CPU restatement of "
                          "path_integral.C in oracle/)" % (r["sweeps"], r["seconds"])}
     w.close()
-    config0 = _leg(run_config0, lg) if rank == 0 and args.config0 else None
+    small_chain = _leg(run_small_chain, lg) if rank == 0 and args.small_chain else None
     batched = None
     if rank == 0 and args.batched_steps > 0:
         batched = _leg(run_batched, lg, args.batched_steps, args.batched_therm)
@@ -589,7 +589,7 @@ def run_ours(args, dist, ws, rank, local):
                    "parallelism": "replicas" if ws > 1 else "single chain"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
         "clocks": clocks,
-        "config0_chain": config0,
+        "small_chain": small_chain,
         "batched": batched,
         "replicas_field": replicas,
         "served": served,
@@ -661,7 +661,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--config0", type=int, default=1, help="run the CPU-runnable chain workload")
+    ap.add_argument("--small-chain", type=int, default=1,
+                    help="run the CPU-runnable chain workload (L=64 chain, beta=10)")
     ap.add_argument("--batched-steps", type=int, default=16)
     ap.add_argument("--batched-therm", type=int, default=128)
     ap.add_argument("--replica-steps", type=int, default=8)

@@ -265,7 +265,7 @@ def test_checkpoint_roundtrip_and_corruption(lg):
 
 
 def test_full_size_invariants_and_one_sweep_parity(lg):
-    # configs[1] shape: 128x128 square Heisenberg AF, beta = 64, seed 7.
+    # the bench workload: 128x128 square Heisenberg AF, beta = 64, seed 7.
     p = lg.make_params(LATTICE="square", L=128, BETA=64.0, J=1.0, SEED=7, SWEEPS=8192,
                        THERMALIZATION=1024, INITIAL_SPINS="random")
     g = lg.LoopWorker(p)
