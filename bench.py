@@ -404,7 +404,7 @@ def served_requests(lg, n=4096, seed=2024):
 
 
 def _leg(fn, *a):
-    """A supplementary measurement (config-0 chain, batched, replicas, served): its failure is
+    """A supplementary measurement (small chain, batched, replicas, served): its failure is
     reported in its own entry of the line instead of ending the run."""
     try:
         return fn(*a)
