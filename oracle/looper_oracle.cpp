@@ -403,7 +403,7 @@ struct chain_t {
   void sweep_once() {
     const int N = lat.N, NB = lat.NB;
     // ---- diagonal proposals: a Poisson stream per bond (rate beta*W_b) ----
-    struct prop { uint64_t tq; int b; int k; int g; };
+    struct prop { uint64_t tq; int b; int g; };  // generated in (b, k) order, k the draw index
     std::vector<prop> props;
     if (bw.W > 0) {
       for (int b = 0; b < NB; ++b) {
@@ -425,23 +425,36 @@ struct chain_t {
           if (ge1) break;
           tq += q;
           if (tq >= FIX52_ONE) break;
-          props.push_back({tq, b, k, graph_of(wg)});
+          props.push_back({tq, b, graph_of(wg)});
         }
       }
     }
-    std::sort(props.begin(), props.end(), [](const prop& a, const prop& b) {
-      if (a.tq != b.tq) return a.tq < b.tq;
-      if (a.b != b.b) return a.b < b.b;
-      return a.k < b.k;
-    });
+    // Order (tq, b, k).  The stream is generated bond by bond and, within a bond, in k order, so
+    // a stable sort by tq alone gives that order: an LSD radix sort, seven passes of 8 bits over
+    // the 52-bit times (256 output streams per pass stay in cache).
+    {
+      std::vector<prop> tmp(props.size());
+      size_t count[256];
+      for (int sh = 0; sh < 52; sh += 8) {
+        std::memset(count, 0, sizeof(count));
+        for (const prop& q : props) ++count[(q.tq >> sh) & 0xFFu];
+        size_t sum = 0;
+        for (size_t& c : count) { const size_t v = c; c = sum; sum += v; }
+        for (const prop& q : props) tmp[count[(q.tq >> sh) & 0xFFu]++] = q;
+        props.swap(tmp);
+      }
+    }
     // ---- old operators: keep the off-diagonal ones (path_integral.C:515-518) ----
     std::vector<op_t> old;
     for (auto& o : ops) if (o.offdiag) old.push_back(o);
-    std::stable_sort(old.begin(), old.end(), [](const op_t& a, const op_t& b) {
+    auto time_bond = [](const op_t& a, const op_t& b) {
       uint64_t ta = d_bits(a.t), tb = d_bits(b.t);
       if (ta != tb) return ta < tb;
       return a.bond < b.bond;
-    });
+    };
+    // usually already in order (the previous sweep wrote the string in time order)
+    if (!std::is_sorted(old.begin(), old.end(), time_bond))
+      std::stable_sort(old.begin(), old.end(), time_bond);
 
     // ---- merge in time order: insertion/removal + labeling (path_integral.C:484-566) ----
     std::vector<int> spins_c = spins;
@@ -450,7 +463,10 @@ struct chain_t {
     for (int s = 0; s < N; ++s) current[s] = s;
     std::vector<op_t> nops; nops.reserve(old.size() + props.size());
     std::vector<int> loop0, loop1, up0, up1;  // per new op: reconnect loops, upper fragments
-    std::vector<int> cnt(N, 0), rank0, rank1;  // endpoint rank on each site (1-based)
+    loop0.reserve(nops.capacity()); loop1.reserve(nops.capacity());
+    up0.reserve(nops.capacity()); up1.reserve(nops.capacity());
+    frag.parent.reserve(N + props.size()); frag.id.reserve(N + props.size());
+    std::vector<int> cnt(N, 0);  // endpoints per site
     std::vector<int> ordinal(NB, 0);
     size_t ip = 0, io = 0;
     while (ip < props.size() || io < old.size()) {
@@ -494,7 +510,7 @@ struct chain_t {
       nops.push_back(o);
       loop0.push_back(l0); loop1.push_back(l1);
       up0.push_back(current[s0]); up1.push_back(current[s1]);
-      rank0.push_back(++cnt[s0]); rank1.push_back(++cnt[s1]);
+      ++cnt[s0]; ++cnt[s1];
     }
     // ---- temporal closure (path_integral.C:582-615) ----
     if (lat.spin2 == 1) {
@@ -521,59 +537,75 @@ struct chain_t {
     // ---- per-site segment lists (site-major, time-minor; bottom segment first) ----
     std::vector<int64_t> base(N + 1, 0);
     for (int s = 0; s < N; ++s) base[s + 1] = base[s] + cnt[s] + 1;
-    // For each site gather endpoints in time order: since ops are processed in time order,
-    // appending in processing order is already time order per site.
-    std::vector<std::vector<int>> ep(N);  // op indices touching site
-    for (int s = 0; s < N; ++s) ep[s].reserve(cnt[s]);
-    for (size_t i = 0; i < nops.size(); ++i) {
-      ep[lat.s0[nops[i].bond]].push_back((int)i);
-      ep[lat.s1[nops[i].bond]].push_back((int)i);
+    // Each site's endpoints in time order: ops are processed in time order, so appending in
+    // processing order is already time order per site.  One flat array, site after site, with
+    // what the segment walk needs of each endpoint.
+    struct endpoint { int64_t t40; int nextfr; int offdiag; int wdir; };  // wdir -1: no winding
+    std::vector<int64_t> eoff(N + 1, 0);
+    for (int s = 0; s < N; ++s) eoff[s + 1] = eoff[s] + cnt[s];
+    std::vector<endpoint> E((size_t)eoff[N]);
+    {
+      std::vector<int64_t> cur(eoff.begin(), eoff.end() - 1);
+      for (size_t i = 0; i < nops.size(); ++i) {
+        const op_t& o = nops[i];
+        const int64_t t40 = time_fix40(o.t);
+        for (int side = 0; side < 2; ++side) {
+          const int s = side ? lat.s1[o.bond] : lat.s0[o.bond];
+          const bool src = lat.s0[o.bond] == s;
+          endpoint& e = E[(size_t)cur[s]++];
+          e.t40 = t40;
+          e.nextfr = src ? up0[i] : up1[i];
+          e.offdiag = o.offdiag;
+          e.wdir = (src && !(o.g & 2)) ? lat.bdir[o.bond] : -1;
+        }
+      }
     }
-    // cluster accumulators
-    std::vector<int64_t> key(nc, INT64_MAX);
-    std::vector<int64_t> L(nc, 0), M(nc, 0), SL(nc, 0), SM(nc, 0);
-    std::vector<int64_t> n0(nc, 0), m0(nc, 0), sn0(nc, 0), sm0(nc, 0);
-    // winding of each cluster per direction (stiffness.h:82-130): the improved accumulator calls
-    // end_bs / begin_bs for the source-site legs of every non-frozen bond vertex
-    // (measurement.h improved_accumulator::end_b / begin_b, path_integral.C:697-709).  The lower
-    // leg's cluster gains (1-2c) e_d with c the spin before the vertex, the upper leg's cluster
-    // loses (1-2c') e_d with c' the spin after; d is the bond's direction (bond = site*dim + d).
-    std::vector<int64_t> wind((size_t)nc * 3, 0);
+    // cluster accumulators, one record per cluster
+    struct cacc {
+      int64_t key = INT64_MAX;
+      int64_t L = 0, M = 0, SL = 0, SM = 0;
+      int64_t n0 = 0, m0 = 0, sn0 = 0, sm0 = 0;
+      // winding per direction (stiffness.h:82-130): the improved accumulator calls end_bs /
+      // begin_bs for the source-site legs of every non-frozen bond vertex (measurement.h
+      // improved_accumulator::end_b / begin_b, path_integral.C:697-709).  The lower leg's
+      // cluster gains (1-2c) e_d with c the spin before the vertex, the upper leg's cluster
+      // loses (1-2c') e_d with c' the spin after; d is the bond's direction (bond = site*dim + d).
+      int64_t w[3] = {0, 0, 0};
+    };
+    std::vector<cacc> A(nc);
     int64_t MA = 0, SMA = 0, M0tot = 0, SM0tot = 0;
     for (int s = 0; s < N; ++s) {
       int c = spins[s];
       int g = lat.gauge[s];
       int64_t tprev = 0;
       int fr = s;
-      for (int j = 0; j <= (int)ep[s].size(); ++j) {
+      const int ne = cnt[s];
+      const endpoint* es = E.data() + eoff[s];
+      for (int j = 0; j <= ne; ++j) {
         int64_t tnext;
         int nextfr = -1, nextc = c;
-        if (j < (int)ep[s].size()) {
-          const op_t& o = nops[ep[s][j]];
-          tnext = time_fix40(o.t);
-          int i = ep[s][j];
-          nextfr = (lat.s0[o.bond] == s) ? up0[i] : up1[i];
-          if (o.offdiag) nextc = c ^ 1;
+        if (j < ne) {
+          tnext = es[j].t40;
+          nextfr = es[j].nextfr;
+          if (es[j].offdiag) nextc = c ^ 1;
         } else {
           tnext = (int64_t)1 << 40;
         }
-        int cl = frag.id[fr];
-        if (j < (int)ep[s].size()) {
-          const op_t& o = nops[ep[s][j]];
-          if (lat.s0[o.bond] == s && !(o.g & 2)) {
-            const int d = lat.bdir[o.bond];
-            wind[(size_t)cl * 3 + d] += 1 - 2 * c;                          // end_bs
-            wind[(size_t)frag.id[nextfr] * 3 + d] -= 1 - 2 * nextc;          // begin_bs
-          }
+        const int cl = frag.id[fr];
+        cacc& a = A[cl];
+        if (j < ne && es[j].wdir >= 0) {
+          const int d = es[j].wdir;
+          a.w[d] += 1 - 2 * c;                              // end_bs
+          A[frag.id[nextfr]].w[d] -= 1 - 2 * nextc;          // begin_bs
         }
         int64_t segidx = base[s] + j;
-        if (segidx < key[cl]) key[cl] = segidx;
+        if (segidx < a.key) a.key = segidx;
         int64_t len = tnext - tprev;
         int sg = 1 - 2 * c;
-        L[cl] += len; M[cl] += sg * len; SL[cl] += g * len; SM[cl] += g * sg * len;
+        a.L += len; a.M += sg * len; a.SL += g * len; a.SM += g * sg * len;
         MA += sg * len; SMA += g * sg * len;
         if (j == 0) {
-          n0[cl] += 1; m0[cl] += sg; sn0[cl] += g; sm0[cl] += g * sg;
+          a.n0 += 1; a.m0 += sg; a.sn0 += g; a.sm0 += g * sg;
           M0tot += sg; SM0tot += g * sg;
         }
         tprev = tnext; c = nextc; fr = nextfr;
@@ -583,11 +615,11 @@ struct chain_t {
     std::vector<uint8_t> flip(nc);
     for (int cl = 0; cl < nc; ++cl) {
       uint32_t w[4];
-      rng4(seed, sweep, (uint32_t)key[cl], TAG_FLIP, 0, w);
+      rng4(seed, sweep, (uint32_t)A[cl].key, TAG_FLIP, 0, w);
       if (!field) {
         flip[cl] = (w[0] < 0x80000000u) ? 1 : 0;
       } else {
-        float x = (float)M[cl] * flip_coef;
+        float x = (float)A[cl].M * flip_coef;
         float q = exp_spec(x);
         float u = uniform_open(w[0]);
         flip[cl] = (u * (1.0f + q) < 1.0f) ? 1 : 0;
@@ -601,23 +633,24 @@ struct chain_t {
     rec[R_SM0] = (uint64_t)SM0tot;
     int64_t fld = 0;
     for (int cl = 0; cl < nc; ++cl) {
-      rec[R_M0SQ] += (uint64_t)(m0[cl] * m0[cl]);
-      rec[R_N0SQ] += (uint64_t)(n0[cl] * n0[cl]);
-      rec[R_SM0SQ] += (uint64_t)(sm0[cl] * sm0[cl]);
-      rec[R_SN0SQ] += (uint64_t)(sn0[cl] * sn0[cl]);
-      auto q4 = [](int64_t x) { u128 a = (u128)(uint64_t)(x * x); return a * a; };
-      add128(rec.data(), R_M0Q_LO, q4(m0[cl]));
-      add128(rec.data(), R_N0Q_LO, q4(n0[cl]));
-      add128(rec.data(), R_SM0Q_LO, q4(sm0[cl]));
-      add128(rec.data(), R_SN0Q_LO, q4(sn0[cl]));
-      auto sq = [](int64_t x) { uint64_t a = (uint64_t)(x < 0 ? -x : x); return (u128)a * a; };
-      add128(rec.data(), R_LSQ_LO, sq(L[cl]));
-      add128(rec.data(), R_MSQ_LO, sq(M[cl]));
-      add128(rec.data(), R_SLSQ_LO, sq(SL[cl]));
-      add128(rec.data(), R_SMSQ_LO, sq(SM[cl]));
-      fld += flip[cl] ? -M[cl] : M[cl];
+      const cacc& a = A[cl];
+      rec[R_M0SQ] += (uint64_t)(a.m0 * a.m0);
+      rec[R_N0SQ] += (uint64_t)(a.n0 * a.n0);
+      rec[R_SM0SQ] += (uint64_t)(a.sm0 * a.sm0);
+      rec[R_SN0SQ] += (uint64_t)(a.sn0 * a.sn0);
+      auto q4 = [](int64_t x) { u128 v = (u128)(uint64_t)(x * x); return v * v; };
+      add128(rec.data(), R_M0Q_LO, q4(a.m0));
+      add128(rec.data(), R_N0Q_LO, q4(a.n0));
+      add128(rec.data(), R_SM0Q_LO, q4(a.sm0));
+      add128(rec.data(), R_SN0Q_LO, q4(a.sn0));
+      auto sq = [](int64_t x) { uint64_t v = (uint64_t)(x < 0 ? -x : x); return (u128)v * v; };
+      add128(rec.data(), R_LSQ_LO, sq(a.L));
+      add128(rec.data(), R_MSQ_LO, sq(a.M));
+      add128(rec.data(), R_SLSQ_LO, sq(a.SL));
+      add128(rec.data(), R_SMSQ_LO, sq(a.SM));
+      fld += flip[cl] ? -a.M : a.M;
       for (int d = 0; d < 3; ++d) {
-        const int64_t w = wind[(size_t)cl * 3 + d];
+        const int64_t w = a.w[d];
         rec[R_WSQ] += (uint64_t)(w * w);
         rec[R_W0 + d] += (uint64_t)w;
       }
