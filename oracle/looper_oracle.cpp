@@ -430,18 +430,35 @@ struct chain_t {
       }
     }
     // Order (tq, b, k).  The stream is generated bond by bond and, within a bond, in k order, so
-    // a stable sort by tq alone gives that order: an LSD radix sort, seven passes of 8 bits over
-    // the 52-bit times (256 output streams per pass stay in cache).
+    // a stable sort by tq alone gives that order.  Times are uniform on [0, 1) (52-bit), so: a
+    // stable scatter by the top 8 bits, the same inside each of those buckets by the next 8, and
+    // a stable insertion sort of each of the small buckets left.
     {
       std::vector<prop> tmp(props.size());
-      size_t count[256];
-      for (int sh = 0; sh < 52; sh += 8) {
-        std::memset(count, 0, sizeof(count));
-        for (const prop& q : props) ++count[(q.tq >> sh) & 0xFFu];
-        size_t sum = 0;
-        for (size_t& c : count) { const size_t v = c; c = sum; sum += v; }
-        for (const prop& q : props) tmp[count[(q.tq >> sh) & 0xFFu]++] = q;
-        props.swap(tmp);
+      size_t start[257];
+      auto scatter = [&](const prop* src, prop* dst, size_t n, int sh, size_t* st) {
+        std::memset(st, 0, 257 * sizeof(size_t));
+        for (size_t i = 0; i < n; ++i) ++st[((src[i].tq >> sh) & 0xFFu) + 1];
+        for (int k = 0; k < 256; ++k) st[k + 1] += st[k];
+        size_t pos[256];
+        std::memcpy(pos, st, sizeof(pos));
+        for (size_t i = 0; i < n; ++i) dst[pos[(src[i].tq >> sh) & 0xFFu]++] = src[i];
+      };
+      scatter(props.data(), tmp.data(), props.size(), 44, start);
+      size_t sub[257];
+      for (int k = 0; k < 256; ++k) {
+        const size_t lo = start[k], n = start[k + 1] - lo;
+        if (!n) continue;
+        prop* dst = props.data() + lo;
+        scatter(tmp.data() + lo, dst, n, 36, sub);
+        for (int k2 = 0; k2 < 256; ++k2) {
+          for (size_t i = sub[k2] + 1; i < sub[k2 + 1]; ++i) {
+            const prop x = dst[i];
+            size_t j = i;
+            while (j > sub[k2] && dst[j - 1].tq > x.tq) { dst[j] = dst[j - 1]; --j; }
+            dst[j] = x;
+          }
+        }
       }
     }
     // ---- old operators: keep the off-diagonal ones (path_integral.C:515-518) ----
@@ -540,7 +557,8 @@ struct chain_t {
     // Each site's endpoints in time order: ops are processed in time order, so appending in
     // processing order is already time order per site.  One flat array, site after site, with
     // what the segment walk needs of each endpoint.
-    struct endpoint { int64_t t40; int nextfr; int offdiag; int wdir; };  // wdir -1: no winding
+    // nextfr: the fragment above the endpoint, later its cluster; wdir -1: no winding
+    struct endpoint { int64_t t40; int nextfr; int offdiag; int wdir; };
     std::vector<int64_t> eoff(N + 1, 0);
     for (int s = 0; s < N; ++s) eoff[s + 1] = eoff[s] + cnt[s];
     std::vector<endpoint> E((size_t)eoff[N]);
@@ -573,30 +591,32 @@ struct chain_t {
       int64_t w[3] = {0, 0, 0};
     };
     std::vector<cacc> A(nc);
+    // the cluster above each endpoint, in one pass of independent reads
+    for (endpoint& e : E) e.nextfr = frag.id[e.nextfr];
     int64_t MA = 0, SMA = 0, M0tot = 0, SM0tot = 0;
     for (int s = 0; s < N; ++s) {
       int c = spins[s];
       int g = lat.gauge[s];
       int64_t tprev = 0;
-      int fr = s;
+      int cl = frag.id[s];
       const int ne = cnt[s];
       const endpoint* es = E.data() + eoff[s];
       for (int j = 0; j <= ne; ++j) {
         int64_t tnext;
-        int nextfr = -1, nextc = c;
+        int nextcl = -1, nextc = c;
         if (j < ne) {
           tnext = es[j].t40;
-          nextfr = es[j].nextfr;
+          nextcl = es[j].nextfr;
           if (es[j].offdiag) nextc = c ^ 1;
+          if (j + 8 < ne) __builtin_prefetch(&A[es[j + 8].nextfr]);
         } else {
           tnext = (int64_t)1 << 40;
         }
-        const int cl = frag.id[fr];
         cacc& a = A[cl];
         if (j < ne && es[j].wdir >= 0) {
           const int d = es[j].wdir;
           a.w[d] += 1 - 2 * c;                              // end_bs
-          A[frag.id[nextfr]].w[d] -= 1 - 2 * nextc;          // begin_bs
+          A[nextcl].w[d] -= 1 - 2 * nextc;                  // begin_bs
         }
         int64_t segidx = base[s] + j;
         if (segidx < a.key) a.key = segidx;
@@ -608,7 +628,7 @@ struct chain_t {
           a.n0 += 1; a.m0 += sg; a.sn0 += g; a.sm0 += g * sg;
           M0tot += sg; SM0tot += g * sg;
         }
-        tprev = tnext; c = nextc; fr = nextfr;
+        tprev = tnext; c = nextc; cl = nextcl;
       }
     }
     // ---- flips (path_integral.C:780-803) ----
